@@ -1,0 +1,422 @@
+"""Benchmark of the stable-fluids step on GB300: cell-steps/s at 2048^2 with
+max|div u| <= 1e-6 after every projection.
+
+Workload (synthetic, seeded): a 2048 x 2048 periodic MAC grid on [0, 2pi]^2,
+a unit stream u = 1 with a divergence-free random perturbation past seeded
+fixed disks (direct-forcing mask, radii 0.02-0.08 of the height), nu = 1e-4,
+MacCormack advection, explicit diffusion, dt at CFL 0.5, and a
+mixed-precision multigrid projection iterated until max|div u| <= 1e-6.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+Prints ONE JSON line (rank 0).  ``value`` is device-timed throughput with the
+fields resident in HBM; ``e2e`` adds a host->device upload of the velocity
+and a device->host read-back to every step, through the public C ABI.
+``--impl reference`` times the reference's CPU solver (the f64 restatement in
+oracle/, all host threads) on the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import importlib.util
+import json
+import math
+import os
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+METRIC = "cell-steps/s @2048^2, max|div u| <= 1e-6 (mixed-precision MG)"
+UNIT = "cell-steps/s"
+N = 2048
+TOL = 1e-6
+NU = 1e-4
+SEED = 5
+
+
+def _package():
+    name = "fluid_sim_gb300"
+    if name in sys.modules:
+        return sys.modules[name]
+    d = ROOT / "fluid-sim_gb300"
+    spec = importlib.util.spec_from_file_location(name, d / "__init__.py", submodule_search_locations=[str(d)])
+    mod = importlib.util.module_from_spec(spec)
+    sys.modules[name] = mod
+    spec.loader.exec_module(mod)
+    return mod
+
+
+def _oracle():
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import oracle
+
+    oracle.build()
+    return oracle
+
+
+# ------------------------------------------------------------------ workload
+def make_workload(n: int = N, seed: int = SEED):
+    """Seeded initial velocity (f64 MAC faces) and disks.
+
+    The perturbation is the discrete curl of a corner streamfunction built from
+    random Fourier modes with 4 <= |k| <= 8, so it is exactly divergence-free
+    on the MAC grid; the disks make every projection non-trivial."""
+    rng = np.random.default_rng(seed)
+    L = 2 * math.pi
+    h = L / n
+    x = np.arange(n) * h
+    X, Y = np.meshgrid(x, x)  # corners (i h, j h), [j, i]
+    psi = np.zeros((n, n))
+    for _ in range(24):
+        while True:
+            kx, ky = rng.integers(-8, 9, size=2)
+            if 4 <= math.hypot(kx, ky) <= 8:
+                break
+        psi += rng.normal() * np.sin(kx * X + ky * Y + rng.uniform(0, 2 * math.pi)) / (kx * kx + ky * ky)
+    du = (np.roll(psi, -1, axis=0) - psi) / h    # (psi[j+1, i] - psi[j, i]) / dy
+    dv = -(np.roll(psi, -1, axis=1) - psi) / h   # -(psi[j, i+1] - psi[j, i]) / dx
+    scale = 0.1 / max(np.abs(du).max(), np.abs(dv).max())
+    u = 1.0 + scale * du
+    v = scale * dv
+    ndisk = int(rng.integers(1, 9))
+    disks = []
+    while len(disks) < ndisk:
+        r = float(rng.uniform(0.02, 0.08)) * L
+        cx, cy = float(rng.uniform(0, L)), float(rng.uniform(0, L))
+        if all(math.hypot(cx - d[0], cy - d[1]) > r + d[2] + 0.3 for d in disks):
+            disks.append((cx, cy, r))
+    umax = float(max(np.abs(u).max(), np.abs(v).max()))
+    dt = 0.5 * h / umax
+    return np.ascontiguousarray(u.ravel()), np.ascontiguousarray(v.ravel()), disks, dt
+
+
+# ------------------------------------------------------------------- clocks
+class ClockSampler:
+    """nvidia-smi samples every 200 ms while the timed region runs."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.lines: list[str] = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (FileNotFoundError, OSError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+            self.t.join(timeout=2)
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for k, name in enumerate(names):
+                if f[5 + k].lower().startswith("active"):
+                    reasons.add(name)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": mx, "reasons": [], "samples": 0}
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# --------------------------------------------------------------- helpers
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def init_dist(world: int):
+    if world <= 1:
+        return None
+    import torch.distributed as dist
+
+    dist.init_process_group("gloo")
+    return dist
+
+
+def barrier(dist):
+    if dist is not None:
+        dist.barrier()
+
+
+def allmax(dist, x: float) -> float:
+    if dist is None:
+        return x
+    import torch
+
+    t = torch.tensor([x], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def allsum(dist, x: float) -> float:
+    if dist is None:
+        return x
+    import torch
+
+    t = torch.tensor([x], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.SUM)
+    return float(t.item())
+
+
+def measured_peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def traffic_from_profiles(kernel: str):
+    """dram bytes per launch of the dominant kernel, from the committed ncu summary."""
+    p = ROOT / "profiles" / "traffic.json"
+    if not p.exists():
+        return None
+    try:
+        d = json.loads(p.read_text())
+        return d.get(kernel)
+    except (ValueError, OSError):
+        return None
+
+
+def make_solver(pkg, n, device, guess="zero"):
+    return pkg.GPUFluidSolver(n=n, nu=NU, advection="maccormack", pressure_solver="multigrid",
+                              pressure_iterations=1, precision="mixed", pressure_tol=TOL, max_cycles=60,
+                              warm_start=(guess == "warm"), device=device)
+
+
+# ------------------------------------------------------------------- GPU arm
+def run_gpu(args):
+    rank, world, local = dist_env()
+    dist = init_dist(world)
+    pkg = _package()
+    pkg.load()
+    n = args.n
+    u0, v0, disks, dt = make_workload(n)
+    s = make_solver(pkg, n, local, args.guess)
+    s.upload_velocity(u0, v0)
+    s.set_solids(disks)
+    # warm-up
+    cycles = []
+    for _ in range(args.warmup):
+        s.step(dt)
+        cycles.append(s.last_stats()["cycles"])
+    s.sync()
+    # timed region: K steps, device events on the solver's stream
+    launches0 = s.launch_count()
+    barrier(dist)
+    with ClockSampler(local) as clk:
+        ms = s.time_steps(dt, args.steps)
+    barrier(dist)
+    launches = s.launch_count() - launches0
+    st = s.last_stats()
+    md = s.max_divergence()
+    ms_max = allmax(dist, ms)
+    cells = allsum(dist, float(n) * n * args.steps)
+    value = cells / (ms_max / 1e3)
+
+    # per-kernel profile (events around every launch), a few steps after the timed region
+    prof = s.profile_step(dt, 3)
+    prof_ms = sum(k["total_ms"] for k in prof)
+    top = max(prof, key=lambda k: k["total_ms"])
+    per_launch_ms = top["total_ms"] / top["launches"]
+    bytes_per_launch = top["bytes"] / top["launches"]
+    peak, peak_src = measured_peaks()
+    achieved = bytes_per_launch / (per_launch_ms / 1e3) / 1e9
+    traffic = traffic_from_profiles(top["name"])
+
+    # cycles per step over the timed steps (from a separate short run of stats)
+    cyc = []
+    for _ in range(5):
+        s.step(dt)
+        cyc.append(s.last_stats()["cycles"])
+
+    # e2e: host upload + step + host read-back per step through the C ABI
+    lib = pkg.load()
+    nbytes = n * n * 8
+    hu = lib.fs_host_alloc(nbytes)
+    hv = lib.fs_host_alloc(nbytes)
+    au = np.ctypeslib.as_array(C.cast(hu, C.POINTER(C.c_double)), shape=(n * n,))
+    av = np.ctypeslib.as_array(C.cast(hv, C.POINTER(C.c_double)), shape=(n * n,))
+    au[:] = u0
+    av[:] = v0
+    e2e_steps = max(3, min(args.steps, 20))
+    s.sync()
+    barrier(dist)
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        pkg._lib.check(lib.fs_upload_velocity(s._h, hu, hv, 1), s._h)
+        pkg._lib.check(lib.fs_step(s._h, dt), s._h)
+        pkg._lib.check(lib.fs_read_velocity(s._h, hu, hv, 1), s._h)
+    e2e_s = time.perf_counter() - t0
+    barrier(dist)
+    e2e_s = allmax(dist, e2e_s)
+    e2e_val = allsum(dist, float(n) * n * e2e_steps) / e2e_s
+    lib.fs_host_free(hu)
+    lib.fs_host_free(hv)
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        cpu = cpu_baseline(n, threads=1, timed_steps=1)
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64 state / f32 advection + V-cycles",
+            "data": "synthetic (seeded stream + divergence-free perturbation + fixed disks)",
+            "config": {
+                "workload": f"periodic {n}x{n} MAC grid, stream u=1 past {len(disks)} fixed disks, nu={NU}, "
+                            "MacCormack, explicit diffusion, mixed-precision multigrid V(2,2) iterated to "
+                            f"max|div u| <= {TOL}",
+                "n": n, "disks": len(disks), "dt": dt, "tol": TOL, "guess": args.guess,
+                "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
+                "l2": "working set ~0.35 GB > 129 MB L2; no flush between steps",
+                "cycles_per_step": float(np.mean(cyc)),
+                "max_div_after": md, "converged": bool(st["converged"]),
+            },
+            "roofline": {
+                "bound": "hbm", "kernel": top["name"], "achieved": achieved, "peak": peak, "unit": "GB/s",
+                "frac": achieved / peak, "traffic": traffic, "peak_source": f"{peak_src} (MEASURED_PEAKS.json hbm_gbs)",
+                "algorithmic_bytes_per_launch": bytes_per_launch, "launch_ms": per_launch_ms,
+                "share_of_step": top["total_ms"] / prof_ms,
+            },
+            "kernels": [{"name": k["name"], "launches": k["launches"], "ms": round(k["total_ms"], 4),
+                         "gbs": (k["bytes"] / (k["total_ms"] / 1e3) / 1e9) if k["total_ms"] > 0 else None}
+                        for k in sorted(prof, key=lambda k: -k["total_ms"])],
+            "e2e": {"value": e2e_val, "unit": UNIT, "h2d_bytes_per_step": 2 * nbytes,
+                    "d2h_bytes_per_step": 2 * nbytes, "steps": e2e_steps},
+            "gpu_launches": launches,
+            "clocks": clk.summary(),
+        }
+        if cpu is not None:
+            line["cpu_baseline"] = cpu
+        print(json.dumps(line), flush=True)
+    s.destroy()
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+# ------------------------------------------------------------ CPU baselines
+def cpu_baseline(n: int, threads: int, timed_steps: int):
+    """The oracle (f64 restatement of the reference CPU solver) on the same
+    workload: MacCormack, explicit diffusion, exact FFT projection, one
+    coupling pass per disk.  One untimed step, then `timed_steps` timed."""
+    O = _oracle()
+    O.set_threads(threads)
+    u0, v0, disks, dt = make_workload(n)
+    cpu = O.CpuSolver(n=n, nu=NU, advection="maccormack", explicit_diffusion=True, projection="fft",
+                      coupling_passes=1)
+    cpu.u[:] = u0
+    cpu.v[:] = v0
+    for d in disks:
+        cpu.add_solid(O.disk(d[0], d[1], d[2], density=8, fixed=True))
+    cpu.step(dt, advect_dye=False)
+    t0 = time.perf_counter()
+    for _ in range(timed_steps):
+        cpu.step(dt, advect_dye=False)
+    sec = time.perf_counter() - t0
+    return {"value": float(n) * n * timed_steps / sec, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"{timed_steps} timed step(s) of the {n}^2 workload after 1 untimed step "
+                      f"({sec:.1f} s), f64 C restatement of src/cpu (FFT projection), "
+                      f"max|div|={cpu.max_divergence():.1e}"}
+
+
+def run_reference(args):
+    rank, world, local = dist_env()
+    if rank != 0:
+        return
+    threads = os.cpu_count() or 1
+    O = _oracle()
+    O.set_threads(threads)
+    n = args.n
+    u0, v0, disks, dt = make_workload(n)
+    cpu = O.CpuSolver(n=n, nu=NU, advection="maccormack", explicit_diffusion=True, projection="fft",
+                      coupling_passes=1)
+    cpu.u[:] = u0
+    cpu.v[:] = v0
+    for d in disks:
+        cpu.add_solid(O.disk(d[0], d[1], d[2], density=8, fixed=True))
+    # bounded sample: at most 1 warm-up and 3 timed steps whatever K and W are
+    warm = min(args.warmup, 1)
+    timed = max(1, min(args.steps, 3))
+    for _ in range(warm):
+        cpu.step(dt, advect_dye=False)
+    t0 = time.perf_counter()
+    for _ in range(timed):
+        cpu.step(dt, advect_dye=False)
+    sec = time.perf_counter() - t0
+    value = float(n) * n * timed / sec
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 0,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": sec * 1e3 / timed,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (same seeded workload)",
+        "config": {"workload": f"periodic {n}x{n}, {len(disks)} fixed disks, nu={NU}, MacCormack, explicit "
+                               "diffusion, exact FFT projection (max|div| ~1e-13)", "n": n},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": f"{timed} timed step(s) after {warm} warm-up step(s) of the {n}^2 "
+                                   f"workload (of K={args.steps}); f64 C restatement of src/cpu with "
+                                   f"{threads} OpenMP threads (the reference is JavaScript; no Node here)"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=100)
+    ap.add_argument("--warmup", type=int, default=10)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--n", type=int, default=N)
+    ap.add_argument("--guess", default="zero", choices=["zero", "warm"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3 and args.impl != "reference":
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

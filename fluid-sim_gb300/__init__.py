@@ -1,0 +1,10 @@
+"""fluid-sim_gb300: the stable-fluids step of fluid-sim on one GB300.
+
+The compute path is libfluidcuda.so (hand-written CUDA for sm_103a behind the
+C ABI in include/fluid.h); this package builds it and mirrors the reference's
+GPUFluidSolver API on top of it.
+"""
+from ._lib import FluidError, build, load, LIB_PATH  # noqa: F401
+from .solver import GPUFluidSolver  # noqa: F401
+
+__all__ = ["GPUFluidSolver", "FluidError", "build", "load", "LIB_PATH"]

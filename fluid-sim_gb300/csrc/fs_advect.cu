@@ -1,0 +1,330 @@
+// fs_advect.cu -- advection, explicit diffusion, band forcing and immersed-disk
+// direct forcing for GB300 (sm_103a).
+//
+// Reference: src/gpu/shaders.js ADVECT_VELOCITY (:126-146), ADVECT_FIELD_BY
+// (:155-171), MACCORMACK_COMBINE (:187-231), DIFFUSE (:401-425), FORCING
+// (:532-566), SOLID_COUPLE (:587-653); the f64 semantics they restate are
+// src/cpu/advect.js:46-206, src/cpu/solver.js:52-69 and src/cpu/solid.js:101-233.
+//
+// Trace arithmetic is done in cell units relative to the destination cell:
+// a position is (home cell integer, f32 offset), so the interpolation weights
+// keep full f32 precision at any grid size.  The reference forms x = i*dx in
+// f32 and divides by dx again, which at n = 2048 quantises the weights to
+// ~2e-4 of a cell; the mathematics is otherwise identical.
+#include <math.h>
+
+#include "fs_internal.cuh"
+
+namespace fs {
+
+__device__ __forceinline__ int wrap_idx(int i, int n) {
+  if ((unsigned)i < (unsigned)n) return i;
+  int r = i % n;
+  return r < 0 ? r + n : r;
+}
+
+template <class T>
+__device__ __forceinline__ float ld(const T* __restrict__ a, int64_t k) {
+  return (float)__ldg(a + k);
+}
+
+// Bilinear sample at (bi + ox, bj + oy) in the field's own index space
+// (src/core/grid.js:147-164 bilerp: top = a + (b-a)fx, bot = c + (d-c)fx).
+template <class T>
+__device__ __forceinline__ float bilerp(const T* __restrict__ f, int nx, int ny, int bi, int bj,
+                                        float ox, float oy) {
+  float fo = floorf(ox), go = floorf(oy);
+  float fx = ox - fo, fy = oy - go;
+  int i0 = wrap_idx(bi + (int)fo, nx), j0 = wrap_idx(bj + (int)go, ny);
+  int i1 = i0 + 1 == nx ? 0 : i0 + 1;
+  int j1 = j0 + 1 == ny ? 0 : j0 + 1;
+  int64_t r0 = (int64_t)j0 * nx, r1 = (int64_t)j1 * nx;
+  float a = ld(f, r0 + i0), b = ld(f, r0 + i1), c = ld(f, r1 + i0), d = ld(f, r1 + i1);
+  float top = a + (b - a) * fx;
+  float bot = c + (d - c) * fx;
+  return top + (bot - top) * fy;
+}
+
+// Range of the four cells a bilinear sample at (bi+ox, bj+oy) reads
+// (src/cpu/advect.js:104-111).
+template <class T>
+__device__ __forceinline__ void bounds4(const T* __restrict__ f, int nx, int ny, int bi, int bj,
+                                        float ox, float oy, float& lo, float& hi) {
+  int i0 = wrap_idx(bi + (int)floorf(ox), nx), j0 = wrap_idx(bj + (int)floorf(oy), ny);
+  int i1 = i0 + 1 == nx ? 0 : i0 + 1;
+  int j1 = j0 + 1 == ny ? 0 : j0 + 1;
+  int64_t r0 = (int64_t)j0 * nx, r1 = (int64_t)j1 * nx;
+  float a = ld(f, r0 + i0), b = ld(f, r0 + i1), c = ld(f, r1 + i0), d = ld(f, r1 + i1);
+  lo = fminf(fminf(a, b), fminf(c, d));
+  hi = fmaxf(fmaxf(a, b), fmaxf(c, d));
+}
+
+// Sample offsets of the u and v grids relative to a home point.  u lives at
+// (i, j+1/2), v at (i+1/2, j) (src/core/grid.js:99-105).  A point at home +
+// (dX, dY) cells has u-grid index (hux + dX, huy + dY) etc.
+struct Home {
+  float ux, uy;  // u-grid offset of the home point
+  float vx, vy;  // v-grid offset of the home point
+};
+__device__ __forceinline__ Home home_u() { return {0.f, 0.f, -0.5f, 0.5f}; }
+__device__ __forceinline__ Home home_v() { return {0.5f, -0.5f, 0.f, 0.f}; }
+
+// RK2 midpoint backward trace (src/cpu/advect.js:46-54, shaders.js:117-122),
+// in cells: returns the displacement (dX, dY) of the departure point.
+template <class TV>
+__device__ __forceinline__ void trace(const TV* __restrict__ u, const TV* __restrict__ v, int nx,
+                                      int ny, int i, int j, Home h, float cx, float cy, float& dX,
+                                      float& dY) {
+  float u1 = bilerp(u, nx, ny, i, j, h.ux, h.uy);
+  float v1 = bilerp(v, nx, ny, i, j, h.vx, h.vy);
+  float mx = -0.5f * cx * u1, my = -0.5f * cy * v1;
+  float u2 = bilerp(u, nx, ny, i, j, h.ux + mx, h.uy + my);
+  float v2 = bilerp(v, nx, ny, i, j, h.vx + mx, h.vy + my);
+  dX = -cx * u2;
+  dY = -cy * v2;
+}
+
+// ADVECT_VELOCITY: each component traced from its own face (shaders.js:126-146)
+template <class TV>
+__global__ void __launch_bounds__(256) k_advect_sl(const TV* __restrict__ u, const TV* __restrict__ v,
+                                                   float* __restrict__ ou, float* __restrict__ ov,
+                                                   int nx, int ny, float cx, float cy) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y;
+  if (i >= nx || j >= ny) return;
+  float dX, dY;
+  Home hu = home_u(), hv = home_v();
+  trace(u, v, nx, ny, i, j, hu, cx, cy, dX, dY);
+  float a = bilerp(u, nx, ny, i, j, hu.ux + dX, hu.uy + dY);
+  trace(u, v, nx, ny, i, j, hv, cx, cy, dX, dY);
+  float b = bilerp(v, nx, ny, i, j, hv.vx + dX, hv.vy + dY);
+  int64_t c = (int64_t)j * nx + i;
+  ou[c] = a;
+  ov[c] = b;
+}
+
+// MACCORMACK: the backward pass (ADVECT_FIELD_BY with -dt) is evaluated inside
+// the combine kernel at the single point it is needed, then the limited
+// correction (shaders.js:187-231, src/cpu/advect.js:149-185).
+template <class TV>
+__global__ void __launch_bounds__(256)
+    k_mc_combine(const TV* __restrict__ u, const TV* __restrict__ v, const float* __restrict__ fu,
+                 const float* __restrict__ fv, float* __restrict__ ou, float* __restrict__ ov, int nx,
+                 int ny, float cx, float cy) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y;
+  if (i >= nx || j >= ny) return;
+  int64_t c = (int64_t)j * nx + i;
+  Home hu = home_u(), hv = home_v();
+  float dX, dY, lo, hi;
+  // u component
+  trace(u, v, nx, ny, i, j, hu, -cx, -cy, dX, dY);  // backward: trace with -dt
+  float bu = bilerp(fu, nx, ny, i, j, hu.ux + dX, hu.uy + dY);
+  float cu = __ldg(fu + c) + 0.5f * ((float)__ldg(u + c) - bu);
+  trace(u, v, nx, ny, i, j, hu, cx, cy, dX, dY);
+  bounds4(u, nx, ny, i, j, hu.ux + dX, hu.uy + dY, lo, hi);
+  cu = cu < lo ? lo : cu > hi ? hi : cu;
+  // v component
+  trace(u, v, nx, ny, i, j, hv, -cx, -cy, dX, dY);
+  float bv = bilerp(fv, nx, ny, i, j, hv.vx + dX, hv.vy + dY);
+  float cv = __ldg(fv + c) + 0.5f * ((float)__ldg(v + c) - bv);
+  trace(u, v, nx, ny, i, j, hv, cx, cy, dX, dY);
+  bounds4(v, nx, ny, i, j, hv.vx + dX, hv.vy + dY, lo, hi);
+  cv = cv < lo ? lo : cv > hi ? hi : cv;
+  ou[c] = cu;
+  ov[c] = cv;
+}
+
+static const dim3 kBlock(32, 8);
+
+template <class TV>
+void launch_advect_sl(Solver* s, const TV* u, const TV* v, float* ou, float* ov, float dt) {
+  const Grid& g = s->g;
+  float cx = (float)((double)dt / g.dxd), cy = (float)((double)dt / g.dyd);
+  FS_LAUNCH(s, "advect_sl", (double)s->n * (2 * sizeof(TV) + 8),
+            k_advect_sl<TV><<<grid2d(g.nx, g.ny, kBlock), kBlock, 0, s->stream>>>(u, v, ou, ov, g.nx,
+                                                                                   g.ny, cx, cy));
+}
+
+template <class TV>
+void launch_advect_mc(Solver* s, const TV* u, const TV* v, float* fu, float* fv, float* ou,
+                      float* ov, float dt) {
+  const Grid& g = s->g;
+  float cx = (float)((double)dt / g.dxd), cy = (float)((double)dt / g.dyd);
+  FS_LAUNCH(s, "advect_sl", (double)s->n * (2 * sizeof(TV) + 8),
+            k_advect_sl<TV><<<grid2d(g.nx, g.ny, kBlock), kBlock, 0, s->stream>>>(u, v, fu, fv, g.nx,
+                                                                                   g.ny, cx, cy));
+  FS_LAUNCH(s, "mc_combine", (double)s->n * (2 * sizeof(TV) + 8 + 8),
+            k_mc_combine<TV><<<grid2d(g.nx, g.ny, kBlock), kBlock, 0, s->stream>>>(
+                u, v, fu, fv, ou, ov, g.nx, g.ny, cx, cy));
+}
+
+template void launch_advect_sl<float>(Solver*, const float*, const float*, float*, float*, float);
+template void launch_advect_sl<double>(Solver*, const double*, const double*, float*, float*, float);
+template void launch_advect_mc<float>(Solver*, const float*, const float*, float*, float*, float*,
+                                      float*, float);
+template void launch_advect_mc<double>(Solver*, const double*, const double*, float*, float*,
+                                       float*, float*, float);
+
+// DIFFUSE (shaders.js:401-425; src/cpu/solver.js:56-68 operand order)
+__global__ void __launch_bounds__(256) k_diffuse(const float* __restrict__ u, const float* __restrict__ v,
+                                                 float* __restrict__ ou, float* __restrict__ ov,
+                                                 int nx, int ny, float a, float b) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y;
+  if (i >= nx || j >= ny) return;
+  int im = i == 0 ? nx - 1 : i - 1, ip = i + 1 == nx ? 0 : i + 1;
+  int jm = j == 0 ? ny - 1 : j - 1, jp = j + 1 == ny ? 0 : j + 1;
+  int64_t r = (int64_t)j * nx, rm = (int64_t)jm * nx, rp = (int64_t)jp * nx;
+  float c = __ldg(u + r + i);
+  ou[r + i] = c + a * (__ldg(u + r + im) - 2.f * c + __ldg(u + r + ip)) +
+              b * (__ldg(u + rm + i) - 2.f * c + __ldg(u + rp + i));
+  c = __ldg(v + r + i);
+  ov[r + i] = c + a * (__ldg(v + r + im) - 2.f * c + __ldg(v + r + ip)) +
+              b * (__ldg(v + rm + i) - 2.f * c + __ldg(v + rp + i));
+}
+
+void launch_diffuse(Solver* s, const float* u, const float* v, float* ou, float* ov, float dt) {
+  const Grid& g = s->g;
+  float a = (float)(s->prm.nu * dt / (g.dxd * g.dxd));
+  float b = (float)(s->prm.nu * dt / (g.dyd * g.dyd));
+  FS_LAUNCH(s, "diffuse", (double)s->n * 16,
+            k_diffuse<<<grid2d(g.nx, g.ny, kBlock), kBlock, 0, s->stream>>>(u, v, ou, ov, g.nx, g.ny,
+                                                                            a, b));
+}
+
+// FORCING + drag, in place (shaders.js:532-566): u <- u*exp(-drag dt) + amp dt/sqrt(M) sum_m
+__global__ void __launch_bounds__(256) k_forcing(float* __restrict__ u, float* __restrict__ v,
+                                                 const float* __restrict__ modes, int m, int nx,
+                                                 int ny, float dx, float dy, float scale, float damp,
+                                                 float drift) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y;
+  if (i >= nx || j >= ny) return;
+  float pux = i * dx, puy = (j + 0.5f) * dy, pvx = (i + 0.5f) * dx, pvy = j * dy;
+  float fu = 0.f, fv = 0.f;
+  for (int k = 0; k < m; k++) {
+    float kx = __ldg(modes + 3 * k), ky = __ldg(modes + 3 * k + 1), ph = __ldg(modes + 3 * k + 2);
+    float kk = sqrtf(kx * kx + ky * ky);
+    if (kk < 1e-6f) continue;
+    fu += (ky / kk) * cosf(kx * pux + ky * puy + ph + drift);
+    fv -= (kx / kk) * cosf(kx * pvx + ky * pvy + ph + drift);
+  }
+  int64_t c = (int64_t)j * nx + i;
+  u[c] = u[c] * damp + scale * fu;
+  v[c] = v[c] * damp + scale * fv;
+}
+
+void launch_forcing(Solver* s, float* u, float* v, float dt) {
+  const Grid& g = s->g;
+  float scale = (float)(s->amp * dt / sqrt((double)s->n_modes));
+  float damp = (float)exp(-s->drag * dt);
+  float drift = (float)(s->drift * s->t);
+  FS_LAUNCH(s, "forcing", (double)s->n * 16,
+            k_forcing<<<grid2d(g.nx, g.ny, kBlock), kBlock, 0, s->stream>>>(
+                u, v, s->modes, s->n_modes, g.nx, g.ny, g.dx, g.dy, scale, damp, drift));
+}
+
+// Direct forcing of immersed disks (src/cpu/solid.js:165-233, shaders.js:587-653):
+// chi = 0.5 (1 - tanh((|d| - r)/w)), u += chi (U_s - u), applied where chi >= 1e-6,
+// disk after disk at each face.  Impulses are summed per disk on the device.
+struct DiskDev {
+  float x, y, r, vx, vy, omega, reach2;
+};
+#define FS_MAX_DISKS 64
+__constant__ DiskDev c_disks[FS_MAX_DISKS];
+
+__device__ __forceinline__ float wrap_delta(float d, float L) { return d - L * floorf(d / L + 0.5f); }
+
+__global__ void __launch_bounds__(256)
+    k_solids(float* __restrict__ u, float* __restrict__ v, int ndisk, int nx, int ny, float dx,
+             float dy, float lx, float ly, float width, float dA, float* __restrict__ imp,
+             double* __restrict__ dimp) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y;
+  bool in = i < nx && j < ny;
+  int64_t c = (int64_t)j * nx + i;
+  float pux = i * dx, puy = (j + 0.5f) * dy, pvx = (i + 0.5f) * dx, pvy = j * dy;
+  float uu = 0.f, vv = 0.f;
+  bool loaded = false;
+  float tix = 0.f, tiy = 0.f, tit = 0.f;
+  for (int k = 0; k < ndisk; k++) {
+    const DiskDev d = c_disks[k];
+    float fx = 0.f, fy = 0.f, tq = 0.f;
+    if (in) {
+      float ax = wrap_delta(pux - d.x, lx), ay = wrap_delta(puy - d.y, ly);
+      float bx = wrap_delta(pvx - d.x, lx), by = wrap_delta(pvy - d.y, ly);
+      bool nu_ = ax * ax + ay * ay <= d.reach2, nv_ = bx * bx + by * by <= d.reach2;
+      if ((nu_ || nv_) && !loaded) {
+        uu = u[c];
+        vv = v[c];
+        loaded = true;
+      }
+      if (nu_) {
+        float chi = 0.5f * (1.f - tanhf((sqrtf(ax * ax + ay * ay) - d.r) / width));
+        if (chi >= 1e-6f) {
+          float du = chi * ((d.vx - d.omega * ay) - uu);
+          uu += du;
+          fx = du;
+          tq += -ay * du;
+        }
+      }
+      if (nv_) {
+        float chi = 0.5f * (1.f - tanhf((sqrtf(bx * bx + by * by) - d.r) / width));
+        if (chi >= 1e-6f) {
+          float dv = chi * ((d.vy + d.omega * bx) - vv);
+          vv += dv;
+          fy = dv;
+          tq += bx * dv;
+        }
+      }
+    }
+    tix += fx;
+    tiy += fy;
+    tit += tq;
+    if (dimp) {
+      // block reduction of this disk's impulse, one f64 atomic per block
+      double sx = fx, sy = fy, st = tq;
+      for (int o = 16; o > 0; o >>= 1) {
+        sx += __shfl_xor_sync(0xffffffffu, sx, o);
+        sy += __shfl_xor_sync(0xffffffffu, sy, o);
+        st += __shfl_xor_sync(0xffffffffu, st, o);
+      }
+      if ((threadIdx.x & 31) == 0 && (sx != 0.0 || sy != 0.0 || st != 0.0)) {
+        atomicAdd(dimp + 3 * k + 0, sx * dA);
+        atomicAdd(dimp + 3 * k + 1, sy * dA);
+        atomicAdd(dimp + 3 * k + 2, st * dA);
+      }
+    }
+  }
+  if (!in) return;
+  if (loaded) {
+    u[c] = uu;
+    v[c] = vv;
+  }
+  if (imp) {
+    imp[c] = tix;
+    imp[(int64_t)nx * ny + c] = tiy;
+    imp[2 * (int64_t)nx * ny + c] = tit;
+  }
+}
+
+void launch_solids(Solver* s, float* u, float* v, float dt, bool record_impulse) {
+  (void)dt;
+  const Grid& g = s->g;
+  int nd = (int)s->disks.size();
+  if (nd == 0) return;
+  double width = s->prm.solid_mask_width * g.dxd;
+  DiskDev hd[FS_MAX_DISKS];
+  for (int k = 0; k < nd; k++) {
+    const fs_disk& d = s->disks[k];
+    // chi >= 1e-6 needs (|d| - r)/w <= atanh(1 - 2e-6) ~ 6.9; one cell of margin
+    double reach = d.r + 7.0 * width + g.dxd + g.dyd;
+    hd[k] = {(float)d.x, (float)d.y, (float)d.r, (float)d.vx, (float)d.vy, (float)d.omega,
+             (float)(reach * reach)};
+  }
+  cudaMemcpyToSymbolAsync(c_disks, hd, sizeof(DiskDev) * nd, 0, cudaMemcpyHostToDevice, s->stream);
+  cudaMemsetAsync(s->d_impulse, 0, sizeof(double) * 3 * nd, s->stream);
+  FS_LAUNCH(s, "solids", (double)s->n * (record_impulse ? 28 : 16),
+            k_solids<<<grid2d(g.nx, g.ny, kBlock), kBlock, 0, s->stream>>>(
+                u, v, nd, g.nx, g.ny, g.dx, g.dy, (float)(g.nx * g.dxd), (float)(g.ny * g.dyd),
+                (float)width, (float)(g.dxd * g.dyd), record_impulse ? s->imp : nullptr,
+                s->d_impulse));
+}
+
+}  // namespace fs

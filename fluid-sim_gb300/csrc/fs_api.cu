@@ -1,0 +1,794 @@
+// fs_api.cu -- the C ABI of libfluidcuda (include/fluid.h): solver lifecycle,
+// field I/O, the step orchestration and diagnostics.
+//
+// Reference: the GPUFluidSolver class, src/gpu/solver.js:64-912, and the
+// Multigrid hierarchy of src/gpu/multigrid.js:159-205.
+#include <math.h>
+#include <stdio.h>
+#include <string.h>
+
+#include <algorithm>
+#include <new>
+#include <string>
+
+#include "fs_internal.cuh"
+
+struct fs_solver {
+  fs::Solver s;
+};
+
+namespace fs {
+
+static thread_local std::string g_create_error;
+
+// ------------------------------------------------------------------ errors
+static int fail(Solver* s, int code, const std::string& msg) {
+  if (s) s->err = msg;
+  else g_create_error = msg;
+  return code;
+}
+
+#define CU(S, call)                                                                          \
+  do {                                                                                       \
+    cudaError_t _e = (call);                                                                 \
+    if (_e != cudaSuccess)                                                                   \
+      return fail((S), _e == cudaErrorMemoryAllocation ? FS_ERR_OUT_OF_MEMORY : FS_ERR_CUDA, \
+                  std::string(#call) + ": " + cudaGetErrorString(_e));                       \
+  } while (0)
+
+static int check_launch(Solver* s) {
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return fail(s, FS_ERR_CUDA, std::string("kernel launch: ") + cudaGetErrorString(e));
+  return FS_OK;
+}
+
+// --------------------------------------------------------------- profiling
+void prof_begin(Solver* s, const char* name, double bytes, int* slot, cudaEvent_t* a) {
+  int idx = -1;
+  for (size_t k = 0; k < s->kstats.size(); k++)
+    if (s->kstats[k].name == name) { idx = (int)k; break; }
+  if (idx < 0) {
+    s->kstats.push_back(KernelStat{name, 0, 0.0, 0.0});
+    idx = (int)s->kstats.size() - 1;
+  }
+  s->kstats[idx].launches++;
+  s->kstats[idx].bytes += bytes;
+  cudaEventCreate(a);
+  cudaEventRecord(*a, s->stream);
+  *slot = idx;
+}
+
+void prof_end(Solver* s, int slot, cudaEvent_t a) {
+  cudaEvent_t b;
+  cudaEventCreate(&b);
+  cudaEventRecord(b, s->stream);
+  s->pending.push_back(Solver::Pending{slot, a, b});
+}
+
+static void prof_collect(Solver* s) {
+  cudaStreamSynchronize(s->stream);
+  for (auto& p : s->pending) {
+    float ms = 0;
+    cudaEventElapsedTime(&ms, p.a, p.b);
+    s->kstats[p.stat].ms += ms;
+    cudaEventDestroy(p.a);
+    cudaEventDestroy(p.b);
+  }
+  s->pending.clear();
+}
+
+// ---------------------------------------------------------------- helpers
+static bool is_pow2_multiple(int n, int levels) { return n % (1 << (levels - 1)) == 0; }
+
+template <class T>
+static int dalloc(Solver* s, T** p, size_t count) {
+  *p = nullptr;
+  if (count == 0) return FS_OK;
+  CU(s, cudaMalloc((void**)p, count * sizeof(T)));
+  return FS_OK;
+}
+
+static void free_all(Solver* s) {
+  auto f = [](void* p) { if (p) cudaFree(p); };
+  f(s->u); f(s->v); f(s->wu); f(s->wv); f(s->tu); f(s->tv); f(s->fu); f(s->fv);
+  f(s->p32); f(s->p32b); f(s->div32); f(s->p64); f(s->p64b); f(s->div64);
+  f(s->r32); f(s->e32); f(s->e32b); f(s->scratch);
+  for (size_t l = 1; l < s->lev.size(); l++) { f(s->lev[l].x); f(s->lev[l].x2); f(s->lev[l].rhs); }
+  if (!s->lev.empty()) f(s->lev[0].x2);
+  f(s->red_partials); f(s->red_out); f(s->modes); f(s->imp); f(s->d_impulse);
+  if (s->h_red) cudaFreeHost(s->h_red);
+  if (s->stream) cudaStreamDestroy(s->stream);
+}
+
+static int sync(Solver* s) {
+  CU(s, cudaStreamSynchronize(s->stream));
+  return FS_OK;
+}
+
+// read the reduction words back (synchronises)
+static int read_red(Solver* s, double* a, double* b = nullptr) {
+  CU(s, cudaMemcpyAsync(s->h_red, s->red_out, 2 * sizeof(double), cudaMemcpyDeviceToHost, s->stream));
+  CU(s, cudaStreamSynchronize(s->stream));
+  if (a) *a = s->h_red[0];
+  if (b) *b = s->h_red[1];
+  return FS_OK;
+}
+
+// -------------------------------------------------------------- creation
+static int create(const fs_params* prm, Solver* s) {
+  s->prm = *prm;
+  const fs_params& P = s->prm;
+  if (P.nx < 2 || P.ny < 2) return fail(nullptr, FS_ERR_INVALID_ARGUMENT, "grid must be at least 2x2");
+  if ((int64_t)P.nx * P.ny > (int64_t)1 << 30) return fail(nullptr, FS_ERR_INVALID_ARGUMENT, "grid larger than 2^30 cells");
+  if (!(P.lx > 0) || !(P.ly > 0)) return fail(nullptr, FS_ERR_INVALID_ARGUMENT, "domain size must be positive");
+  if (!(P.nu >= 0)) return fail(nullptr, FS_ERR_INVALID_ARGUMENT, "nu must be >= 0");
+  if (P.confinement != 0)
+    return fail(nullptr, FS_ERR_UNSUPPORTED, "vorticity confinement is not part of this path (it must stay off)");
+  if (P.advection != FS_ADVECT_SEMI_LAGRANGIAN && P.advection != FS_ADVECT_MACCORMACK)
+    return fail(nullptr, FS_ERR_INVALID_ARGUMENT, "unknown advection scheme");
+  if (P.pressure_solver < FS_PRESSURE_JACOBI || P.pressure_solver > FS_PRESSURE_MULTIGRID)
+    return fail(nullptr, FS_ERR_INVALID_ARGUMENT, "unknown pressure solver");
+  if (P.precision != FS_PRECISION_F32 && P.precision != FS_PRECISION_MIXED)
+    return fail(nullptr, FS_ERR_INVALID_ARGUMENT, "unknown precision");
+  if (P.pressure_iterations < 0 || P.max_cycles < 1 || !(P.pressure_tol >= 0))
+    return fail(nullptr, FS_ERR_INVALID_ARGUMENT, "bad iteration settings");
+  if (P.mg_pre_smooth < 0 || P.mg_post_smooth < 0 || P.mg_coarse_sweeps < 0 || P.mg_min_size < 2)
+    return fail(nullptr, FS_ERR_INVALID_ARGUMENT, "bad multigrid settings");
+  if (!(P.solid_mask_width > 0)) return fail(nullptr, FS_ERR_INVALID_ARGUMENT, "solid_mask_width must be > 0");
+
+  s->mixed = P.precision == FS_PRECISION_MIXED;
+  s->odd = (P.nx & 1) || (P.ny & 1);
+  s->n = (int64_t)P.nx * P.ny;
+  Grid& g = s->g;
+  g.nx = P.nx; g.ny = P.ny;
+  g.dxd = P.lx / P.nx; g.dyd = P.ly / P.ny;
+  g.idxd = 1.0 / g.dxd; g.idyd = 1.0 / g.dyd;
+  g.dx = (float)g.dxd; g.dy = (float)g.dyd;
+  g.idx = (float)g.idxd; g.idy = (float)g.idyd;
+
+  // multigrid hierarchy (multigrid.js:177-197): square, n -> n/2 while >= min
+  if (P.pressure_solver == FS_PRESSURE_MULTIGRID) {
+    if (P.nx != P.ny) return fail(nullptr, FS_ERR_INVALID_ARGUMENT, "multigrid needs a square grid");
+    int m = P.nx, count = 0;
+    while (m >= P.mg_min_size) {
+      count++;
+      if (m / 2 < P.mg_min_size) break;
+      if (m & 1) break;
+      m /= 2;
+    }
+    if (count < 1) return fail(nullptr, FS_ERR_INVALID_ARGUMENT, "grid smaller than mg_min_size");
+    if (!is_pow2_multiple(P.nx, count))
+      return fail(nullptr, FS_ERR_INVALID_ARGUMENT, "multigrid needs n divisible by 2^(levels-1)");
+    int n = P.nx;
+    double fine = g.dxd * P.nx;
+    for (int l = 0; l < count; l++, n /= 2) {
+      Level L{};
+      L.n = n;
+      L.dx = (float)(fine / n);
+      L.h2 = L.dx * L.dx;
+      s->lev.push_back(L);
+    }
+  }
+
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+    cudaGetLastError();
+    return fail(nullptr, FS_ERR_NO_DEVICE, "no CUDA device available");
+  }
+  if (P.device < 0 || P.device >= ndev) return fail(nullptr, FS_ERR_INVALID_ARGUMENT, "device ordinal out of range");
+  s->device = P.device;
+  if (cudaSetDevice(s->device) != cudaSuccess) return fail(nullptr, FS_ERR_CUDA, "cudaSetDevice failed");
+
+  CU(nullptr, cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking));
+  const int64_t n = s->n;
+  int rc;
+#define A(ptr, T, cnt) if ((rc = dalloc(s, (T**)&(ptr), (size_t)(cnt))) != FS_OK) return rc
+  if (s->mixed) {
+    A(s->u, double, n); A(s->v, double, n);
+    A(s->p64, double, n); A(s->p64b, double, n); A(s->div64, double, n);
+    A(s->r32, float, n); A(s->e32, float, n); A(s->e32b, float, n);
+  } else {
+    A(s->u, float, n); A(s->v, float, n);
+    A(s->p32, float, n); A(s->p32b, float, n); A(s->div32, float, n);
+  }
+  A(s->wu, float, n); A(s->wv, float, n); A(s->tu, float, n); A(s->tv, float, n);
+  if (P.advection == FS_ADVECT_MACCORMACK) { A(s->fu, float, n); A(s->fv, float, n); }
+  if (!s->lev.empty()) {
+    A(s->scratch, float, n);
+    s->lev[0].x = s->mixed ? s->e32 : s->p32;
+    s->lev[0].rhs = s->mixed ? s->r32 : s->div32;
+    if (s->lev[0].n & 1) A(s->lev[0].x2, float, n);
+    for (size_t l = 1; l < s->lev.size(); l++) {
+      int64_t m = (int64_t)s->lev[l].n * s->lev[l].n;
+      A(s->lev[l].x, float, m); A(s->lev[l].rhs, float, m);
+      if (s->lev[l].n & 1) A(s->lev[l].x2, float, m);
+    }
+  }
+  // reductions: partial buffer for the largest grid launch plus the counter word
+  int64_t blocks = (int64_t)((P.nx + 31) / 32) * ((P.ny + 7) / 8);
+  s->red_cap = (int)std::max<int64_t>(blocks, 4096);
+  A(s->red_partials, double, 2 * (int64_t)s->red_cap + 1);
+  A(s->red_out, double, 4);
+#undef A
+  CU(s, cudaMemsetAsync(s->red_partials, 0, (2 * (size_t)s->red_cap + 1) * sizeof(double), s->stream));
+  CU(s, cudaMallocHost((void**)&s->h_red, 4 * sizeof(double)));
+  // every field starts at zero
+  CU(s, cudaMemsetAsync(s->u, 0, n * (s->mixed ? 8 : 4), s->stream));
+  CU(s, cudaMemsetAsync(s->v, 0, n * (s->mixed ? 8 : 4), s->stream));
+  if (s->mixed) {
+    CU(s, cudaMemsetAsync(s->p64, 0, n * 8, s->stream));
+    CU(s, cudaMemsetAsync(s->div64, 0, n * 8, s->stream));
+  } else {
+    CU(s, cudaMemsetAsync(s->p32, 0, n * 4, s->stream));
+    CU(s, cudaMemsetAsync(s->div32, 0, n * 4, s->stream));
+  }
+  CU(s, cudaStreamSynchronize(s->stream));
+  return FS_OK;
+}
+
+// -------------------------------------------------------- the projection
+// F32 Poisson solve on (p32, div32): `iterations` sweeps or V-cycles
+// (_encodePoisson, solver.js:686-738)
+static void poisson_f32(Solver* s, int iterations) {
+  const fs_params& P = s->prm;
+  const Grid& g = s->g;
+  float h2 = g.dx * g.dx;
+  if (P.pressure_solver == FS_PRESSURE_MULTIGRID) {
+    for (int k = 0; k < iterations; k++) mg_vcycle(s);
+  } else if (P.pressure_solver == FS_PRESSURE_RED_BLACK) {
+    for (int k = 0; k < iterations; k++)
+      for (int colour = 0; colour < 2; colour++) {
+        if (!s->odd) {
+          launch_rb_half(s, s->p32, s->div32, s->p32, h2, colour, g.nx, g.ny);
+        } else {
+          launch_rb_half(s, s->p32, s->div32, s->p32b, h2, colour, g.nx, g.ny);
+          std::swap(s->p32, s->p32b);
+        }
+      }
+  } else {
+    for (int k = 0; k < iterations; k++) {
+      launch_jacobi(s, s->p32, s->div32, s->p32b, h2, g.nx, g.ny);
+      std::swap(s->p32, s->p32b);
+    }
+  }
+  if (!s->lev.empty()) s->lev[0].x = s->p32;
+}
+
+// correction solve of the MIXED mode: e32 from r32 starting at zero
+static void correction_solve(Solver* s, int iterations) {
+  const fs_params& P = s->prm;
+  const Grid& g = s->g;
+  float h2 = g.dx * g.dx;
+  launch_fill(s, s->e32, 0.f, s->n);
+  if (P.pressure_solver == FS_PRESSURE_MULTIGRID) {
+    s->lev[0].x = s->e32;
+    for (int k = 0; k < iterations; k++) mg_vcycle(s);
+  } else if (P.pressure_solver == FS_PRESSURE_RED_BLACK) {
+    for (int k = 0; k < iterations; k++)
+      for (int colour = 0; colour < 2; colour++) {
+        if (!s->odd) {
+          launch_rb_half(s, s->e32, s->r32, s->e32, h2, colour, g.nx, g.ny);
+        } else {
+          launch_rb_half(s, s->e32, s->r32, s->e32b, h2, colour, g.nx, g.ny);
+          std::swap(s->e32, s->e32b);
+        }
+      }
+  } else {
+    for (int k = 0; k < iterations; k++) {
+      launch_jacobi(s, s->e32, s->r32, s->e32b, h2, g.nx, g.ny);
+      std::swap(s->e32, s->e32b);
+    }
+  }
+}
+
+// Pressure solve from the divergence already in div32 / div64.
+// Tolerance loop: each cycle is `pressure_iterations` sweeps or V-cycles; in
+// the MIXED mode each cycle ends with the f64 update p += e, r = d - lap p.
+static int pressure_solve(Solver* s) {
+  const fs_params& P = s->prm;
+  const Grid& g = s->g;
+  int iters = P.pressure_iterations;
+  bool tol = P.pressure_tol > 0;
+  s->stats = fs_step_stats{0, 1, -1.0, -1.0};
+  if (!s->mixed) {
+    if (!P.warm_start) launch_fill(s, s->p32, 0.f, s->n);
+    if (!tol) {
+      poisson_f32(s, iters);
+      s->stats.cycles = iters;
+      return check_launch(s);
+    }
+    double m;
+    launch_absmax_residual32(s, s->p32, s->div32);
+    int rc = read_red(s, &m);
+    if (rc) return rc;
+    s->stats.residual_initial = m;
+    int c = 0;
+    while (!(m <= P.pressure_tol) && c < P.max_cycles && std::isfinite(m)) {
+      poisson_f32(s, iters);
+      launch_absmax_residual32(s, s->p32, s->div32);
+      if ((rc = read_red(s, &m))) return rc;
+      c++;
+    }
+    s->stats.cycles = c;
+    s->stats.residual_max = m;
+    s->stats.converged = m <= P.pressure_tol;
+    if (!std::isfinite(m)) return fail(s, FS_ERR_NONFINITE, "non-finite Poisson residual");
+    if (!s->stats.converged) return fail(s, FS_ERR_NOT_CONVERGED, "pressure tolerance not met within max_cycles");
+    return check_launch(s);
+  }
+  // MIXED: iterative refinement
+  launch_refine_init(s, s->div64, s->p64, s->r32, !P.warm_start);
+  if (!P.warm_start) launch_fill64(s, s->p64, 0.0, s->n);
+  double m = -1.0;
+  int rc;
+  if (tol) {
+    if ((rc = read_red(s, &m))) return rc;
+    s->stats.residual_initial = m;
+  }
+  int c = 0;
+  int cycles_fixed = 1;
+  while (true) {
+    if (tol) {
+      if (m <= P.pressure_tol || !std::isfinite(m) || c >= P.max_cycles) break;
+    } else if (c >= cycles_fixed) {
+      break;
+    }
+    correction_solve(s, iters);
+    launch_refine_update(s, s->p64, s->e32, s->div64, s->p64b, s->r32);
+    std::swap(s->p64, s->p64b);
+    c++;
+    if (tol && (rc = read_red(s, &m))) return rc;
+  }
+  s->stats.cycles = c;
+  if (tol) {
+    s->stats.residual_max = m;
+    s->stats.converged = m <= P.pressure_tol;
+    if (!std::isfinite(m)) return fail(s, FS_ERR_NONFINITE, "non-finite Poisson residual");
+    if (!s->stats.converged) return fail(s, FS_ERR_NOT_CONVERGED, "pressure tolerance not met within max_cycles");
+  }
+  (void)g;
+  return check_launch(s);
+}
+
+// divergence of (wu, wv) -> solve -> state velocity = w - grad p
+static int project_from(Solver* s, const float* wu, const float* wv) {
+  if (s->mixed) launch_divergence<float, double>(s, wu, wv, s->div64);
+  else launch_divergence<float, float>(s, wu, wv, s->div32);
+  int rc = pressure_solve(s);
+  if (s->mixed) launch_subtract_gradient_mixed(s, wu, wv, s->p64, (double*)s->u, (double*)s->v);
+  else launch_subtract_gradient_f32(s, wu, wv, s->p32, (float*)s->u, (float*)s->v);
+  int rc2 = check_launch(s);
+  return rc ? rc : rc2;
+}
+
+// advection of the state into (wu, wv)
+static void advect_into(Solver* s, float dt, float* ou, float* ov) {
+  if (s->prm.advection == FS_ADVECT_MACCORMACK) {
+    if (s->mixed) launch_advect_mc<double>(s, (const double*)s->u, (const double*)s->v, s->fu, s->fv, ou, ov, dt);
+    else launch_advect_mc<float>(s, (const float*)s->u, (const float*)s->v, s->fu, s->fv, ou, ov, dt);
+  } else {
+    if (s->mixed) launch_advect_sl<double>(s, (const double*)s->u, (const double*)s->v, ou, ov, dt);
+    else launch_advect_sl<float>(s, (const float*)s->u, (const float*)s->v, ou, ov, dt);
+  }
+}
+
+// step(dt), solver.js:518-591
+static int step(Solver* s, double dt) {
+  float fdt = (float)dt;
+  advect_into(s, fdt, s->wu, s->wv);
+  float *cu = s->wu, *cv = s->wv;
+  if (s->prm.nu > 0) {
+    launch_diffuse(s, cu, cv, s->tu, s->tv, fdt);
+    cu = s->tu; cv = s->tv;
+  }
+  if (s->n_modes > 0) launch_forcing(s, cu, cv, fdt);
+  if (!s->disks.empty()) launch_solids(s, cu, cv, fdt, false);
+  int rc = project_from(s, cu, cv);
+  s->t += dt;
+  s->steps++;
+  return rc;
+}
+
+// state <-> working f32 copies for the stage-by-stage entry point
+static void state_to_w(Solver* s) {
+  launch_convert(s, s->u, s->mixed, s->wu, 0, s->n);
+  launch_convert(s, s->v, s->mixed, s->wv, 0, s->n);
+}
+static void w_to_state(Solver* s, const float* a, const float* b) {
+  launch_convert(s, a, 0, s->u, s->mixed, s->n);
+  launch_convert(s, b, 0, s->v, s->mixed, s->n);
+}
+
+static int run_stage(Solver* s, int stage, double dt) {
+  float fdt = (float)dt;
+  switch (stage) {
+    case FS_STAGE_ADVECT:
+      advect_into(s, fdt, s->tu, s->tv);
+      w_to_state(s, s->tu, s->tv);
+      break;
+    case FS_STAGE_DIFFUSE:
+      state_to_w(s);
+      launch_diffuse(s, s->wu, s->wv, s->tu, s->tv, fdt);
+      w_to_state(s, s->tu, s->tv);
+      break;
+    case FS_STAGE_FORCING:
+      if (s->n_modes == 0) break;
+      state_to_w(s);
+      launch_forcing(s, s->wu, s->wv, fdt);
+      w_to_state(s, s->wu, s->wv);
+      break;
+    case FS_STAGE_SOLID:
+      if (s->disks.empty()) break;
+      state_to_w(s);
+      launch_solids(s, s->wu, s->wv, fdt, s->imp != nullptr);
+      w_to_state(s, s->wu, s->wv);
+      break;
+    case FS_STAGE_DIVERGENCE:
+      if (s->mixed) launch_divergence<double, double>(s, (const double*)s->u, (const double*)s->v, s->div64);
+      else launch_divergence<float, float>(s, (const float*)s->u, (const float*)s->v, s->div32);
+      break;
+    case FS_STAGE_PRESSURE: {
+      int rc = pressure_solve(s);
+      if (rc) return rc;
+      break;
+    }
+    case FS_STAGE_SUBTRACT_GRADIENT:
+      state_to_w(s);
+      if (s->mixed) launch_subtract_gradient_mixed(s, s->wu, s->wv, s->p64, (double*)s->u, (double*)s->v);
+      else launch_subtract_gradient_f32(s, s->wu, s->wv, s->p32, (float*)s->u, (float*)s->v);
+      break;
+    case FS_STAGE_PROJECT: {
+      state_to_w(s);
+      int rc = project_from(s, s->wu, s->wv);
+      if (rc) return rc;
+      break;
+    }
+    default:
+      return fail(s, FS_ERR_INVALID_ARGUMENT, "unknown stage");
+  }
+  return check_launch(s);
+}
+
+}  // namespace fs
+
+using namespace fs;
+
+// =================================================================== C ABI
+extern "C" {
+
+FS_API void fs_params_default(fs_params* p) {
+  if (!p) return;
+  memset(p, 0, sizeof(*p));
+  p->nx = 256; p->ny = 256;
+  p->lx = 2 * M_PI; p->ly = 2 * M_PI;
+  p->nu = 0.0;
+  p->confinement = 0.0;
+  p->advection = FS_ADVECT_MACCORMACK;
+  p->solid_mask_width = 1.5;
+  p->pressure_solver = FS_PRESSURE_JACOBI;
+  p->pressure_iterations = 40;
+  p->precision = FS_PRECISION_F32;
+  p->pressure_tol = 0.0;
+  p->max_cycles = 50;
+  p->mg_pre_smooth = 2;
+  p->mg_post_smooth = 2;
+  p->mg_coarse_sweeps = 40;
+  p->mg_min_size = 8;
+  p->warm_start = 0;
+  p->device = 0;
+}
+
+FS_API int fs_create(const fs_params* params, fs_solver** out) {
+  if (!out) return fail(nullptr, FS_ERR_INVALID_ARGUMENT, "out is NULL");
+  *out = nullptr;
+  if (!params) return fail(nullptr, FS_ERR_INVALID_ARGUMENT, "params is NULL");
+  fs_solver* h = new (std::nothrow) fs_solver();
+  if (!h) return fail(nullptr, FS_ERR_OUT_OF_MEMORY, "host allocation failed");
+  int rc = create(params, &h->s);
+  if (rc != FS_OK) {
+    if (!h->s.err.empty()) g_create_error = h->s.err;
+    free_all(&h->s);
+    delete h;
+    return rc;
+  }
+  *out = h;
+  return FS_OK;
+}
+
+FS_API void fs_destroy(fs_solver* h) {
+  if (!h) return;
+  cudaSetDevice(h->s.device);
+  cudaStreamSynchronize(h->s.stream);
+  for (auto& p : h->s.pending) { cudaEventDestroy(p.a); cudaEventDestroy(p.b); }
+  free_all(&h->s);
+  delete h;
+}
+
+FS_API const char* fs_last_error(const fs_solver* h) {
+  if (!h) return g_create_error.c_str();
+  return h->s.err.c_str();
+}
+
+FS_API const char* fs_status_string(int st) {
+  switch (st) {
+    case FS_OK: return "ok";
+    case FS_ERR_INVALID_ARGUMENT: return "invalid argument";
+    case FS_ERR_CUDA: return "CUDA error";
+    case FS_ERR_OUT_OF_MEMORY: return "out of device memory";
+    case FS_ERR_NOT_CONVERGED: return "pressure tolerance not met";
+    case FS_ERR_NONFINITE: return "non-finite residual";
+    case FS_ERR_UNSUPPORTED: return "unsupported";
+    case FS_ERR_NO_DEVICE: return "no CUDA device";
+    default: return "unknown status";
+  }
+}
+
+FS_API int fs_get_params(const fs_solver* h, fs_params* out) {
+  if (!h || !out) return FS_ERR_INVALID_ARGUMENT;
+  *out = h->s.prm;
+  return FS_OK;
+}
+
+#define SOLVER(h)                                                          \
+  if (!h) return fail(nullptr, FS_ERR_INVALID_ARGUMENT, "solver is NULL"); \
+  Solver* s = &h->s;                                                       \
+  if (cudaSetDevice(s->device) != cudaSuccess) return fail(s, FS_ERR_CUDA, "cudaSetDevice failed")
+
+static int upload_array(Solver* s, const void* src, int dtype, void* dst, bool dst_f64) {
+  if (dtype != FS_DTYPE_F32 && dtype != FS_DTYPE_F64) return fail(s, FS_ERR_INVALID_ARGUMENT, "unknown dtype");
+  size_t esz = dtype == FS_DTYPE_F64 ? 8 : 4;
+  bool same = (dtype == FS_DTYPE_F64) == dst_f64;
+  if (same) {
+    CU(s, cudaMemcpyAsync(dst, src, s->n * esz, cudaMemcpyHostToDevice, s->stream));
+  } else {
+    // stage through the f32 work buffer tu/tv area: tu,tv are contiguous n floats each
+    void* stage = nullptr;
+    CU(s, cudaMallocAsync(&stage, s->n * esz, s->stream));
+    CU(s, cudaMemcpyAsync(stage, src, s->n * esz, cudaMemcpyHostToDevice, s->stream));
+    launch_convert(s, stage, dtype == FS_DTYPE_F64, dst, dst_f64, s->n);
+    CU(s, cudaFreeAsync(stage, s->stream));
+  }
+  return check_launch(s);
+}
+
+static int download_array(Solver* s, const void* src, bool src_f64, void* dst, int dtype) {
+  if (dtype != FS_DTYPE_F32 && dtype != FS_DTYPE_F64) return fail(s, FS_ERR_INVALID_ARGUMENT, "unknown dtype");
+  size_t esz = dtype == FS_DTYPE_F64 ? 8 : 4;
+  bool same = (dtype == FS_DTYPE_F64) == src_f64;
+  if (same) {
+    CU(s, cudaMemcpyAsync(dst, src, s->n * esz, cudaMemcpyDeviceToHost, s->stream));
+  } else {
+    void* stage = nullptr;
+    CU(s, cudaMallocAsync(&stage, s->n * esz, s->stream));
+    launch_convert(s, src, src_f64, stage, dtype == FS_DTYPE_F64, s->n);
+    CU(s, cudaMemcpyAsync(dst, stage, s->n * esz, cudaMemcpyDeviceToHost, s->stream));
+    CU(s, cudaFreeAsync(stage, s->stream));
+  }
+  CU(s, cudaStreamSynchronize(s->stream));
+  return check_launch(s);
+}
+
+FS_API int fs_upload_velocity(fs_solver* h, const void* u, const void* v, int dtype) {
+  SOLVER(h);
+  if (!u || !v) return fail(s, FS_ERR_INVALID_ARGUMENT, "u or v is NULL");
+  int rc = upload_array(s, u, dtype, s->u, s->mixed);
+  if (rc) return rc;
+  return upload_array(s, v, dtype, s->v, s->mixed);
+}
+
+FS_API int fs_read_velocity(fs_solver* h, void* u, void* v, int dtype) {
+  SOLVER(h);
+  if (!u || !v) return fail(s, FS_ERR_INVALID_ARGUMENT, "u or v is NULL");
+  int rc = download_array(s, s->u, s->mixed, u, dtype);
+  if (rc) return rc;
+  return download_array(s, s->v, s->mixed, v, dtype);
+}
+
+FS_API int fs_read_field(fs_solver* h, int field, void* out, int dtype) {
+  SOLVER(h);
+  if (!out) return fail(s, FS_ERR_INVALID_ARGUMENT, "out is NULL");
+  switch (field) {
+    case FS_FIELD_U: return download_array(s, s->u, s->mixed, out, dtype);
+    case FS_FIELD_V: return download_array(s, s->v, s->mixed, out, dtype);
+    case FS_FIELD_PRESSURE:
+      return s->mixed ? download_array(s, s->p64, true, out, dtype) : download_array(s, s->p32, false, out, dtype);
+    case FS_FIELD_DIVERGENCE:
+      return s->mixed ? download_array(s, s->div64, true, out, dtype) : download_array(s, s->div32, false, out, dtype);
+    case FS_FIELD_IMPULSE_X:
+    case FS_FIELD_IMPULSE_Y:
+    case FS_FIELD_IMPULSE_TORQUE:
+      if (!s->imp) return fail(s, FS_ERR_INVALID_ARGUMENT, "no solid attached");
+      return download_array(s, s->imp + (int64_t)(field - FS_FIELD_IMPULSE_X) * s->n, false, out, dtype);
+    default:
+      return fail(s, FS_ERR_INVALID_ARGUMENT, "unknown field");
+  }
+}
+
+FS_API int fs_upload_field(fs_solver* h, int field, const void* data, int dtype) {
+  SOLVER(h);
+  if (!data) return fail(s, FS_ERR_INVALID_ARGUMENT, "data is NULL");
+  if (field != FS_FIELD_PRESSURE) return fail(s, FS_ERR_INVALID_ARGUMENT, "only the pressure can be uploaded");
+  return s->mixed ? upload_array(s, data, dtype, s->p64, true) : upload_array(s, data, dtype, s->p32, false);
+}
+
+FS_API int fs_set_forcing(fs_solver* h, const fs_mode* modes, int count, double amplitude, double drag,
+                          double phase_drift) {
+  SOLVER(h);
+  if (count < 0 || (count > 0 && !modes)) return fail(s, FS_ERR_INVALID_ARGUMENT, "bad mode list");
+  if (count > 4096) return fail(s, FS_ERR_INVALID_ARGUMENT, "at most 4096 forcing modes");
+  CU(s, cudaStreamSynchronize(s->stream));
+  if (s->modes) { cudaFree(s->modes); s->modes = nullptr; }
+  s->n_modes = 0;
+  if (count == 0) return FS_OK;
+  std::vector<float> hm(3 * (size_t)count);
+  for (int k = 0; k < count; k++) {
+    hm[3 * k] = (float)modes[k].kx; hm[3 * k + 1] = (float)modes[k].ky; hm[3 * k + 2] = (float)modes[k].phase;
+  }
+  CU(s, cudaMalloc((void**)&s->modes, hm.size() * sizeof(float)));
+  CU(s, cudaMemcpy(s->modes, hm.data(), hm.size() * sizeof(float), cudaMemcpyHostToDevice));
+  s->n_modes = count;
+  s->amp = amplitude; s->drag = drag; s->drift = phase_drift;
+  return FS_OK;
+}
+
+FS_API int fs_set_solids(fs_solver* h, const fs_disk* disks, int count) {
+  SOLVER(h);
+  if (count < 0 || (count > 0 && !disks)) return fail(s, FS_ERR_INVALID_ARGUMENT, "bad disk list");
+  if (count > 64) return fail(s, FS_ERR_INVALID_ARGUMENT, "at most 64 disks");
+  for (int k = 0; k < count; k++)
+    if (!(disks[k].r > 0) || !std::isfinite(disks[k].x) || !std::isfinite(disks[k].y))
+      return fail(s, FS_ERR_INVALID_ARGUMENT, "disk needs a finite centre and r > 0");
+  s->disks.assign(disks, disks + count);
+  if (count > 0) {
+    if (!s->imp) {
+      CU(s, cudaMalloc((void**)&s->imp, 3 * (size_t)s->n * sizeof(float)));
+      CU(s, cudaMemsetAsync(s->imp, 0, 3 * (size_t)s->n * sizeof(float), s->stream));
+    }
+    if (s->imp_cap < count) {
+      if (s->d_impulse) cudaFree(s->d_impulse);
+      CU(s, cudaMalloc((void**)&s->d_impulse, 3 * 64 * sizeof(double)));
+      CU(s, cudaMemsetAsync(s->d_impulse, 0, 3 * 64 * sizeof(double), s->stream));
+      s->imp_cap = 64;
+    }
+  }
+  return FS_OK;
+}
+
+FS_API int fs_solid_impulse(fs_solver* h, double* out, int count) {
+  SOLVER(h);
+  if (!out || count < (int)s->disks.size()) return fail(s, FS_ERR_INVALID_ARGUMENT, "out too small");
+  if (s->disks.empty()) return FS_OK;
+  CU(s, cudaMemcpyAsync(out, s->d_impulse, 3 * s->disks.size() * sizeof(double), cudaMemcpyDeviceToHost, s->stream));
+  CU(s, cudaStreamSynchronize(s->stream));
+  return FS_OK;
+}
+
+FS_API int fs_step(fs_solver* h, double dt) {
+  SOLVER(h);
+  if (!std::isfinite(dt)) return fail(s, FS_ERR_INVALID_ARGUMENT, "dt must be finite");
+  return step(s, dt);
+}
+
+FS_API int fs_advance(fs_solver* h, double dt, int nsteps) {
+  SOLVER(h);
+  if (!std::isfinite(dt) || nsteps < 0) return fail(s, FS_ERR_INVALID_ARGUMENT, "bad dt or nsteps");
+  for (int k = 0; k < nsteps; k++) {
+    int rc = step(s, dt);
+    if (rc) return rc;
+  }
+  return FS_OK;
+}
+
+FS_API int fs_sync(fs_solver* h) {
+  SOLVER(h);
+  return sync(s);
+}
+
+FS_API int fs_last_stats(fs_solver* h, fs_step_stats* out) {
+  SOLVER(h);
+  if (!out) return fail(s, FS_ERR_INVALID_ARGUMENT, "out is NULL");
+  int rc = sync(s);
+  *out = s->stats;
+  return rc;
+}
+
+FS_API int fs_get_time(const fs_solver* h, double* t, int64_t* steps) {
+  if (!h) return FS_ERR_INVALID_ARGUMENT;
+  if (t) *t = h->s.t;
+  if (steps) *steps = h->s.steps;
+  return FS_OK;
+}
+
+FS_API int fs_run_stage(fs_solver* h, int stage, double dt) {
+  SOLVER(h);
+  return run_stage(s, stage, dt);
+}
+
+FS_API int fs_max_divergence(fs_solver* h, double* out) {
+  SOLVER(h);
+  if (!out) return fail(s, FS_ERR_INVALID_ARGUMENT, "out is NULL");
+  if (s->mixed) {
+    launch_divergence<double, double>(s, (const double*)s->u, (const double*)s->v, s->div64);
+    launch_absmax<double>(s, s->div64, s->n, s->red_out);
+  } else {
+    launch_divergence<float, float>(s, (const float*)s->u, (const float*)s->v, s->div32);
+    launch_absmax<float>(s, s->div32, s->n, s->red_out);
+  }
+  int rc = check_launch(s);
+  if (rc) return rc;
+  return read_red(s, out);
+}
+
+FS_API int fs_poisson_residual_after(fs_solver* h, int iterations, double dt, double* out) {
+  SOLVER(h);
+  (void)dt;
+  if (!out || iterations < 0) return fail(s, FS_ERR_INVALID_ARGUMENT, "bad arguments");
+  if (s->mixed) return fail(s, FS_ERR_UNSUPPORTED, "poisson_residual_after measures the F32 solver");
+  launch_divergence<float, float>(s, (const float*)s->u, (const float*)s->v, s->div32);
+  launch_fill(s, s->p32, 0.f, s->n);
+  poisson_f32(s, iterations);
+  launch_poisson_norms(s, s->p32, s->div32, s->g.dx * s->g.dx, s->g.dxd * s->g.dxd);
+  int rc = check_launch(s);
+  if (rc) return rc;
+  double num, den;
+  if ((rc = read_red(s, &num, &den))) return rc;
+  double sd = sqrt(den);
+  *out = sqrt(num) / (sd == 0 ? 1 : sd);
+  return FS_OK;
+}
+
+FS_API int fs_time_steps(fs_solver* h, double dt, int nsteps, double* elapsed_ms) {
+  SOLVER(h);
+  if (!elapsed_ms || nsteps < 0) return fail(s, FS_ERR_INVALID_ARGUMENT, "bad arguments");
+  cudaEvent_t a, b;
+  CU(s, cudaEventCreate(&a));
+  CU(s, cudaEventCreate(&b));
+  CU(s, cudaStreamSynchronize(s->stream));
+  CU(s, cudaEventRecord(a, s->stream));
+  int rc = FS_OK;
+  for (int k = 0; k < nsteps && rc == FS_OK; k++) rc = step(s, dt);
+  CU(s, cudaEventRecord(b, s->stream));
+  CU(s, cudaEventSynchronize(b));
+  float ms = 0;
+  cudaEventElapsedTime(&ms, a, b);
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  *elapsed_ms = ms;
+  return rc;
+}
+
+FS_API int fs_profile_step(fs_solver* h, double dt, int nsteps, fs_kernel_time* out, int cap, int* count) {
+  SOLVER(h);
+  if (nsteps < 0 || cap < 0 || (cap > 0 && !out)) return fail(s, FS_ERR_INVALID_ARGUMENT, "bad arguments");
+  CU(s, cudaStreamSynchronize(s->stream));
+  s->kstats.clear();
+  s->profiling = true;
+  int rc = FS_OK;
+  for (int k = 0; k < nsteps && rc == FS_OK; k++) rc = step(s, dt);
+  s->profiling = false;
+  prof_collect(s);
+  int m = std::min<int>(cap, (int)s->kstats.size());
+  for (int k = 0; k < m; k++) {
+    memset(&out[k], 0, sizeof(fs_kernel_time));
+    strncpy(out[k].name, s->kstats[k].name.c_str(), sizeof(out[k].name) - 1);
+    out[k].launches = s->kstats[k].launches;
+    out[k].total_ms = s->kstats[k].ms;
+    out[k].bytes = s->kstats[k].bytes;
+  }
+  if (count) *count = (int)s->kstats.size();
+  return rc;
+}
+
+FS_API int64_t fs_launch_count(const fs_solver* h) { return h ? h->s.launches : 0; }
+
+FS_API void* fs_host_alloc(size_t bytes) {
+  void* p = nullptr;
+  if (cudaMallocHost(&p, bytes) != cudaSuccess) return nullptr;
+  return p;
+}
+
+FS_API void fs_host_free(void* p) {
+  if (p) cudaFreeHost(p);
+}
+
+}  // extern "C"

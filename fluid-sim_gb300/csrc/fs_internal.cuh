@@ -1,0 +1,173 @@
+// fs_internal.cuh -- shared definitions of libfluidcuda (GB300, sm_103a).
+//
+// Data layout in HBM: every field is a planar row-major nx*ny array, i fastest
+// (the reference packs u and v into one rgba32float texel per cell,
+// src/gpu/shaders.js:4-14, and uses only .x of its scalar textures; planar
+// arrays move a quarter of the bytes for p, div and the multigrid levels).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/fluid.h"
+
+namespace fs {
+
+// Grid spacing as every kernel sees it.  dx/dy are the f32 values the
+// reference uploads in its uniform block (src/gpu/solver.js:249-256); the
+// reciprocals replace its per-sample divisions.
+struct Grid {
+  int nx, ny;
+  float dx, dy, idx, idy;
+  double dxd, dyd, idxd, idyd;
+};
+
+// One multigrid level (src/gpu/multigrid.js:177-197).  Level 0 aliases the
+// solver's pressure (or correction) and right-hand side.
+struct Level {
+  int n;
+  float dx;    // (dx * nx) / n, rounded to f32 as multigrid.js:186,220 does
+  float h2;    // dx * dx
+  float* x;    // solution / correction, in place
+  float* x2;   // second buffer for odd n, where red-black needs ping-pong
+  float* rhs;
+};
+
+struct KernelStat {
+  std::string name;
+  int launches = 0;
+  double ms = 0;
+  double bytes = 0;
+};
+
+struct Solver {
+  fs_params prm{};
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  Grid g{};
+  int64_t n = 0;
+  bool mixed = false;
+  bool odd = false;  // nx or ny odd: red-black ping-pong semantics
+
+  // velocity state: float (F32) or double (MIXED)
+  void* u = nullptr;
+  void* v = nullptr;
+  // working velocity of the step before projection (f32 in both modes)
+  float* wu = nullptr;
+  float* wv = nullptr;
+  float* tu = nullptr;  // ping-pong partner of wu/wv
+  float* tv = nullptr;
+  float* fu = nullptr;  // MacCormack forward field
+  float* fv = nullptr;
+
+  // pressure: F32 -> p32/div32 are the Poisson unknown/rhs.
+  //           MIXED -> p64/div64 hold the f64 pressure and divergence, r32/e32
+  //           the f32 residual and correction of one refinement cycle.
+  float* p32 = nullptr;
+  float* p32b = nullptr;  // ping-pong (Jacobi, odd red-black)
+  float* div32 = nullptr;
+  double* p64 = nullptr;
+  double* p64b = nullptr;
+  double* div64 = nullptr;
+  float* r32 = nullptr;
+  float* e32 = nullptr;
+  float* e32b = nullptr;
+  float* scratch = nullptr;  // n floats: multigrid residual before restriction
+
+  std::vector<Level> lev;
+
+  // reductions: per-block partials and the final words
+  double* red_partials = nullptr;  // 2 * red_cap doubles
+  int red_cap = 0;
+  double* red_out = nullptr;       // device: [0] max, [1] sum a, [2] sum b
+  double* h_red = nullptr;         // pinned host copy
+
+  // forcing (solver.js:370-385)
+  float* modes = nullptr;  // kx, ky, phase triplets
+  int n_modes = 0;
+  double amp = 0, drag = 0, drift = 0;
+
+  // solids
+  std::vector<fs_disk> disks;
+  float* imp = nullptr;         // 3 * n impulse field (x, y, torque)
+  double* d_impulse = nullptr;  // 3 * disks
+  int imp_cap = 0;
+
+  double t = 0;
+  int64_t steps = 0;
+  fs_step_stats stats{0, 1, -1.0, -1.0};
+  std::string err;
+  int64_t launches = 0;
+
+  // profiling: an event pair around every launch when enabled
+  bool profiling = false;
+  struct Pending {
+    int stat;
+    cudaEvent_t a, b;
+  };
+  std::vector<Pending> pending;
+  std::vector<KernelStat> kstats;
+};
+
+// ----------------------------------------------------------------- launching
+void prof_begin(Solver* s, const char* name, double bytes, int* slot, cudaEvent_t* a);
+void prof_end(Solver* s, int slot, cudaEvent_t a);
+
+// Wrap one kernel launch: counts it and, when profiling, brackets it with
+// events on the solver's stream.
+#define FS_LAUNCH(S, NAME, BYTES, ...)                                   \
+  do {                                                                   \
+    int _slot = -1;                                                      \
+    cudaEvent_t _ev = nullptr;                                           \
+    if ((S)->profiling) fs::prof_begin((S), (NAME), (BYTES), &_slot, &_ev); \
+    __VA_ARGS__;                                                         \
+    (S)->launches++;                                                     \
+    if ((S)->profiling) fs::prof_end((S), _slot, _ev);                   \
+  } while (0)
+
+inline dim3 grid2d(int nx, int ny, dim3 b) { return dim3((nx + b.x - 1) / b.x, (ny + b.y - 1) / b.y); }
+
+// --------------------------------------------------------- kernel launchers
+// fs_advect.cu
+template <class TV>
+void launch_advect_sl(Solver* s, const TV* u, const TV* v, float* ou, float* ov, float dt);
+template <class TV>
+void launch_advect_mc(Solver* s, const TV* u, const TV* v, float* fu, float* fv, float* ou,
+                      float* ov, float dt);
+void launch_diffuse(Solver* s, const float* u, const float* v, float* ou, float* ov, float dt);
+void launch_forcing(Solver* s, float* u, float* v, float dt);
+void launch_solids(Solver* s, float* u, float* v, float dt, bool record_impulse);
+
+// fs_pressure.cu
+template <class TV, class TD>
+void launch_divergence(Solver* s, const TV* u, const TV* v, TD* d);
+void launch_subtract_gradient_f32(Solver* s, const float* wu, const float* wv, const float* p,
+                                  float* ou, float* ov);
+void launch_subtract_gradient_mixed(Solver* s, const float* wu, const float* wv, const double* p,
+                                    double* ou, double* ov);
+void launch_jacobi(Solver* s, const float* p, const float* d, float* out, float h2, int nx, int ny);
+void launch_rb_half(Solver* s, const float* src, const float* d, float* dst, float h2, int colour,
+                    int nx, int ny);
+void launch_residual(Solver* s, const float* x, const float* rhs, float* out, float h2, int n);
+void launch_restrict(Solver* s, const float* fine, float* coarse, int nc);
+void launch_prolong_add(Solver* s, const float* coarse, float* fine, int nf);
+void launch_fill(Solver* s, float* x, float value, int64_t n);
+void launch_fill64(Solver* s, double* x, double value, int64_t n);
+// mixed-precision refinement
+void launch_refine_init(Solver* s, const double* d, const double* p, float* r32, bool zero_p);
+void launch_refine_update(Solver* s, const double* p_in, const float* e, const double* d,
+                          double* p_out, float* r32);
+// reductions (results land in s->red_out)
+template <class T>
+void launch_absmax(Solver* s, const T* x, int64_t n, double* out_word);
+void launch_absmax_residual32(Solver* s, const float* p, const float* d);
+void launch_poisson_norms(Solver* s, const float* p, const float* d, float h2f, double h2);
+void launch_convert(Solver* s, const void* src, int src_f64, void* dst, int dst_f64, int64_t n);
+
+// multigrid driver (fs_pressure.cu)
+void mg_vcycle(Solver* s);
+
+}  // namespace fs

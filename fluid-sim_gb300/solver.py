@@ -1,0 +1,241 @@
+"""Host-side mirror of fluid-sim's GPU backend API (src/gpu/solver.js).
+
+``GPUFluidSolver`` keeps the reference class's constructor options, method
+names and argument meaning (camelCase aliases included), and drives the CUDA
+library through its C ABI.  Reads return numpy arrays; every GPU failure
+raises ``FluidError`` -- there is no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import math
+from typing import Iterable, Sequence
+
+import numpy as np
+
+from . import _lib as L
+
+ADVECTION = {"semi-lagrangian": 0, "maccormack": 1}
+PRESSURE = {"jacobi": 0, "red-black": 1, "multigrid": 2}
+PRECISION = {"f32": 0, "mixed": 1}
+FIELDS = {"u": 0, "v": 1, "pressure": 2, "divergence": 3, "impulse_x": 4, "impulse_y": 5, "impulse_torque": 6}
+STAGES = {"advect": 0, "diffuse": 1, "forcing": 2, "solid": 3, "divergence": 4, "pressure": 5,
+          "subtract_gradient": 6, "project": 7}
+
+
+def _ptr(a: np.ndarray):
+    return C.c_void_p(a.ctypes.data)
+
+
+class GPUFluidSolver:
+    """new GPUFluidSolver(device, {n, nx, ny, lx, ly, nu, confinement, advection,
+    solidMaskWidth, pressureSolver, pressureIterations}) -- src/gpu/solver.js:65-98.
+
+    Extra options: ``precision`` ("f32" | "mixed"), ``pressure_tol`` (> 0 runs
+    cycles until max|div u| <= tol), ``max_cycles``, ``warm_start``, the
+    multigrid sweep counts and ``device`` (CUDA ordinal).
+    """
+
+    def __init__(self, n: int = 256, nx: int | None = None, ny: int | None = None, lx: float = 2 * math.pi,
+                 ly: float = 2 * math.pi, nu: float = 0.0, confinement: float = 0.0,
+                 advection: str = "maccormack", solid_mask_width: float = 1.5,
+                 pressure_solver: str = "jacobi", pressure_iterations: int = 40, precision: str = "f32",
+                 pressure_tol: float = 0.0, max_cycles: int = 50, mg_pre_smooth: int = 2,
+                 mg_post_smooth: int = 2, mg_coarse_sweeps: int = 40, mg_min_size: int = 8,
+                 warm_start: bool = False, device: int = 0, **camel):
+        # accept the reference's camelCase option names too
+        solid_mask_width = camel.pop("solidMaskWidth", solid_mask_width)
+        pressure_solver = camel.pop("pressureSolver", pressure_solver)
+        pressure_iterations = camel.pop("pressureIterations", pressure_iterations)
+        if camel:
+            raise TypeError(f"unknown options {sorted(camel)}")
+        lib = L.load()
+        p = L.Params()
+        lib.fs_params_default(C.byref(p))
+        p.nx = nx or n
+        p.ny = ny or n
+        p.lx, p.ly, p.nu, p.confinement = lx, ly, nu, confinement
+        # unknown names are rejected here (the reference silently defaults)
+        if advection not in ADVECTION:
+            raise L.FluidError(1, f"unknown advection scheme {advection!r}")
+        if pressure_solver not in PRESSURE:
+            raise L.FluidError(1, f"unknown pressure solver {pressure_solver!r}")
+        if precision not in PRECISION:
+            raise L.FluidError(1, f"unknown precision {precision!r}")
+        p.advection = ADVECTION[advection]
+        p.solid_mask_width = solid_mask_width
+        p.pressure_solver = PRESSURE[pressure_solver]
+        p.pressure_iterations = pressure_iterations
+        p.precision = PRECISION[precision]
+        p.pressure_tol = pressure_tol
+        p.max_cycles = max_cycles
+        p.mg_pre_smooth, p.mg_post_smooth = mg_pre_smooth, mg_post_smooth
+        p.mg_coarse_sweeps, p.mg_min_size = mg_coarse_sweeps, mg_min_size
+        p.warm_start = int(bool(warm_start))
+        p.device = device
+        h = C.c_void_p()
+        L.check(lib.fs_create(C.byref(p), C.byref(h)), None)
+        self._h = h
+        self._lib = lib
+        self.params = p
+        self.nx, self.ny = p.nx, p.ny
+        self.n = p.nx * p.ny
+        self.dx, self.dy = lx / p.nx, ly / p.ny
+        self.nu = nu
+        self.advection = advection
+        self.pressure_solver = pressure_solver
+        self.pressure_iterations = pressure_iterations
+        self.precision = precision
+        self.solid = None
+
+    # ------------------------------------------------------------ lifecycle
+    def destroy(self) -> None:
+        """destroy() (solver.js:898-911)"""
+        if getattr(self, "_h", None):
+            self._lib.fs_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.destroy()
+        except Exception:
+            pass
+
+    def _chk(self, st: int) -> None:
+        L.check(st, self._h)
+
+    # ---------------------------------------------------------------- upload
+    def upload_velocity(self, u: np.ndarray, v: np.ndarray) -> None:
+        """uploadVelocity(u, v) (solver.js:301-315), f64 or f32 arrays of n*n."""
+        dt = np.float64 if np.asarray(u).dtype == np.float64 else np.float32
+        u = np.ascontiguousarray(u, dtype=dt).reshape(-1)
+        v = np.ascontiguousarray(v, dtype=dt).reshape(-1)
+        if u.size != self.n or v.size != self.n:
+            raise L.FluidError(1, f"expected {self.n} values per component")
+        self._chk(self._lib.fs_upload_velocity(self._h, _ptr(u), _ptr(v), 1 if dt is np.float64 else 0))
+
+    uploadVelocity = upload_velocity
+
+    def read_velocity(self, dtype=np.float64):
+        """readVelocity() (solver.js:356-362) -> (u, v)"""
+        u = np.empty(self.n, dtype=dtype)
+        v = np.empty(self.n, dtype=dtype)
+        self._chk(self._lib.fs_read_velocity(self._h, _ptr(u), _ptr(v), 1 if dtype == np.float64 else 0))
+        return u, v
+
+    readVelocity = read_velocity
+
+    def read_field(self, field: str, dtype=np.float64) -> np.ndarray:
+        """readTexture for pressure / divergence / impulse fields (solver.js:336-353)"""
+        out = np.empty(self.n, dtype=dtype)
+        self._chk(self._lib.fs_read_field(self._h, FIELDS[field], _ptr(out), 1 if dtype == np.float64 else 0))
+        return out
+
+    def upload_pressure(self, p: np.ndarray) -> None:
+        p = np.ascontiguousarray(p, dtype=np.float64).reshape(-1)
+        self._chk(self._lib.fs_upload_field(self._h, FIELDS["pressure"], _ptr(p), 1))
+
+    # ------------------------------------------------------- forces, solids
+    def set_forcing(self, modes: Sequence | None, amplitude: float = 1.0, drag: float = 0.0,
+                    phase_drift: float = 0.3) -> None:
+        """setForcing(modes, {amplitude, drag, phaseDrift}) (solver.js:370-385)"""
+        modes = list(modes or [])
+        arr = (L.Mode * max(1, len(modes)))()
+        for k, m in enumerate(modes):
+            if isinstance(m, dict):
+                arr[k] = L.Mode(m["kx"], m["ky"], m["phase"])
+            else:
+                arr[k] = L.Mode(*m)
+        self._chk(self._lib.fs_set_forcing(self._h, arr, len(modes), amplitude, drag, phase_drift))
+
+    setForcing = set_forcing
+
+    def set_solids(self, disks: Iterable) -> None:
+        """setSolid(disk) generalised to several disks (solver.js:425-438)"""
+        disks = list(disks or [])
+        arr = (L.Disk * max(1, len(disks)))()
+        for k, d in enumerate(disks):
+            if isinstance(d, dict):
+                arr[k] = L.Disk(d["x"], d["y"], d["r"], d.get("vx", 0.0), d.get("vy", 0.0), d.get("omega", 0.0))
+            else:
+                arr[k] = L.Disk(*d)
+        self._chk(self._lib.fs_set_solids(self._h, arr, len(disks)))
+        self.solid = disks[0] if disks else None
+
+    def set_solid(self, disk) -> None:
+        self.set_solids([disk] if disk is not None else [])
+
+    setSolid = set_solid
+
+    def solid_impulse(self) -> np.ndarray:
+        """per-disk (fx, fy, torque) impulse of the last coupling pass, summed on the device"""
+        k = len(self.solid and [self.solid] or [])
+        out = np.zeros(3 * 64)
+        self._chk(self._lib.fs_solid_impulse(self._h, out.ctypes.data_as(C.POINTER(C.c_double)), 64))
+        return out.reshape(64, 3)
+
+    # ------------------------------------------------------------------ step
+    def step(self, dt: float) -> None:
+        """step(dt) (solver.js:518-591)"""
+        self._chk(self._lib.fs_step(self._h, dt))
+
+    def advance(self, dt: float, nsteps: int) -> None:
+        self._chk(self._lib.fs_advance(self._h, dt, nsteps))
+
+    def sync(self) -> None:
+        self._chk(self._lib.fs_sync(self._h))
+
+    def run_stage(self, stage: str, dt: float) -> None:
+        self._chk(self._lib.fs_run_stage(self._h, STAGES[stage], dt))
+
+    def last_stats(self) -> dict:
+        st = L.StepStats()
+        self._chk(self._lib.fs_last_stats(self._h, C.byref(st)))
+        return {"cycles": st.cycles, "converged": bool(st.converged), "residual_max": st.residual_max,
+                "residual_initial": st.residual_initial}
+
+    @property
+    def t(self) -> float:
+        t = C.c_double()
+        self._lib.fs_get_time(self._h, C.byref(t), None)
+        return t.value
+
+    @property
+    def steps(self) -> int:
+        n = C.c_int64()
+        self._lib.fs_get_time(self._h, None, C.byref(n))
+        return n.value
+
+    # ----------------------------------------------------------- diagnostics
+    def max_divergence(self) -> float:
+        """maxDivergence() (solver.js:835-850)"""
+        out = C.c_double()
+        self._chk(self._lib.fs_max_divergence(self._h, C.byref(out)))
+        return out.value
+
+    maxDivergence = max_divergence
+
+    def poisson_residual_after(self, iterations: int, dt: float = 0.01) -> float:
+        """poissonResidualAfter(iterations, dt) (solver.js:857-896)"""
+        out = C.c_double()
+        self._chk(self._lib.fs_poisson_residual_after(self._h, iterations, dt, C.byref(out)))
+        return out.value
+
+    poissonResidualAfter = poisson_residual_after
+
+    # ----------------------------------------------------------- measurement
+    def time_steps(self, dt: float, nsteps: int) -> float:
+        ms = C.c_double()
+        self._chk(self._lib.fs_time_steps(self._h, dt, nsteps, C.byref(ms)))
+        return ms.value
+
+    def profile_step(self, dt: float, nsteps: int = 1) -> list[dict]:
+        cap = 64
+        arr = (L.KernelTime * cap)()
+        cnt = C.c_int()
+        self._chk(self._lib.fs_profile_step(self._h, dt, nsteps, arr, cap, C.byref(cnt)))
+        return [{"name": arr[k].name.decode(), "launches": arr[k].launches, "total_ms": arr[k].total_ms,
+                 "bytes": arr[k].bytes} for k in range(min(cap, cnt.value))]
+
+    def launch_count(self) -> int:
+        return int(self._lib.fs_launch_count(self._h))

@@ -1,0 +1,230 @@
+/*
+ * fluid.h -- C ABI of libfluidcuda.so, the GB300 (sm_103a) stable-fluids step.
+ *
+ * This is the drop-in boundary for fluid-sim's GPU backend, the JavaScript
+ * class GPUFluidSolver in src/gpu/solver.js.  Each entry point below names the
+ * reference member it replaces.  The signatures carry only plain C types
+ * (pointers, sizes, enums, PODs) so any FFI -- an N-API addon for the
+ * reference's Node host, ctypes, C/C++ -- can bind them.
+ *
+ * Conventions
+ *  - Every function returns an int status (fs_status; 0 = FS_OK) unless
+ *    stated otherwise.  On failure fs_last_error() returns a message.
+ *  - Fields are row-major n = nx*ny arrays, i fastest: u[j*nx+i] is u on the
+ *    LEFT face of cell (i,j), v[j*nx+i] on its BOTTOM face, p at its centre
+ *    (src/core/grid.js:95-105).  Inputs are copied; outputs are written to
+ *    caller memory.
+ *  - A solver owns its device memory and one CUDA stream.  Calls on one
+ *    handle are not thread-safe; distinct handles are independent.  Work is
+ *    enqueued asynchronously; every read-back call synchronises the stream.
+ *  - Unknown enum values are rejected with FS_ERR_INVALID_ARGUMENT (the
+ *    reference silently falls back to semi-Lagrangian / Jacobi,
+ *    src/gpu/solver.js:606,687; this boundary is deliberately stricter).
+ *  - Nothing here falls back to the CPU: with no usable CUDA device fs_create
+ *    fails with FS_ERR_NO_DEVICE.
+ */
+#ifndef FLUIDCUDA_H
+#define FLUIDCUDA_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#if defined(_WIN32)
+#define FS_API __declspec(dllexport)
+#else
+#define FS_API __attribute__((visibility("default")))
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct fs_solver fs_solver;
+
+typedef enum fs_status {
+  FS_OK = 0,
+  FS_ERR_INVALID_ARGUMENT = 1,
+  FS_ERR_CUDA = 2,
+  FS_ERR_OUT_OF_MEMORY = 3,
+  FS_ERR_NOT_CONVERGED = 4, /* tolerance not met within max_cycles (state is still advanced) */
+  FS_ERR_NONFINITE = 5,     /* a residual reduction saw NaN or Inf */
+  FS_ERR_UNSUPPORTED = 6,
+  FS_ERR_NO_DEVICE = 7
+} fs_status;
+
+/* advection option of src/gpu/solver.js:68 */
+typedef enum fs_advection { FS_ADVECT_SEMI_LAGRANGIAN = 0, FS_ADVECT_MACCORMACK = 1 } fs_advection;
+
+/* pressureSolver option of src/gpu/solver.js:70 */
+typedef enum fs_pressure_solver {
+  FS_PRESSURE_JACOBI = 0,
+  FS_PRESSURE_RED_BLACK = 1,
+  FS_PRESSURE_MULTIGRID = 2
+} fs_pressure_solver;
+
+/* Arithmetic of the step.
+ *  F32:   every field f32, as the reference WebGPU backend computes.
+ *  MIXED: velocity, pressure and divergence held in f64; advection, forcing
+ *         and the Poisson corrections (V-cycles / sweeps) in f32 inside an
+ *         iterative refinement whose residual and pressure accumulation are
+ *         f64.  Needed for max|div u| <= 1e-6 and below at large n, where an
+ *         f32-stored velocity alone floors max|div| near 1e-5. */
+typedef enum fs_precision { FS_PRECISION_F32 = 0, FS_PRECISION_MIXED = 1 } fs_precision;
+
+typedef enum fs_dtype { FS_DTYPE_F32 = 0, FS_DTYPE_F64 = 1 } fs_dtype;
+
+typedef enum fs_field {
+  FS_FIELD_U = 0,
+  FS_FIELD_V = 1,
+  FS_FIELD_PRESSURE = 2,   /* last projection's pressure (readTexture(presCur)) */
+  FS_FIELD_DIVERGENCE = 3, /* last computed divergence (readTexture(div)) */
+  FS_FIELD_IMPULSE_X = 4,  /* last solid-coupling impulse per cell (impulseTex .x/.y/.z) */
+  FS_FIELD_IMPULSE_Y = 5,
+  FS_FIELD_IMPULSE_TORQUE = 6
+} fs_field;
+
+/* One stage of the step, for fs_run_stage (the verification harness's reach
+ * into private _bind/_dispatch, tools/gputest.html:91-100, made public). */
+typedef enum fs_stage {
+  FS_STAGE_ADVECT = 0,            /* _encodeAdvection, solver.js:604-647 */
+  FS_STAGE_DIFFUSE = 1,           /* DIFFUSE pass, solver.js:532-540 */
+  FS_STAGE_FORCING = 2,           /* _encodeForcing, solver.js:387-414 */
+  FS_STAGE_SOLID = 3,             /* _encodeSolid, solver.js:440-465 */
+  FS_STAGE_DIVERGENCE = 4,        /* DIVERGENCE pass, solver.js:659-664 */
+  FS_STAGE_PRESSURE = 5,          /* zero p + _encodePoisson, solver.js:669-674 */
+  FS_STAGE_SUBTRACT_GRADIENT = 6, /* SUBTRACT_GRADIENT pass, solver.js:676-683 */
+  FS_STAGE_PROJECT = 7            /* _encodeProjection, solver.js:658-684 */
+} fs_stage;
+
+/* Constructor options of GPUFluidSolver (src/gpu/solver.js:65-72) plus the
+ * tolerance loop, precision and multigrid settings.  Fill with
+ * fs_params_default() first; it sets the reference defaults. */
+typedef struct fs_params {
+  int32_t nx, ny;             /* cells (default 256 x 256) */
+  double lx, ly;              /* domain (default 2*pi x 2*pi) */
+  double nu;                  /* viscosity, explicit diffusion (default 0) */
+  double confinement;         /* must be 0: vorticity confinement is not on this path */
+  int32_t advection;          /* fs_advection (default MacCormack) */
+  double solid_mask_width;    /* mask width in cells (default 1.5) */
+  int32_t pressure_solver;    /* fs_pressure_solver (default Jacobi) */
+  int32_t pressure_iterations;/* sweeps (Jacobi, red-black) or V-cycles (multigrid)
+                                 per projection when pressure_tol == 0 (default 40) */
+  int32_t precision;          /* fs_precision (default F32) */
+  double pressure_tol;        /* > 0: repeat cycles until max|div u| <= tol
+                                 (each cycle = pressure_iterations sweeps or V-cycles) */
+  int32_t max_cycles;         /* cap of the tolerance loop (default 50) */
+  int32_t mg_pre_smooth;      /* red-black sweeps before restriction (default 2) */
+  int32_t mg_post_smooth;     /* red-black sweeps after prolongation (default 2) */
+  int32_t mg_coarse_sweeps;   /* sweeps on the coarsest level (default 40) */
+  int32_t mg_min_size;        /* stop coarsening below this size (default 8) */
+  int32_t warm_start;         /* 1: start each projection from the previous pressure
+                                 instead of zero (the reference zeroes it,
+                                 solver.js:669-672) */
+  int32_t device;             /* CUDA device ordinal (default 0) */
+} fs_params;
+
+/* one forcing mode, as setForcing's {kx, ky, phase} (solver.js:370-385) */
+typedef struct fs_mode {
+  double kx, ky, phase;
+} fs_mode;
+
+/* an immersed rigid disk (src/cpu/solid.js:42-146 RigidDisk: centre, radius,
+ * velocity, angular velocity); the step applies its direct forcing */
+typedef struct fs_disk {
+  double x, y, r, vx, vy, omega;
+} fs_disk;
+
+typedef struct fs_step_stats {
+  int32_t cycles;            /* cycles (sweeps or V-cycles) the last projection ran */
+  int32_t converged;         /* 1 if pressure_tol was met (always 1 when tol == 0) */
+  double residual_max;       /* max|div u| after the last projection, -1 if not measured */
+  double residual_initial;   /* max|div u| entering the last projection, -1 if not measured */
+} fs_step_stats;
+
+/* per-kernel timing from fs_profile_step */
+typedef struct fs_kernel_time {
+  char name[48];
+  int32_t launches;
+  double total_ms;
+  double bytes;              /* algorithmic bytes moved by those launches */
+} fs_kernel_time;
+
+/* ---------------------------------------------------------------- lifecycle */
+FS_API void fs_params_default(fs_params* params);
+/* new GPUFluidSolver(device, opts) + createDevice (solver.js:43-98) */
+FS_API int fs_create(const fs_params* params, fs_solver** out);
+/* destroy() (solver.js:898-911) */
+FS_API void fs_destroy(fs_solver* s);
+/* Message of the last failure on s; with s == NULL, of the last failed
+ * fs_create on this thread.  Valid until the next call on the same handle. */
+FS_API const char* fs_last_error(const fs_solver* s);
+FS_API const char* fs_status_string(int status);
+FS_API int fs_get_params(const fs_solver* s, fs_params* out);
+
+/* -------------------------------------------------------------- field I/O */
+/* uploadVelocity(u, v) (solver.js:301-315); dtype selects f32 or f64 input */
+FS_API int fs_upload_velocity(fs_solver* s, const void* u, const void* v, int dtype);
+/* readVelocity() (solver.js:356-362); synchronises */
+FS_API int fs_read_velocity(fs_solver* s, void* u, void* v, int dtype);
+/* readTexture(tex) for the other fields (solver.js:336-353); synchronises */
+FS_API int fs_read_field(fs_solver* s, int field, void* out, int dtype);
+/* set the pressure a warm-started projection starts from (FS_FIELD_PRESSURE only) */
+FS_API int fs_upload_field(fs_solver* s, int field, const void* data, int dtype);
+
+/* ----------------------------------------------------- forces and solids */
+/* setForcing(modes, {amplitude, drag, phaseDrift}) (solver.js:370-385);
+ * count == 0 disables the forcing pass */
+FS_API int fs_set_forcing(fs_solver* s, const fs_mode* modes, int count, double amplitude,
+                          double drag, double phase_drift);
+/* setSolid(disk) (solver.js:425-438), generalised to count disks applied in
+ * order (src/cpu/solid.js:181-230); count == 0 removes them */
+FS_API int fs_set_solids(fs_solver* s, const fs_disk* disks, int count);
+/* Impulse the last coupling pass gave the fluid, per disk: out[3k+0..2] =
+ * (sum du dA, sum dv dA, sum torque dA), reduced on the device (replaces the
+ * readback + CPU sum of integrateSolid, solver.js:477-510); synchronises */
+FS_API int fs_solid_impulse(fs_solver* s, double* out, int count);
+
+/* ------------------------------------------------------------------ step */
+/* step(dt) (solver.js:518-591): advect, diffuse, force, solids, project.
+ * Enqueued on the solver's stream; returns without waiting unless the
+ * tolerance loop is active, in which case the loop's convergence test reads
+ * one residual word per cycle.  Returns FS_ERR_NOT_CONVERGED / FS_ERR_NONFINITE
+ * when the tolerance loop fails (the step is still applied). */
+FS_API int fs_step(fs_solver* s, double dt);
+/* nsteps consecutive steps */
+FS_API int fs_advance(fs_solver* s, double dt, int nsteps);
+FS_API int fs_sync(fs_solver* s);
+/* statistics of the last projection; synchronises */
+FS_API int fs_last_stats(fs_solver* s, fs_step_stats* out);
+/* simulation time and step count (the public fields t and steps) */
+FS_API int fs_get_time(const fs_solver* s, double* t, int64_t* steps);
+/* run one stage of the step by itself (see fs_stage) */
+FS_API int fs_run_stage(fs_solver* s, int stage, double dt);
+
+/* ------------------------------------------------------------ diagnostics */
+/* maxDivergence() (solver.js:835-850), reduced on the device; synchronises */
+FS_API int fs_max_divergence(fs_solver* s, double* out);
+/* poissonResidualAfter(iterations, dt) (solver.js:857-896): divergence, zero
+ * pressure, `iterations` sweeps / V-cycles, then ||lap p - div|| / ||div||
+ * reduced in f64 on the device; synchronises */
+FS_API int fs_poisson_residual_after(fs_solver* s, int iterations, double dt, double* out);
+
+/* -------------------------------------------------------------- measurement */
+/* Time nsteps steps with CUDA events recorded on the solver's stream; writes
+ * the elapsed milliseconds.  Synchronises. */
+FS_API int fs_time_steps(fs_solver* s, double dt, int nsteps, double* elapsed_ms);
+/* Run nsteps steps with a CUDA event pair around every kernel launch and
+ * return per-kernel launch counts, total times and algorithmic bytes
+ * (out has room for cap entries; *count gets the number written). */
+FS_API int fs_profile_step(fs_solver* s, double dt, int nsteps, fs_kernel_time* out, int cap,
+                           int* count);
+/* Number of kernel launches enqueued by this handle since creation. */
+FS_API int64_t fs_launch_count(const fs_solver* s);
+/* Page-locked host memory for fast uploads and read-backs (cudaMallocHost). */
+FS_API void* fs_host_alloc(size_t bytes);
+FS_API void fs_host_free(void* p);
+
+#ifdef __cplusplus
+}
+#endif
+#endif
