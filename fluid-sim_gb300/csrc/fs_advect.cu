@@ -234,7 +234,7 @@ __device__ __forceinline__ float wrap_delta(float d, float L) { return d - L * f
 
 __global__ void __launch_bounds__(256)
     k_solids(float* __restrict__ u, float* __restrict__ v, int ndisk, int nx, int ny, float dx,
-             float dy, float lx, float ly, float width, float dA, float* __restrict__ imp,
+             float dy, float lx, float ly, float width, double dA, float* __restrict__ imp,
              double* __restrict__ dimp) {
   int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y;
   bool in = i < nx && j < ny;
@@ -277,18 +277,20 @@ __global__ void __launch_bounds__(256)
     tix += fx;
     tiy += fy;
     tit += tq;
-    if (dimp) {
-      // block reduction of this disk's impulse, one f64 atomic per block
-      double sx = fx, sy = fy, st = tq;
+    // warp sum of this disk's impulse (only warps that touched the disk), one
+    // f64 atomic per warp; the order of the atomics is not fixed, so the
+    // impulse sums (not the velocity field) may differ in the last bits run to run
+    if (dimp && __any_sync(0xffffffffu, fx != 0.f || fy != 0.f || tq != 0.f)) {
+      float sx = fx, sy = fy, st = tq;
       for (int o = 16; o > 0; o >>= 1) {
         sx += __shfl_xor_sync(0xffffffffu, sx, o);
         sy += __shfl_xor_sync(0xffffffffu, sy, o);
         st += __shfl_xor_sync(0xffffffffu, st, o);
       }
-      if ((threadIdx.x & 31) == 0 && (sx != 0.0 || sy != 0.0 || st != 0.0)) {
-        atomicAdd(dimp + 3 * k + 0, sx * dA);
-        atomicAdd(dimp + 3 * k + 1, sy * dA);
-        atomicAdd(dimp + 3 * k + 2, st * dA);
+      if ((threadIdx.x & 31) == 0) {
+        atomicAdd(dimp + 3 * k + 0, (double)sx * dA);
+        atomicAdd(dimp + 3 * k + 1, (double)sy * dA);
+        atomicAdd(dimp + 3 * k + 2, (double)st * dA);
       }
     }
   }
@@ -323,7 +325,7 @@ void launch_solids(Solver* s, float* u, float* v, float dt, bool record_impulse)
   FS_LAUNCH(s, "solids", (double)s->n * (record_impulse ? 28 : 16),
             k_solids<<<grid2d(g.nx, g.ny, kBlock), kBlock, 0, s->stream>>>(
                 u, v, nd, g.nx, g.ny, g.dx, g.dy, (float)(g.nx * g.dxd), (float)(g.ny * g.dyd),
-                (float)width, (float)(g.dxd * g.dyd), record_impulse ? s->imp : nullptr,
+                (float)width, g.dxd * g.dyd, record_impulse ? s->imp : nullptr,
                 s->d_impulse));
 }
 

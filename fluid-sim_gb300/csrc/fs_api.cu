@@ -91,10 +91,11 @@ static int dalloc(Solver* s, T** p, size_t count) {
 static void free_all(Solver* s) {
   auto f = [](void* p) { if (p) cudaFree(p); };
   f(s->u); f(s->v); f(s->wu); f(s->wv); f(s->tu); f(s->tv); f(s->fu); f(s->fv);
-  f(s->p32); f(s->p32b); f(s->div32); f(s->p64); f(s->p64b); f(s->div64);
+  f(s->ulo); f(s->vlo);
+  f(s->p32); f(s->p32b); f(s->div32); f(s->ph); f(s->pl); f(s->pbh); f(s->pbl); f(s->dh); f(s->dl);
   f(s->r32); f(s->e32); f(s->e32b); f(s->scratch);
   for (size_t l = 1; l < s->lev.size(); l++) { f(s->lev[l].x); f(s->lev[l].x2); f(s->lev[l].rhs); }
-  if (!s->lev.empty()) f(s->lev[0].x2);
+  f(s->stage);
   f(s->red_partials); f(s->red_out); f(s->modes); f(s->imp); f(s->d_impulse);
   if (s->h_red) cudaFreeHost(s->h_red);
   if (s->stream) cudaStreamDestroy(s->stream);
@@ -135,6 +136,7 @@ static int create(const fs_params* prm, Solver* s) {
   if (P.mg_pre_smooth < 0 || P.mg_post_smooth < 0 || P.mg_coarse_sweeps < 0 || P.mg_min_size < 2)
     return fail(nullptr, FS_ERR_INVALID_ARGUMENT, "bad multigrid settings");
   if (!(P.solid_mask_width > 0)) return fail(nullptr, FS_ERR_INVALID_ARGUMENT, "solid_mask_width must be > 0");
+  if (P.kernel_variant < 0 || P.kernel_variant > 1) return fail(nullptr, FS_ERR_INVALID_ARGUMENT, "unknown kernel_variant");
 
   s->mixed = P.precision == FS_PRECISION_MIXED;
   s->odd = (P.nx & 1) || (P.ny & 1);
@@ -183,12 +185,13 @@ static int create(const fs_params* prm, Solver* s) {
   const int64_t n = s->n;
   int rc;
 #define A(ptr, T, cnt) if ((rc = dalloc(s, (T**)&(ptr), (size_t)(cnt))) != FS_OK) return rc
+  A(s->u, float, n); A(s->v, float, n);
   if (s->mixed) {
-    A(s->u, double, n); A(s->v, double, n);
-    A(s->p64, double, n); A(s->p64b, double, n); A(s->div64, double, n);
+    A(s->ulo, float, n); A(s->vlo, float, n);
+    A(s->ph, float, n); A(s->pl, float, n); A(s->pbh, float, n); A(s->pbl, float, n);
+    A(s->dh, float, n); A(s->dl, float, n);
     A(s->r32, float, n); A(s->e32, float, n); A(s->e32b, float, n);
   } else {
-    A(s->u, float, n); A(s->v, float, n);
     A(s->p32, float, n); A(s->p32b, float, n); A(s->div32, float, n);
   }
   A(s->wu, float, n); A(s->wv, float, n); A(s->tu, float, n); A(s->tv, float, n);
@@ -196,28 +199,29 @@ static int create(const fs_params* prm, Solver* s) {
   if (!s->lev.empty()) {
     A(s->scratch, float, n);
     s->lev[0].x = s->mixed ? s->e32 : s->p32;
+    s->lev[0].x2 = s->mixed ? s->e32b : s->p32b;
     s->lev[0].rhs = s->mixed ? s->r32 : s->div32;
-    if (s->lev[0].n & 1) A(s->lev[0].x2, float, n);
     for (size_t l = 1; l < s->lev.size(); l++) {
       int64_t m = (int64_t)s->lev[l].n * s->lev[l].n;
-      A(s->lev[l].x, float, m); A(s->lev[l].rhs, float, m);
-      if (s->lev[l].n & 1) A(s->lev[l].x2, float, m);
+      A(s->lev[l].x, float, m); A(s->lev[l].rhs, float, m); A(s->lev[l].x2, float, m);
     }
+    s->fused = P.kernel_variant == 0 && mg_fused_supported(s);
   }
   // reductions: partial buffer for the largest grid launch plus the counter word
   int64_t blocks = (int64_t)((P.nx + 31) / 32) * ((P.ny + 7) / 8);
   s->red_cap = (int)std::max<int64_t>(blocks, 4096);
-  A(s->red_partials, double, 2 * (int64_t)s->red_cap + 1);
+  // [2*cap f64 sums][cap f32 maxima][counter word]
+  A(s->red_partials, double, 2 * (int64_t)s->red_cap + (s->red_cap + 2) / 2 + 1);
   A(s->red_out, double, 4);
 #undef A
-  CU(s, cudaMemsetAsync(s->red_partials, 0, (2 * (size_t)s->red_cap + 1) * sizeof(double), s->stream));
+  CU(s, cudaMemsetAsync(s->red_partials, 0, (2 * (size_t)s->red_cap + (s->red_cap + 2) / 2 + 1) * sizeof(double),
+                        s->stream));
   CU(s, cudaMallocHost((void**)&s->h_red, 4 * sizeof(double)));
   // every field starts at zero
-  CU(s, cudaMemsetAsync(s->u, 0, n * (s->mixed ? 8 : 4), s->stream));
-  CU(s, cudaMemsetAsync(s->v, 0, n * (s->mixed ? 8 : 4), s->stream));
+  CU(s, cudaMemsetAsync(s->u, 0, n * 4, s->stream));
+  CU(s, cudaMemsetAsync(s->v, 0, n * 4, s->stream));
   if (s->mixed) {
-    CU(s, cudaMemsetAsync(s->p64, 0, n * 8, s->stream));
-    CU(s, cudaMemsetAsync(s->div64, 0, n * 8, s->stream));
+    for (float* q : {s->ulo, s->vlo, s->ph, s->pl, s->dh, s->dl}) CU(s, cudaMemsetAsync(q, 0, n * 4, s->stream));
   } else {
     CU(s, cudaMemsetAsync(s->p32, 0, n * 4, s->stream));
     CU(s, cudaMemsetAsync(s->div32, 0, n * 4, s->stream));
@@ -229,12 +233,20 @@ static int create(const fs_params* prm, Solver* s) {
 // -------------------------------------------------------- the projection
 // F32 Poisson solve on (p32, div32): `iterations` sweeps or V-cycles
 // (_encodePoisson, solver.js:686-738)
-static void poisson_f32(Solver* s, int iterations) {
+static void poisson_f32(Solver* s, int iterations, bool p_nonzero) {
   const fs_params& P = s->prm;
   const Grid& g = s->g;
   float h2 = g.dx * g.dx;
   if (P.pressure_solver == FS_PRESSURE_MULTIGRID) {
-    for (int k = 0; k < iterations; k++) mg_vcycle(s);
+    s->lev[0].x = s->p32;
+    s->lev[0].x2 = s->p32b;
+    for (int k = 0; k < iterations; k++) {
+      if (s->fused) mg_vcycle_fused(s, p_nonzero || k > 0);
+      else mg_vcycle(s);
+    }
+    s->p32 = s->lev[0].x;
+    s->p32b = s->lev[0].x2;
+    return;
   } else if (P.pressure_solver == FS_PRESSURE_RED_BLACK) {
     for (int k = 0; k < iterations; k++)
       for (int colour = 0; colour < 2; colour++) {
@@ -251,7 +263,6 @@ static void poisson_f32(Solver* s, int iterations) {
       std::swap(s->p32, s->p32b);
     }
   }
-  if (!s->lev.empty()) s->lev[0].x = s->p32;
 }
 
 // correction solve of the MIXED mode: e32 from r32 starting at zero
@@ -259,11 +270,20 @@ static void correction_solve(Solver* s, int iterations) {
   const fs_params& P = s->prm;
   const Grid& g = s->g;
   float h2 = g.dx * g.dx;
-  launch_fill(s, s->e32, 0.f, s->n);
   if (P.pressure_solver == FS_PRESSURE_MULTIGRID) {
     s->lev[0].x = s->e32;
-    for (int k = 0; k < iterations; k++) mg_vcycle(s);
-  } else if (P.pressure_solver == FS_PRESSURE_RED_BLACK) {
+    s->lev[0].x2 = s->e32b;
+    if (!s->fused) launch_fill(s, s->e32, 0.f, s->n);  // the fused cycle starts from zero itself
+    for (int k = 0; k < iterations; k++) {
+      if (s->fused) mg_vcycle_fused(s, k > 0);
+      else mg_vcycle(s);
+    }
+    s->e32 = s->lev[0].x;
+    s->e32b = s->lev[0].x2;
+    return;
+  }
+  launch_fill(s, s->e32, 0.f, s->n);
+  if (P.pressure_solver == FS_PRESSURE_RED_BLACK) {
     for (int k = 0; k < iterations; k++)
       for (int colour = 0; colour < 2; colour++) {
         if (!s->odd) {
@@ -281,7 +301,7 @@ static void correction_solve(Solver* s, int iterations) {
   }
 }
 
-// Pressure solve from the divergence already in div32 / div64.
+// Pressure solve from the divergence already in div32 / (dh, dl).
 // Tolerance loop: each cycle is `pressure_iterations` sweeps or V-cycles; in
 // the MIXED mode each cycle ends with the f64 update p += e, r = d - lap p.
 static int pressure_solve(Solver* s) {
@@ -293,7 +313,7 @@ static int pressure_solve(Solver* s) {
   if (!s->mixed) {
     if (!P.warm_start) launch_fill(s, s->p32, 0.f, s->n);
     if (!tol) {
-      poisson_f32(s, iters);
+      poisson_f32(s, iters, P.warm_start != 0);
       s->stats.cycles = iters;
       return check_launch(s);
     }
@@ -304,7 +324,7 @@ static int pressure_solve(Solver* s) {
     s->stats.residual_initial = m;
     int c = 0;
     while (!(m <= P.pressure_tol) && c < P.max_cycles && std::isfinite(m)) {
-      poisson_f32(s, iters);
+      poisson_f32(s, iters, c > 0 || P.warm_start != 0);
       launch_absmax_residual32(s, s->p32, s->div32);
       if ((rc = read_red(s, &m))) return rc;
       c++;
@@ -317,8 +337,11 @@ static int pressure_solve(Solver* s) {
     return check_launch(s);
   }
   // MIXED: iterative refinement
-  launch_refine_init(s, s->div64, s->p64, s->r32, !P.warm_start);
-  if (!P.warm_start) launch_fill64(s, s->p64, 0.0, s->n);
+  launch_refine_init(s, s->dh, s->dl, s->ph, s->pl, s->r32, !P.warm_start);
+  if (!P.warm_start) {
+    launch_fill(s, s->ph, 0.f, s->n);
+    launch_fill(s, s->pl, 0.f, s->n);
+  }
   double m = -1.0;
   int rc;
   if (tol) {
@@ -334,8 +357,9 @@ static int pressure_solve(Solver* s) {
       break;
     }
     correction_solve(s, iters);
-    launch_refine_update(s, s->p64, s->e32, s->div64, s->p64b, s->r32);
-    std::swap(s->p64, s->p64b);
+    launch_refine_update(s, s->ph, s->pl, s->e32, s->dh, s->dl, s->pbh, s->pbl, s->r32);
+    std::swap(s->ph, s->pbh);
+    std::swap(s->pl, s->pbl);
     c++;
     if (tol && (rc = read_red(s, &m))) return rc;
   }
@@ -352,24 +376,20 @@ static int pressure_solve(Solver* s) {
 
 // divergence of (wu, wv) -> solve -> state velocity = w - grad p
 static int project_from(Solver* s, const float* wu, const float* wv) {
-  if (s->mixed) launch_divergence<float, double>(s, wu, wv, s->div64);
+  if (s->mixed) launch_div_df(s, wu, nullptr, wv, nullptr, s->dh, s->dl);
   else launch_divergence<float, float>(s, wu, wv, s->div32);
   int rc = pressure_solve(s);
-  if (s->mixed) launch_subtract_gradient_mixed(s, wu, wv, s->p64, (double*)s->u, (double*)s->v);
-  else launch_subtract_gradient_f32(s, wu, wv, s->p32, (float*)s->u, (float*)s->v);
+  if (s->mixed) launch_subgrad_df(s, wu, nullptr, wv, nullptr, s->ph, s->pl, s->u, s->ulo, s->v, s->vlo);
+  else launch_subtract_gradient_f32(s, wu, wv, s->p32, s->u, s->v);
   int rc2 = check_launch(s);
   return rc ? rc : rc2;
 }
 
 // advection of the state into (wu, wv)
 static void advect_into(Solver* s, float dt, float* ou, float* ov) {
-  if (s->prm.advection == FS_ADVECT_MACCORMACK) {
-    if (s->mixed) launch_advect_mc<double>(s, (const double*)s->u, (const double*)s->v, s->fu, s->fv, ou, ov, dt);
-    else launch_advect_mc<float>(s, (const float*)s->u, (const float*)s->v, s->fu, s->fv, ou, ov, dt);
-  } else {
-    if (s->mixed) launch_advect_sl<double>(s, (const double*)s->u, (const double*)s->v, ou, ov, dt);
-    else launch_advect_sl<float>(s, (const float*)s->u, (const float*)s->v, ou, ov, dt);
-  }
+  // the MIXED state is advected from its f32 hi planes
+  if (s->prm.advection == FS_ADVECT_MACCORMACK) launch_advect_mc<float>(s, s->u, s->v, s->fu, s->fv, ou, ov, dt);
+  else launch_advect_sl<float>(s, s->u, s->v, ou, ov, dt);
 }
 
 // step(dt), solver.js:518-591
@@ -391,12 +411,21 @@ static int step(Solver* s, double dt) {
 
 // state <-> working f32 copies for the stage-by-stage entry point
 static void state_to_w(Solver* s) {
-  launch_convert(s, s->u, s->mixed, s->wu, 0, s->n);
-  launch_convert(s, s->v, s->mixed, s->wv, 0, s->n);
+  if (s->mixed) {
+    launch_df_to_f(s, s->u, s->ulo, s->wu, s->n);
+    launch_df_to_f(s, s->v, s->vlo, s->wv, s->n);
+  } else {
+    cudaMemcpyAsync(s->wu, s->u, s->n * 4, cudaMemcpyDeviceToDevice, s->stream);
+    cudaMemcpyAsync(s->wv, s->v, s->n * 4, cudaMemcpyDeviceToDevice, s->stream);
+  }
 }
 static void w_to_state(Solver* s, const float* a, const float* b) {
-  launch_convert(s, a, 0, s->u, s->mixed, s->n);
-  launch_convert(s, b, 0, s->v, s->mixed, s->n);
+  cudaMemcpyAsync(s->u, a, s->n * 4, cudaMemcpyDeviceToDevice, s->stream);
+  cudaMemcpyAsync(s->v, b, s->n * 4, cudaMemcpyDeviceToDevice, s->stream);
+  if (s->mixed) {
+    cudaMemsetAsync(s->ulo, 0, s->n * 4, s->stream);
+    cudaMemsetAsync(s->vlo, 0, s->n * 4, s->stream);
+  }
 }
 
 static int run_stage(Solver* s, int stage, double dt) {
@@ -424,8 +453,8 @@ static int run_stage(Solver* s, int stage, double dt) {
       w_to_state(s, s->wu, s->wv);
       break;
     case FS_STAGE_DIVERGENCE:
-      if (s->mixed) launch_divergence<double, double>(s, (const double*)s->u, (const double*)s->v, s->div64);
-      else launch_divergence<float, float>(s, (const float*)s->u, (const float*)s->v, s->div32);
+      if (s->mixed) launch_div_df(s, s->u, s->ulo, s->v, s->vlo, s->dh, s->dl);
+      else launch_divergence<float, float>(s, s->u, s->v, s->div32);
       break;
     case FS_STAGE_PRESSURE: {
       int rc = pressure_solve(s);
@@ -433,14 +462,33 @@ static int run_stage(Solver* s, int stage, double dt) {
       break;
     }
     case FS_STAGE_SUBTRACT_GRADIENT:
-      state_to_w(s);
-      if (s->mixed) launch_subtract_gradient_mixed(s, s->wu, s->wv, s->p64, (double*)s->u, (double*)s->v);
-      else launch_subtract_gradient_f32(s, s->wu, s->wv, s->p32, (float*)s->u, (float*)s->v);
+      if (s->mixed) {
+        // keep the full df state: copy it aside, then u = w - grad p
+        cudaMemcpyAsync(s->wu, s->u, s->n * 4, cudaMemcpyDeviceToDevice, s->stream);
+        cudaMemcpyAsync(s->wv, s->v, s->n * 4, cudaMemcpyDeviceToDevice, s->stream);
+        cudaMemcpyAsync(s->tu, s->ulo, s->n * 4, cudaMemcpyDeviceToDevice, s->stream);
+        cudaMemcpyAsync(s->tv, s->vlo, s->n * 4, cudaMemcpyDeviceToDevice, s->stream);
+        launch_subgrad_df(s, s->wu, s->tu, s->wv, s->tv, s->ph, s->pl, s->u, s->ulo, s->v, s->vlo);
+      } else {
+        state_to_w(s);
+        launch_subtract_gradient_f32(s, s->wu, s->wv, s->p32, s->u, s->v);
+      }
       break;
     case FS_STAGE_PROJECT: {
-      state_to_w(s);
-      int rc = project_from(s, s->wu, s->wv);
-      if (rc) return rc;
+      if (s->mixed) {
+        cudaMemcpyAsync(s->wu, s->u, s->n * 4, cudaMemcpyDeviceToDevice, s->stream);
+        cudaMemcpyAsync(s->wv, s->v, s->n * 4, cudaMemcpyDeviceToDevice, s->stream);
+        cudaMemcpyAsync(s->tu, s->ulo, s->n * 4, cudaMemcpyDeviceToDevice, s->stream);
+        cudaMemcpyAsync(s->tv, s->vlo, s->n * 4, cudaMemcpyDeviceToDevice, s->stream);
+        launch_div_df(s, s->wu, s->tu, s->wv, s->tv, s->dh, s->dl);
+        int rc = pressure_solve(s);
+        launch_subgrad_df(s, s->wu, s->tu, s->wv, s->tv, s->ph, s->pl, s->u, s->ulo, s->v, s->vlo);
+        if (rc) return rc;
+      } else {
+        state_to_w(s);
+        int rc = project_from(s, s->wu, s->wv);
+        if (rc) return rc;
+      }
       break;
     }
     default:
@@ -476,6 +524,7 @@ FS_API void fs_params_default(fs_params* p) {
   p->mg_min_size = 8;
   p->warm_start = 0;
   p->device = 0;
+  p->kernel_variant = 0;
 }
 
 FS_API int fs_create(const fs_params* params, fs_solver** out) {
@@ -534,35 +583,49 @@ FS_API int fs_get_params(const fs_solver* h, fs_params* out) {
   Solver* s = &h->s;                                                       \
   if (cudaSetDevice(s->device) != cudaSuccess) return fail(s, FS_ERR_CUDA, "cudaSetDevice failed")
 
-static int upload_array(Solver* s, const void* src, int dtype, void* dst, bool dst_f64) {
+// persistent device staging buffer for dtype conversion on upload / read-back
+static int staging(Solver* s, void** out) {
+  if (!s->stage) CU(s, cudaMalloc(&s->stage, (size_t)s->n * 8));
+  *out = s->stage;
+  return FS_OK;
+}
+
+// host array -> device field; lo == nullptr means an f32 field, otherwise a
+// double-float pair (hi, lo)
+static int upload_to(Solver* s, const void* src, int dtype, float* hi, float* lo) {
   if (dtype != FS_DTYPE_F32 && dtype != FS_DTYPE_F64) return fail(s, FS_ERR_INVALID_ARGUMENT, "unknown dtype");
-  size_t esz = dtype == FS_DTYPE_F64 ? 8 : 4;
-  bool same = (dtype == FS_DTYPE_F64) == dst_f64;
-  if (same) {
-    CU(s, cudaMemcpyAsync(dst, src, s->n * esz, cudaMemcpyHostToDevice, s->stream));
+  const size_t n = (size_t)s->n;
+  if (dtype == FS_DTYPE_F32) {
+    CU(s, cudaMemcpyAsync(hi, src, n * 4, cudaMemcpyHostToDevice, s->stream));
+    if (lo) CU(s, cudaMemsetAsync(lo, 0, n * 4, s->stream));
   } else {
-    // stage through the f32 work buffer tu/tv area: tu,tv are contiguous n floats each
-    void* stage = nullptr;
-    CU(s, cudaMallocAsync(&stage, s->n * esz, s->stream));
-    CU(s, cudaMemcpyAsync(stage, src, s->n * esz, cudaMemcpyHostToDevice, s->stream));
-    launch_convert(s, stage, dtype == FS_DTYPE_F64, dst, dst_f64, s->n);
-    CU(s, cudaFreeAsync(stage, s->stream));
+    void* st;
+    int rc = staging(s, &st);
+    if (rc) return rc;
+    CU(s, cudaMemcpyAsync(st, src, n * 8, cudaMemcpyHostToDevice, s->stream));
+    if (lo) launch_d_to_df(s, (const double*)st, hi, lo, s->n);
+    else launch_convert(s, st, 1, hi, 0, s->n);
   }
   return check_launch(s);
 }
 
-static int download_array(Solver* s, const void* src, bool src_f64, void* dst, int dtype) {
+// device field -> host array (synchronises)
+static int download_from(Solver* s, const float* hi, const float* lo, void* dst, int dtype) {
   if (dtype != FS_DTYPE_F32 && dtype != FS_DTYPE_F64) return fail(s, FS_ERR_INVALID_ARGUMENT, "unknown dtype");
-  size_t esz = dtype == FS_DTYPE_F64 ? 8 : 4;
-  bool same = (dtype == FS_DTYPE_F64) == src_f64;
-  if (same) {
-    CU(s, cudaMemcpyAsync(dst, src, s->n * esz, cudaMemcpyDeviceToHost, s->stream));
+  const size_t n = (size_t)s->n;
+  if (dtype == FS_DTYPE_F32 && !lo) {
+    CU(s, cudaMemcpyAsync(dst, hi, n * 4, cudaMemcpyDeviceToHost, s->stream));
   } else {
-    void* stage = nullptr;
-    CU(s, cudaMallocAsync(&stage, s->n * esz, s->stream));
-    launch_convert(s, src, src_f64, stage, dtype == FS_DTYPE_F64, s->n);
-    CU(s, cudaMemcpyAsync(dst, stage, s->n * esz, cudaMemcpyDeviceToHost, s->stream));
-    CU(s, cudaFreeAsync(stage, s->stream));
+    void* st;
+    int rc = staging(s, &st);
+    if (rc) return rc;
+    if (dtype == FS_DTYPE_F32) {
+      launch_df_to_f(s, hi, lo, (float*)st, s->n);
+      CU(s, cudaMemcpyAsync(dst, st, n * 4, cudaMemcpyDeviceToHost, s->stream));
+    } else {
+      launch_df_to_d(s, hi, lo, (double*)st, s->n);
+      CU(s, cudaMemcpyAsync(dst, st, n * 8, cudaMemcpyDeviceToHost, s->stream));
+    }
   }
   CU(s, cudaStreamSynchronize(s->stream));
   return check_launch(s);
@@ -571,34 +634,34 @@ static int download_array(Solver* s, const void* src, bool src_f64, void* dst, i
 FS_API int fs_upload_velocity(fs_solver* h, const void* u, const void* v, int dtype) {
   SOLVER(h);
   if (!u || !v) return fail(s, FS_ERR_INVALID_ARGUMENT, "u or v is NULL");
-  int rc = upload_array(s, u, dtype, s->u, s->mixed);
+  int rc = upload_to(s, u, dtype, s->u, s->ulo);
   if (rc) return rc;
-  return upload_array(s, v, dtype, s->v, s->mixed);
+  return upload_to(s, v, dtype, s->v, s->vlo);
 }
 
 FS_API int fs_read_velocity(fs_solver* h, void* u, void* v, int dtype) {
   SOLVER(h);
   if (!u || !v) return fail(s, FS_ERR_INVALID_ARGUMENT, "u or v is NULL");
-  int rc = download_array(s, s->u, s->mixed, u, dtype);
+  int rc = download_from(s, s->u, s->ulo, u, dtype);
   if (rc) return rc;
-  return download_array(s, s->v, s->mixed, v, dtype);
+  return download_from(s, s->v, s->vlo, v, dtype);
 }
 
 FS_API int fs_read_field(fs_solver* h, int field, void* out, int dtype) {
   SOLVER(h);
   if (!out) return fail(s, FS_ERR_INVALID_ARGUMENT, "out is NULL");
   switch (field) {
-    case FS_FIELD_U: return download_array(s, s->u, s->mixed, out, dtype);
-    case FS_FIELD_V: return download_array(s, s->v, s->mixed, out, dtype);
+    case FS_FIELD_U: return download_from(s, s->u, s->ulo, out, dtype);
+    case FS_FIELD_V: return download_from(s, s->v, s->vlo, out, dtype);
     case FS_FIELD_PRESSURE:
-      return s->mixed ? download_array(s, s->p64, true, out, dtype) : download_array(s, s->p32, false, out, dtype);
+      return s->mixed ? download_from(s, s->ph, s->pl, out, dtype) : download_from(s, s->p32, nullptr, out, dtype);
     case FS_FIELD_DIVERGENCE:
-      return s->mixed ? download_array(s, s->div64, true, out, dtype) : download_array(s, s->div32, false, out, dtype);
+      return s->mixed ? download_from(s, s->dh, s->dl, out, dtype) : download_from(s, s->div32, nullptr, out, dtype);
     case FS_FIELD_IMPULSE_X:
     case FS_FIELD_IMPULSE_Y:
     case FS_FIELD_IMPULSE_TORQUE:
       if (!s->imp) return fail(s, FS_ERR_INVALID_ARGUMENT, "no solid attached");
-      return download_array(s, s->imp + (int64_t)(field - FS_FIELD_IMPULSE_X) * s->n, false, out, dtype);
+      return download_from(s, s->imp + (int64_t)(field - FS_FIELD_IMPULSE_X) * s->n, nullptr, out, dtype);
     default:
       return fail(s, FS_ERR_INVALID_ARGUMENT, "unknown field");
   }
@@ -608,7 +671,7 @@ FS_API int fs_upload_field(fs_solver* h, int field, const void* data, int dtype)
   SOLVER(h);
   if (!data) return fail(s, FS_ERR_INVALID_ARGUMENT, "data is NULL");
   if (field != FS_FIELD_PRESSURE) return fail(s, FS_ERR_INVALID_ARGUMENT, "only the pressure can be uploaded");
-  return s->mixed ? upload_array(s, data, dtype, s->p64, true) : upload_array(s, data, dtype, s->p32, false);
+  return s->mixed ? upload_to(s, data, dtype, s->ph, s->pl) : upload_to(s, data, dtype, s->p32, nullptr);
 }
 
 FS_API int fs_set_forcing(fs_solver* h, const fs_mode* modes, int count, double amplitude, double drag,
@@ -708,10 +771,10 @@ FS_API int fs_max_divergence(fs_solver* h, double* out) {
   SOLVER(h);
   if (!out) return fail(s, FS_ERR_INVALID_ARGUMENT, "out is NULL");
   if (s->mixed) {
-    launch_divergence<double, double>(s, (const double*)s->u, (const double*)s->v, s->div64);
-    launch_absmax<double>(s, s->div64, s->n, s->red_out);
+    launch_div_df(s, s->u, s->ulo, s->v, s->vlo, s->dh, s->dl);
+    launch_absmax<float>(s, s->dh, s->n, s->red_out);
   } else {
-    launch_divergence<float, float>(s, (const float*)s->u, (const float*)s->v, s->div32);
+    launch_divergence<float, float>(s, s->u, s->v, s->div32);
     launch_absmax<float>(s, s->div32, s->n, s->red_out);
   }
   int rc = check_launch(s);
@@ -724,9 +787,9 @@ FS_API int fs_poisson_residual_after(fs_solver* h, int iterations, double dt, do
   (void)dt;
   if (!out || iterations < 0) return fail(s, FS_ERR_INVALID_ARGUMENT, "bad arguments");
   if (s->mixed) return fail(s, FS_ERR_UNSUPPORTED, "poisson_residual_after measures the F32 solver");
-  launch_divergence<float, float>(s, (const float*)s->u, (const float*)s->v, s->div32);
+  launch_divergence<float, float>(s, s->u, s->v, s->div32);
   launch_fill(s, s->p32, 0.f, s->n);
-  poisson_f32(s, iterations);
+  poisson_f32(s, iterations, false);
   launch_poisson_norms(s, s->p32, s->div32, s->g.dx * s->g.dx, s->g.dxd * s->g.dxd);
   int rc = check_launch(s);
   if (rc) return rc;

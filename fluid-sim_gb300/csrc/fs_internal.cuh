@@ -51,10 +51,13 @@ struct Solver {
   int64_t n = 0;
   bool mixed = false;
   bool odd = false;  // nx or ny odd: red-black ping-pong semantics
+  bool fused = false;  // fused multigrid cycle in use
 
-  // velocity state: float (F32) or double (MIXED)
-  void* u = nullptr;
-  void* v = nullptr;
+  // velocity state.  F32: u, v.  MIXED: double-float planes (u, ulo), (v, vlo).
+  float* u = nullptr;
+  float* v = nullptr;
+  float* ulo = nullptr;
+  float* vlo = nullptr;
   // working velocity of the step before projection (f32 in both modes)
   float* wu = nullptr;
   float* wv = nullptr;
@@ -64,18 +67,19 @@ struct Solver {
   float* fv = nullptr;
 
   // pressure: F32 -> p32/div32 are the Poisson unknown/rhs.
-  //           MIXED -> p64/div64 hold the f64 pressure and divergence, r32/e32
-  //           the f32 residual and correction of one refinement cycle.
+  //           MIXED -> (ph, pl) and (dh, dl) hold the double-float pressure and
+  //           divergence, r32/e32 the f32 residual and correction of one
+  //           refinement cycle.
   float* p32 = nullptr;
-  float* p32b = nullptr;  // ping-pong (Jacobi, odd red-black)
+  float* p32b = nullptr;  // ping-pong (Jacobi, odd red-black, fused cycle)
   float* div32 = nullptr;
-  double* p64 = nullptr;
-  double* p64b = nullptr;
-  double* div64 = nullptr;
+  float *ph = nullptr, *pl = nullptr, *pbh = nullptr, *pbl = nullptr;
+  float *dh = nullptr, *dl = nullptr;
   float* r32 = nullptr;
   float* e32 = nullptr;
   float* e32b = nullptr;
   float* scratch = nullptr;  // n floats: multigrid residual before restriction
+  void* stage = nullptr;     // n doubles: host I/O conversion staging
 
   std::vector<Level> lev;
 
@@ -146,8 +150,14 @@ template <class TV, class TD>
 void launch_divergence(Solver* s, const TV* u, const TV* v, TD* d);
 void launch_subtract_gradient_f32(Solver* s, const float* wu, const float* wv, const float* p,
                                   float* ou, float* ov);
-void launch_subtract_gradient_mixed(Solver* s, const float* wu, const float* wv, const double* p,
-                                    double* ou, double* ov);
+// double-float (MIXED) variants; lo planes of the input velocity may be nullptr
+void launch_div_df(Solver* s, const float* uh, const float* ul, const float* vh, const float* vl, float* dh,
+                   float* dl);
+void launch_subgrad_df(Solver* s, const float* wuh, const float* wul, const float* wvh, const float* wvl,
+                       const float* ph, const float* pl, float* uh, float* ul, float* vh, float* vl);
+void launch_d_to_df(Solver* s, const double* x, float* hi, float* lo, int64_t n);
+void launch_df_to_d(Solver* s, const float* hi, const float* lo, double* x, int64_t n);
+void launch_df_to_f(Solver* s, const float* hi, const float* lo, float* x, int64_t n);
 void launch_jacobi(Solver* s, const float* p, const float* d, float* out, float h2, int nx, int ny);
 void launch_rb_half(Solver* s, const float* src, const float* d, float* dst, float h2, int colour,
                     int nx, int ny);
@@ -156,10 +166,11 @@ void launch_restrict(Solver* s, const float* fine, float* coarse, int nc);
 void launch_prolong_add(Solver* s, const float* coarse, float* fine, int nf);
 void launch_fill(Solver* s, float* x, float value, int64_t n);
 void launch_fill64(Solver* s, double* x, double value, int64_t n);
-// mixed-precision refinement
-void launch_refine_init(Solver* s, const double* d, const double* p, float* r32, bool zero_p);
-void launch_refine_update(Solver* s, const double* p_in, const float* e, const double* d,
-                          double* p_out, float* r32);
+// mixed-precision refinement (double-float pressure and divergence)
+void launch_refine_init(Solver* s, const float* dh, const float* dl, const float* ph, const float* pl,
+                        float* r32, bool zero_p);
+void launch_refine_update(Solver* s, const float* ph, const float* pl, const float* e, const float* dh,
+                          const float* dl, float* poh, float* pol, float* r32);
 // reductions (results land in s->red_out)
 template <class T>
 void launch_absmax(Solver* s, const T* x, int64_t n, double* out_word);
@@ -167,7 +178,11 @@ void launch_absmax_residual32(Solver* s, const float* p, const float* d);
 void launch_poisson_norms(Solver* s, const float* p, const float* d, float h2f, double h2);
 void launch_convert(Solver* s, const void* src, int src_f64, void* dst, int dst_f64, int64_t n);
 
-// multigrid driver (fs_pressure.cu)
+// multigrid drivers: one pass per reference operation (fs_pressure.cu) and
+// the fused cycle (fs_multigrid.cu).  Both leave the result in lev[0].x; the
+// fused cycle may swap lev[0].x with lev[0].x2.
 void mg_vcycle(Solver* s);
+void mg_vcycle_fused(Solver* s, bool first_has_x);
+bool mg_fused_supported(const Solver* s);
 
 }  // namespace fs

@@ -14,7 +14,9 @@
 // the same colour, and a ping-pong pass is used to keep the reference result.
 #include <math.h>
 
+#include "fs_df.cuh"
 #include "fs_internal.cuh"
+#include "fs_stencil.cuh"
 
 namespace fs {
 
@@ -46,8 +48,6 @@ void launch_divergence(Solver* s, const TV* u, const TV* v, TD* d) {
                                                                                         g.ny, ix, iy));
 }
 template void launch_divergence<float, float>(Solver*, const float*, const float*, float*);
-template void launch_divergence<float, double>(Solver*, const float*, const float*, double*);
-template void launch_divergence<double, double>(Solver*, const double*, const double*, double*);
 
 // ------------------------------------------------------ gradient subtraction
 // u -= (p_i - p_{i-1})/dx, v -= (p_j - p_{j-1})/dy (grid.js:209-218)
@@ -63,19 +63,6 @@ __global__ void __launch_bounds__(256)
   ov[c] = __ldg(wv + c) - (pc - __ldg(p + (int64_t)jm * nx + i)) * idy;
 }
 
-__global__ void __launch_bounds__(256)
-    k_subgrad_mixed(const float* __restrict__ wu, const float* __restrict__ wv, const double* __restrict__ p,
-                    double* __restrict__ ou, double* __restrict__ ov, int nx, int ny, double idx,
-                    double idy) {
-  int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y;
-  if (i >= nx || j >= ny) return;
-  int im = i == 0 ? nx - 1 : i - 1, jm = j == 0 ? ny - 1 : j - 1;
-  int64_t c = (int64_t)j * nx + i;
-  double pc = __ldg(p + c);
-  ou[c] = (double)__ldg(wu + c) - (pc - __ldg(p + (int64_t)j * nx + im)) * idx;
-  ov[c] = (double)__ldg(wv + c) - (pc - __ldg(p + (int64_t)jm * nx + i)) * idy;
-}
-
 void launch_subtract_gradient_f32(Solver* s, const float* wu, const float* wv, const float* p,
                                   float* ou, float* ov) {
   const Grid& g = s->g;
@@ -83,14 +70,6 @@ void launch_subtract_gradient_f32(Solver* s, const float* wu, const float* wv, c
             k_subgrad_f32<<<grid2d(g.nx, g.ny, kBlock), kBlock, 0, s->stream>>>(wu, wv, p, ou, ov, g.nx,
                                                                                 g.ny, g.idx, g.idy));
 }
-void launch_subtract_gradient_mixed(Solver* s, const float* wu, const float* wv, const double* p,
-                                    double* ou, double* ov) {
-  const Grid& g = s->g;
-  FS_LAUNCH(s, "subtract_gradient", (double)s->n * 32,
-            k_subgrad_mixed<<<grid2d(g.nx, g.ny, kBlock), kBlock, 0, s->stream>>>(
-                wu, wv, p, ou, ov, g.nx, g.ny, g.idxd, g.idyd));
-}
-
 // ----------------------------------------------------------------- smoothers
 // damped Jacobi, omega = 1 (shaders.js:302-325)
 __global__ void __launch_bounds__(256) k_jacobi(const float* __restrict__ p, const float* __restrict__ d,
@@ -100,11 +79,8 @@ __global__ void __launch_bounds__(256) k_jacobi(const float* __restrict__ p, con
   int im = i == 0 ? nx - 1 : i - 1, ip = i + 1 == nx ? 0 : i + 1;
   int jm = j == 0 ? ny - 1 : j - 1, jp = j + 1 == ny ? 0 : j + 1;
   int64_t r = (int64_t)j * nx;
-  float s = __ldg(p + r + im) + __ldg(p + r + ip) + __ldg(p + (int64_t)jm * nx + i) +
-            __ldg(p + (int64_t)jp * nx + i);
-  float jac = (s - h2 * __ldg(d + r + i)) * 0.25f;
-  float cur = __ldg(p + r + i);
-  o[r + i] = cur + (jac - cur);
+  o[r + i] = gs_update(__ldg(p + r + i), __ldg(p + r + im), __ldg(p + r + ip), __ldg(p + (int64_t)jm * nx + i),
+                       __ldg(p + (int64_t)jp * nx + i), __ldg(d + r + i), h2);
 }
 
 void launch_jacobi(Solver* s, const float* p, const float* d, float* out, float h2, int nx, int ny) {
@@ -125,9 +101,8 @@ __global__ void __launch_bounds__(256) k_rb_half(const float* src, const float* 
   }
   int im = i == 0 ? nx - 1 : i - 1, ip = i + 1 == nx ? 0 : i + 1;
   int jm = j == 0 ? ny - 1 : j - 1, jp = j + 1 == ny ? 0 : j + 1;
-  float s = src[r + im] + src[r + ip] + src[(int64_t)jm * nx + i] + src[(int64_t)jp * nx + i];
-  float gs = (s - h2 * __ldg(d + r + i)) * 0.25f;
-  dst[r + i] = cur + (gs - cur);
+  dst[r + i] = gs_update(cur, src[r + im], src[r + ip], src[(int64_t)jm * nx + i], src[(int64_t)jp * nx + i],
+                         __ldg(d + r + i), h2);
 }
 
 void launch_rb_half(Solver* s, const float* src, const float* d, float* dst, float h2, int colour,
@@ -145,9 +120,8 @@ __global__ void __launch_bounds__(256) k_residual(const float* __restrict__ x, c
   int im = i == 0 ? n - 1 : i - 1, ip = i + 1 == n ? 0 : i + 1;
   int jm = j == 0 ? n - 1 : j - 1, jp = j + 1 == n ? 0 : j + 1;
   int64_t r = (int64_t)j * n;
-  float lap = (__ldg(x + r + im) + __ldg(x + r + ip) + __ldg(x + (int64_t)jm * n + i) +
-               __ldg(x + (int64_t)jp * n + i) - 4.f * __ldg(x + r + i)) / h2;
-  o[r + i] = __ldg(rhs + r + i) - lap;
+  o[r + i] = residual_at(__ldg(x + r + i), __ldg(x + r + im), __ldg(x + r + ip), __ldg(x + (int64_t)jm * n + i),
+                         __ldg(x + (int64_t)jp * n + i), __ldg(rhs + r + i), h2);
 }
 
 void launch_residual(Solver* s, const float* x, const float* rhs, float* out, float h2, int n) {
@@ -161,12 +135,8 @@ __global__ void __launch_bounds__(256) k_restrict(const float* __restrict__ f, f
   if (i >= nc || j >= nc) return;
   int nf = 2 * nc;
   int64_t r0 = (int64_t)(2 * j) * nf, r1 = r0 + nf;
-  float s = 0.f;
-  s = s + __ldg(f + r0 + 2 * i);
-  s = s + __ldg(f + r0 + 2 * i + 1);
-  s = s + __ldg(f + r1 + 2 * i);
-  s = s + __ldg(f + r1 + 2 * i + 1);
-  c[(int64_t)j * nc + i] = s * 0.25f;
+  c[(int64_t)j * nc + i] = restrict4(__ldg(f + r0 + 2 * i), __ldg(f + r0 + 2 * i + 1), __ldg(f + r1 + 2 * i),
+                                      __ldg(f + r1 + 2 * i + 1));
 }
 
 void launch_restrict(Solver* s, const float* fine, float* coarse, int nc) {
@@ -187,9 +157,8 @@ __global__ void __launch_bounds__(256) k_prolong_add(const float* __restrict__ c
   int x0 = wrapm(i0, nc), x1 = wrapm(i0 + 1, nc), y0 = wrapm(j0, nc), y1 = wrapm(j0 + 1, nc);
   float a = __ldg(c + (int64_t)y0 * nc + x0), b = __ldg(c + (int64_t)y0 * nc + x1);
   float cc = __ldg(c + (int64_t)y1 * nc + x0), d = __ldg(c + (int64_t)y1 * nc + x1);
-  float top = a * (1.f - fx) + b * fx, bot = cc * (1.f - fx) + d * fx;
   int64_t k = (int64_t)j * nf + i;
-  f[k] = f[k] + (top * (1.f - fy) + bot * fy);
+  f[k] = __fadd_rn(f[k], prolong_val(a, b, cc, d, fx, fy));
 }
 
 void launch_prolong_add(Solver* s, const float* coarse, float* fine, int nf) {
@@ -218,78 +187,116 @@ void launch_fill64(Solver* s, double* x, double value, int64_t n) {
 
 // ------------------------------------------------------------- reductions
 // Per-block partials, then the last block to finish folds them in a fixed
-// order, so every reduction is deterministic run to run.
+// order, so every reduction is deterministic run to run.  Max reductions stay
+// in f32 end to end (exact for a max, and off the FP64 pipe, which runs at
+// 1/54 of the FP32 rate on GB300); the f64 sums serve diagnostics only.
 struct RedCtx {
-  double* partials;  // 2 per block
+  double* partials;  // 2 per block (sums)
+  float* fpartials;  // 1 per block (max)
   unsigned* counter;
   double* out;       // out[0], out[1]
 };
 
-template <int OP>  // 0: max of a (b ignored), 1: sums of a and b
-__device__ __forceinline__ void block_reduce_finish(double a, double b, RedCtx ctx) {
-  __shared__ double sa[32], sb[32];
+__device__ __forceinline__ bool commit_partial_is_last(RedCtx ctx) {
   __shared__ bool last;
-  for (int o = 16; o > 0; o >>= 1) {
-    double oa = __shfl_xor_sync(0xffffffffu, a, o), ob = __shfl_xor_sync(0xffffffffu, b, o);
-    if (OP == 0) a = fmax(a, oa); else { a += oa; b += ob; }
-  }
-  int tid = threadIdx.y * blockDim.x + threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  int nwarp = (blockDim.x * blockDim.y + 31) >> 5;
-  if (lane == 0) { sa[warp] = a; sb[warp] = b; }
-  __syncthreads();
-  int bid = blockIdx.y * gridDim.x + blockIdx.x, nblk = gridDim.x * gridDim.y;
+  int tid = threadIdx.y * blockDim.x + threadIdx.x;
+  int nblk = gridDim.x * gridDim.y;
   if (tid == 0) {
-    double ta = sa[0], tb = sb[0];
-    for (int w = 1; w < nwarp; w++) {
-      if (OP == 0) ta = fmax(ta, sa[w]); else { ta += sa[w]; tb += sb[w]; }
-    }
-    ctx.partials[2 * bid] = ta;
-    ctx.partials[2 * bid + 1] = tb;
     __threadfence();
     unsigned done = atomicAdd(ctx.counter, 1u);
     last = done == (unsigned)nblk - 1;
   }
   __syncthreads();
-  if (!last) return;
-  __threadfence();
-  // fold partials: each thread a strided subset in fixed order, then the warps
-  double ta = OP == 0 ? 0.0 : 0.0, tb = 0.0;
-  int nthr = blockDim.x * blockDim.y;
+  if (last) __threadfence();
+  return last;
+}
+
+// every thread passes its value; the block max lands in out[0]
+__device__ __forceinline__ void block_max_finish(float m, RedCtx ctx) {
+  __shared__ float sm[32];
+  int tid = threadIdx.y * blockDim.x + threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  int nthr = blockDim.x * blockDim.y, nwarp = (nthr + 31) >> 5;
+  for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+  if (lane == 0) sm[warp] = m;
+  __syncthreads();
+  if (tid == 0) {
+    float t = sm[0];
+    for (int w = 1; w < nwarp; w++) t = fmaxf(t, sm[w]);
+    ctx.fpartials[blockIdx.y * gridDim.x + blockIdx.x] = t;
+  }
+  if (!commit_partial_is_last(ctx)) return;
+  int nblk = gridDim.x * gridDim.y;
+  float t = 0.f;
+  for (int k = tid; k < nblk; k += nthr) t = fmaxf(t, ((volatile float*)ctx.fpartials)[k]);
+  for (int o = 16; o > 0; o >>= 1) t = fmaxf(t, __shfl_xor_sync(0xffffffffu, t, o));
+  __syncthreads();
+  if (lane == 0) sm[warp] = t;
+  __syncthreads();
+  if (tid == 0) {
+    float f = sm[0];
+    for (int w = 1; w < nwarp; w++) f = fmaxf(f, sm[w]);
+    ctx.out[0] = (double)f;
+    *ctx.counter = 0;  // ready for the next reduction
+  }
+}
+
+// every thread passes (a, b); the block sums land in out[0], out[1] (f64)
+__device__ __forceinline__ void block_sum2_finish(double a, double b, RedCtx ctx) {
+  __shared__ double sa[32], sb[32];
+  int tid = threadIdx.y * blockDim.x + threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  int nthr = blockDim.x * blockDim.y, nwarp = (nthr + 31) >> 5;
+  for (int o = 16; o > 0; o >>= 1) {
+    a += __shfl_xor_sync(0xffffffffu, a, o);
+    b += __shfl_xor_sync(0xffffffffu, b, o);
+  }
+  if (lane == 0) { sa[warp] = a; sb[warp] = b; }
+  __syncthreads();
+  int bid = blockIdx.y * gridDim.x + blockIdx.x;
+  if (tid == 0) {
+    double ta = sa[0], tb = sb[0];
+    for (int w = 1; w < nwarp; w++) { ta += sa[w]; tb += sb[w]; }
+    ctx.partials[2 * bid] = ta;
+    ctx.partials[2 * bid + 1] = tb;
+  }
+  if (!commit_partial_is_last(ctx)) return;
+  int nblk = gridDim.x * gridDim.y;
+  double ta = 0.0, tb = 0.0;
   for (int k = tid; k < nblk; k += nthr) {
-    double pa = ((volatile double*)ctx.partials)[2 * k], pb = ((volatile double*)ctx.partials)[2 * k + 1];
-    if (OP == 0) ta = fmax(ta, pa); else { ta += pa; tb += pb; }
+    ta += ((volatile double*)ctx.partials)[2 * k];
+    tb += ((volatile double*)ctx.partials)[2 * k + 1];
   }
   for (int o = 16; o > 0; o >>= 1) {
-    double oa = __shfl_xor_sync(0xffffffffu, ta, o), ob = __shfl_xor_sync(0xffffffffu, tb, o);
-    if (OP == 0) ta = fmax(ta, oa); else { ta += oa; tb += ob; }
+    ta += __shfl_xor_sync(0xffffffffu, ta, o);
+    tb += __shfl_xor_sync(0xffffffffu, tb, o);
   }
   __syncthreads();
   if (lane == 0) { sa[warp] = ta; sb[warp] = tb; }
   __syncthreads();
   if (tid == 0) {
     double fa = sa[0], fb = sb[0];
-    for (int w = 1; w < nwarp; w++) {
-      if (OP == 0) fa = fmax(fa, sa[w]); else { fa += sa[w]; fb += sb[w]; }
-    }
+    for (int w = 1; w < nwarp; w++) { fa += sa[w]; fb += sb[w]; }
     ctx.out[0] = fa;
-    if (OP == 1) ctx.out[1] = fb;
-    *ctx.counter = 0;  // ready for the next reduction
+    ctx.out[1] = fb;
+    *ctx.counter = 0;
   }
 }
 
 // NaN must not vanish in a max: fmax(x, NaN) = x, so NaN is mapped to +inf.
 __device__ __forceinline__ double absnan(double x) { return x != x ? INFINITY : fabs(x); }
+__device__ __forceinline__ float absnanf(float x) { return x != x ? INFINITY : fabsf(x); }
 
 template <class T>
 __global__ void __launch_bounds__(256) k_absmax(const T* __restrict__ x, int64_t n, RedCtx ctx) {
-  double m = 0.0;
+  float m = 0.f;
   for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x)
-    m = fmax(m, absnan((double)__ldg(x + k)));
-  block_reduce_finish<0>(m, 0.0, ctx);
+    m = fmaxf(m, absnanf((float)__ldg(x + k)));
+  block_max_finish(m, ctx);
 }
 
 static RedCtx red_ctx(Solver* s, double* out) {
-  return RedCtx{s->red_partials, (unsigned*)(s->red_partials + 2 * s->red_cap), out};
+  // layout of red_partials: [2*cap doubles][cap floats][counter]
+  float* fp = (float*)(s->red_partials + 2 * s->red_cap);
+  return RedCtx{s->red_partials, fp, (unsigned*)(fp + s->red_cap), out};
 }
 static int red_blocks(Solver* s, int64_t n) {
   int64_t b = (n + 255) / 256;
@@ -322,7 +329,7 @@ __global__ void __launch_bounds__(256) k_poisson_norms(const float* __restrict__
     num = rr * rr;
     den = dd * dd;
   }
-  block_reduce_finish<1>(num, den, ctx);
+  block_sum2_finish(num, den, ctx);
 }
 
 void launch_poisson_norms(Solver* s, const float* p, const float* d, float h2f, double h2) {
@@ -335,86 +342,183 @@ void launch_poisson_norms(Solver* s, const float* p, const float* d, float h2f, 
 }
 
 // ------------------------------------------------ mixed-precision refinement
-// r = d - lap(p) in f64; r32 = (float) r; max|r| reduced.  With zero_p, r = d.
-__global__ void __launch_bounds__(256) k_refine_init(const double* __restrict__ d, const double* __restrict__ p,
-                                                     float* __restrict__ r32, int nx, int ny, double ih2x,
-                                                     double ih2y, int zero_p, RedCtx ctx) {
+// The MIXED mode keeps velocity, divergence and pressure as double-float
+// planes (hi, lo) and does this arithmetic on the FP32 pipe (fs_df.cuh).
+
+// divergence of (hi + lo) faces, lo planes optional (nullptr = 0):
+// d = (uR - uL)/dx + (vT - vB)/dy with every operation error-free or df
+__global__ void __launch_bounds__(256)
+    k_div_df(const float* __restrict__ uh, const float* __restrict__ ul, const float* __restrict__ vh,
+             const float* __restrict__ vl, float* __restrict__ dh, float* __restrict__ dl, int nx, int ny, df idx,
+             df idy) {
   int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y;
-  double m = 0.0;
+  if (i >= nx || j >= ny) return;
+  int ip = i + 1 == nx ? 0 : i + 1, jp = j + 1 == ny ? 0 : j + 1;
+  int64_t c = (int64_t)j * nx + i, cr = (int64_t)j * nx + ip, ct = (int64_t)jp * nx + i;
+  df du = two_diff(__ldg(uh + cr), __ldg(uh + c));
+  df dv = two_diff(__ldg(vh + ct), __ldg(vh + c));
+  if (ul) du = df_add(du, two_diff(__ldg(ul + cr), __ldg(ul + c)));
+  if (vl) dv = df_add(dv, two_diff(__ldg(vl + ct), __ldg(vl + c)));
+  df d = df_add(df_mul(du, idx), df_mul(dv, idy));
+  dh[c] = d.hi;
+  dl[c] = d.lo;
+}
+
+void launch_div_df(Solver* s, const float* uh, const float* ul, const float* vh, const float* vl, float* dh,
+                   float* dl) {
+  const Grid& g = s->g;
+  FS_LAUNCH(s, "divergence", (double)s->n * ((ul ? 16 : 8) + 8),
+            k_div_df<<<grid2d(g.nx, g.ny, kBlock), kBlock, 0, s->stream>>>(
+                uh, ul, vh, vl, dh, dl, g.nx, g.ny, df_host(g.idxd), df_host(g.idyd)));
+}
+
+// u = w - (p_i - p_{i-1})/dx, v = w - (p_j - p_{j-1})/dy in df; w lo planes optional
+__global__ void __launch_bounds__(256)
+    k_subgrad_df(const float* __restrict__ wuh, const float* __restrict__ wul, const float* __restrict__ wvh,
+                 const float* __restrict__ wvl, const float* __restrict__ ph, const float* __restrict__ pl,
+                 float* __restrict__ uh, float* __restrict__ ul, float* __restrict__ vh, float* __restrict__ vl,
+                 int nx, int ny, df idx, df idy) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y;
+  if (i >= nx || j >= ny) return;
+  int im = i == 0 ? nx - 1 : i - 1, jm = j == 0 ? ny - 1 : j - 1;
+  int64_t c = (int64_t)j * nx + i, cl = (int64_t)j * nx + im, cb = (int64_t)jm * nx + i;
+  df pc = {__ldg(ph + c), __ldg(pl + c)};
+  df gx = df_mul(df_sub(pc, df{__ldg(ph + cl), __ldg(pl + cl)}), idx);
+  df gy = df_mul(df_sub(pc, df{__ldg(ph + cb), __ldg(pl + cb)}), idy);
+  df wu = {__ldg(wuh + c), wul ? __ldg(wul + c) : 0.f};
+  df wv = {__ldg(wvh + c), wvl ? __ldg(wvl + c) : 0.f};
+  df u = df_sub(wu, gx), v = df_sub(wv, gy);
+  uh[c] = u.hi; ul[c] = u.lo;
+  vh[c] = v.hi; vl[c] = v.lo;
+}
+
+void launch_subgrad_df(Solver* s, const float* wuh, const float* wul, const float* wvh, const float* wvl,
+                       const float* ph, const float* pl, float* uh, float* ul, float* vh, float* vl) {
+  const Grid& g = s->g;
+  FS_LAUNCH(s, "subtract_gradient", (double)s->n * ((wul ? 16 : 8) + 8 + 16),
+            k_subgrad_df<<<grid2d(g.nx, g.ny, kBlock), kBlock, 0, s->stream>>>(
+                wuh, wul, wvh, wvl, ph, pl, uh, ul, vh, vl, g.nx, g.ny, df_host(g.idxd), df_host(g.idyd)));
+}
+
+// df Laplacian of p at (i, j): ((pl - pc) + (pr - pc)) / dx^2 + ((pb - pc) + (pt - pc)) / dy^2
+__device__ __forceinline__ df lap_df(df pc, df pl, df pr, df pb, df pt, df ih2x, df ih2y) {
+  df ax = df_add(df_sub(pl, pc), df_sub(pr, pc));
+  df ay = df_add(df_sub(pb, pc), df_sub(pt, pc));
+  return df_add(df_mul(ax, ih2x), df_mul(ay, ih2y));
+}
+
+// r = d - lap(p) (or r = d when zero_p); r32 = (float) r; max|r| reduced
+__global__ void __launch_bounds__(256)
+    k_refine_init(const float* __restrict__ dh, const float* __restrict__ dl, const float* __restrict__ ph,
+                  const float* __restrict__ pl, float* __restrict__ r32, int nx, int ny, df ih2x, df ih2y,
+                  int zero_p, RedCtx ctx) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y;
+  float m = 0.f;
   if (i < nx && j < ny) {
     int64_t r = (int64_t)j * nx, c = r + i;
-    double res = __ldg(d + c);
+    df res = {__ldg(dh + c), __ldg(dl + c)};
     if (!zero_p) {
       int im = i == 0 ? nx - 1 : i - 1, ip = i + 1 == nx ? 0 : i + 1;
       int jm = j == 0 ? ny - 1 : j - 1, jp = j + 1 == ny ? 0 : j + 1;
-      double pc = __ldg(p + c);
-      double lap = (__ldg(p + r + im) - 2.0 * pc + __ldg(p + r + ip)) * ih2x +
-                   (__ldg(p + (int64_t)jm * nx + i) - 2.0 * pc + __ldg(p + (int64_t)jp * nx + i)) * ih2y;
-      res = res - lap;
+      int64_t cl = r + im, cr = r + ip, cb = (int64_t)jm * nx + i, ct = (int64_t)jp * nx + i;
+      df lap = lap_df(df{__ldg(ph + c), __ldg(pl + c)}, df{__ldg(ph + cl), __ldg(pl + cl)},
+                      df{__ldg(ph + cr), __ldg(pl + cr)}, df{__ldg(ph + cb), __ldg(pl + cb)},
+                      df{__ldg(ph + ct), __ldg(pl + ct)}, ih2x, ih2y);
+      res = df_sub(res, lap);
     }
-    r32[c] = (float)res;
-    m = absnan(res);
+    float rf = df_to_f(res);
+    r32[c] = rf;
+    m = absnanf(rf);
   }
-  block_reduce_finish<0>(m, 0.0, ctx);
+  block_max_finish(m, ctx);
 }
 
-// p' = p + e; r = d - lap(p') in f64; r32 = (float) r; max|r| reduced
+// p' = p + e; r = d - lap(p') in df; r32 = (float) r; max|r| reduced
 __global__ void __launch_bounds__(256)
-    k_refine_update(const double* __restrict__ p, const float* __restrict__ e, const double* __restrict__ d,
-                    double* __restrict__ po, float* __restrict__ r32, int nx, int ny, double ih2x,
-                    double ih2y, RedCtx ctx) {
+    k_refine_update(const float* __restrict__ ph, const float* __restrict__ pl, const float* __restrict__ e,
+                    const float* __restrict__ dh, const float* __restrict__ dl, float* __restrict__ poh,
+                    float* __restrict__ pol, float* __restrict__ r32, int nx, int ny, df ih2x, df ih2y,
+                    RedCtx ctx) {
   int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y;
-  double m = 0.0;
+  float m = 0.f;
   if (i < nx && j < ny) {
     int im = i == 0 ? nx - 1 : i - 1, ip = i + 1 == nx ? 0 : i + 1;
     int jm = j == 0 ? ny - 1 : j - 1, jp = j + 1 == ny ? 0 : j + 1;
     int64_t r = (int64_t)j * nx, c = r + i;
     int64_t cl = r + im, cr = r + ip, cb = (int64_t)jm * nx + i, ct = (int64_t)jp * nx + i;
-    double pc = __ldg(p + c) + (double)__ldg(e + c);
-    double pl = __ldg(p + cl) + (double)__ldg(e + cl);
-    double pr = __ldg(p + cr) + (double)__ldg(e + cr);
-    double pb = __ldg(p + cb) + (double)__ldg(e + cb);
-    double pt = __ldg(p + ct) + (double)__ldg(e + ct);
-    double lap = (pl - 2.0 * pc + pr) * ih2x + (pb - 2.0 * pc + pt) * ih2y;
-    double res = __ldg(d + c) - lap;
-    po[c] = pc;
-    r32[c] = (float)res;
-    m = absnan(res);
+    df pc = df_add_f(df{__ldg(ph + c), __ldg(pl + c)}, __ldg(e + c));
+    df pL = df_add_f(df{__ldg(ph + cl), __ldg(pl + cl)}, __ldg(e + cl));
+    df pR = df_add_f(df{__ldg(ph + cr), __ldg(pl + cr)}, __ldg(e + cr));
+    df pB = df_add_f(df{__ldg(ph + cb), __ldg(pl + cb)}, __ldg(e + cb));
+    df pT = df_add_f(df{__ldg(ph + ct), __ldg(pl + ct)}, __ldg(e + ct));
+    df res = df_sub(df{__ldg(dh + c), __ldg(dl + c)}, lap_df(pc, pL, pR, pB, pT, ih2x, ih2y));
+    poh[c] = pc.hi;
+    pol[c] = pc.lo;
+    float rf = df_to_f(res);
+    r32[c] = rf;
+    m = absnanf(rf);
   }
-  block_reduce_finish<0>(m, 0.0, ctx);
+  block_max_finish(m, ctx);
 }
 
-void launch_refine_init(Solver* s, const double* d, const double* p, float* r32, bool zero_p) {
+void launch_refine_init(Solver* s, const float* dh, const float* dl, const float* ph, const float* pl,
+                        float* r32, bool zero_p) {
   const Grid& g = s->g;
   FS_LAUNCH(s, "refine_init", (double)s->n * (zero_p ? 12 : 20),
             k_refine_init<<<grid2d(g.nx, g.ny, kBlock), kBlock, 0, s->stream>>>(
-                d, p, r32, g.nx, g.ny, g.idxd * g.idxd, g.idyd * g.idyd, zero_p ? 1 : 0,
-                red_ctx(s, s->red_out)));
+                dh, dl, ph, pl, r32, g.nx, g.ny, df_host(g.idxd * g.idxd), df_host(g.idyd * g.idyd),
+                zero_p ? 1 : 0, red_ctx(s, s->red_out)));
 }
 
-void launch_refine_update(Solver* s, const double* p_in, const float* e, const double* d,
-                          double* p_out, float* r32) {
+void launch_refine_update(Solver* s, const float* ph, const float* pl, const float* e, const float* dh,
+                          const float* dl, float* poh, float* pol, float* r32) {
   const Grid& g = s->g;
   FS_LAUNCH(s, "refine_update", (double)s->n * 32,
             k_refine_update<<<grid2d(g.nx, g.ny, kBlock), kBlock, 0, s->stream>>>(
-                p_in, e, d, p_out, r32, g.nx, g.ny, g.idxd * g.idxd, g.idyd * g.idyd,
-                red_ctx(s, s->red_out)));
+                ph, pl, e, dh, dl, poh, pol, r32, g.nx, g.ny, df_host(g.idxd * g.idxd),
+                df_host(g.idyd * g.idyd), red_ctx(s, s->red_out)));
+}
+
+// ------------------------------------------------------- df <-> host types
+__global__ void k_d_to_df(const double* __restrict__ x, float* __restrict__ hi, float* __restrict__ lo, int64_t n) {
+  for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x) {
+    df v = df_from_d(x[k]);
+    hi[k] = v.hi;
+    lo[k] = v.lo;
+  }
+}
+__global__ void k_df_to_d(const float* __restrict__ hi, const float* __restrict__ lo, double* __restrict__ x, int64_t n) {
+  for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x)
+    x[k] = df_to_d(df{hi[k], lo ? lo[k] : 0.f});
+}
+__global__ void k_df_to_f(const float* __restrict__ hi, const float* __restrict__ lo, float* __restrict__ x, int64_t n) {
+  for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x)
+    x[k] = df_to_f(df{hi[k], lo[k]});
+}
+void launch_d_to_df(Solver* s, const double* x, float* hi, float* lo, int64_t n) {
+  FS_LAUNCH(s, "convert", (double)n * 16, k_d_to_df<<<fill_blocks(n), 256, 0, s->stream>>>(x, hi, lo, n));
+}
+void launch_df_to_d(Solver* s, const float* hi, const float* lo, double* x, int64_t n) {
+  FS_LAUNCH(s, "convert", (double)n * 16, k_df_to_d<<<fill_blocks(n), 256, 0, s->stream>>>(hi, lo, x, n));
+}
+void launch_df_to_f(Solver* s, const float* hi, const float* lo, float* x, int64_t n) {
+  FS_LAUNCH(s, "convert", (double)n * 12, k_df_to_f<<<fill_blocks(n), 256, 0, s->stream>>>(hi, lo, x, n));
 }
 
 // max|d - lap p| over an f32 pair (tolerance loop of the F32 mode)
 __global__ void __launch_bounds__(256) k_absmax_res32(const float* __restrict__ p, const float* __restrict__ d,
                                                       int nx, int ny, float ih2x, float ih2y, RedCtx ctx) {
   int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y;
-  double m = 0.0;
+  float m = 0.f;
   if (i < nx && j < ny) {
     int im = i == 0 ? nx - 1 : i - 1, ip = i + 1 == nx ? 0 : i + 1;
     int jm = j == 0 ? ny - 1 : j - 1, jp = j + 1 == ny ? 0 : j + 1;
     int64_t r = (int64_t)j * nx;
     float pc = p[r + i];
     float lap = (p[r + im] - 2.f * pc + p[r + ip]) * ih2x + (p[(int64_t)jm * nx + i] - 2.f * pc + p[(int64_t)jp * nx + i]) * ih2y;
-    m = absnan((double)(d[r + i] - lap));
+    m = absnanf(d[r + i] - lap);
   }
-  block_reduce_finish<0>(m, 0.0, ctx);
+  block_max_finish(m, ctx);
 }
 
 void launch_absmax_residual32(Solver* s, const float* p, const float* d) {

@@ -1,0 +1,47 @@
+// fs_stencil.cuh -- the per-cell arithmetic of the Poisson kernels, with every
+// rounding step spelled out.
+//
+// Both the one-pass-per-operation kernels and the fused multigrid kernels
+// call these, so the two paths round identically (nvcc would otherwise be free
+// to contract a*b + c*d either way round in different kernels).  The operand
+// order is the reference's: src/gpu/shaders.js RED_BLACK_GS / JACOBI
+// (l + r + b + t - h^2 d) / 4, multigrid.js RESIDUAL rhs - (l + r + b + t - 4c)/h^2
+// and PROLONG mix(mix(a, b, fx), mix(c, d, fx), fy).
+#pragma once
+
+#include <cuda_runtime.h>
+
+namespace fs {
+
+__device__ __forceinline__ float sum4(float l, float r, float b, float t) {
+  return __fadd_rn(__fadd_rn(__fadd_rn(l, r), b), t);
+}
+
+// Gauss-Seidel / Jacobi point update with omega = 1: cur + ((sum - h2 d)/4 - cur)
+__device__ __forceinline__ float gs_update(float cur, float l, float r, float b, float t, float d, float h2) {
+  float gs = __fmul_rn(__fmaf_rn(-h2, d, sum4(l, r, b, t)), 0.25f);
+  return __fadd_rn(cur, __fsub_rn(gs, cur));
+}
+
+// rhs - (l + r + b + t - 4c) / h2
+__device__ __forceinline__ float residual_at(float c, float l, float r, float b, float t, float rhs, float h2) {
+  float lap = __fdiv_rn(__fmaf_rn(-4.f, c, sum4(l, r, b, t)), h2);
+  return __fsub_rn(rhs, lap);
+}
+
+// a (1 - t) + b t
+__device__ __forceinline__ float mix_rn(float a, float b, float t) {
+  return __fmaf_rn(b, t, __fmul_rn(a, __fsub_rn(1.f, t)));
+}
+
+// bilinear prolongation sample; fx, fy are 1/4 or 3/4
+__device__ __forceinline__ float prolong_val(float a, float b, float c, float d, float fx, float fy) {
+  return mix_rn(mix_rn(a, b, fx), mix_rn(c, d, fx), fy);
+}
+
+// restriction: ((r00 + r10) + r01) + r11, times 1/4
+__device__ __forceinline__ float restrict4(float r00, float r10, float r01, float r11) {
+  return __fmul_rn(__fadd_rn(__fadd_rn(__fadd_rn(__fadd_rn(0.f, r00), r10), r01), r11), 0.25f);
+}
+
+}  // namespace fs

@@ -42,7 +42,7 @@ class GPUFluidSolver:
                  pressure_solver: str = "jacobi", pressure_iterations: int = 40, precision: str = "f32",
                  pressure_tol: float = 0.0, max_cycles: int = 50, mg_pre_smooth: int = 2,
                  mg_post_smooth: int = 2, mg_coarse_sweeps: int = 40, mg_min_size: int = 8,
-                 warm_start: bool = False, device: int = 0, **camel):
+                 warm_start: bool = False, device: int = 0, kernel_variant: int = 0, **camel):
         # accept the reference's camelCase option names too
         solid_mask_width = camel.pop("solidMaskWidth", solid_mask_width)
         pressure_solver = camel.pop("pressureSolver", pressure_solver)
@@ -73,6 +73,7 @@ class GPUFluidSolver:
         p.mg_coarse_sweeps, p.mg_min_size = mg_coarse_sweeps, mg_min_size
         p.warm_start = int(bool(warm_start))
         p.device = device
+        p.kernel_variant = kernel_variant
         h = C.c_void_p()
         L.check(lib.fs_create(C.byref(p), C.byref(h)), None)
         self._h = h

@@ -121,6 +121,9 @@ typedef struct fs_params {
                                  instead of zero (the reference zeroes it,
                                  solver.js:669-672) */
   int32_t device;             /* CUDA device ordinal (default 0) */
+  int32_t kernel_variant;     /* 0: fused multigrid kernels (default); 1: one kernel per
+                                 reference pass (RBGS colour, residual, restriction,
+                                 prolongation), kept to cross-check the fused cycle */
 } fs_params;
 
 /* one forcing mode, as setForcing's {kx, ky, phase} (solver.js:370-385) */
