@@ -137,6 +137,7 @@ SIGNATURES = {
     "fs_launch_count": (C.c_int64, [VP]),
     "fs_host_alloc": (VP, [C.c_size_t]),
     "fs_host_free": (None, [VP]),
+    "fs_max_divergence_noalloc": (I, [VP, VP, C.c_int32, C.c_int32, D, D, VP, VP]),
 }
 
 _lib = None

@@ -21,6 +21,9 @@ namespace fs {
 
 static thread_local std::string g_create_error;
 
+// message for fs_last_error(NULL) from entry points that take no handle
+void record_error(const std::string& msg) { g_create_error = msg; }
+
 // ------------------------------------------------------------------ errors
 static int fail(Solver* s, int code, const std::string& msg) {
   if (s) s->err = msg;

@@ -227,6 +227,32 @@ FS_API int64_t fs_launch_count(const fs_solver* s);
 FS_API void* fs_host_alloc(size_t bytes);
 FS_API void fs_host_free(void* p);
 
+/* ---------------------------------------------------- allocation-free entry */
+/* No counterpart in the reference.  max|div u| of an f32 MAC velocity field
+ * that the caller already holds on the CURRENT device (d_u, d_v: nx*ny floats,
+ * row-major), written as one double to the device pointer d_out, enqueued on
+ * `stream` (a cudaStream_t; NULL = the legacy default stream).
+ *
+ * For callers that cannot allocate device memory while they run -- hosts that
+ * reserve the GPU through their own pool, frame loops that must not call
+ * cudaMalloc/cudaFree (they can synchronise the device), code being recorded
+ * into a CUDA graph.  It calls no cudaMalloc, cudaFree or allocating library
+ * routine: its scratch (per-block maxima and an arrival counter) is a static
+ * device array of 65536 + 64 floats (256 KB) that every GPU loading the library
+ * holds until the process exits.
+ *
+ *  - Grids are limited to 65536 blocks of 32x8 cells (at most 16,777,216
+ *    cells, e.g. 4096 x 4096); larger grids return FS_ERR_INVALID_ARGUMENT.
+ *  - The first call on a device looks up the device address of that array
+ *    (with the device current); make that first call before any stream
+ *    capture begins.
+ *  - All calls share the one array: calls that can overlap on the GPU
+ *    (different streams, no ordering between them) race and may return
+ *    wrong maxima.  Each call clears the counter it needs before its kernel.
+ *  - On failure fs_last_error(NULL) returns the message. */
+FS_API int fs_max_divergence_noalloc(const float* d_u, const float* d_v, int32_t nx, int32_t ny, double lx,
+                                     double ly, double* d_out, void* stream);
+
 #ifdef __cplusplus
 }
 #endif
