@@ -13,6 +13,8 @@
 // ~2e-4 of a cell; the mathematics is otherwise identical.
 #include <math.h>
 
+#include <vector>
+
 #include "fs_internal.cuh"
 
 namespace fs {
@@ -191,10 +193,17 @@ void launch_diffuse(Solver* s, const float* u, const float* v, float* ou, float*
 }
 
 // FORCING + drag, in place (shaders.js:532-566): u <- u*exp(-drag dt) + amp dt/sqrt(M) sum_m
+// The phase drift is drift_rate * t with t read from the device step state, so
+// a captured step needs no host update per step (solver.js:396 passes
+// phaseDrift * t as param_b).
 __global__ void __launch_bounds__(256) k_forcing(float* __restrict__ u, float* __restrict__ v,
                                                  const float* __restrict__ modes, int m, int nx,
                                                  int ny, float dx, float dy, float scale, float damp,
-                                                 float drift) {
+                                                 double drift_rate, const DevState* __restrict__ st) {
+  __shared__ float s_drift;
+  if (threadIdx.x == 0 && threadIdx.y == 0) s_drift = (float)(drift_rate * st->t);
+  __syncthreads();
+  const float drift = s_drift;
   int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y;
   if (i >= nx || j >= ny) return;
   float pux = i * dx, puy = (j + 0.5f) * dy, pvx = (i + 0.5f) * dx, pvy = j * dy;
@@ -215,10 +224,9 @@ void launch_forcing(Solver* s, float* u, float* v, float dt) {
   const Grid& g = s->g;
   float scale = (float)(s->amp * dt / sqrt((double)s->n_modes));
   float damp = (float)exp(-s->drag * dt);
-  float drift = (float)(s->drift * s->t);
   FS_LAUNCH(s, "forcing", (double)s->n * 16,
             k_forcing<<<grid2d(g.nx, g.ny, kBlock), kBlock, 0, s->stream>>>(
-                u, v, s->modes, s->n_modes, g.nx, g.ny, g.dx, g.dy, scale, damp, drift));
+                u, v, s->modes, s->n_modes, g.nx, g.ny, g.dx, g.dy, scale, damp, s->drift, s->dev));
 }
 
 // Direct forcing of immersed disks (src/cpu/solid.js:165-233, shaders.js:587-653):
@@ -228,27 +236,32 @@ struct DiskDev {
   float x, y, r, vx, vy, omega, reach2;
 };
 #define FS_MAX_DISKS 64
-__constant__ DiskDev c_disks[FS_MAX_DISKS];
 
-__device__ __forceinline__ float wrap_delta(float d, float L) { return d - L * floorf(d / L + 0.5f); }
+// shortest signed separation on a periodic axis (src/cpu/solid.js:38-40), with 1/L precomputed
+__device__ __forceinline__ float wrap_delta(float d, float L, float iL) { return d - L * floorf(d * iL + 0.5f); }
 
+// One CTA per 32x8 tile from `tiles` (the tiles some disk can reach, listed
+// when the disks are set); cells elsewhere are left untouched.
 __global__ void __launch_bounds__(256)
-    k_solids(float* __restrict__ u, float* __restrict__ v, int ndisk, int nx, int ny, float dx,
+    k_solids(float* __restrict__ u, float* __restrict__ v, const DiskDev* __restrict__ disks, int ndisk,
+             const int* __restrict__ tiles, int nx, int ny, float dx,
              float dy, float lx, float ly, float width, double dA, float* __restrict__ imp,
              double* __restrict__ dimp) {
-  int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y;
+  const int t = __ldg(tiles + blockIdx.x), ntx = (nx + 31) >> 5;
+  int i = (t % ntx) * 32 + threadIdx.x, j = (t / ntx) * 8 + threadIdx.y;
   bool in = i < nx && j < ny;
   int64_t c = (int64_t)j * nx + i;
   float pux = i * dx, puy = (j + 0.5f) * dy, pvx = (i + 0.5f) * dx, pvy = j * dy;
+  const float ilx = 1.f / lx, ily = 1.f / ly;
   float uu = 0.f, vv = 0.f;
   bool loaded = false;
   float tix = 0.f, tiy = 0.f, tit = 0.f;
   for (int k = 0; k < ndisk; k++) {
-    const DiskDev d = c_disks[k];
+    const DiskDev d = disks[k];
     float fx = 0.f, fy = 0.f, tq = 0.f;
     if (in) {
-      float ax = wrap_delta(pux - d.x, lx), ay = wrap_delta(puy - d.y, ly);
-      float bx = wrap_delta(pvx - d.x, lx), by = wrap_delta(pvy - d.y, ly);
+      float ax = wrap_delta(pux - d.x, lx, ilx), ay = wrap_delta(puy - d.y, ly, ily);
+      float bx = wrap_delta(pvx - d.x, lx, ilx), by = wrap_delta(pvy - d.y, ly, ily);
       bool nu_ = ax * ax + ay * ay <= d.reach2, nv_ = bx * bx + by * by <= d.reach2;
       if ((nu_ || nv_) && !loaded) {
         uu = u[c];
@@ -306,11 +319,12 @@ __global__ void __launch_bounds__(256)
   }
 }
 
-void launch_solids(Solver* s, float* u, float* v, float dt, bool record_impulse) {
-  (void)dt;
+// Disk parameters go to the device once, when they are set; the per-step
+// launch then needs nothing from the host (and can be captured in a graph).
+int upload_disks(Solver* s) {
   const Grid& g = s->g;
   int nd = (int)s->disks.size();
-  if (nd == 0) return;
+  if (nd == 0) return 0;
   double width = s->prm.solid_mask_width * g.dxd;
   DiskDev hd[FS_MAX_DISKS];
   for (int k = 0; k < nd; k++) {
@@ -320,12 +334,48 @@ void launch_solids(Solver* s, float* u, float* v, float dt, bool record_impulse)
     hd[k] = {(float)d.x, (float)d.y, (float)d.r, (float)d.vx, (float)d.vy, (float)d.omega,
              (float)(reach * reach)};
   }
-  cudaMemcpyToSymbolAsync(c_disks, hd, sizeof(DiskDev) * nd, 0, cudaMemcpyHostToDevice, s->stream);
+  if (!s->d_disks && cudaMalloc(&s->d_disks, sizeof(DiskDev) * FS_MAX_DISKS) != cudaSuccess) return -1;
+  if (cudaMemcpy(s->d_disks, hd, sizeof(DiskDev) * nd, cudaMemcpyHostToDevice) != cudaSuccess) return -1;
+  // the 32x8 tiles any disk can reach (periodic), as a compact list
+  const int ntx = (g.nx + 31) / 32, nty = (g.ny + 7) / 8;
+  std::vector<char> mark((size_t)ntx * nty, 0);
+  for (int k = 0; k < nd; k++) {
+    const fs_disk& d = s->disks[k];
+    double reach = d.r + 7.0 * width + g.dxd + g.dyd;
+    int i0 = (int)floor((d.x - reach) / g.dxd) - 1, i1 = (int)ceil((d.x + reach) / g.dxd) + 1;
+    int j0 = (int)floor((d.y - reach) / g.dyd) - 1, j1 = (int)ceil((d.y + reach) / g.dyd) + 1;
+    if (i1 - i0 >= g.nx) { i0 = 0; i1 = g.nx - 1; }
+    if (j1 - j0 >= g.ny) { j0 = 0; j1 = g.ny - 1; }
+    for (int j = j0; j <= j1; j++)
+      for (int i = i0; i <= i1; i++) {
+        int wi = ((i % g.nx) + g.nx) % g.nx, wj = ((j % g.ny) + g.ny) % g.ny;
+        mark[(size_t)(wj / 8) * ntx + wi / 32] = 1;
+      }
+  }
+  std::vector<int> list;
+  for (size_t t = 0; t < mark.size(); t++)
+    if (mark[t]) list.push_back((int)t);
+  if (s->d_tiles) cudaFree(s->d_tiles);
+  s->d_tiles = nullptr;
+  s->n_tiles = (int)list.size();
+  if (cudaMalloc((void**)&s->d_tiles, sizeof(int) * list.size()) != cudaSuccess) return -1;
+  if (cudaMemcpy(s->d_tiles, list.data(), sizeof(int) * list.size(), cudaMemcpyHostToDevice) != cudaSuccess) return -1;
+  return 0;
+}
+
+void launch_solids(Solver* s, float* u, float* v, float dt, bool record_impulse) {
+  (void)dt;
+  const Grid& g = s->g;
+  int nd = (int)s->disks.size();
+  if (nd == 0) return;
+  double width = s->prm.solid_mask_width * g.dxd;
   cudaMemsetAsync(s->d_impulse, 0, sizeof(double) * 3 * nd, s->stream);
-  FS_LAUNCH(s, "solids", (double)s->n * (record_impulse ? 28 : 16),
-            k_solids<<<grid2d(g.nx, g.ny, kBlock), kBlock, 0, s->stream>>>(
-                u, v, nd, g.nx, g.ny, g.dx, g.dy, (float)(g.nx * g.dxd), (float)(g.ny * g.dyd),
-                (float)width, g.dxd * g.dyd, record_impulse ? s->imp : nullptr,
+  // the per-cell impulse field is only written inside the listed tiles
+  if (record_impulse) cudaMemsetAsync(s->imp, 0, sizeof(float) * 3 * (size_t)s->n, s->stream);
+  FS_LAUNCH(s, "solids", (double)s->n_tiles * 256 * (record_impulse ? 28 : 16),
+            k_solids<<<s->n_tiles, kBlock, 0, s->stream>>>(
+                u, v, (const DiskDev*)s->d_disks, nd, s->d_tiles, g.nx, g.ny, g.dx, g.dy, (float)(g.nx * g.dxd),
+                (float)(g.ny * g.dyd), (float)width, g.dxd * g.dyd, record_impulse ? s->imp : nullptr,
                 s->d_impulse));
 }
 

@@ -100,7 +100,10 @@ static void free_all(Solver* s) {
   for (size_t l = 1; l < s->lev.size(); l++) { f(s->lev[l].x); f(s->lev[l].x2); f(s->lev[l].rhs); }
   f(s->stage);
   f(s->red_partials); f(s->red_out); f(s->modes); f(s->imp); f(s->d_impulse);
+  f(s->dev); f(s->d_disks); f(s->d_tiles);
+  if (s->graph_exec) cudaGraphExecDestroy(s->graph_exec);
   if (s->h_red) cudaFreeHost(s->h_red);
+  if (s->body_stream) cudaStreamDestroy(s->body_stream);
   if (s->stream) cudaStreamDestroy(s->stream);
 }
 
@@ -216,10 +219,13 @@ static int create(const fs_params* prm, Solver* s) {
   // [2*cap f64 sums][cap f32 maxima][counter word]
   A(s->red_partials, double, 2 * (int64_t)s->red_cap + (s->red_cap + 2) / 2 + 1);
   A(s->red_out, double, 4);
+  A(s->dev, DevState, 1);
 #undef A
   CU(s, cudaMemsetAsync(s->red_partials, 0, (2 * (size_t)s->red_cap + (s->red_cap + 2) / 2 + 1) * sizeof(double),
                         s->stream));
   CU(s, cudaMallocHost((void**)&s->h_red, 4 * sizeof(double)));
+  CU(s, cudaMemsetAsync(s->dev, 0, sizeof(DevState), s->stream));
+  CU(s, cudaStreamCreateWithFlags(&s->body_stream, cudaStreamNonBlocking));
   // every field starts at zero
   CU(s, cudaMemsetAsync(s->u, 0, n * 4, s->stream));
   CU(s, cudaMemsetAsync(s->v, 0, n * 4, s->stream));
@@ -304,84 +310,150 @@ static void correction_solve(Solver* s, int iterations) {
   }
 }
 
-// Pressure solve from the divergence already in div32 / (dh, dl).
-// Tolerance loop: each cycle is `pressure_iterations` sweeps or V-cycles; in
-// the MIXED mode each cycle ends with the f64 update p += e, r = d - lap p.
-static int pressure_solve(Solver* s) {
-  const fs_params& P = s->prm;
-  const Grid& g = s->g;
-  int iters = P.pressure_iterations;
-  bool tol = P.pressure_tol > 0;
-  s->stats = fs_step_stats{0, 1, -1.0, -1.0};
-  if (!s->mixed) {
-    if (!P.warm_start) launch_fill(s, s->p32, 0.f, s->n);
-    if (!tol) {
-      poisson_f32(s, iters, P.warm_start != 0);
-      s->stats.cycles = iters;
-      return check_launch(s);
+// One cycle of the multigrid tolerance loop (both precisions):
+//   F32:   one V-cycle on (p32, div32) from the current p [+ max|div - lap p|]
+//   MIXED: one V-cycle on (r32 -> e) from zero, p += e (double-float), then
+//          r = d - lap p -> r32 and max|r|.
+// The fused F32 cycle always reads p (the zero-initial-guess shortcut would
+// change the kernel sequence from the first cycle to the next, which a
+// replayed loop body cannot do); reading a zero p gives the same bits.
+static void mg_cycle(Solver* s, bool residual) {
+  if (s->mixed) {
+    s->lev[0].x = s->e32;
+    s->lev[0].x2 = s->e32b;
+    if (s->fused) {
+      mg_vcycle_fused(s, false, s->ph, s->pl);
+      launch_refine_init(s, s->dh, s->dl, s->ph, s->pl, s->r32, false);
+    } else {
+      launch_fill(s, s->e32, 0.f, s->n);
+      mg_vcycle(s);
+      launch_refine_update(s, s->ph, s->pl, s->e32, s->dh, s->dl, s->pbh, s->pbl, s->r32);
+      std::swap(s->ph, s->pbh);
+      std::swap(s->pl, s->pbl);
     }
-    double m;
-    launch_absmax_residual32(s, s->p32, s->div32);
-    int rc = read_red(s, &m);
-    if (rc) return rc;
-    s->stats.residual_initial = m;
-    int c = 0;
-    while (!(m <= P.pressure_tol) && c < P.max_cycles && std::isfinite(m)) {
-      poisson_f32(s, iters, c > 0 || P.warm_start != 0);
-      launch_absmax_residual32(s, s->p32, s->div32);
-      if ((rc = read_red(s, &m))) return rc;
-      c++;
-    }
-    s->stats.cycles = c;
-    s->stats.residual_max = m;
-    s->stats.converged = m <= P.pressure_tol;
-    if (!std::isfinite(m)) return fail(s, FS_ERR_NONFINITE, "non-finite Poisson residual");
-    if (!s->stats.converged) return fail(s, FS_ERR_NOT_CONVERGED, "pressure tolerance not met within max_cycles");
-    return check_launch(s);
+    return;
   }
-  // MIXED: iterative refinement
-  launch_refine_init(s, s->dh, s->dl, s->ph, s->pl, s->r32, !P.warm_start);
-  if (!P.warm_start) {
-    launch_fill(s, s->ph, 0.f, s->n);
-    launch_fill(s, s->pl, 0.f, s->n);
-  }
-  double m = -1.0;
-  int rc;
-  if (tol) {
-    if ((rc = read_red(s, &m))) return rc;
-    s->stats.residual_initial = m;
-  }
-  int c = 0;
-  int cycles_fixed = 1;
-  while (true) {
-    if (tol) {
-      if (m <= P.pressure_tol || !std::isfinite(m) || c >= P.max_cycles) break;
-    } else if (c >= cycles_fixed) {
-      break;
-    }
-    correction_solve(s, iters);
+  s->lev[0].x = s->p32;
+  s->lev[0].x2 = s->p32b;
+  if (s->fused) mg_vcycle_fused(s, true);
+  else mg_vcycle(s);
+  s->p32 = s->lev[0].x;
+  s->p32b = s->lev[0].x2;
+  if (residual) launch_absmax_residual32(s, s->p32, s->div32);
+}
+
+// One cycle of the flat solvers: `iterations` sweeps; MIXED adds the
+// double-float update p += e, r = d - lap p.
+static void flat_cycle(Solver* s, int iterations, bool residual) {
+  if (s->mixed) {
+    correction_solve(s, iterations);
     launch_refine_update(s, s->ph, s->pl, s->e32, s->dh, s->dl, s->pbh, s->pbl, s->r32);
     std::swap(s->ph, s->pbh);
     std::swap(s->pl, s->pbl);
+    return;
+  }
+  poisson_f32(s, iterations, true);
+  if (residual) launch_absmax_residual32(s, s->p32, s->div32);
+}
+
+// Records the tolerance loop into a conditional WHILE node of the step graph
+// being captured on s->stream: k_cond (init) sets the condition from the
+// initial residual, the body is one multigrid cycle followed by k_cond (step).
+static int capture_tolerance_loop(Solver* s) {
+  cudaStreamCaptureStatus cst;
+  cudaGraph_t cg = nullptr;
+  const cudaGraphNode_t* deps = nullptr;
+  size_t nd = 0;
+  CU(s, cudaStreamGetCaptureInfo(s->stream, &cst, nullptr, &cg, &deps, nullptr, &nd));
+  cudaGraphConditionalHandle h;
+  CU(s, cudaGraphConditionalHandleCreate(&h, cg, 0, 0));
+  launch_cond_init(s, h, true);
+  CU(s, cudaStreamGetCaptureInfo(s->stream, &cst, nullptr, &cg, &deps, nullptr, &nd));
+  cudaGraphNodeParams cp = {};
+  cp.type = cudaGraphNodeTypeConditional;
+  cp.conditional.handle = h;
+  cp.conditional.type = cudaGraphCondTypeWhile;
+  cp.conditional.size = 1;
+  cudaGraphNode_t node;
+  CU(s, cudaGraphAddNode(&node, cg, deps, nullptr, nd, &cp));
+  cudaGraph_t body = cp.conditional.phGraph_out[0];
+  CU(s, cudaStreamUpdateCaptureDependencies(s->stream, &node, nullptr, 1, cudaStreamSetCaptureDependencies));
+  CU(s, cudaStreamBeginCaptureToGraph(s->body_stream, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
+  cudaStream_t main = s->stream;
+  s->stream = s->body_stream;
+  int64_t l0 = s->launches;
+  mg_cycle(s, true);
+  launch_cond_step(s, h, true);
+  s->graph_launches_body = s->launches - l0;
+  s->stream = main;
+  cudaGraph_t tmp = nullptr;
+  CU(s, cudaStreamEndCapture(s->body_stream, &tmp));
+  return check_launch(s);
+}
+
+// Pressure solve from the divergence already in div32 / (dh, dl).
+//  pressure_tol == 0: multigrid runs pressure_iterations cycles (V-cycles);
+//    Jacobi / red-black run pressure_iterations sweeps (MIXED: then one update).
+//  pressure_tol > 0: cycles (one V-cycle, or pressure_iterations sweeps) until
+//    max|div u| <= tol or max_cycles.  In a captured step the loop is a
+//    conditional node evaluated on the device; otherwise the host reads the
+//    residual after every cycle.
+static int pressure_solve(Solver* s, bool capture) {
+  const fs_params& P = s->prm;
+  const int iters = P.pressure_iterations;
+  const bool tol = P.pressure_tol > 0;
+  const bool mg = P.pressure_solver == FS_PRESSURE_MULTIGRID;
+  s->stats = fs_step_stats{0, 1, -1.0, -1.0};
+  s->stats_on_device = false;
+  if (s->mixed) {
+    launch_refine_init(s, s->dh, s->dl, s->ph, s->pl, s->r32, !P.warm_start);
+    if (!P.warm_start) {
+      launch_fill(s, s->ph, 0.f, s->n);
+      launch_fill(s, s->pl, 0.f, s->n);
+    }
+  } else {
+    if (!P.warm_start) launch_fill(s, s->p32, 0.f, s->n);
+    if (tol) launch_absmax_residual32(s, s->p32, s->div32);
+  }
+  if (!tol) {
+    if (mg) {
+      for (int k = 0; k < iters; k++) mg_cycle(s, false);
+    } else if (s->mixed) {
+      flat_cycle(s, iters, false);
+    } else {
+      poisson_f32(s, iters, P.warm_start != 0);
+    }
+    s->stats.cycles = mg ? iters : (s->mixed ? 1 : iters);
+    return check_launch(s);
+  }
+  if (capture) {
+    s->stats_on_device = true;
+    return capture_tolerance_loop(s);
+  }
+  double m;
+  int rc = read_red(s, &m);
+  if (rc) return rc;
+  s->stats.residual_initial = m;
+  int c = 0;
+  while (!(m <= P.pressure_tol) && c < P.max_cycles && std::isfinite(m)) {
+    if (mg) mg_cycle(s, true);
+    else flat_cycle(s, iters, true);
+    if ((rc = read_red(s, &m))) return rc;
     c++;
-    if (tol && (rc = read_red(s, &m))) return rc;
   }
   s->stats.cycles = c;
-  if (tol) {
-    s->stats.residual_max = m;
-    s->stats.converged = m <= P.pressure_tol;
-    if (!std::isfinite(m)) return fail(s, FS_ERR_NONFINITE, "non-finite Poisson residual");
-    if (!s->stats.converged) return fail(s, FS_ERR_NOT_CONVERGED, "pressure tolerance not met within max_cycles");
-  }
-  (void)g;
+  s->stats.residual_max = m;
+  s->stats.converged = m <= P.pressure_tol;
+  if (!std::isfinite(m)) return fail(s, FS_ERR_NONFINITE, "non-finite Poisson residual");
+  if (!s->stats.converged) return fail(s, FS_ERR_NOT_CONVERGED, "pressure tolerance not met within max_cycles");
   return check_launch(s);
 }
 
 // divergence of (wu, wv) -> solve -> state velocity = w - grad p
-static int project_from(Solver* s, const float* wu, const float* wv) {
+static int project_from(Solver* s, const float* wu, const float* wv, bool capture) {
   if (s->mixed) launch_div_df(s, wu, nullptr, wv, nullptr, s->dh, s->dl);
   else launch_divergence<float, float>(s, wu, wv, s->div32);
-  int rc = pressure_solve(s);
+  int rc = pressure_solve(s, capture);
   if (s->mixed) launch_subgrad_df(s, wu, nullptr, wv, nullptr, s->ph, s->pl, s->u, s->ulo, s->v, s->vlo);
   else launch_subtract_gradient_f32(s, wu, wv, s->p32, s->u, s->v);
   int rc2 = check_launch(s);
@@ -395,8 +467,8 @@ static void advect_into(Solver* s, float dt, float* ou, float* ov) {
   else launch_advect_sl<float>(s, s->u, s->v, ou, ov, dt);
 }
 
-// step(dt), solver.js:518-591
-static int step(Solver* s, double dt) {
+// step(dt), solver.js:518-591, enqueued on s->stream (eagerly or under capture)
+static int enqueue_step(Solver* s, double dt, bool capture) {
   float fdt = (float)dt;
   advect_into(s, fdt, s->wu, s->wv);
   float *cu = s->wu, *cv = s->wv;
@@ -406,7 +478,59 @@ static int step(Solver* s, double dt) {
   }
   if (s->n_modes > 0) launch_forcing(s, cu, cv, fdt);
   if (!s->disks.empty()) launch_solids(s, cu, cv, fdt, false);
-  int rc = project_from(s, cu, cv);
+  int rc = project_from(s, cu, cv, capture);
+  launch_step_finish(s, dt);
+  return rc;
+}
+
+static void drop_graph(Solver* s) {
+  if (s->graph_exec) cudaGraphExecDestroy(s->graph_exec);
+  s->graph_exec = nullptr;
+  s->graph_ok = false;
+}
+
+// Capture one step into a CUDA graph (the fused multigrid configurations):
+// every kernel argument is fixed for a given dt, the time the forcing needs
+// and the loop statistics live on the device.
+static int build_step_graph(Solver* s, double dt) {
+  drop_graph(s);
+  int64_t l0 = s->launches;
+  CU(s, cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal));
+  int rc = enqueue_step(s, dt, true);
+  cudaGraph_t g = nullptr;
+  cudaError_t e = cudaStreamEndCapture(s->stream, &g);
+  if (rc != FS_OK) {
+    if (g) cudaGraphDestroy(g);
+    return rc;
+  }
+  if (e != cudaSuccess) return fail(s, FS_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(e));
+  e = cudaGraphInstantiate(&s->graph_exec, g, 0);
+  cudaGraphDestroy(g);
+  if (e != cudaSuccess) return fail(s, FS_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(e));
+  int64_t captured = s->launches - l0;
+  s->graph_launches_fixed = captured - (s->prm.pressure_tol > 0 ? s->graph_launches_body : 0);
+  if (s->prm.pressure_tol <= 0) s->graph_launches_body = 0;
+  s->launches = l0;  // launches are counted when the graph runs
+  s->graph_dt = dt;
+  s->graph_ok = true;
+  return FS_OK;
+}
+
+static int step(Solver* s, double dt) {
+  if (s->fused && !s->profiling) {
+    if (!s->graph_ok || s->graph_dt != dt) {
+      int rc = build_step_graph(s, dt);
+      if (rc) return rc;
+    }
+    CU(s, cudaGraphLaunch(s->graph_exec, s->stream));
+    s->graph_replays++;
+    s->stats_on_device = s->prm.pressure_tol > 0;
+    if (!s->stats_on_device) s->stats = fs_step_stats{s->prm.pressure_iterations, 1, -1.0, -1.0};
+    s->t += dt;
+    s->steps++;
+    return FS_OK;
+  }
+  int rc = enqueue_step(s, dt, false);
   s->t += dt;
   s->steps++;
   return rc;
@@ -460,7 +584,7 @@ static int run_stage(Solver* s, int stage, double dt) {
       else launch_divergence<float, float>(s, s->u, s->v, s->div32);
       break;
     case FS_STAGE_PRESSURE: {
-      int rc = pressure_solve(s);
+      int rc = pressure_solve(s, false);
       if (rc) return rc;
       break;
     }
@@ -484,12 +608,12 @@ static int run_stage(Solver* s, int stage, double dt) {
         cudaMemcpyAsync(s->tu, s->ulo, s->n * 4, cudaMemcpyDeviceToDevice, s->stream);
         cudaMemcpyAsync(s->tv, s->vlo, s->n * 4, cudaMemcpyDeviceToDevice, s->stream);
         launch_div_df(s, s->wu, s->tu, s->wv, s->tv, s->dh, s->dl);
-        int rc = pressure_solve(s);
+        int rc = pressure_solve(s, false);
         launch_subgrad_df(s, s->wu, s->tu, s->wv, s->tv, s->ph, s->pl, s->u, s->ulo, s->v, s->vlo);
         if (rc) return rc;
       } else {
         state_to_w(s);
-        int rc = project_from(s, s->wu, s->wv);
+        int rc = project_from(s, s->wu, s->wv, false);
         if (rc) return rc;
       }
       break;
@@ -683,6 +807,7 @@ FS_API int fs_set_forcing(fs_solver* h, const fs_mode* modes, int count, double 
   if (count < 0 || (count > 0 && !modes)) return fail(s, FS_ERR_INVALID_ARGUMENT, "bad mode list");
   if (count > 4096) return fail(s, FS_ERR_INVALID_ARGUMENT, "at most 4096 forcing modes");
   CU(s, cudaStreamSynchronize(s->stream));
+  drop_graph(s);  // the captured step has or lacks a forcing kernel
   if (s->modes) { cudaFree(s->modes); s->modes = nullptr; }
   s->n_modes = 0;
   if (count == 0) return FS_OK;
@@ -704,6 +829,8 @@ FS_API int fs_set_solids(fs_solver* h, const fs_disk* disks, int count) {
   for (int k = 0; k < count; k++)
     if (!(disks[k].r > 0) || !std::isfinite(disks[k].x) || !std::isfinite(disks[k].y))
       return fail(s, FS_ERR_INVALID_ARGUMENT, "disk needs a finite centre and r > 0");
+  CU(s, cudaStreamSynchronize(s->stream));
+  drop_graph(s);  // the captured step has or lacks a solids kernel
   s->disks.assign(disks, disks + count);
   if (count > 0) {
     if (!s->imp) {
@@ -716,6 +843,7 @@ FS_API int fs_set_solids(fs_solver* h, const fs_disk* disks, int count) {
       CU(s, cudaMemsetAsync(s->d_impulse, 0, 3 * 64 * sizeof(double), s->stream));
       s->imp_cap = 64;
     }
+    if (upload_disks(s) != 0) return fail(s, FS_ERR_CUDA, "uploading the disk parameters failed");
   }
   return FS_OK;
 }
@@ -754,8 +882,19 @@ FS_API int fs_last_stats(fs_solver* h, fs_step_stats* out) {
   SOLVER(h);
   if (!out) return fail(s, FS_ERR_INVALID_ARGUMENT, "out is NULL");
   int rc = sync(s);
+  if (rc) return rc;
+  if (s->stats_on_device) {
+    // the last projection's loop ran inside a captured step
+    DevState d;
+    CU(s, cudaMemcpy(&d, s->dev, sizeof(DevState), cudaMemcpyDeviceToHost));
+    s->stats = fs_step_stats{d.cycles, d.converged, d.res_max, d.res_initial};
+    *out = s->stats;
+    if (d.nonfinite) return fail(s, FS_ERR_NONFINITE, "non-finite Poisson residual in the last step");
+    if (!d.converged) return fail(s, FS_ERR_NOT_CONVERGED, "pressure tolerance not met within max_cycles in the last step");
+    return FS_OK;
+  }
   *out = s->stats;
-  return rc;
+  return FS_OK;
 }
 
 FS_API int fs_get_time(const fs_solver* h, double* t, int64_t* steps) {
@@ -845,7 +984,20 @@ FS_API int fs_profile_step(fs_solver* h, double dt, int nsteps, fs_kernel_time* 
   return rc;
 }
 
-FS_API int64_t fs_launch_count(const fs_solver* h) { return h ? h->s.launches : 0; }
+FS_API int64_t fs_launch_count(const fs_solver* h) {
+  if (!h) return 0;
+  const Solver* s = &h->s;
+  int64_t n = s->launches + s->graph_replays * s->graph_launches_fixed;
+  if (s->graph_launches_body > 0) {
+    // the loop bodies run a device-decided number of times: count them from
+    // the device tally (this synchronises)
+    DevState d;
+    cudaStreamSynchronize(s->stream);
+    if (cudaMemcpy(&d, s->dev, sizeof(DevState), cudaMemcpyDeviceToHost) == cudaSuccess)
+      n += d.total_cycles * s->graph_launches_body;
+  }
+  return n;
+}
 
 FS_API void* fs_host_alloc(size_t bytes) {
   void* p = nullptr;

@@ -36,6 +36,18 @@ struct Level {
   float* rhs;
 };
 
+// step state kept on the device so that a captured step can run without the host
+struct DevState {
+  double t;            // simulation time
+  double res_initial;  // max|div| entering the last projection
+  double res_max;      // max|div| after it
+  long long total_cycles;  // cycles run by every projection since creation
+  int cycles;          // cycles the last projection ran
+  int converged;
+  int nonfinite;
+  int pad;
+};
+
 struct KernelStat {
   std::string name;
   int launches = 0;
@@ -99,6 +111,23 @@ struct Solver {
   float* imp = nullptr;         // 3 * n impulse field (x, y, torque)
   double* d_impulse = nullptr;  // 3 * disks
   int imp_cap = 0;
+  void* d_disks = nullptr;      // device copy of the disk parameters (set by fs_set_solids)
+  int* d_tiles = nullptr;       // 32x8 tiles any disk can reach
+  int n_tiles = 0;
+
+  // device-side step state: simulation time (read by the forcing kernel) and
+  // the statistics of the last projection (written by the tolerance loop)
+  DevState* dev = nullptr;
+
+  // CUDA graph of one step (fused multigrid configurations), captured per dt
+  cudaGraphExec_t graph_exec = nullptr;
+  double graph_dt = 0;
+  bool graph_ok = false;        // graph_exec matches the current forcing / solids
+  bool stats_on_device = false; // the last projection ran inside a graph
+  cudaStream_t body_stream = nullptr;  // captures the body of the tolerance loop
+  int64_t graph_launches_fixed = 0;    // kernels per replay outside the loop body
+  int64_t graph_launches_body = 0;     // kernels per loop iteration
+  int64_t graph_replays = 0;
 
   double t = 0;
   int64_t steps = 0;
@@ -143,6 +172,7 @@ void launch_advect_mc(Solver* s, const TV* u, const TV* v, float* fu, float* fv,
                       float* ov, float dt);
 void launch_diffuse(Solver* s, const float* u, const float* v, float* ou, float* ov, float dt);
 void launch_forcing(Solver* s, float* u, float* v, float dt);
+int upload_disks(Solver* s);
 void launch_solids(Solver* s, float* u, float* v, float dt, bool record_impulse);
 
 // fs_pressure.cu
@@ -175,6 +205,10 @@ void launch_refine_update(Solver* s, const float* ph, const float* pl, const flo
 template <class T>
 void launch_absmax(Solver* s, const T* x, int64_t n, double* out_word);
 void launch_absmax_residual32(Solver* s, const float* p, const float* d);
+// tolerance loop state on the device (fs_pressure.cu)
+void launch_cond_init(Solver* s, cudaGraphConditionalHandle h, bool graph);
+void launch_cond_step(Solver* s, cudaGraphConditionalHandle h, bool graph);
+void launch_step_finish(Solver* s, double dt);
 void launch_poisson_norms(Solver* s, const float* p, const float* d, float h2f, double h2);
 void launch_convert(Solver* s, const void* src, int src_f64, void* dst, int dst_f64, int64_t n);
 
@@ -182,7 +216,9 @@ void launch_convert(Solver* s, const void* src, int src_f64, void* dst, int dst_
 // the fused cycle (fs_multigrid.cu).  Both leave the result in lev[0].x; the
 // fused cycle may swap lev[0].x with lev[0].x2.
 void mg_vcycle(Solver* s);
-void mg_vcycle_fused(Solver* s, bool first_has_x);
+// acc_h/acc_l != nullptr: the level-0 up kernel adds its correction to the
+// double-float pressure (acc_h, acc_l) in place instead of writing lev[0].x2
+void mg_vcycle_fused(Solver* s, bool first_has_x, float* acc_h = nullptr, float* acc_l = nullptr);
 bool mg_fused_supported(const Solver* s);
 
 }  // namespace fs

@@ -24,84 +24,108 @@
 // (stride 2 in the row), hit consecutive words.
 #include <utility>
 
+#include "fs_df.cuh"
 #include "fs_internal.cuh"
 #include "fs_stencil.cuh"
 
 namespace fs {
 
-constexpr int kTile = 64;  // fine cells per tile side (even)
+// Fine cells per tile side (even).  Large levels use 64x64 tiles; the small
+// levels use 32 or 16 so that they still spread over >= 256 CTAs -- a level
+// with a handful of CTAs is bound by one CTA's serial latency, not by HBM.
 
 __device__ __forceinline__ int wrap_n(int i, int n) {
   i %= n;
   return i < 0 ? i + n : i;
 }
 
-// R x R region with split columns: cell (li, lj) at lj*R + (li&1)*(R/2) + (li>>1)
+// i in (-n, 2n): one correction wraps it (halo offsets are far below n)
+__device__ __forceinline__ int wrap1(int i, int n) { return i < 0 ? i + n : (i >= n ? i - n : i); }
+
+// Checkerboard layout of an R x R region (R even): the cells of one colour
+// (global parity of i + j) of row lj are stored contiguously, S = R/2 per
+// row, colour q in array q.  For a cell of colour q at (li, lj) with
+// b = index offset of its row, the four neighbours are all of colour 1-q at
+//   left  row*S + m,  right row*S + m + 1,  up/down (row -+ 1)*S + m + b
+// where li = 2m + 1 + b; array 1 starts at a word offset = 16 (mod 32) past
+// array 0 so that the paired writes of the staging loop never share a bank.
 template <int R>
-__device__ __forceinline__ int sidx(int li, int lj) {
-  return lj * R + (li & 1) * (R / 2) + (li >> 1);
-}
+struct Checker {
+  static constexpr int S = R / 2;
+  static constexpr int N = R * S;
+  static constexpr int PAD = (16 - (N % 32) + 32) % 32;
+  static constexpr int STRIDE = N + PAD;  // offset of colour 1
+  // position of (li, lj) given the parity par0 of the global index of (0, 0)
+  __device__ static __forceinline__ int at(int li, int lj, int par0) {
+    return ((par0 + li + lj) & 1) * STRIDE + lj * S + (li >> 1);
+  }
+};
 
 // One red-black half-sweep of colour c over li, lj in [1, R-2] (in place).
-// par0 is the parity of the global index of local (0, 0) (n even, so the
-// parity survives the periodic wrap).  Cells whose neighbours are stale give
-// stale values; they lie outside the valid region and are never written back.
+// Cells whose neighbours are stale give stale values; they lie outside the
+// valid region and are never written back.
 template <int R>
 __device__ __forceinline__ void rb_half_smem(float* xs, const float* rs, int c, int par0, float h2) {
-  constexpr int W = R - 2;   // rows / columns updated
-  constexpr int S = W / 2;   // cells of one colour per row
+  using CK = Checker<R>;
+  constexpr int S = CK::S;
+  constexpr int SW = S - 1;  // cells of one colour per row inside [1, R-2]
+  constexpr int W = R - 2;
   const int tid = threadIdx.y * blockDim.x + threadIdx.x, nthr = blockDim.x * blockDim.y;
-  for (int idx = tid; idx < W * S; idx += nthr) {
-    int row = idx / S, m = idx - row * S;
+  float* xc = xs + c * CK::STRIDE;             // colour c (updated)
+  const float* xo = xs + (1 - c) * CK::STRIDE; // colour 1-c (read)
+  const float* rc = rs + c * CK::STRIDE;
+  for (int idx = tid; idx < W * SW; idx += nthr) {
+    int row = idx / SW, m = idx - row * SW;
     int lj = 1 + row;
-    int li = (((par0 + 1 + lj) & 1) == c ? 1 : 2) + 2 * m;
-    int k = sidx<R>(li, lj);
-    xs[k] = gs_update(xs[k], xs[sidx<R>(li - 1, lj)], xs[sidx<R>(li + 1, lj)], xs[sidx<R>(li, lj - 1)],
-                      xs[sidx<R>(li, lj + 1)], rs[k], h2);
+    int b = ((par0 + 1 + lj) & 1) != c ? 1 : 0;  // first colour-c cell at li = 1 + b
+    int base = lj * S + m;
+    int k = base + b;
+    xc[k] = gs_update(xc[k], xo[base], xo[base + 1], xo[base + b - S], xo[base + b + S], rc[k], h2);
   }
 }
 
 // ------------------------------------------------------------------ down
 // H = 2 * pre + 1.  xin == nullptr means the level starts from zero; otherwise
 // xin and xout must differ (the halo of a tile is another tile's interior).
-template <int H>
+template <int T, int H>
 __global__ void __launch_bounds__(256) k_mg_down(const float* __restrict__ rhs, const float* __restrict__ xin,
                                                  float* __restrict__ xout, float* __restrict__ crhs, int n,
                                                  float h2, int pre) {
-  constexpr int R = kTile + 2 * H;
-  __shared__ float xs[R * R];
-  __shared__ float rs[R * R];
-  const int i0 = blockIdx.x * kTile, j0 = blockIdx.y * kTile;
+  constexpr int R = T + 2 * H;
+  using CK = Checker<R>;
+  __shared__ float xs[CK::STRIDE + CK::N];
+  __shared__ float rs[CK::STRIDE + CK::N];
+  const int i0 = blockIdx.x * T, j0 = blockIdx.y * T;
   const int gi0 = i0 - H, gj0 = j0 - H;
+  const int par0 = (gi0 + gj0) & 1;  // n even: the parity of the wrapped index is the same
   const int tid = threadIdx.y * blockDim.x + threadIdx.x, nthr = blockDim.x * blockDim.y;
   for (int k = tid; k < R * R; k += nthr) {
     int lj = k / R, li = k - lj * R;
-    int64_t g = (int64_t)wrap_n(gj0 + lj, n) * n + wrap_n(gi0 + li, n);
-    int s = sidx<R>(li, lj);
-    rs[s] = __ldg(rhs + g);
-    xs[s] = xin ? __ldg(xin + g) : 0.f;
+    int64_t g = (int64_t)wrap1(gj0 + lj, n) * n + wrap1(gi0 + li, n);
+    int q = CK::at(li, lj, par0);
+    rs[q] = __ldg(rhs + g);
+    xs[q] = xin ? __ldg(xin + g) : 0.f;
   }
   __syncthreads();
-  const int par0 = (gi0 + gj0) & 1;
   for (int s = 0; s < 2 * pre; s++) {
     rb_half_smem<R>(xs, rs, s & 1, par0, h2);
     __syncthreads();
   }
-  for (int k = tid; k < kTile * kTile; k += nthr) {
-    int y = k / kTile, x = k - y * kTile;
+  for (int k = tid; k < T * T; k += nthr) {
+    int y = k / T, x = k - y * T;
     int gi = i0 + x, gj = j0 + y;
-    if (gi < n && gj < n) xout[(int64_t)gj * n + gi] = xs[sidx<R>(H + x, H + y)];
+    if (gi < n && gj < n) xout[(int64_t)gj * n + gi] = xs[CK::at(H + x, H + y, par0)];
   }
   // residual on each 2x2 block and its restriction (multigrid.js:48-93)
   const int nc = n >> 1;
-  for (int k = tid; k < (kTile / 2) * (kTile / 2); k += nthr) {
-    int cj = k / (kTile / 2), ci = k - cj * (kTile / 2);
+  for (int k = tid; k < (T / 2) * (T / 2); k += nthr) {
+    int cj = k / (T / 2), ci = k - cj * (T / 2);
     float r4[4];
 #pragma unroll
     for (int q = 0; q < 4; q++) {
       int li = H + 2 * ci + (q & 1), lj = H + 2 * cj + (q >> 1);
-      r4[q] = residual_at(xs[sidx<R>(li, lj)], xs[sidx<R>(li - 1, lj)], xs[sidx<R>(li + 1, lj)],
-                          xs[sidx<R>(li, lj - 1)], xs[sidx<R>(li, lj + 1)], rs[sidx<R>(li, lj)], h2);
+      r4[q] = residual_at(xs[CK::at(li, lj, par0)], xs[CK::at(li - 1, lj, par0)], xs[CK::at(li + 1, lj, par0)],
+                          xs[CK::at(li, lj - 1, par0)], xs[CK::at(li, lj + 1, par0)], rs[CK::at(li, lj, par0)], h2);
     }
     int gci = (i0 >> 1) + ci, gcj = (j0 >> 1) + cj;
     if (gci < nc && gcj < nc) crhs[(int64_t)gcj * nc + gci] = restrict4(r4[0], r4[1], r4[2], r4[3]);
@@ -110,21 +134,27 @@ __global__ void __launch_bounds__(256) k_mg_down(const float* __restrict__ rhs, 
 
 // -------------------------------------------------------------------- up
 // H = 2 * post.  x += P(coarse) on the region, then the post sweeps.  xin and
-// xout must differ: the halo of a tile is another tile's interior.
-template <int H>
+// xout must differ: the halo of a tile is another tile's interior.  With ACC
+// (level 0 of a MIXED refinement cycle) the tile's correction is added to the
+// double-float pressure (ph, pl) in place instead of being written to xout:
+// each cell is read and written by its own tile only.
+template <int T, int H, bool ACC>
 __global__ void __launch_bounds__(256) k_mg_up(const float* __restrict__ rhs, const float* __restrict__ xin,
                                                float* __restrict__ xout, const float* __restrict__ xc, int n,
-                                               float h2, int post) {
-  constexpr int R = kTile + 2 * H;
-  __shared__ float xs[R * R];
-  __shared__ float rs[R * R];
-  const int i0 = blockIdx.x * kTile, j0 = blockIdx.y * kTile;
+                                               float h2, int post, float* __restrict__ ph,
+                                               float* __restrict__ pl) {
+  constexpr int R = T + 2 * H;
+  using CK = Checker<R>;
+  __shared__ float xs[CK::STRIDE + CK::N];
+  __shared__ float rs[CK::STRIDE + CK::N];
+  const int i0 = blockIdx.x * T, j0 = blockIdx.y * T;
   const int gi0 = i0 - H, gj0 = j0 - H;
+  const int par0 = (gi0 + gj0) & 1;
   const int tid = threadIdx.y * blockDim.x + threadIdx.x, nthr = blockDim.x * blockDim.y;
   const int nc = n >> 1;
   for (int k = tid; k < R * R; k += nthr) {
     int lj = k / R, li = k - lj * R;
-    int gi = wrap_n(gi0 + li, n), gj = wrap_n(gj0 + lj, n);
+    int gi = wrap1(gi0 + li, n), gj = wrap1(gj0 + lj, n);
     int64_t g = (int64_t)gj * n + gi;
     // PROLONG (multigrid.js:99-131): sample at ((i+1/2)/2 - 1/2, (j+1/2)/2 - 1/2)
     int ci0 = (gi & 1) ? (gi >> 1) : (gi >> 1) - 1;
@@ -134,20 +164,29 @@ __global__ void __launch_bounds__(256) k_mg_up(const float* __restrict__ rhs, co
     int y0 = cj0 < 0 ? cj0 + nc : cj0, y1 = cj0 + 1 >= nc ? cj0 + 1 - nc : cj0 + 1;
     float p = prolong_val(__ldg(xc + (int64_t)y0 * nc + x0), __ldg(xc + (int64_t)y0 * nc + x1),
                           __ldg(xc + (int64_t)y1 * nc + x0), __ldg(xc + (int64_t)y1 * nc + x1), fx, fy);
-    int s = sidx<R>(li, lj);
-    xs[s] = __fadd_rn(__ldg(xin + g), p);
-    rs[s] = __ldg(rhs + g);
+    int q = CK::at(li, lj, par0);
+    xs[q] = __fadd_rn(__ldg(xin + g), p);
+    rs[q] = __ldg(rhs + g);
   }
   __syncthreads();
-  const int par0 = (gi0 + gj0) & 1;
   for (int s = 0; s < 2 * post; s++) {
     rb_half_smem<R>(xs, rs, s & 1, par0, h2);
     __syncthreads();
   }
-  for (int k = tid; k < kTile * kTile; k += nthr) {
-    int y = k / kTile, x = k - y * kTile;
+  for (int k = tid; k < T * T; k += nthr) {
+    int y = k / T, x = k - y * T;
     int gi = i0 + x, gj = j0 + y;
-    if (gi < n && gj < n) xout[(int64_t)gj * n + gi] = xs[sidx<R>(H + x, H + y)];
+    if (gi < n && gj < n) {
+      int64_t g = (int64_t)gj * n + gi;
+      float e = xs[CK::at(H + x, H + y, par0)];
+      if (ACC) {
+        df p = df_add_f(df{ph[g], pl[g]}, e);
+        ph[g] = p.hi;
+        pl[g] = p.lo;
+      } else {
+        xout[g] = e;
+      }
+    }
   }
 }
 
@@ -244,7 +283,8 @@ __device__ void bottom_prolong(float* sm, const BottomLevels& L, int l, Group G)
 }
 
 __global__ void __launch_bounds__(1024) k_mg_bottom(const float* __restrict__ rhs_top, float* __restrict__ x_top,
-                                                    int has_x, BottomLevels L, int pre, int post, int coarse) {
+                                                    int has_x, BottomLevels L, int pre, int post, int coarse,
+                                                    float* __restrict__ acc_h, float* __restrict__ acc_l) {
   extern __shared__ float sm[];
   const int tid = threadIdx.x;
   const Group CTA{tid, (int)blockDim.x, false};
@@ -295,32 +335,226 @@ __global__ void __launch_bounds__(1024) k_mg_bottom(const float* __restrict__ rh
   }
   {
     const int n = L.n[0];
-    for (int k = tid; k < n * n; k += CTA.nthr) x_top[k] = sm[L.off_x[0] + k];
+    for (int k = tid; k < n * n; k += CTA.nthr) {
+      float e = sm[L.off_x[0] + k];
+      if (acc_h) {  // the whole hierarchy fits here: add the correction to the pressure
+        df p = df_add_f(df{acc_h[k], acc_l[k]}, e);
+        acc_h[k] = p.hi;
+        acc_l[k] = p.lo;
+      } else {
+        x_top[k] = e;
+      }
+    }
+  }
+}
+
+// ------------------------------------------------- bottom, power-of-two levels
+// The common case (n a power of two, coarsest level 8): the bottom levels are
+// N0, N0/2, ..., 8 with N0 <= 64, all sizes known at compile time, so cell
+// indices are shifts and masks.  Levels >= 32 run on the whole CTA (256
+// threads), levels <= 16 -- including the coarse sweeps -- on warp 0 alone,
+// where one lane updates one cell of the 8x8 level per half-sweep.  Same
+// arithmetic (fs_stencil.cuh) and order as the generic kernel above.
+struct BottomH2 {
+  float h2[4];
+};
+
+template <int N>
+constexpr int ilog2() {
+  return N <= 1 ? 0 : 1 + ilog2<N / 2>();
+}
+
+template <int N, bool WARP>
+__device__ __forceinline__ void p2_sync() {
+  if (WARP) __syncwarp();
+  else __syncthreads();
+}
+
+template <int N, bool WARP>
+__device__ void p2_smooth(float* x, const float* r, float h2, int sweeps) {
+  constexpr int HALF = N / 2, LH = ilog2<HALF>();
+  const int tid = WARP ? (int)(threadIdx.x & 31) : (int)threadIdx.x;
+  const int nthr = WARP ? 32 : (int)blockDim.x;
+  for (int s = 0; s < 2 * sweeps; s++) {
+    const int c = s & 1;
+    for (int idx = tid; idx < N * HALF; idx += nthr) {
+      int j = idx >> LH, m = idx & (HALF - 1);
+      int i = 2 * m + ((j + c) & 1);
+      int row = j * N, k = row + i;
+      int rm = ((j - 1) & (N - 1)) * N, rp = ((j + 1) & (N - 1)) * N;
+      x[k] = gs_update(x[k], x[row + ((i - 1) & (N - 1))], x[row + ((i + 1) & (N - 1))], x[rm + i], x[rp + i], r[k],
+                       h2);
+    }
+    p2_sync<N, WARP>();
+  }
+}
+
+// residual of level N restricted into (cr, cx = 0) of level N/2
+template <int N, bool WARP>
+__device__ void p2_restrict(const float* x, const float* r, float h2, float* cr, float* cx) {
+  constexpr int NC = N / 2, LC = ilog2<NC>();
+  const int tid = WARP ? (int)(threadIdx.x & 31) : (int)threadIdx.x;
+  const int nthr = WARP ? 32 : (int)blockDim.x;
+  for (int k = tid; k < NC * NC; k += nthr) {
+    int cj = k >> LC, ci = k & (NC - 1);
+    float r4[4];
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+      int i = 2 * ci + (q & 1), j = 2 * cj + (q >> 1);
+      int row = j * N;
+      int rm = ((j - 1) & (N - 1)) * N, rp = ((j + 1) & (N - 1)) * N;
+      r4[q] = residual_at(x[row + i], x[row + ((i - 1) & (N - 1))], x[row + ((i + 1) & (N - 1))], x[rm + i], x[rp + i],
+                          r[row + i], h2);
+    }
+    cr[k] = restrict4(r4[0], r4[1], r4[2], r4[3]);
+    cx[k] = 0.f;
+  }
+  p2_sync<N, WARP>();
+}
+
+// x (level N) += bilinear prolongation of c (level N/2)
+template <int N, bool WARP>
+__device__ void p2_prolong(float* x, const float* c) {
+  constexpr int NC = N / 2, LN = ilog2<N>();
+  const int tid = WARP ? (int)(threadIdx.x & 31) : (int)threadIdx.x;
+  const int nthr = WARP ? 32 : (int)blockDim.x;
+  for (int k = tid; k < N * N; k += nthr) {
+    int j = k >> LN, i = k & (N - 1);
+    int ci0 = (i & 1) ? (i >> 1) : (i >> 1) - 1;
+    int cj0 = (j & 1) ? (j >> 1) : (j >> 1) - 1;
+    float fx = (i & 1) ? 0.25f : 0.75f, fy = (j & 1) ? 0.25f : 0.75f;
+    int x0 = ci0 & (NC - 1), x1 = (ci0 + 1) & (NC - 1), y0 = (cj0 & (NC - 1)) * NC, y1 = ((cj0 + 1) & (NC - 1)) * NC;
+    x[k] = __fadd_rn(x[k], prolong_val(c[y0 + x0], c[y0 + x1], c[y1 + x0], c[y1 + x1], fx, fy));
+  }
+  p2_sync<N, WARP>();
+}
+
+// sub-cycle from level N down to 8 and back; levels <= 16 are called by warp 0 only
+template <int N>
+__device__ void p2_cycle(float* const* X, float* const* R, const BottomH2& H, int lvl, int pre, int post,
+                         int coarse) {
+  constexpr bool W = N <= 16;
+  if constexpr (N == 8) {
+    p2_smooth<8, true>(X[lvl], R[lvl], H.h2[lvl], coarse);
+  } else {
+    p2_smooth<N, W>(X[lvl], R[lvl], H.h2[lvl], pre);
+    p2_restrict<N, W>(X[lvl], R[lvl], H.h2[lvl], R[lvl + 1], X[lvl + 1]);
+    if constexpr (!W && N / 2 <= 16) {
+      if (threadIdx.x < 32) p2_cycle<N / 2>(X, R, H, lvl + 1, pre, post, coarse);
+      __syncthreads();
+    } else {
+      p2_cycle<N / 2>(X, R, H, lvl + 1, pre, post, coarse);
+    }
+    p2_prolong<N, W>(X[lvl], X[lvl + 1]);
+    p2_smooth<N, W>(X[lvl], R[lvl], H.h2[lvl], post);
+  }
+}
+
+template <int N0>
+__global__ void __launch_bounds__(256) k_mg_bottom_p2(const float* __restrict__ rhs_top, float* __restrict__ x_top,
+                                                      int has_x, BottomH2 H, int pre, int post, int coarse,
+                                                      float* __restrict__ acc_h, float* __restrict__ acc_l) {
+  constexpr int L = ilog2<N0>() - 2;  // levels N0 .. 8
+  constexpr int SZ = (N0 * N0 * 4 - 64) / 3 + 64;  // N0^2 + N0^2/4 + ... + 64
+  __shared__ float sx[SZ], sr[SZ];
+  float* X[4];
+  float* R[4];
+  {
+    int off = 0, n = N0;
+    for (int l = 0; l < L; l++) {
+      X[l] = sx + off;
+      R[l] = sr + off;
+      off += n * n;
+      n >>= 1;
+    }
+  }
+  const int tid = threadIdx.x;
+  for (int k = tid; k < N0 * N0; k += blockDim.x) {
+    R[0][k] = __ldg(rhs_top + k);
+    X[0][k] = has_x ? x_top[k] : 0.f;
+  }
+  __syncthreads();
+  if constexpr (N0 <= 16) {
+    if (tid < 32) p2_cycle<N0>(X, R, H, 0, pre, post, coarse);
+    __syncthreads();
+  } else {
+    p2_cycle<N0>(X, R, H, 0, pre, post, coarse);
+  }
+  for (int k = tid; k < N0 * N0; k += blockDim.x) {
+    float e = X[0][k];
+    if (acc_h) {
+      df p = df_add_f(df{acc_h[k], acc_l[k]}, e);
+      acc_h[k] = p.hi;
+      acc_l[k] = p.lo;
+    } else {
+      x_top[k] = e;
+    }
   }
 }
 
 // ------------------------------------------------------------------ host
 static const dim3 kTileBlock(32, 8);
 
-template <int H>
-static void down(Solver* s, Level& L, const Level& C, bool has_x) {
-  dim3 grid((L.n + kTile - 1) / kTile, (L.n + kTile - 1) / kTile);
+// tile side for a level of n cells: the largest of 64, 32, 16 that still
+// gives >= 256 CTAs (16 for the smallest levels)
+static int tile_for(int n) {
+  for (int t : {64, 32}) {
+    int c = (n + t - 1) / t;
+    if (c * c >= 256) return t;
+  }
+  return 16;
+}
+
+template <int T, int H>
+static void down_t(Solver* s, Level& L, const Level& C, bool has_x) {
+  dim3 grid((L.n + T - 1) / T, (L.n + T - 1) / T);
   double bytes = (double)L.n * L.n * (has_x ? 12.0 : 8.0) + (double)C.n * C.n * 4.0;
   float* out = has_x ? L.x2 : L.x;
   FS_LAUNCH(s, "mg_down", bytes,
-            k_mg_down<H><<<grid, kTileBlock, 0, s->stream>>>(L.rhs, has_x ? L.x : nullptr, out, C.rhs, L.n,
-                                                             L.h2, s->prm.mg_pre_smooth));
+            k_mg_down<T, H><<<grid, kTileBlock, 0, s->stream>>>(L.rhs, has_x ? L.x : nullptr, out, C.rhs, L.n,
+                                                                L.h2, s->prm.mg_pre_smooth));
   if (has_x) std::swap(L.x, L.x2);
 }
 
 template <int H>
-static void up(Solver* s, Level& L, const Level& C) {
-  dim3 grid((L.n + kTile - 1) / kTile, (L.n + kTile - 1) / kTile);
+static void down(Solver* s, Level& L, const Level& C, bool has_x) {
+  switch (tile_for(L.n)) {
+    case 64: down_t<64, H>(s, L, C, has_x); break;
+    case 32: down_t<32, H>(s, L, C, has_x); break;
+    default: down_t<16, H>(s, L, C, has_x); break;
+  }
+}
+
+template <int T, int H>
+static void up_t(Solver* s, Level& L, const Level& C, float* acc_h, float* acc_l) {
+  dim3 grid((L.n + T - 1) / T, (L.n + T - 1) / T);
+  if (acc_h) {
+    double bytes = (double)L.n * L.n * 24.0 + (double)C.n * C.n * 4.0;
+    FS_LAUNCH(s, "mg_up", bytes,
+              k_mg_up<T, H, true><<<grid, kTileBlock, 0, s->stream>>>(L.rhs, L.x, nullptr, C.x, L.n, L.h2,
+                                                                      s->prm.mg_post_smooth, acc_h, acc_l));
+    return;
+  }
   double bytes = (double)L.n * L.n * 12.0 + (double)C.n * C.n * 4.0;
   FS_LAUNCH(s, "mg_up", bytes,
-            k_mg_up<H><<<grid, kTileBlock, 0, s->stream>>>(L.rhs, L.x, L.x2, C.x, L.n, L.h2,
-                                                           s->prm.mg_post_smooth));
+            k_mg_up<T, H, false><<<grid, kTileBlock, 0, s->stream>>>(L.rhs, L.x, L.x2, C.x, L.n, L.h2,
+                                                                     s->prm.mg_post_smooth, nullptr, nullptr));
   std::swap(L.x, L.x2);
+}
+
+template <int H>
+static void up(Solver* s, Level& L, const Level& C, float* acc_h, float* acc_l) {
+  switch (tile_for(L.n)) {
+    case 64: up_t<64, H>(s, L, C, acc_h, acc_l); break;
+    case 32: up_t<32, H>(s, L, C, acc_h, acc_l); break;
+    default: up_t<16, H>(s, L, C, acc_h, acc_l); break;
+  }
+}
+
+static int ilog2_host(int n) {
+  int l = 0;
+  while (n > 1) { n >>= 1; l++; }
+  return l;
 }
 
 // first level of the bottom solve: every level from there down is <= 64
@@ -364,7 +598,7 @@ static size_t bottom_layout(const Solver* s, BottomLevels* B) {
   return (size_t)off * sizeof(float);
 }
 
-void mg_vcycle_fused(Solver* s, bool first_has_x) {
+void mg_vcycle_fused(Solver* s, bool first_has_x, float* acc_h, float* acc_l) {
   std::vector<Level>& L = s->lev;
   const int lb = bottom_first_level(s);
   const fs_params& P = s->prm;
@@ -376,20 +610,40 @@ void mg_vcycle_fused(Solver* s, bool first_has_x) {
       default: down<7>(s, L[l], L[l + 1], hx); break;
     }
   }
-  BottomLevels B;
-  size_t smem = bottom_layout(s, &B);
   int nb = L[lb].n;
-  int threads = std::min(1024, std::max(32, ((nb * nb / 4 + 31) / 32) * 32));
   bool hx = lb == 0 && first_has_x;
+  float* bah = lb == 0 ? acc_h : nullptr;
+  float* bal = lb == 0 ? acc_l : nullptr;
   double bytes = (double)nb * nb * (hx ? 12.0 : 8.0);
-  FS_LAUNCH(s, "mg_bottom", bytes,
-            k_mg_bottom<<<1, threads, smem, s->stream>>>(L[lb].rhs, L[lb].x, hx ? 1 : 0, B, P.mg_pre_smooth,
-                                                         P.mg_post_smooth, P.mg_coarse_sweeps));
+  // power-of-two bottom N0 .. 8 (N0 <= 64): the compile-time-size kernel
+  bool p2 = (nb & (nb - 1)) == 0 && nb >= 8 && nb <= 64 && L.back().n == 8 &&
+            (int)L.size() - lb == ilog2_host(nb) - 2;
+  if (p2) {
+    BottomH2 H{};
+    for (int k = 0; k < (int)L.size() - lb && k < 4; k++) H.h2[k] = L[lb + k].h2;
+#define FS_P2(N0)                                                                                               FS_LAUNCH(s, "mg_bottom", bytes,                                                                                        k_mg_bottom_p2<N0><<<1, 256, 0, s->stream>>>(L[lb].rhs, L[lb].x, hx ? 1 : 0, H, P.mg_pre_smooth,                                                           P.mg_post_smooth, P.mg_coarse_sweeps, bah, bal))
+    switch (nb) {
+      case 64: FS_P2(64); break;
+      case 32: FS_P2(32); break;
+      case 16: FS_P2(16); break;
+      default: FS_P2(8); break;
+    }
+#undef FS_P2
+  } else {
+    BottomLevels B;
+    size_t smem = bottom_layout(s, &B);
+    int threads = std::min(1024, std::max(32, ((nb * nb / 4 + 31) / 32) * 32));
+    FS_LAUNCH(s, "mg_bottom", bytes,
+              k_mg_bottom<<<1, threads, smem, s->stream>>>(L[lb].rhs, L[lb].x, hx ? 1 : 0, B, P.mg_pre_smooth,
+                                                           P.mg_post_smooth, P.mg_coarse_sweeps, bah, bal));
+  }
   for (int l = lb - 1; l >= 0; l--) {
+    float* ah = l == 0 ? acc_h : nullptr;
+    float* al = l == 0 ? acc_l : nullptr;
     switch (P.mg_post_smooth) {
-      case 1: up<2>(s, L[l], L[l + 1]); break;
-      case 2: up<4>(s, L[l], L[l + 1]); break;
-      default: up<6>(s, L[l], L[l + 1]); break;
+      case 1: up<2>(s, L[l], L[l + 1], ah, al); break;
+      case 2: up<4>(s, L[l], L[l + 1], ah, al); break;
+      default: up<6>(s, L[l], L[l + 1], ah, al); break;
     }
   }
 }

@@ -16,6 +16,7 @@
 
 #include "fs_df.cuh"
 #include "fs_internal.cuh"
+#include "fs_reduce.cuh"
 #include "fs_stencil.cuh"
 
 namespace fs {
@@ -185,100 +186,14 @@ void launch_fill64(Solver* s, double* x, double value, int64_t n) {
   FS_LAUNCH(s, "fill", (double)n * 8, k_fill64<<<fill_blocks(n), 256, 0, s->stream>>>(x, value, n));
 }
 
-// ------------------------------------------------------------- reductions
-// Per-block partials, then the last block to finish folds them in a fixed
-// order, so every reduction is deterministic run to run.  Max reductions stay
-// in f32 end to end (exact for a max, and off the FP64 pipe, which runs at
-// 1/54 of the FP32 rate on GB300); the f64 sums serve diagnostics only.
-struct RedCtx {
-  double* partials;  // 2 per block (sums)
-  float* fpartials;  // 1 per block (max)
-  unsigned* counter;
-  double* out;       // out[0], out[1]
-};
-
-__device__ __forceinline__ bool commit_partial_is_last(RedCtx ctx) {
-  __shared__ bool last;
-  int tid = threadIdx.y * blockDim.x + threadIdx.x;
-  int nblk = gridDim.x * gridDim.y;
-  if (tid == 0) {
-    __threadfence();
-    unsigned done = atomicAdd(ctx.counter, 1u);
-    last = done == (unsigned)nblk - 1;
-  }
-  __syncthreads();
-  if (last) __threadfence();
-  return last;
-}
-
-// every thread passes its value; the block max lands in out[0]
-__device__ __forceinline__ void block_max_finish(float m, RedCtx ctx) {
-  __shared__ float sm[32];
-  int tid = threadIdx.y * blockDim.x + threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  int nthr = blockDim.x * blockDim.y, nwarp = (nthr + 31) >> 5;
-  for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
-  if (lane == 0) sm[warp] = m;
-  __syncthreads();
-  if (tid == 0) {
-    float t = sm[0];
-    for (int w = 1; w < nwarp; w++) t = fmaxf(t, sm[w]);
-    ctx.fpartials[blockIdx.y * gridDim.x + blockIdx.x] = t;
-  }
-  if (!commit_partial_is_last(ctx)) return;
-  int nblk = gridDim.x * gridDim.y;
-  float t = 0.f;
-  for (int k = tid; k < nblk; k += nthr) t = fmaxf(t, ((volatile float*)ctx.fpartials)[k]);
-  for (int o = 16; o > 0; o >>= 1) t = fmaxf(t, __shfl_xor_sync(0xffffffffu, t, o));
-  __syncthreads();
-  if (lane == 0) sm[warp] = t;
-  __syncthreads();
-  if (tid == 0) {
-    float f = sm[0];
-    for (int w = 1; w < nwarp; w++) f = fmaxf(f, sm[w]);
-    ctx.out[0] = (double)f;
-    *ctx.counter = 0;  // ready for the next reduction
-  }
-}
-
-// every thread passes (a, b); the block sums land in out[0], out[1] (f64)
-__device__ __forceinline__ void block_sum2_finish(double a, double b, RedCtx ctx) {
-  __shared__ double sa[32], sb[32];
-  int tid = threadIdx.y * blockDim.x + threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  int nthr = blockDim.x * blockDim.y, nwarp = (nthr + 31) >> 5;
-  for (int o = 16; o > 0; o >>= 1) {
-    a += __shfl_xor_sync(0xffffffffu, a, o);
-    b += __shfl_xor_sync(0xffffffffu, b, o);
-  }
-  if (lane == 0) { sa[warp] = a; sb[warp] = b; }
-  __syncthreads();
-  int bid = blockIdx.y * gridDim.x + blockIdx.x;
-  if (tid == 0) {
-    double ta = sa[0], tb = sb[0];
-    for (int w = 1; w < nwarp; w++) { ta += sa[w]; tb += sb[w]; }
-    ctx.partials[2 * bid] = ta;
-    ctx.partials[2 * bid + 1] = tb;
-  }
-  if (!commit_partial_is_last(ctx)) return;
-  int nblk = gridDim.x * gridDim.y;
-  double ta = 0.0, tb = 0.0;
-  for (int k = tid; k < nblk; k += nthr) {
-    ta += ((volatile double*)ctx.partials)[2 * k];
-    tb += ((volatile double*)ctx.partials)[2 * k + 1];
-  }
-  for (int o = 16; o > 0; o >>= 1) {
-    ta += __shfl_xor_sync(0xffffffffu, ta, o);
-    tb += __shfl_xor_sync(0xffffffffu, tb, o);
-  }
-  __syncthreads();
-  if (lane == 0) { sa[warp] = ta; sb[warp] = tb; }
-  __syncthreads();
-  if (tid == 0) {
-    double fa = sa[0], fb = sb[0];
-    for (int w = 1; w < nwarp; w++) { fa += sa[w]; fb += sb[w]; }
-    ctx.out[0] = fa;
-    ctx.out[1] = fb;
-    *ctx.counter = 0;
-  }
+// Reduction kernels walk 32x8-cell tiles with a capped 1-D grid, so the
+// last-block fold reads at most kRedGrid partials (a fold over one partial per
+// tile of a 2048^2 grid, 16384 of them, was latency-bound at ~40 us).
+constexpr int kRedGrid = 152 * 8;
+__host__ __device__ __forceinline__ int ntiles(int nx, int ny) { return ((nx + 31) >> 5) * ((ny + 7) >> 3); }
+static int red_grid(int nx, int ny) {
+  int t = ntiles(nx, ny);
+  return t < kRedGrid ? t : kRedGrid;
 }
 
 // NaN must not vanish in a max: fmax(x, NaN) = x, so NaN is mapped to +inf.
@@ -293,13 +208,9 @@ __global__ void __launch_bounds__(256) k_absmax(const T* __restrict__ x, int64_t
   block_max_finish(m, ctx);
 }
 
-static RedCtx red_ctx(Solver* s, double* out) {
-  // layout of red_partials: [2*cap doubles][cap floats][counter]
-  float* fp = (float*)(s->red_partials + 2 * s->red_cap);
-  return RedCtx{s->red_partials, fp, (unsigned*)(fp + s->red_cap), out};
-}
 static int red_blocks(Solver* s, int64_t n) {
   int64_t b = (n + 255) / 256;
+  if (b > kRedGrid) b = kRedGrid;
   if (b > s->red_cap) b = s->red_cap;
   return (int)(b < 1 ? 1 : b);
 }
@@ -316,8 +227,10 @@ template void launch_absmax<double>(Solver*, const double*, int64_t, double*);
 // solver.js:878-895; h2 = dx*dx in f64 as the host computes it there)
 __global__ void __launch_bounds__(256) k_poisson_norms(const float* __restrict__ p, const float* __restrict__ d,
                                                        int nx, int ny, double h2, RedCtx ctx) {
-  int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y;
   double num = 0.0, den = 0.0;
+  const int ntx = (nx + 31) >> 5, nt = ntiles(nx, ny);
+  for (int t = blockIdx.x; t < nt; t += gridDim.x) {
+  int i = (t % ntx) * 32 + threadIdx.x, j = (t / ntx) * 8 + threadIdx.y;
   if (i < nx && j < ny) {
     int im = i == 0 ? nx - 1 : i - 1, ip = i + 1 == nx ? 0 : i + 1;
     int jm = j == 0 ? ny - 1 : j - 1, jp = j + 1 == ny ? 0 : j + 1;
@@ -326,8 +239,9 @@ __global__ void __launch_bounds__(256) k_poisson_norms(const float* __restrict__
                   (double)p[(int64_t)jp * nx + i] - 4.0 * (double)p[r + i]) / h2;
     double dd = (double)d[r + i];
     double rr = lap - dd;
-    num = rr * rr;
-    den = dd * dd;
+    num += rr * rr;
+    den += dd * dd;
+  }
   }
   block_sum2_finish(num, den, ctx);
 }
@@ -335,10 +249,9 @@ __global__ void __launch_bounds__(256) k_poisson_norms(const float* __restrict__
 void launch_poisson_norms(Solver* s, const float* p, const float* d, float h2f, double h2) {
   (void)h2f;
   const Grid& g = s->g;
-  dim3 grid = grid2d(g.nx, g.ny, kBlock);
-  if ((int64_t)grid.x * grid.y > s->red_cap) return;  // partial buffer sized for this grid at create
   FS_LAUNCH(s, "poisson_norms", (double)s->n * 8,
-            k_poisson_norms<<<grid, kBlock, 0, s->stream>>>(p, d, g.nx, g.ny, h2, red_ctx(s, s->red_out)));
+            k_poisson_norms<<<red_grid(g.nx, g.ny), kBlock, 0, s->stream>>>(p, d, g.nx, g.ny, h2,
+                                                                             red_ctx(s, s->red_out)));
 }
 
 // ------------------------------------------------ mixed-precision refinement
@@ -400,8 +313,19 @@ void launch_subgrad_df(Solver* s, const float* wuh, const float* wul, const floa
                 wuh, wul, wvh, wvl, ph, pl, uh, ul, vh, vl, g.nx, g.ny, df_host(g.idxd), df_host(g.idyd)));
 }
 
-// df Laplacian of p at (i, j): ((pl - pc) + (pr - pc)) / dx^2 + ((pb - pc) + (pt - pc)) / dy^2
+// df Laplacian of p at (i, j).  Square cells (ih2x == ih2y, the uniform
+// branch taken in practice): ((pl + pr) + (pb + pt) - 4 pc) / h^2 with the hi
+// parts combined error-free (two_sum, 4*x is exact) and the lo parts, each
+// below an ulp of p, summed in f32.  Otherwise the x and y second differences
+// are formed and scaled separately.  Both orders of evaluation are fixed, so
+// every kernel that calls this rounds alike.
 __device__ __forceinline__ df lap_df(df pc, df pl, df pr, df pb, df pt, df ih2x, df ih2y) {
+  if (ih2x.hi == ih2y.hi && ih2x.lo == ih2y.lo) {
+    df sum = df_add(two_sum(pl.hi, pr.hi), two_sum(pb.hi, pt.hi));
+    sum = df_add(sum, df{__fmul_rn(-4.f, pc.hi), 0.f});
+    float lo = __fsub_rn(__fadd_rn(__fadd_rn(pl.lo, pr.lo), __fadd_rn(pb.lo, pt.lo)), __fmul_rn(4.f, pc.lo));
+    return df_mul(df_add_f(sum, lo), ih2x);
+  }
   df ax = df_add(df_sub(pl, pc), df_sub(pr, pc));
   df ay = df_add(df_sub(pb, pc), df_sub(pt, pc));
   return df_add(df_mul(ax, ih2x), df_mul(ay, ih2y));
@@ -412,8 +336,10 @@ __global__ void __launch_bounds__(256)
     k_refine_init(const float* __restrict__ dh, const float* __restrict__ dl, const float* __restrict__ ph,
                   const float* __restrict__ pl, float* __restrict__ r32, int nx, int ny, df ih2x, df ih2y,
                   int zero_p, RedCtx ctx) {
-  int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y;
   float m = 0.f;
+  const int ntx = (nx + 31) >> 5, nt = ntiles(nx, ny);
+  for (int t = blockIdx.x; t < nt; t += gridDim.x) {
+  int i = (t % ntx) * 32 + threadIdx.x, j = (t / ntx) * 8 + threadIdx.y;
   if (i < nx && j < ny) {
     int64_t r = (int64_t)j * nx, c = r + i;
     df res = {__ldg(dh + c), __ldg(dl + c)};
@@ -428,7 +354,8 @@ __global__ void __launch_bounds__(256)
     }
     float rf = df_to_f(res);
     r32[c] = rf;
-    m = absnanf(rf);
+    m = fmaxf(m, absnanf(rf));
+  }
   }
   block_max_finish(m, ctx);
 }
@@ -439,8 +366,10 @@ __global__ void __launch_bounds__(256)
                     const float* __restrict__ dh, const float* __restrict__ dl, float* __restrict__ poh,
                     float* __restrict__ pol, float* __restrict__ r32, int nx, int ny, df ih2x, df ih2y,
                     RedCtx ctx) {
-  int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y;
   float m = 0.f;
+  const int ntx = (nx + 31) >> 5, nt = ntiles(nx, ny);
+  for (int t = blockIdx.x; t < nt; t += gridDim.x) {
+  int i = (t % ntx) * 32 + threadIdx.x, j = (t / ntx) * 8 + threadIdx.y;
   if (i < nx && j < ny) {
     int im = i == 0 ? nx - 1 : i - 1, ip = i + 1 == nx ? 0 : i + 1;
     int jm = j == 0 ? ny - 1 : j - 1, jp = j + 1 == ny ? 0 : j + 1;
@@ -456,7 +385,8 @@ __global__ void __launch_bounds__(256)
     pol[c] = pc.lo;
     float rf = df_to_f(res);
     r32[c] = rf;
-    m = absnanf(rf);
+    m = fmaxf(m, absnanf(rf));
+  }
   }
   block_max_finish(m, ctx);
 }
@@ -465,7 +395,7 @@ void launch_refine_init(Solver* s, const float* dh, const float* dl, const float
                         float* r32, bool zero_p) {
   const Grid& g = s->g;
   FS_LAUNCH(s, "refine_init", (double)s->n * (zero_p ? 12 : 20),
-            k_refine_init<<<grid2d(g.nx, g.ny, kBlock), kBlock, 0, s->stream>>>(
+            k_refine_init<<<red_grid(g.nx, g.ny), kBlock, 0, s->stream>>>(
                 dh, dl, ph, pl, r32, g.nx, g.ny, df_host(g.idxd * g.idxd), df_host(g.idyd * g.idyd),
                 zero_p ? 1 : 0, red_ctx(s, s->red_out)));
 }
@@ -474,7 +404,7 @@ void launch_refine_update(Solver* s, const float* ph, const float* pl, const flo
                           const float* dl, float* poh, float* pol, float* r32) {
   const Grid& g = s->g;
   FS_LAUNCH(s, "refine_update", (double)s->n * 32,
-            k_refine_update<<<grid2d(g.nx, g.ny, kBlock), kBlock, 0, s->stream>>>(
+            k_refine_update<<<red_grid(g.nx, g.ny), kBlock, 0, s->stream>>>(
                 ph, pl, e, dh, dl, poh, pol, r32, g.nx, g.ny, df_host(g.idxd * g.idxd),
                 df_host(g.idyd * g.idyd), red_ctx(s, s->red_out)));
 }
@@ -508,15 +438,18 @@ void launch_df_to_f(Solver* s, const float* hi, const float* lo, float* x, int64
 // max|d - lap p| over an f32 pair (tolerance loop of the F32 mode)
 __global__ void __launch_bounds__(256) k_absmax_res32(const float* __restrict__ p, const float* __restrict__ d,
                                                       int nx, int ny, float ih2x, float ih2y, RedCtx ctx) {
-  int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y;
   float m = 0.f;
+  const int ntx = (nx + 31) >> 5, nt = ntiles(nx, ny);
+  for (int t = blockIdx.x; t < nt; t += gridDim.x) {
+  int i = (t % ntx) * 32 + threadIdx.x, j = (t / ntx) * 8 + threadIdx.y;
   if (i < nx && j < ny) {
     int im = i == 0 ? nx - 1 : i - 1, ip = i + 1 == nx ? 0 : i + 1;
     int jm = j == 0 ? ny - 1 : j - 1, jp = j + 1 == ny ? 0 : j + 1;
     int64_t r = (int64_t)j * nx;
     float pc = p[r + i];
     float lap = (p[r + im] - 2.f * pc + p[r + ip]) * ih2x + (p[(int64_t)jm * nx + i] - 2.f * pc + p[(int64_t)jp * nx + i]) * ih2y;
-    m = absnanf(d[r + i] - lap);
+    m = fmaxf(m, absnanf(d[r + i] - lap));
+  }
   }
   block_max_finish(m, ctx);
 }
@@ -524,8 +457,46 @@ __global__ void __launch_bounds__(256) k_absmax_res32(const float* __restrict__ 
 void launch_absmax_residual32(Solver* s, const float* p, const float* d) {
   const Grid& g = s->g;
   FS_LAUNCH(s, "absmax_residual", (double)s->n * 8,
-            k_absmax_res32<<<grid2d(g.nx, g.ny, kBlock), kBlock, 0, s->stream>>>(
+            k_absmax_res32<<<red_grid(g.nx, g.ny), kBlock, 0, s->stream>>>(
                 p, d, g.nx, g.ny, g.idx * g.idx, g.idy * g.idy, red_ctx(s, s->red_out)));
+}
+
+// ------------------------------------------------- tolerance-loop bookkeeping
+// One thread: reads the max residual the last reduction left in red[0], keeps
+// the statistics in the device step state and, inside a captured step, sets
+// the condition of the WHILE node that repeats the refinement cycle.
+__global__ void k_cond(cudaGraphConditionalHandle h, int use_handle, const double* __restrict__ red,
+                       DevState* __restrict__ st, double tol, int max_cycles, int init) {
+  double m = red[0];
+  if (init) {
+    st->cycles = 0;
+    st->res_initial = m;
+  } else {
+    st->cycles += 1;
+    st->total_cycles += 1;
+  }
+  st->res_max = m;
+  bool finite = isfinite(m);
+  st->nonfinite = finite ? 0 : 1;
+  st->converged = (finite && m <= tol) ? 1 : 0;
+  bool again = finite && m > tol && st->cycles < max_cycles;
+  if (use_handle) cudaGraphSetConditional(h, again ? 1u : 0u);
+}
+
+__global__ void k_step_finish(DevState* __restrict__ st, double dt) { st->t += dt; }
+
+void launch_cond_init(Solver* s, cudaGraphConditionalHandle h, bool graph) {
+  FS_LAUNCH(s, "cond", 0.0,
+            k_cond<<<1, 1, 0, s->stream>>>(h, graph ? 1 : 0, s->red_out, s->dev, s->prm.pressure_tol,
+                                           s->prm.max_cycles, 1));
+}
+void launch_cond_step(Solver* s, cudaGraphConditionalHandle h, bool graph) {
+  FS_LAUNCH(s, "cond", 0.0,
+            k_cond<<<1, 1, 0, s->stream>>>(h, graph ? 1 : 0, s->red_out, s->dev, s->prm.pressure_tol,
+                                           s->prm.max_cycles, 0));
+}
+void launch_step_finish(Solver* s, double dt) {
+  FS_LAUNCH(s, "step_finish", 0.0, k_step_finish<<<1, 1, 0, s->stream>>>(s->dev, dt));
 }
 
 // ---------------------------------------------------------------- conversion

@@ -107,11 +107,14 @@ typedef struct fs_params {
   int32_t advection;          /* fs_advection (default MacCormack) */
   double solid_mask_width;    /* mask width in cells (default 1.5) */
   int32_t pressure_solver;    /* fs_pressure_solver (default Jacobi) */
-  int32_t pressure_iterations;/* sweeps (Jacobi, red-black) or V-cycles (multigrid)
-                                 per projection when pressure_tol == 0 (default 40) */
+  int32_t pressure_iterations;/* pressure_tol == 0: sweeps (Jacobi, red-black) or
+                                 V-cycles (multigrid) per projection (default 40);
+                                 pressure_tol > 0: sweeps per cycle (Jacobi, red-black) */
   int32_t precision;          /* fs_precision (default F32) */
-  double pressure_tol;        /* > 0: repeat cycles until max|div u| <= tol
-                                 (each cycle = pressure_iterations sweeps or V-cycles) */
+  double pressure_tol;        /* > 0: repeat cycles until max|div u| <= tol; a cycle is
+                                 one V-cycle (multigrid) or pressure_iterations sweeps.
+                                 In MIXED precision every cycle ends with the
+                                 double-float update p += e, r = d - lap p. */
   int32_t max_cycles;         /* cap of the tolerance loop (default 50) */
   int32_t mg_pre_smooth;      /* red-black sweeps before restriction (default 2) */
   int32_t mg_post_smooth;     /* red-black sweeps after prolongation (default 2) */
@@ -189,15 +192,20 @@ FS_API int fs_solid_impulse(fs_solver* s, double* out, int count);
 
 /* ------------------------------------------------------------------ step */
 /* step(dt) (solver.js:518-591): advect, diffuse, force, solids, project.
- * Enqueued on the solver's stream; returns without waiting unless the
- * tolerance loop is active, in which case the loop's convergence test reads
- * one residual word per cycle.  Returns FS_ERR_NOT_CONVERGED / FS_ERR_NONFINITE
- * when the tolerance loop fails (the step is still applied). */
+ * Fused multigrid configurations (kernel_variant 0) run the step as one CUDA
+ * graph, captured on the first call for a given dt; its tolerance loop is a
+ * conditional node decided on the device, so fs_step never waits, and a
+ * tolerance failure is reported by fs_last_stats.  Other configurations run
+ * eagerly; with pressure_tol > 0 they read one residual word per cycle and
+ * return FS_ERR_NOT_CONVERGED / FS_ERR_NONFINITE themselves (the step is
+ * still applied). */
 FS_API int fs_step(fs_solver* s, double dt);
 /* nsteps consecutive steps */
 FS_API int fs_advance(fs_solver* s, double dt, int nsteps);
 FS_API int fs_sync(fs_solver* s);
-/* statistics of the last projection; synchronises */
+/* statistics of the last projection; synchronises.  Returns
+ * FS_ERR_NOT_CONVERGED / FS_ERR_NONFINITE when that projection's tolerance
+ * loop failed inside a captured step. */
 FS_API int fs_last_stats(fs_solver* s, fs_step_stats* out);
 /* simulation time and step count (the public fields t and steps) */
 FS_API int fs_get_time(const fs_solver* s, double* t, int64_t* steps);
@@ -221,7 +229,8 @@ FS_API int fs_time_steps(fs_solver* s, double dt, int nsteps, double* elapsed_ms
  * (out has room for cap entries; *count gets the number written). */
 FS_API int fs_profile_step(fs_solver* s, double dt, int nsteps, fs_kernel_time* out, int cap,
                            int* count);
-/* Number of kernel launches enqueued by this handle since creation. */
+/* Number of kernels this handle has run since creation (graph replays
+ * included; synchronises when a captured tolerance loop has to be counted). */
 FS_API int64_t fs_launch_count(const fs_solver* s);
 /* Page-locked host memory for fast uploads and read-backs (cudaMallocHost). */
 FS_API void* fs_host_alloc(size_t bytes);

@@ -365,13 +365,14 @@ def test_bitwise_repeatable(G, O):
 
 # ---------------------------------------------------- fused multigrid cycle
 @pytest.mark.parametrize("precision", ["f32", "mixed"])
-@pytest.mark.parametrize("n", [64, 256, 320])
+@pytest.mark.parametrize("n", [64, 200, 256, 320, 1056])
 def test_fused_vcycle_bitwise_equals_one_pass_kernels(G, O, precision, n):
     """The fused V-cycle (tile kernels + one-CTA bottom solve) evaluates the same
     expressions in the same order as the one-kernel-per-pass path, so the two
-    agree bit for bit.  n = 64 runs entirely in the bottom kernel (with a
-    non-zero initial x on V-cycles 2 and 3 in F32), n = 320 has partial tiles
-    (80 = 64 + 16) and a 40 -> 20 -> 10 bottom."""
+    agree bit for bit.  n = 64 runs entirely in the power-of-two bottom kernel
+    (with a non-zero initial x on V-cycles 2 and 3 in F32); n = 200 has partial
+    16-cell tiles and a 50 -> 25 generic bottom with an odd coarsest level;
+    n = 1056 has partial 64-, 32- and 16-cell tiles and an odd 33 bottom."""
     u0, v0 = O.lcg_uv(4242, n * n)
     out = []
     for variant in (0, 1):
@@ -395,3 +396,50 @@ def test_fused_tolerance_loop_f32(G, O):
     st = s.last_stats()
     assert st["converged"] and st["cycles"] >= 2
     assert s.max_divergence() < 1.5e-3
+
+
+# ------------------------------------------------------------ CUDA graphs
+@pytest.mark.parametrize("precision", ["f32", "mixed"])
+def test_graph_step_equals_eager_step(G, O, precision):
+    """fs_step captures the fused configuration into a CUDA graph whose tolerance
+    loop is a conditional node; fs_profile_step runs the same kernels eagerly
+    with the host reading the residual.  Fields and cycle counts agree bit for
+    bit after three steps with solids and forcing."""
+    n = 256
+    u0, v0 = O.lcg_uv(123, n * n)
+    outs, cycles = [], []
+    for graph in (True, False):
+        s = G.GPUFluidSolver(n=n, nu=1e-3, advection="maccormack", pressure_solver="multigrid",
+                             pressure_iterations=1, precision=precision,
+                             pressure_tol=1e-6 if precision == "mixed" else 1e-3, max_cycles=40)
+        s.upload_velocity(u0, v0)
+        s.set_solids([(2.0, 3.0, 0.4)])
+        s.set_forcing([(4.0, 3.0, 0.2), (-2.0, 5.0, 1.0)], amplitude=0.5, drag=0.1)
+        if graph:
+            s.advance(0.01, 3)
+        else:
+            s.profile_step(0.01, 3)
+        cycles.append(s.last_stats()["cycles"])
+        outs.append(s.read_velocity())
+    assert cycles[0] == cycles[1] and cycles[0] > 1
+    assert np.array_equal(outs[0][0], outs[1][0]) and np.array_equal(outs[0][1], outs[1][1])
+
+
+def test_graph_step_reports_tolerance_failure(G, O):
+    n = 128
+    u0, v0 = O.lcg_uv(8, n * n)
+    s = G.GPUFluidSolver(n=n, pressure_solver="multigrid", pressure_iterations=1, precision="mixed",
+                         pressure_tol=1e-12, max_cycles=2)
+    s.upload_velocity(u0, v0)
+    s.step(0.01)  # enqueued; the failure is known only on the device
+    with pytest.raises(G.FluidError) as e:
+        s.last_stats()
+    assert e.value.status == 4
+    s2 = G.GPUFluidSolver(n=n, pressure_solver="multigrid", pressure_iterations=1, precision="mixed",
+                          pressure_tol=1e-6, max_cycles=40)
+    s2.upload_velocity(u0, v0)
+    l0 = s2.launch_count()
+    s2.advance(0.01, 2)
+    st = s2.last_stats()
+    assert st["converged"] and st["residual_max"] <= 1e-6
+    assert s2.launch_count() - l0 > 2 * 10 * st["cycles"] // 2
