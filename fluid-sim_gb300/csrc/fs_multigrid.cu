@@ -39,6 +39,8 @@ __device__ __forceinline__ int wrap_n(int i, int n) {
   return i < 0 ? i + n : i;
 }
 
+constexpr int kTileThreads = 256;  // threads of a tile kernel (32 x 8)
+
 // i in (-n, 2n): one correction wraps it (halo offsets are far below n)
 __device__ __forceinline__ int wrap1(int i, int n) { return i < 0 ? i + n : (i >= n ? i - n : i); }
 
@@ -63,24 +65,38 @@ struct Checker {
 
 // One red-black half-sweep of colour c over li, lj in [1, R-2] (in place).
 // Cells whose neighbours are stale give stale values; they lie outside the
-// valid region and are never written back.
+// valid region and are never written back.  Each thread walks one colour
+// column m down a chunk of rows: row lj's down neighbour is one of row lj-1's
+// left/right pair and its up neighbour one of row lj+1's, so a row costs two
+// new loads of the other colour (plus the cell and its rhs) instead of four.
 template <int R>
 __device__ __forceinline__ void rb_half_smem(float* xs, const float* rs, int c, int par0, float h2) {
   using CK = Checker<R>;
   constexpr int S = CK::S;
-  constexpr int SW = S - 1;  // cells of one colour per row inside [1, R-2]
-  constexpr int W = R - 2;
-  const int tid = threadIdx.y * blockDim.x + threadIdx.x, nthr = blockDim.x * blockDim.y;
-  float* xc = xs + c * CK::STRIDE;             // colour c (updated)
-  const float* xo = xs + (1 - c) * CK::STRIDE; // colour 1-c (read)
+  constexpr int SW = S - 1;              // cells of one colour per row inside [1, R-2]
+  constexpr int W = R - 2;               // rows
+  constexpr int NCH = kTileThreads / SW;  // row chunks
+  constexpr int CH = (W + NCH - 1) / NCH;
+  const int tid = threadIdx.y * blockDim.x + threadIdx.x;
+  const int chunk = tid / SW, m = tid - chunk * SW;
+  if (chunk >= NCH) return;
+  int lj = 1 + chunk * CH;
+  const int lend = min(lj + CH, W + 1);
+  if (lj >= lend) return;
+  float* xc = xs + c * CK::STRIDE;              // colour c (updated)
+  const float* xo = xs + (1 - c) * CK::STRIDE;  // colour 1-c (read)
   const float* rc = rs + c * CK::STRIDE;
-  for (int idx = tid; idx < W * SW; idx += nthr) {
-    int row = idx / SW, m = idx - row * SW;
-    int lj = 1 + row;
-    int b = ((par0 + 1 + lj) & 1) != c ? 1 : 0;  // first colour-c cell at li = 1 + b
-    int base = lj * S + m;
+  int b = ((par0 + 1 + lj) & 1) != c ? 1 : 0;   // first colour-c cell of row lj at li = 1 + b
+  int base = lj * S + m;
+  float pl = xo[base - S], pr = xo[base - S + 1];  // row lj - 1
+  float cl = xo[base], cr = xo[base + 1];          // row lj
+  for (; lj < lend; lj++) {
+    float nl = xo[base + S], nr = xo[base + S + 1];  // row lj + 1
     int k = base + b;
-    xc[k] = gs_update(xc[k], xo[base], xo[base + 1], xo[base + b - S], xo[base + b + S], rc[k], h2);
+    xc[k] = gs_update(xc[k], cl, cr, b ? pr : pl, b ? nr : nl, rc[k], h2);
+    pl = cl; pr = cr; cl = nl; cr = nr;
+    base += S;
+    b ^= 1;
   }
 }
 
@@ -493,7 +509,7 @@ __global__ void __launch_bounds__(256) k_mg_bottom_p2(const float* __restrict__ 
 }
 
 // ------------------------------------------------------------------ host
-static const dim3 kTileBlock(32, 8);
+static const dim3 kTileBlock(32, kTileThreads / 32);
 
 // tile side for a level of n cells: the largest of 64, 32, 16 that still
 // gives >= 256 CTAs (16 for the smallest levels)

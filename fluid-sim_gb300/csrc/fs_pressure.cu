@@ -190,11 +190,19 @@ void launch_fill64(Solver* s, double* x, double value, int64_t n) {
 // last-block fold reads at most kRedGrid partials (a fold over one partial per
 // tile of a 2048^2 grid, 16384 of them, was latency-bound at ~40 us).
 constexpr int kRedGrid = 152 * 8;
-__host__ __device__ __forceinline__ int ntiles(int nx, int ny) { return ((nx + 31) >> 5) * ((ny + 7) >> 3); }
-static int red_grid(int nx, int ny) {
-  int t = ntiles(nx, ny);
-  return t < kRedGrid ? t : kRedGrid;
+// a 2-D grid over tile columns and rows (no index division in the walk)
+static dim3 red_grid2(int nx, int ny) {
+  int ntx = (nx + 31) >> 5, nty = (ny + 7) >> 3;
+  int gx = ntx < kRedGrid ? ntx : kRedGrid;
+  int gy = kRedGrid / gx;
+  if (gy > nty) gy = nty;
+  return dim3(gx, gy < 1 ? 1 : gy);
 }
+
+// 2-D tile walk of the capped reduction grid: tile (tx, ty) of 32x8 cells
+#define FOR_RED_TILES(nx, ny)                                                          \
+  for (int ty = blockIdx.y, nty_ = ((ny) + 7) >> 3; ty < nty_; ty += gridDim.y)        \
+    for (int tx = blockIdx.x, ntx_ = ((nx) + 31) >> 5; tx < ntx_; tx += gridDim.x)
 
 // NaN must not vanish in a max: fmax(x, NaN) = x, so NaN is mapped to +inf.
 __device__ __forceinline__ double absnan(double x) { return x != x ? INFINITY : fabs(x); }
@@ -228,9 +236,8 @@ template void launch_absmax<double>(Solver*, const double*, int64_t, double*);
 __global__ void __launch_bounds__(256) k_poisson_norms(const float* __restrict__ p, const float* __restrict__ d,
                                                        int nx, int ny, double h2, RedCtx ctx) {
   double num = 0.0, den = 0.0;
-  const int ntx = (nx + 31) >> 5, nt = ntiles(nx, ny);
-  for (int t = blockIdx.x; t < nt; t += gridDim.x) {
-  int i = (t % ntx) * 32 + threadIdx.x, j = (t / ntx) * 8 + threadIdx.y;
+  FOR_RED_TILES(nx, ny) {
+  int i = tx * 32 + threadIdx.x, j = ty * 8 + threadIdx.y;
   if (i < nx && j < ny) {
     int im = i == 0 ? nx - 1 : i - 1, ip = i + 1 == nx ? 0 : i + 1;
     int jm = j == 0 ? ny - 1 : j - 1, jp = j + 1 == ny ? 0 : j + 1;
@@ -250,7 +257,7 @@ void launch_poisson_norms(Solver* s, const float* p, const float* d, float h2f, 
   (void)h2f;
   const Grid& g = s->g;
   FS_LAUNCH(s, "poisson_norms", (double)s->n * 8,
-            k_poisson_norms<<<red_grid(g.nx, g.ny), kBlock, 0, s->stream>>>(p, d, g.nx, g.ny, h2,
+            k_poisson_norms<<<red_grid2(g.nx, g.ny), kBlock, 0, s->stream>>>(p, d, g.nx, g.ny, h2,
                                                                              red_ctx(s, s->red_out)));
 }
 
@@ -319,43 +326,83 @@ void launch_subgrad_df(Solver* s, const float* wuh, const float* wul, const floa
 // below an ulp of p, summed in f32.  Otherwise the x and y second differences
 // are formed and scaled separately.  Both orders of evaluation are fixed, so
 // every kernel that calls this rounds alike.
-__device__ __forceinline__ df lap_df(df pc, df pl, df pr, df pb, df pt, df ih2x, df ih2y) {
-  if (ih2x.hi == ih2y.hi && ih2x.lo == ih2y.lo) {
-    df sum = df_add(two_sum(pl.hi, pr.hi), two_sum(pb.hi, pt.hi));
-    sum = df_add(sum, df{__fmul_rn(-4.f, pc.hi), 0.f});
-    float lo = __fsub_rn(__fadd_rn(__fadd_rn(pl.lo, pr.lo), __fadd_rn(pb.lo, pt.lo)), __fmul_rn(4.f, pc.lo));
-    return df_mul(df_add_f(sum, lo), ih2x);
+// Scale of the 5-point Laplacian.  mode 0: square cells and 1/dx^2 a power of
+// two (the unit domain at power-of-two n), so scaling is one exact multiply;
+// mode 1: square cells, df scale; mode 2: dx != dy.
+struct LapScale {
+  df ih2x, ih2y;
+  int mode;
+};
+
+static LapScale lap_scale(const Grid& g) {
+  double sx = g.idxd * g.idxd, sy = g.idyd * g.idyd;
+  LapScale k{df_host(sx), df_host(sy), 2};
+  if (sx == sy) {
+    int e;
+    double m = frexp(sx, &e);
+    k.mode = (m == 0.5 && e > -120 && e < 120) ? 0 : 1;
   }
-  df ax = df_add(df_sub(pl, pc), df_sub(pr, pc));
-  df ay = df_add(df_sub(pb, pc), df_sub(pt, pc));
-  return df_add(df_mul(ax, ih2x), df_mul(ay, ih2y));
+  return k;
+}
+
+// (float)(d - lap p) for df d and the df pressures of a cell and its four
+// neighbours.  For square cells h^2 lap p = pl + pr + pb + pt - 4 pc is summed
+// as in Sum2 of Ogita, Rump & Oishi (SIAM J. Sci. Comput. 26, 2005): a chain
+// of error-free two_sums over the hi parts, the lo parts and the rounding
+// errors gathered in one f32 term; d - lap then takes one more two_sum.  The
+// result is as accurate as a sum in twice the working precision, which is
+// what the cancellation between the five terms (and between d and lap p near
+// convergence) needs.
+__device__ __forceinline__ float residual_df(df d, df pc, df pl, df pr, df pb, df pt, const LapScale& k) {
+  if (k.mode == 2) {
+    df ax = df_add(df_sub(pl, pc), df_sub(pr, pc));
+    df ay = df_add(df_sub(pb, pc), df_sub(pt, pc));
+    return df_to_f(df_sub(d, df_add(df_mul(ax, k.ih2x), df_mul(ay, k.ih2y))));
+  }
+  df a = two_sum(pl.hi, pr.hi);
+  df b = two_sum(a.hi, pb.hi);
+  df c = two_sum(b.hi, pt.hi);
+  df e = two_sum(c.hi, __fmul_rn(-4.f, pc.hi));
+  float lo = __fmaf_rn(-4.f, pc.lo, __fadd_rn(__fadd_rn(pl.lo, pr.lo), __fadd_rn(pb.lo, pt.lo)));
+  lo = __fadd_rn(lo, __fadd_rn(__fadd_rn(a.lo, b.lo), __fadd_rn(c.lo, e.lo)));
+  float lh, ll;  // lap p = lh + ll
+  if (k.mode == 0) {
+    lh = __fmul_rn(e.hi, k.ih2x.hi);
+    ll = __fmul_rn(lo, k.ih2x.hi);
+  } else {
+    df q = two_prod(e.hi, k.ih2x.hi);
+    lh = q.hi;
+    ll = __fmaf_rn(e.hi, k.ih2x.lo, __fmaf_rn(lo, k.ih2x.hi, q.lo));
+  }
+  df r = two_sum(d.hi, -lh);
+  return __fadd_rn(r.hi, __fsub_rn(__fadd_rn(r.lo, d.lo), ll));
 }
 
 // r = d - lap(p) (or r = d when zero_p); r32 = (float) r; max|r| reduced
 __global__ void __launch_bounds__(256)
     k_refine_init(const float* __restrict__ dh, const float* __restrict__ dl, const float* __restrict__ ph,
-                  const float* __restrict__ pl, float* __restrict__ r32, int nx, int ny, df ih2x, df ih2y,
+                  const float* __restrict__ pl, float* __restrict__ r32, int nx, int ny, LapScale ks,
                   int zero_p, RedCtx ctx) {
   float m = 0.f;
-  const int ntx = (nx + 31) >> 5, nt = ntiles(nx, ny);
-  for (int t = blockIdx.x; t < nt; t += gridDim.x) {
-  int i = (t % ntx) * 32 + threadIdx.x, j = (t / ntx) * 8 + threadIdx.y;
-  if (i < nx && j < ny) {
-    int64_t r = (int64_t)j * nx, c = r + i;
-    df res = {__ldg(dh + c), __ldg(dl + c)};
-    if (!zero_p) {
-      int im = i == 0 ? nx - 1 : i - 1, ip = i + 1 == nx ? 0 : i + 1;
-      int jm = j == 0 ? ny - 1 : j - 1, jp = j + 1 == ny ? 0 : j + 1;
-      int64_t cl = r + im, cr = r + ip, cb = (int64_t)jm * nx + i, ct = (int64_t)jp * nx + i;
-      df lap = lap_df(df{__ldg(ph + c), __ldg(pl + c)}, df{__ldg(ph + cl), __ldg(pl + cl)},
-                      df{__ldg(ph + cr), __ldg(pl + cr)}, df{__ldg(ph + cb), __ldg(pl + cb)},
-                      df{__ldg(ph + ct), __ldg(pl + ct)}, ih2x, ih2y);
-      res = df_sub(res, lap);
+  FOR_RED_TILES(nx, ny) {
+    int i = tx * 32 + threadIdx.x, j = ty * 8 + threadIdx.y;
+    if (i < nx && j < ny) {
+      int64_t r = (int64_t)j * nx, c = r + i;
+      df d = {__ldg(dh + c), __ldg(dl + c)};
+      float rf;
+      if (zero_p) {
+        rf = df_to_f(d);
+      } else {
+        int im = i == 0 ? nx - 1 : i - 1, ip = i + 1 == nx ? 0 : i + 1;
+        int jm = j == 0 ? ny - 1 : j - 1, jp = j + 1 == ny ? 0 : j + 1;
+        int64_t cl = r + im, cr = r + ip, cb = (int64_t)jm * nx + i, ct = (int64_t)jp * nx + i;
+        rf = residual_df(d, df{__ldg(ph + c), __ldg(pl + c)}, df{__ldg(ph + cl), __ldg(pl + cl)},
+                         df{__ldg(ph + cr), __ldg(pl + cr)}, df{__ldg(ph + cb), __ldg(pl + cb)},
+                         df{__ldg(ph + ct), __ldg(pl + ct)}, ks);
+      }
+      r32[c] = rf;
+      m = fmaxf(m, absnanf(rf));
     }
-    float rf = df_to_f(res);
-    r32[c] = rf;
-    m = fmaxf(m, absnanf(rf));
-  }
   }
   block_max_finish(m, ctx);
 }
@@ -364,29 +411,26 @@ __global__ void __launch_bounds__(256)
 __global__ void __launch_bounds__(256)
     k_refine_update(const float* __restrict__ ph, const float* __restrict__ pl, const float* __restrict__ e,
                     const float* __restrict__ dh, const float* __restrict__ dl, float* __restrict__ poh,
-                    float* __restrict__ pol, float* __restrict__ r32, int nx, int ny, df ih2x, df ih2y,
-                    RedCtx ctx) {
+                    float* __restrict__ pol, float* __restrict__ r32, int nx, int ny, LapScale ks, RedCtx ctx) {
   float m = 0.f;
-  const int ntx = (nx + 31) >> 5, nt = ntiles(nx, ny);
-  for (int t = blockIdx.x; t < nt; t += gridDim.x) {
-  int i = (t % ntx) * 32 + threadIdx.x, j = (t / ntx) * 8 + threadIdx.y;
-  if (i < nx && j < ny) {
-    int im = i == 0 ? nx - 1 : i - 1, ip = i + 1 == nx ? 0 : i + 1;
-    int jm = j == 0 ? ny - 1 : j - 1, jp = j + 1 == ny ? 0 : j + 1;
-    int64_t r = (int64_t)j * nx, c = r + i;
-    int64_t cl = r + im, cr = r + ip, cb = (int64_t)jm * nx + i, ct = (int64_t)jp * nx + i;
-    df pc = df_add_f(df{__ldg(ph + c), __ldg(pl + c)}, __ldg(e + c));
-    df pL = df_add_f(df{__ldg(ph + cl), __ldg(pl + cl)}, __ldg(e + cl));
-    df pR = df_add_f(df{__ldg(ph + cr), __ldg(pl + cr)}, __ldg(e + cr));
-    df pB = df_add_f(df{__ldg(ph + cb), __ldg(pl + cb)}, __ldg(e + cb));
-    df pT = df_add_f(df{__ldg(ph + ct), __ldg(pl + ct)}, __ldg(e + ct));
-    df res = df_sub(df{__ldg(dh + c), __ldg(dl + c)}, lap_df(pc, pL, pR, pB, pT, ih2x, ih2y));
-    poh[c] = pc.hi;
-    pol[c] = pc.lo;
-    float rf = df_to_f(res);
-    r32[c] = rf;
-    m = fmaxf(m, absnanf(rf));
-  }
+  FOR_RED_TILES(nx, ny) {
+    int i = tx * 32 + threadIdx.x, j = ty * 8 + threadIdx.y;
+    if (i < nx && j < ny) {
+      int im = i == 0 ? nx - 1 : i - 1, ip = i + 1 == nx ? 0 : i + 1;
+      int jm = j == 0 ? ny - 1 : j - 1, jp = j + 1 == ny ? 0 : j + 1;
+      int64_t r = (int64_t)j * nx, c = r + i;
+      int64_t cl = r + im, cr = r + ip, cb = (int64_t)jm * nx + i, ct = (int64_t)jp * nx + i;
+      df pc = df_add_f(df{__ldg(ph + c), __ldg(pl + c)}, __ldg(e + c));
+      df pL = df_add_f(df{__ldg(ph + cl), __ldg(pl + cl)}, __ldg(e + cl));
+      df pR = df_add_f(df{__ldg(ph + cr), __ldg(pl + cr)}, __ldg(e + cr));
+      df pB = df_add_f(df{__ldg(ph + cb), __ldg(pl + cb)}, __ldg(e + cb));
+      df pT = df_add_f(df{__ldg(ph + ct), __ldg(pl + ct)}, __ldg(e + ct));
+      float rf = residual_df(df{__ldg(dh + c), __ldg(dl + c)}, pc, pL, pR, pB, pT, ks);
+      poh[c] = pc.hi;
+      pol[c] = pc.lo;
+      r32[c] = rf;
+      m = fmaxf(m, absnanf(rf));
+    }
   }
   block_max_finish(m, ctx);
 }
@@ -395,18 +439,16 @@ void launch_refine_init(Solver* s, const float* dh, const float* dl, const float
                         float* r32, bool zero_p) {
   const Grid& g = s->g;
   FS_LAUNCH(s, "refine_init", (double)s->n * (zero_p ? 12 : 20),
-            k_refine_init<<<red_grid(g.nx, g.ny), kBlock, 0, s->stream>>>(
-                dh, dl, ph, pl, r32, g.nx, g.ny, df_host(g.idxd * g.idxd), df_host(g.idyd * g.idyd),
-                zero_p ? 1 : 0, red_ctx(s, s->red_out)));
+            k_refine_init<<<red_grid2(g.nx, g.ny), kBlock, 0, s->stream>>>(
+                dh, dl, ph, pl, r32, g.nx, g.ny, lap_scale(g), zero_p ? 1 : 0, red_ctx(s, s->red_out)));
 }
 
 void launch_refine_update(Solver* s, const float* ph, const float* pl, const float* e, const float* dh,
                           const float* dl, float* poh, float* pol, float* r32) {
   const Grid& g = s->g;
   FS_LAUNCH(s, "refine_update", (double)s->n * 32,
-            k_refine_update<<<red_grid(g.nx, g.ny), kBlock, 0, s->stream>>>(
-                ph, pl, e, dh, dl, poh, pol, r32, g.nx, g.ny, df_host(g.idxd * g.idxd),
-                df_host(g.idyd * g.idyd), red_ctx(s, s->red_out)));
+            k_refine_update<<<red_grid2(g.nx, g.ny), kBlock, 0, s->stream>>>(
+                ph, pl, e, dh, dl, poh, pol, r32, g.nx, g.ny, lap_scale(g), red_ctx(s, s->red_out)));
 }
 
 // ------------------------------------------------------- df <-> host types
@@ -439,9 +481,8 @@ void launch_df_to_f(Solver* s, const float* hi, const float* lo, float* x, int64
 __global__ void __launch_bounds__(256) k_absmax_res32(const float* __restrict__ p, const float* __restrict__ d,
                                                       int nx, int ny, float ih2x, float ih2y, RedCtx ctx) {
   float m = 0.f;
-  const int ntx = (nx + 31) >> 5, nt = ntiles(nx, ny);
-  for (int t = blockIdx.x; t < nt; t += gridDim.x) {
-  int i = (t % ntx) * 32 + threadIdx.x, j = (t / ntx) * 8 + threadIdx.y;
+  FOR_RED_TILES(nx, ny) {
+  int i = tx * 32 + threadIdx.x, j = ty * 8 + threadIdx.y;
   if (i < nx && j < ny) {
     int im = i == 0 ? nx - 1 : i - 1, ip = i + 1 == nx ? 0 : i + 1;
     int jm = j == 0 ? ny - 1 : j - 1, jp = j + 1 == ny ? 0 : j + 1;
@@ -457,7 +498,7 @@ __global__ void __launch_bounds__(256) k_absmax_res32(const float* __restrict__ 
 void launch_absmax_residual32(Solver* s, const float* p, const float* d) {
   const Grid& g = s->g;
   FS_LAUNCH(s, "absmax_residual", (double)s->n * 8,
-            k_absmax_res32<<<red_grid(g.nx, g.ny), kBlock, 0, s->stream>>>(
+            k_absmax_res32<<<red_grid2(g.nx, g.ny), kBlock, 0, s->stream>>>(
                 p, d, g.nx, g.ny, g.idx * g.idx, g.idy * g.idy, red_ctx(s, s->red_out)));
 }
 
