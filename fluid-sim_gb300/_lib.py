@@ -138,6 +138,9 @@ SIGNATURES = {
     "fs_host_alloc": (VP, [C.c_size_t]),
     "fs_host_free": (None, [VP]),
     "fs_max_divergence_noalloc": (I, [VP, VP, C.c_int32, C.c_int32, D, D, VP, VP]),
+    "fs_conv3x3_bf16": (I, [VP, VP, VP, VP, C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_int32,
+                            VP, VP]),
+    "fs_tc_gemm_check": (I, [VP, VP, VP, C.c_int32, C.c_int32, VP, VP]),
 }
 
 _lib = None

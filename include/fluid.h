@@ -262,6 +262,30 @@ FS_API void fs_host_free(void* p);
 FS_API int fs_max_divergence_noalloc(const float* d_u, const float* d_v, int32_t nx, int32_t ny, double lx,
                                      double ly, double* d_out, void* stream);
 
+/* ------------------------------------------------------------------------
+ * Tensor-core building blocks of the learned pressure guess.  No counterpart
+ * in the reference (which has no learned component); these sit beside the
+ * solver, not in place of any reference function.
+ * ------------------------------------------------------------------------ */
+
+/* 3x3 periodic convolution of NHWC bf16 images on the tcgen05 tensor cores:
+ *   out[b,y,x,co] = bias[co] + sum_{ky,kx,ci} w[co,ci,ky,kx] in[b, y+ky-1, x+kx-1, ci]
+ * with x, y wrapped.  d_wpacked holds w as bf16 in the layout
+ * [ky*3+kx][ci/8][co][ci%8].  epilogue 0: bf16 out, 1: bf16 out after ReLU,
+ * 2: f32 planar [b][y][x] of output channel 0 only (c_out must be 16).
+ * Instantiated channel pairs: 16->16, 16->32, 32->16, 32->64, 64->32,
+ * 64->128, 128->64.  Buffers 16-byte aligned; device pointers; enqueued on
+ * `stream`.  *d_err is set to 1 if a tensor-core completion wait timed out. */
+FS_API int fs_conv3x3_bf16(const void* d_in, const void* d_wpacked, const float* d_bias, void* d_out, int32_t batch,
+                           int32_t h, int32_t w, int32_t c_in, int32_t c_out, int32_t epilogue, int32_t* d_err,
+                           void* stream);
+
+/* One 128 x n tile D = A B^T (A 128 x k, B n x k, row-major bf16; D f32
+ * row-major) through the same tcgen05 path: a device self-check of the
+ * descriptors and the accumulator read-back.  n in {16, 64}, k in {16..64}. */
+FS_API int fs_tc_gemm_check(const void* d_a, const void* d_b, float* d_d, int32_t n, int32_t k, int32_t* d_err,
+                            void* stream);
+
 #ifdef __cplusplus
 }
 #endif
