@@ -6,5 +6,8 @@ GPUFluidSolver API on top of it.
 """
 from ._lib import FluidError, build, load, LIB_PATH  # noqa: F401
 from .solver import GPUFluidSolver  # noqa: F401
+from . import workload  # noqa: F401
+from .guess import PressureGuess, normalize_pair, read_pair_file, write_pair_file  # noqa: F401
 
-__all__ = ["GPUFluidSolver", "FluidError", "build", "load", "LIB_PATH"]
+__all__ = ["GPUFluidSolver", "PressureGuess", "FluidError", "build", "load", "LIB_PATH", "normalize_pair",
+           "read_pair_file", "write_pair_file", "workload"]

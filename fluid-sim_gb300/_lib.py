@@ -141,6 +141,21 @@ SIGNATURES = {
     "fs_conv3x3_bf16": (I, [VP, VP, VP, VP, C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_int32,
                             VP, VP]),
     "fs_tc_gemm_check": (I, [VP, VP, VP, C.c_int32, C.c_int32, VP, VP]),
+    "fs_guess_create": (I, [C.c_int32, C.c_uint64, C.POINTER(VP)]),
+    "fs_guess_destroy": (None, [VP]),
+    "fs_guess_num_params": (C.c_int64, [VP]),
+    "fs_guess_get_params": (I, [VP, VP, C.c_int64]),
+    "fs_guess_set_params": (I, [VP, VP, C.c_int64]),
+    "fs_guess_predict": (I, [VP, VP, VP, C.c_int32, C.c_int32, C.c_int32, VP]),
+    "fs_guess_loss_grad": (I, [VP, VP, VP, VP, C.c_int32, C.c_int32, C.c_int32, C.POINTER(C.c_double), VP]),
+    "fs_guess_train_step": (I, [VP, VP, VP, VP, C.c_int32, C.c_int32, C.c_int32, C.c_float,
+                                C.POINTER(C.c_double)]),
+    "fs_guess_sync": (I, [VP]),
+    "fs_guess_launch_count": (C.c_int64, [VP]),
+    "fs_set_guess": (I, [VP, VP]),
+    "fs_dump_pair": (I, [VP, C.c_int32, VP, VP, VP]),
+    "fs_write_pair_file": (I, [C.c_char_p, C.c_int32, C.c_int32, D, VP, VP, VP]),
+    "fs_read_pair_file": (I, [C.c_char_p, C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.POINTER(D), VP, VP, VP]),
 }
 
 _lib = None

@@ -30,6 +30,7 @@ static int fail(Solver* s, int code, const std::string& msg) {
   else g_create_error = msg;
   return code;
 }
+int fail_status(Solver* s, int code, const std::string& msg) { return fail(s, code, msg); }
 
 #define CU(S, call)                                                                          \
   do {                                                                                       \
@@ -405,7 +406,13 @@ static int pressure_solve(Solver* s, bool capture) {
   const bool mg = P.pressure_solver == FS_PRESSURE_MULTIGRID;
   s->stats = fs_step_stats{0, 1, -1.0, -1.0};
   s->stats_on_device = false;
-  if (s->mixed) {
+  if (s->guess) {
+    // learned initial pressure; the cycles below correct it to the tolerance
+    int rc = guess_enqueue(s, s->guess);
+    if (rc) return rc;
+    if (s->mixed) launch_refine_init(s, s->dh, s->dl, s->ph, s->pl, s->r32, false);
+    else if (tol) launch_absmax_residual32(s, s->p32, s->div32);
+  } else if (s->mixed) {
     launch_refine_init(s, s->dh, s->dl, s->ph, s->pl, s->r32, !P.warm_start);
     if (!P.warm_start) {
       launch_fill(s, s->ph, 0.f, s->n);
@@ -855,6 +862,30 @@ FS_API int fs_solid_impulse(fs_solver* h, double* out, int count) {
   CU(s, cudaMemcpyAsync(out, s->d_impulse, 3 * s->disks.size() * sizeof(double), cudaMemcpyDeviceToHost, s->stream));
   CU(s, cudaStreamSynchronize(s->stream));
   return FS_OK;
+}
+
+FS_API int fs_set_guess(fs_solver* h, fs_guess* g) {
+  SOLVER(h);
+  if (g && !guess_supported(s))
+    return fail(s, FS_ERR_UNSUPPORTED, "the pressure guess needs nx and ny multiples of 16");
+  if (g && s->prm.pressure_solver != FS_PRESSURE_MULTIGRID)
+    return fail(s, FS_ERR_UNSUPPORTED, "the pressure guess seeds multigrid cycles only");
+  CU(s, cudaStreamSynchronize(s->stream));
+  if (g) {
+    int rc = guess_prepare(s, g);
+    if (rc) return rc;
+  }
+  drop_graph(s);  // the captured step gains or loses the guess
+  s->guess = g;
+  return FS_OK;
+}
+
+FS_API int fs_dump_pair(fs_solver* h, int32_t factor, float* div, float* mask, float* p) {
+  SOLVER(h);
+  if (!div || !mask || !p) return fail(s, FS_ERR_INVALID_ARGUMENT, "fs_dump_pair: NULL output");
+  if (factor < 1 || s->g.nx % factor || s->g.ny % factor)
+    return fail(s, FS_ERR_INVALID_ARGUMENT, "fs_dump_pair: factor must divide nx and ny");
+  return dump_pair(s, factor, div, mask, p);
 }
 
 FS_API int fs_step(fs_solver* h, double dt) {

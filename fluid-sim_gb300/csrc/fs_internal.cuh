@@ -108,6 +108,7 @@ struct Solver {
 
   // solids
   std::vector<fs_disk> disks;
+  fs_guess* guess = nullptr;    // learned initial pressure (fs_set_guess), not owned
   float* imp = nullptr;         // 3 * n impulse field (x, y, torque)
   double* d_impulse = nullptr;  // 3 * disks
   int imp_cap = 0;
@@ -220,5 +221,15 @@ void mg_vcycle(Solver* s);
 // double-float pressure (acc_h, acc_l) in place instead of writing lev[0].x2
 void mg_vcycle_fused(Solver* s, bool first_has_x, float* acc_h = nullptr, float* acc_l = nullptr);
 bool mg_fused_supported(const Solver* s);
+
+// errors (fs_api.cu): message into the handle (or the thread's last error)
+int fail_status(Solver* s, int code, const std::string& msg);
+void record_error(const std::string& msg);
+
+// learned pressure guess (fs_guess.cu)
+bool guess_supported(const Solver* s);
+int guess_prepare(Solver* s, fs_guess* g);   // buffers for this grid (outside any capture)
+int guess_enqueue(Solver* s, fs_guess* g);   // initial pressure from the divergence
+int dump_pair(Solver* s, int factor, float* div, float* mask, float* p);
 
 }  // namespace fs

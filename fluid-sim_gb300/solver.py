@@ -240,3 +240,20 @@ class GPUFluidSolver:
 
     def launch_count(self) -> int:
         return int(self._lib.fs_launch_count(self._h))
+
+    # ------------------------------------------------ learned pressure guess
+    def set_guess(self, guess) -> None:
+        """Seed every projection with a PressureGuess (None detaches it);
+        the cycles still run to pressure_tol."""
+        self._guess = guess  # keep it alive while attached
+        self._chk(self._lib.fs_set_guess(self._h, guess.handle if guess is not None else None))
+
+    def dump_pair(self, factor: int = 1):
+        """(div, mask, p) of the last projection averaged over factor x factor
+        cells, f32 [ny/factor, nx/factor] each, and their grid spacing."""
+        ny, nx = self.ny // factor, self.nx // factor
+        d = np.empty((ny, nx), np.float32)
+        m = np.empty_like(d)
+        p = np.empty_like(d)
+        self._chk(self._lib.fs_dump_pair(self._h, factor, _ptr(d), _ptr(m), _ptr(p)))
+        return d, m, p, self.dx * factor

@@ -286,6 +286,62 @@ FS_API int fs_conv3x3_bf16(const void* d_in, const void* d_wpacked, const float*
 FS_API int fs_tc_gemm_check(const void* d_a, const void* d_b, float* d_d, int32_t n, int32_t k, int32_t* d_err,
                             void* stream);
 
+/* ------------------------------------------------------------------------
+ * Learned pressure guess: a periodic U-Net (4 levels, 16/32/64/128 channels,
+ * 3x3 convolutions, ReLU, 2x2 average pooling, nearest upsampling with
+ * additive skips; bf16 weights and activations, f32 accumulation) mapping
+ * the divergence and the solid mask at half the grid resolution to an
+ * initial pressure.  With a guess attached, the multigrid projection starts
+ * from it instead of zero and still iterates to pressure_tol, so plain
+ * multigrid stays both the fallback and the judge.  No reference counterpart.
+ *
+ * Network inputs at its own resolution H x W (multiples of 8):
+ *   div_n = h^2 d / sigma, sigma = RMS(h^2 d) per sample (h = grid spacing),
+ *   mask  = solid mask in [0, 1];
+ * output p / sigma (pressure up to a constant).  Parameters: f32, flattened
+ * layer by layer (A..J) as w[c_out][c_in][3][3] then b[c_out].  Data pointers
+ * of predict / loss_grad / train_step are device pointers, f32 [B][H][W].
+ * ------------------------------------------------------------------------ */
+typedef struct fs_guess fs_guess;
+
+/* He-normal initial weights from `seed` (SplitMix64 + Box-Muller). */
+FS_API int fs_guess_create(int32_t device, uint64_t seed, fs_guess** out);
+FS_API void fs_guess_destroy(fs_guess* g);
+FS_API int64_t fs_guess_num_params(const fs_guess* g);
+FS_API int fs_guess_get_params(fs_guess* g, float* host, int64_t n);
+/* also resets the Adam moments and step count */
+FS_API int fs_guess_set_params(fs_guess* g, const float* host, int64_t n);
+FS_API int fs_guess_predict(fs_guess* g, const float* d_div_n, const float* d_mask, int32_t batch, int32_t h,
+                            int32_t w, float* d_out);
+/* loss = mean over batch and pixels of (e - mean_b e)^2, e = out - target;
+ * d_grad (nullable, n floats on the device) receives dloss/dparams */
+FS_API int fs_guess_loss_grad(fs_guess* g, const float* d_div_n, const float* d_mask, const float* d_target,
+                              int32_t batch, int32_t h, int32_t w, double* loss, float* d_grad);
+/* loss_grad then one Adam step (beta1 0.9, beta2 0.999, eps 1e-8, bias
+ * corrected).  With loss == NULL the call does not synchronise. */
+FS_API int fs_guess_train_step(fs_guess* g, const float* d_div_n, const float* d_mask, const float* d_target,
+                               int32_t batch, int32_t h, int32_t w, float lr, double* loss);
+FS_API int fs_guess_sync(fs_guess* g);
+FS_API int64_t fs_guess_launch_count(const fs_guess* g);
+
+/* Attach (or with NULL detach) a guess to a multigrid solver; nx, ny must be
+ * multiples of 16.  The solver does not own g; keep g alive while attached. */
+FS_API int fs_set_guess(fs_solver* s, fs_guess* g);
+
+/* The training pair of the last projection: divergence, solid mask and
+ * pressure averaged over factor x factor cells (mask at the coarse cell
+ * centres), host f32 arrays of (nx/factor) x (ny/factor).  Synchronises. */
+FS_API int fs_dump_pair(fs_solver* s, int32_t factor, float* div, float* mask, float* p);
+
+/* Training-pair file ("FSPAIR" v1): 40-byte header {magic "FSPAIR\0\1",
+ * u32 version = 1, u32 nx, u32 ny, u32 dtype = 0 (f32), f64 dx, u32 nfields =
+ * 3, u32 0} then div, mask, p as f32 [ny][nx], little-endian.  Reading with
+ * div == NULL fills only nx, ny, dx. */
+FS_API int fs_write_pair_file(const char* path, int32_t nx, int32_t ny, double dx, const float* div,
+                              const float* mask, const float* p);
+FS_API int fs_read_pair_file(const char* path, int32_t* nx, int32_t* ny, double* dx, float* div, float* mask,
+                             float* p);
+
 #ifdef __cplusplus
 }
 #endif

@@ -1,0 +1,194 @@
+"""The learned pressure guess on the GPU, checked against the CPU oracle
+(oracle/guess_oracle.py) and inside the projection.
+
+Tolerances.  The device stores activations and activation gradients in bf16
+(8 significant bits) and accumulates in f32; the oracle rounds to bf16 at the
+same points and accumulates in float64, so the two differ by accumulation
+order plus the occasional bf16 tie that rounds the other way:
+  forward output      relative L2 <= 2e-2
+  loss                relative    <= 2e-2
+  gradient            relative L2 <= 5e-2 per layer, cosine >= 0.999 overall
+  Adam update         exact formula on the device's own gradient, 1e-6
+With a guess attached the projection still runs to pressure_tol, so the
+velocity must match the zero-guess solver to the tolerance's order.
+"""
+from __future__ import annotations
+
+import math
+
+import numpy as np
+import pytest
+
+torch = pytest.importorskip("torch")
+pytestmark = pytest.mark.gpu
+
+import guess_oracle as G  # noqa: E402
+
+
+def rnd(x):
+    return torch.from_numpy(np.asarray(x, np.float32)).to(torch.bfloat16).double().numpy()
+
+
+@pytest.fixture(scope="module")
+def pkg(fs):
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    fs._lib.load()
+    return fs
+
+
+def _inputs(seed, B, H, W):
+    rng = np.random.default_rng(seed)
+    div = rng.standard_normal((B, H, W)).astype(np.float32)
+    mask = (rng.random((B, H, W)) > 0.8).astype(np.float32)
+    tgt = rng.standard_normal((B, H, W)).astype(np.float32)
+    return div, mask, tgt
+
+
+def _rel(a, b):
+    return float(np.linalg.norm(np.ravel(a) - np.ravel(b)) / max(np.linalg.norm(np.ravel(b)), 1e-30))
+
+
+@pytest.mark.parametrize("shape", [(2, 32, 32), (1, 16, 48)])
+def test_forward_matches_oracle(pkg, shape):
+    B, H, W = shape
+    g = pkg.PressureGuess(seed=11)
+    theta = g.get_params().astype(np.float64)
+    div, mask, _ = _inputs(1, B, H, W)
+    out = g.predict(div, mask).cpu().numpy()
+    ref, _ = G.forward(theta, G.make_input(div.astype(np.float64), mask.astype(np.float64)), rnd)
+    assert _rel(out, ref) <= 2e-2
+    g.close()
+
+
+def test_loss_and_gradient_match_oracle(pkg):
+    B, H, W = 2, 32, 32
+    g = pkg.PressureGuess(seed=12)
+    theta = g.get_params().astype(np.float64)
+    div, mask, tgt = _inputs(2, B, H, W)
+    loss, grad = g.loss_grad(div, mask, tgt)
+    grad = grad.cpu().numpy().astype(np.float64)
+    L, gref, _ = G.loss_grad(theta, div.astype(np.float64), mask.astype(np.float64), tgt.astype(np.float64), rnd)
+    assert abs(loss - L) <= 2e-2 * L
+    k = 0
+    for name, ci, co, _ in G.LAYERS:
+        n = ci * co * 9 + co
+        assert _rel(grad[k:k + n], gref[k:k + n]) <= 5e-2, name
+        k += n
+    cos = grad @ gref / (np.linalg.norm(grad) * np.linalg.norm(gref))
+    assert cos >= 0.999
+    # the zero-padded input channels of layer A get exactly zero gradient
+    assert np.all(grad[:16 * 16 * 9].reshape(16, 16, 3, 3)[:, 2:] == 0.0)
+    g.close()
+
+
+def test_adam_step_matches_formula(pkg):
+    B, H, W = 1, 32, 32
+    g = pkg.PressureGuess(seed=13)
+    theta0 = g.get_params().astype(np.float64)
+    div, mask, tgt = _inputs(3, B, H, W)
+    _, grad = g.loss_grad(div, mask, tgt)
+    grad = grad.cpu().numpy().astype(np.float64)
+    lr = 1e-3
+    g.train_step(div, mask, tgt, lr)
+    theta1 = g.get_params().astype(np.float64)
+    ref, _, _ = G.adam(theta0, grad, np.zeros_like(grad), np.zeros_like(grad), 1, lr)
+    np.testing.assert_allclose(theta1, ref, rtol=0, atol=1e-6 * max(1.0, np.abs(theta0).max()) + 1e-3 * lr)
+    g.close()
+
+
+def _poisson_pairs(seed, B, n):
+    """Band-limited mean-free divergence and the exact periodic 5-point solve."""
+    rng = np.random.default_rng(seed)
+    k = np.fft.fftfreq(n) * n
+    KX, KY = np.meshgrid(k, k)
+    lam = 2 * np.cos(2 * np.pi * KX / n) + 2 * np.cos(2 * np.pi * KY / n) - 4
+    band = (np.hypot(KX, KY) >= 3) & (np.hypot(KX, KY) <= 8)
+    divs, ps = [], []
+    for _ in range(B):
+        spec = (rng.standard_normal((n, n)) + 1j * rng.standard_normal((n, n))) * band
+        d = np.real(np.fft.ifft2(spec))
+        d /= np.sqrt(np.mean(d * d))
+        ph = np.fft.fft2(d)
+        ph[lam != 0] /= lam[lam != 0]
+        ph[0, 0] = 0
+        divs.append(d)
+        ps.append(np.real(np.fft.ifft2(ph)))
+    return np.array(divs, np.float32), np.zeros((B, n, n), np.float32), np.array(ps, np.float32)
+
+
+def test_training_reduces_loss(pkg):
+    g = pkg.PressureGuess(seed=14)
+    div, mask, p = _poisson_pairs(5, 4, 64)
+    first = g.train_step(div, mask, p, 3e-3)
+    for _ in range(150):
+        last = g.train_step(div, mask, p, 3e-3, want_loss=False)
+    last = g.train_step(div, mask, p, 3e-3)
+    assert math.isfinite(first) and last < 0.5 * first, (first, last)
+    g.close()
+
+
+def _solver(pkg, n, disks, guess=None, tol=1e-8):
+    s = pkg.GPUFluidSolver(n=n, nu=1e-3, advection="maccormack", pressureSolver="multigrid",
+                           pressureIterations=1, precision="mixed", pressure_tol=tol, max_cycles=60)
+    s.set_solids(disks)
+    if guess is not None:
+        s.set_guess(guess)
+    return s
+
+
+def test_solver_with_guess_converges_to_the_same_flow(pkg):
+    n = 64
+    u, v, disks, dt = pkg.workload.make_workload(n, seed=3)
+    g = pkg.PressureGuess(seed=15)
+    a = _solver(pkg, n, disks)
+    b = _solver(pkg, n, disks, g)
+    for s in (a, b):
+        s.upload_velocity(u, v)
+        for _ in range(4):
+            s.step(dt)
+        st = s.last_stats()
+        assert st["converged"] and st["residual_max"] <= 1e-8
+        assert s.max_divergence() <= 2e-8
+    ua, va = a.read_velocity()
+    ub, vb = b.read_velocity()
+    assert max(np.abs(ua - ub).max(), np.abs(va - vb).max()) <= 1e-6
+    # detaching restores the zero initial pressure
+    b.set_guess(None)
+    b.step(dt)
+    assert b.last_stats()["converged"]
+    a.destroy()
+    b.destroy()
+    g.close()
+
+
+def test_dump_pair(pkg):
+    n = 64
+    u, v, disks, dt = pkg.workload.make_workload(n, seed=4)
+    s = _solver(pkg, n, disks)
+    s.upload_velocity(u, v)
+    s.step(dt)
+    d1, m1, p1, dx1 = s.dump_pair(1)
+    d2, m2, p2, dx2 = s.dump_pair(2)
+    assert d1.shape == (n, n) and d2.shape == (n // 2, n // 2) and dx2 == 2 * dx1
+    assert 0.0 <= m1.min() and m1.max() <= 1.0 and m1.max() > 0.5
+    np.testing.assert_allclose(d2, d1.reshape(n // 2, 2, n // 2, 2).mean(axis=(1, 3)), rtol=1e-5, atol=1e-6)
+    np.testing.assert_allclose(p2, p1.reshape(n // 2, 2, n // 2, 2).mean(axis=(1, 3)), rtol=1e-5, atol=1e-6)
+    # the dumped pair solves the 5-point Poisson problem (to f32 rounding of p)
+    pd = p1.astype(np.float64)
+    lap = (np.roll(pd, 1, 0) + np.roll(pd, -1, 0) + np.roll(pd, 1, 1) + np.roll(pd, -1, 1) - 4 * pd) / dx1 ** 2
+    assert np.linalg.norm(lap - d1) <= 1e-3 * np.linalg.norm(d1)
+    s.destroy()
+
+
+def test_set_guess_rejections(pkg):
+    g = pkg.PressureGuess(seed=16)
+    s = pkg.GPUFluidSolver(n=72, pressureSolver="multigrid", precision="mixed", pressure_tol=1e-6)
+    with pytest.raises(pkg.FluidError):
+        s.set_guess(g)
+    s.destroy()
+    s = pkg.GPUFluidSolver(n=64, pressureSolver="jacobi", pressureIterations=10)
+    with pytest.raises(pkg.FluidError):
+        s.set_guess(g)
+    s.destroy()
+    g.close()
