@@ -18,8 +18,9 @@ gradients can be checked independently.  Both sides use:
   L = sum_b sum_p (e - mean_b e)^2 / (B H W).
 
 ``rnd`` (optional) rounds a tensor to the device's storage type at each point
-where the device stores an activation or an activation gradient in bf16, so
-the comparison can be tight.
+where the device stores one in bf16 -- the convolution weights, every
+activation and every activation gradient -- so the comparison can be tight.
+(Biases stay f32 on the device and are not rounded.)
 """
 from __future__ import annotations
 
@@ -136,8 +137,15 @@ def make_input(div_n, mask):
     return x
 
 
-def forward(theta, x0, rnd=_id):
+def _params(theta, rnd):
     P = unflatten(np.asarray(theta, np.float64))
+    if rnd is not _id:
+        P = {n: (rnd(w), b) for n, (w, b) in P.items()}
+    return P
+
+
+def forward(theta, x0, rnd=_id):
+    P = _params(theta, rnd)
     relu = lambda t: np.maximum(t, 0.0)
     a = {"x0": rnd(x0)}
     a["a0"] = rnd(relu(conv(a["x0"], *P["A"])))
@@ -169,7 +177,7 @@ def loss_and_seed(out, target):
 
 def backward(theta, acts, gout, rnd=_id):
     """Gradient of the loss w.r.t. the flattened parameters, given dL/dout."""
-    P = unflatten(np.asarray(theta, np.float64))
+    P = _params(theta, rnd)
     a = acts
     G = {}
     mask = lambda g, t: g * (t > 0)
