@@ -150,9 +150,10 @@ SIGNATURES = {
     "fs_guess_loss_grad": (I, [VP, VP, VP, VP, C.c_int32, C.c_int32, C.c_int32, C.POINTER(C.c_double), VP]),
     "fs_guess_train_step": (I, [VP, VP, VP, VP, C.c_int32, C.c_int32, C.c_int32, C.c_float,
                                 C.POINTER(C.c_double)]),
+    "fs_guess_set_loss": (I, [VP, D, D]),
     "fs_guess_sync": (I, [VP]),
     "fs_guess_launch_count": (C.c_int64, [VP]),
-    "fs_set_guess": (I, [VP, VP]),
+    "fs_set_guess": (I, [VP, VP, C.c_int32]),
     "fs_dump_pair": (I, [VP, C.c_int32, VP, VP, VP]),
     "fs_write_pair_file": (I, [C.c_char_p, C.c_int32, C.c_int32, D, VP, VP, VP]),
     "fs_read_pair_file": (I, [C.c_char_p, C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.POINTER(D), VP, VP, VP]),

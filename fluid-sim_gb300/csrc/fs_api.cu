@@ -408,7 +408,7 @@ static int pressure_solve(Solver* s, bool capture) {
   s->stats_on_device = false;
   if (s->guess) {
     // learned initial pressure; the cycles below correct it to the tolerance
-    int rc = guess_enqueue(s, s->guess);
+    int rc = guess_enqueue(s, s->guess, s->guess_factor);
     if (rc) return rc;
     if (s->mixed) launch_refine_init(s, s->dh, s->dl, s->ph, s->pl, s->r32, false);
     else if (tol) launch_absmax_residual32(s, s->p32, s->div32);
@@ -864,19 +864,21 @@ FS_API int fs_solid_impulse(fs_solver* h, double* out, int count) {
   return FS_OK;
 }
 
-FS_API int fs_set_guess(fs_solver* h, fs_guess* g) {
+FS_API int fs_set_guess(fs_solver* h, fs_guess* g, int32_t factor) {
   SOLVER(h);
-  if (g && !guess_supported(s))
-    return fail(s, FS_ERR_UNSUPPORTED, "the pressure guess needs nx and ny multiples of 16");
+  if (g && factor != 1 && factor != 2) return fail(s, FS_ERR_INVALID_ARGUMENT, "fs_set_guess: factor must be 1 or 2");
+  if (g && !guess_supported(s, factor))
+    return fail(s, FS_ERR_UNSUPPORTED, "the pressure guess needs nx and ny multiples of 8 * factor");
   if (g && s->prm.pressure_solver != FS_PRESSURE_MULTIGRID)
     return fail(s, FS_ERR_UNSUPPORTED, "the pressure guess seeds multigrid cycles only");
   CU(s, cudaStreamSynchronize(s->stream));
   if (g) {
-    int rc = guess_prepare(s, g);
+    int rc = guess_prepare(s, g, factor);
     if (rc) return rc;
   }
   drop_graph(s);  // the captured step gains or loses the guess
   s->guess = g;
+  s->guess_factor = g ? factor : 2;
   return FS_OK;
 }
 

@@ -6,7 +6,7 @@
 // with periodic wrap in x and y (the flow domain is periodic), optional ReLU.
 //
 // GEMM view: M = 128 consecutive pixels of one image row, N = C_out,
-// K = 9 taps x C_in.  A CTA owns TY rows x 128 pixels.  It stages the input
+// K = 9 taps x C_in.  A CTA (four warps) owns TY rows x 128 pixels.  It stages the input
 // halo tile once, as channel-chunk planes [kc][TY + 2][130][8 channels], so
 // that 8 consecutive pixels of one chunk form one 128-byte core matrix and
 // every tap's A operand is the same tile seen through a descriptor whose start
@@ -15,7 +15,7 @@
 // operand, K-major) and staged one tap at a time into two alternating buffers,
 // so the copy of tap t+1 overlaps the MMAs of tap t.  One thread issues the
 // MMAs; the accumulators (TY x C_out f32 columns x 128 lanes) live in TMEM and
-// four warps read them back (lane = pixel) for the bias/ReLU/bf16 epilogue.
+// the four warps read them back (lane = pixel) for the bias/ReLU/bf16 epilogue.
 // Images narrower than 128 pixels are staged wrapped around, so the extra
 // lanes compute copies of real pixels and are not stored.
 #include <cuda_bf16.h>
@@ -34,23 +34,28 @@ void record_error(const std::string& msg);
 namespace fs {
 namespace conv {
 
-constexpr int kThreads = 256;
+constexpr int kThreads = 128;  // four warps: one per TMEM lane quarter
 constexpr int kTX = 128;       // pixels per M tile
 constexpr int kTW = kTX + 2;   // staged tile width (halo of 1)
 
 __host__ __device__ constexpr int align128(int x) { return (x + 127) & ~127; }
 
-template <int CIN, int COUT, int TY>
+template <int CIN, int COUT, int TY, int NS>
 struct Cfg {
   static constexpr int KC = CIN / 8;
+  static constexpr int NSPLIT = COUT / NS;                   // CTAs sharing one pixel tile
   static constexpr int PLANE = (TY + 2) * kTW * 16;          // bytes of one chunk plane
   static constexpr int IN_BYTES = align128(KC * PLANE);
-  static constexpr int WTAP = KC * COUT * 16;                // bytes of one tap of weights
+  static constexpr int WTAP = KC * NS * 16;                  // bytes of one tap of this CTA's weights
   static constexpr int W_BYTES = align128(WTAP);
-  static constexpr int NCOL_USED = TY * COUT;
+  // all nine taps of weights resident (one staging pass, one commit) when small
+  static constexpr bool WALL = 9 * WTAP <= 40 * 1024;
+  static constexpr int WALL_BYTES = align128(9 * WTAP);
+  static constexpr int NCOL_USED = TY * NS;
   static constexpr int NCOL = NCOL_USED <= 32 ? 32 : NCOL_USED <= 64 ? 64 : NCOL_USED <= 128 ? 128 : NCOL_USED <= 256 ? 256 : 512;
-  static constexpr int SMEM = IN_BYTES + 2 * W_BYTES + 128;  // + barriers and the TMEM slot
-  static_assert(CIN % 16 == 0 && COUT % 16 == 0 && COUT <= 256, "channel counts");
+  static constexpr int WREGION = WALL ? WALL_BYTES : 2 * W_BYTES;
+  static constexpr int SMEM = IN_BYTES + WREGION + 128;  // + barriers and the TMEM slot
+  static_assert(CIN % 16 == 0 && NS % 16 == 0 && NS <= 256 && COUT % NS == 0, "channel counts");
   static_assert(NCOL_USED <= 512, "TMEM columns");
 };
 
@@ -66,20 +71,21 @@ __device__ __forceinline__ uint32_t pack_bf16(float a, float b) {
 
 // EPI: 0 = bias, 1 = bias + ReLU (bf16 NHWC out); 2 = bias, channel 0 only,
 // f32 planar out (the network's output layer)
-template <int CIN, int COUT, int TY, int EPI>
+template <int CIN, int COUT, int TY, int NS, int EPI>
 __global__ void __launch_bounds__(kThreads) k_conv3x3(const uint4* __restrict__ in, const uint4* __restrict__ wpk,
                                                       const float* __restrict__ bias, void* __restrict__ out,
                                                       int H, int W, int* __restrict__ err) {
-  using C = Cfg<CIN, COUT, TY>;
+  using C = Cfg<CIN, COUT, TY, NS>;
   extern __shared__ __align__(128) unsigned char smem[];
   unsigned char* tile = smem;
   unsigned char* wbuf0 = smem + C::IN_BYTES;
-  uint64_t* bar = reinterpret_cast<uint64_t*>(smem + C::IN_BYTES + 2 * C::W_BYTES);
+  uint64_t* bar = reinterpret_cast<uint64_t*>(smem + C::IN_BYTES + C::WREGION);
   uint32_t* tslot = reinterpret_cast<uint32_t*>(bar + 2);
   int* failed = reinterpret_cast<int*>(bar + 3);
 
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const int x0 = blockIdx.x * kTX, y0 = blockIdx.y * TY, b = blockIdx.z;
+  const int x0 = blockIdx.x * kTX, y0 = blockIdx.y * TY;
+  const int b = blockIdx.z / C::NSPLIT, n0 = (blockIdx.z % C::NSPLIT) * NS;  // image, first output channel
 
   if (warp == 0) {
     tc::tmem_alloc(tslot, C::NCOL);
@@ -92,20 +98,65 @@ __global__ void __launch_bounds__(kThreads) k_conv3x3(const uint4* __restrict__ 
     tc::mbar_fence_init();
     *failed = 0;
   }
-  // input halo tile, periodic wrap, one 16-byte chunk (8 channels) per load
-  for (int k = tid; k < (TY + 2) * kTW * C::KC; k += kThreads) {
-    int kc = k % C::KC, rest = k / C::KC;
-    int xx = rest % kTW, yy = rest / kTW;
-    int gy = wrapm(y0 - 1 + yy, H), gx = wrapm(x0 - 1 + xx, W);
-    uint4 v = in[(((int64_t)b * H + gy) * W + gx) * C::KC + kc];
-    *reinterpret_cast<uint4*>(tile + kc * C::PLANE + (yy * kTW + xx) * 16) = v;
+  // input halo tile, periodic wrap: each thread owns one (column, 8-channel
+  // chunk) of the tile and loads its TY + 2 rows, all in flight before the
+  // shared-memory stores
+  {
+    const uint4* img = in + (int64_t)b * H * W * C::KC;
+    const bool wide = W >= kTW, tall = H >= TY + 2;  // coordinates wrap at most once
+    for (int cc = tid; cc < kTW * C::KC; cc += kThreads) {
+      const int xx = cc / C::KC, kc = cc - xx * C::KC;
+      int gx = x0 - 1 + xx;
+      gx = wide ? (gx < 0 ? gx + W : (gx >= W ? gx - W : gx)) : wrapm(gx, W);
+      const uint4* col = img + (int64_t)gx * C::KC + kc;
+      uint4 v[TY + 2];
+#pragma unroll
+      for (int yy = 0; yy < TY + 2; yy++) {
+        int gy = y0 - 1 + yy;
+        gy = tall ? (gy < 0 ? gy + H : (gy >= H ? gy - H : gy)) : wrapm(gy, H);
+        v[yy] = col[(int64_t)gy * W * C::KC];
+      }
+      unsigned char* dst = tile + kc * C::PLANE + xx * 16;
+#pragma unroll
+      for (int yy = 0; yy < TY + 2; yy++) *reinterpret_cast<uint4*>(dst + yy * kTW * 16) = v[yy];
+    }
+  }
+  if constexpr (C::WALL) {
+    // every tap's weights: global rows [tap][kc][co] of 16 bytes, this CTA's
+    // co in [n0, n0 + NS)
+    for (int k = tid; k < 9 * C::KC * NS; k += kThreads) {
+      const int blk = k / NS, co = k - blk * NS;
+      reinterpret_cast<uint4*>(wbuf0)[k] = wpk[(int64_t)blk * COUT + n0 + co];
+    }
+    tc::fence_async_smem();
   }
   __syncthreads();
   tc::fence_after_sync();
   const uint32_t taddr = *tslot;
   const uint32_t tile_s = tc::smem_u32(tile), wbuf_s = tc::smem_u32(wbuf0);
-  constexpr uint32_t IDESC = tc::idesc_bf16(128, COUT);
+  constexpr uint32_t IDESC = tc::idesc_bf16(128, NS);
 
+  if constexpr (C::WALL) {
+    // weights and tile are staged: all MMAs back to back and one commit
+    if (tid == 0) {
+#pragma unroll 1
+      for (int t = 0; t < 9; t++) {
+        const int dy = t / 3 - 1, dx = t % 3 - 1;
+        const uint32_t wb = wbuf_s + t * C::WTAP;
+#pragma unroll 1
+        for (int r = 0; r < TY; r++) {
+#pragma unroll
+          for (int j = 0; j < C::KC / 2; j++) {
+            uint32_t a = tile_s + 2 * j * C::PLANE + ((r + 1 + dy) * kTW + (1 + dx)) * 16;
+            uint32_t bb = wb + 2 * j * NS * 16;
+            tc::mma_bf16(taddr + r * NS, tc::sdesc(a, C::PLANE, 128), tc::sdesc(bb, NS * 16, 128), IDESC,
+                         (t > 0 || j > 0) ? 1u : 0u);
+          }
+        }
+      }
+      tc::mma_commit(&bar[0]);
+    }
+  } else {
   // Only thread 0 waits on the barriers; the outcome reaches the other
   // threads through *failed after a __syncthreads, so every exit is uniform.
   for (int t = 0; t < 9; t++) {
@@ -117,9 +168,11 @@ __global__ void __launch_bounds__(kThreads) k_conv3x3(const uint4* __restrict__ 
       if (*failed) break;
     }
     {
-      const uint4* src = wpk + (int64_t)t * (C::WTAP / 16);
       uint4* dst = reinterpret_cast<uint4*>(wbuf0 + buf * C::W_BYTES);
-      for (int k = tid; k < C::WTAP / 16; k += kThreads) dst[k] = src[k];
+      for (int k = tid; k < C::KC * NS; k += kThreads) {
+        const int kc = k / NS, co = k - kc * NS;
+        dst[k] = wpk[((int64_t)t * C::KC + kc) * COUT + n0 + co];
+      }
     }
     tc::fence_async_smem();
     __syncthreads();
@@ -132,15 +185,18 @@ __global__ void __launch_bounds__(kThreads) k_conv3x3(const uint4* __restrict__ 
 #pragma unroll
         for (int j = 0; j < C::KC / 2; j++) {
           uint32_t a = tile_s + 2 * j * C::PLANE + ((r + 1 + dy) * kTW + (1 + dx)) * 16;
-          uint32_t bb = wb + 2 * j * COUT * 16;
-          tc::mma_bf16(taddr + r * COUT, tc::sdesc(a, C::PLANE, 128), tc::sdesc(bb, COUT * 16, 128), IDESC,
+          uint32_t bb = wb + 2 * j * NS * 16;
+          tc::mma_bf16(taddr + r * NS, tc::sdesc(a, C::PLANE, 128), tc::sdesc(bb, NS * 16, 128), IDESC,
                        (t > 0 || j > 0) ? 1u : 0u);
         }
       }
       tc::mma_commit(&bar[buf]);
     }
   }
-  // tap 8 is the fifth use of buffer 0 (parity 0); its commit covers every MMA
+  }
+  // the last commit went to buffer 0 at parity 0 (tap 8 is the fifth use of
+  // buffer 0 in the alternating scheme; the only commit in the resident one)
+  // and covers every MMA
   if (tid == 0) {
     if (*failed) {
       // let whatever was issued drain (bounded) before the TMEM is released
@@ -153,33 +209,37 @@ __global__ void __launch_bounds__(kThreads) k_conv3x3(const uint4* __restrict__ 
   __syncthreads();
   tc::fence_after_sync();
   if (!*failed) {
-    const int q = warp & 3, half = warp >> 2;
+    constexpr int GROUPS = kThreads / 128;  // warp groups share the rows
+    const int q = warp & 3, grp = warp >> 2;
     const int p = 32 * q + lane, x = x0 + p;
     const bool xin = x < W && (x0 > 0 || p < W);
-    for (int r = half; r < TY; r += 2) {
-      const int y = y0 + r;
-      const bool valid = xin && y < H;
+#pragma unroll 1
+    for (int c0 = 0; c0 < (EPI == 2 ? 16 : NS); c0 += 16) {
+      float bv[16];
 #pragma unroll
-      for (int c0 = 0; c0 < COUT; c0 += 16) {
+      for (int k = 0; k < 16; k++) bv[k] = EPI == 2 ? (k == 0 ? bias[0] : 0.f) : bias[n0 + c0 + k];
+      for (int r = grp; r < TY; r += GROUPS) {
+        const int y = y0 + r;
+        const bool valid = xin && y < H;
         float v[16];
-        tc::tmem_ld16(taddr + ((uint32_t)(32 * q) << 16) + r * COUT + c0, v);
+        tc::tmem_ld16(taddr + ((uint32_t)(32 * q) << 16) + r * NS + c0, v);
         if (!valid) continue;
         if constexpr (EPI == 2) {
-          if (c0 == 0) reinterpret_cast<float*>(out)[((int64_t)b * H + y) * W + x] = v[0] + bias[0];
-          continue;
-        }
+          if (n0 == 0) reinterpret_cast<float*>(out)[((int64_t)b * H + y) * W + x] = v[0] + bv[0];
+        } else {
+          const int cg = n0 + c0;  // global output channel of v[0]
 #pragma unroll
-        for (int k = 0; k < 16; k++) {
-          v[k] += bias[c0 + k];
-          if (EPI == 1) v[k] = fmaxf(v[k], 0.f);
+          for (int k = 0; k < 16; k++) {
+            v[k] += bv[k];
+            if (EPI == 1) v[k] = fmaxf(v[k], 0.f);
+          }
+          uint4* o = reinterpret_cast<uint4*>(reinterpret_cast<__nv_bfloat16*>(out) +
+                                              (((int64_t)b * H + y) * W + x) * COUT + cg);
+          o[0] = make_uint4(pack_bf16(v[0], v[1]), pack_bf16(v[2], v[3]), pack_bf16(v[4], v[5]),
+                            pack_bf16(v[6], v[7]));
+          o[1] = make_uint4(pack_bf16(v[8], v[9]), pack_bf16(v[10], v[11]), pack_bf16(v[12], v[13]),
+                            pack_bf16(v[14], v[15]));
         }
-        uint4 lo = make_uint4(pack_bf16(v[0], v[1]), pack_bf16(v[2], v[3]), pack_bf16(v[4], v[5]), pack_bf16(v[6], v[7]));
-        uint4 hi = make_uint4(pack_bf16(v[8], v[9]), pack_bf16(v[10], v[11]), pack_bf16(v[12], v[13]),
-                              pack_bf16(v[14], v[15]));
-        uint4* o = reinterpret_cast<uint4*>(reinterpret_cast<__nv_bfloat16*>(out) +
-                                            (((int64_t)b * H + y) * W + x) * COUT + c0);
-        o[0] = lo;
-        o[1] = hi;
       }
     }
   }
@@ -250,19 +310,19 @@ __global__ void __launch_bounds__(128) k_gemm_check(const uint16_t* __restrict__
 }
 
 // ------------------------------------------------------------------ host
-template <int CIN, int COUT, int TY, int EPI>
+template <int CIN, int COUT, int TY, int NS, int EPI>
 static cudaError_t launch_t(const void* in, const void* w, const float* bias, void* out, int B, int H, int W,
                             int* err, cudaStream_t st) {
-  using C = Cfg<CIN, COUT, TY>;
+  using C = Cfg<CIN, COUT, TY, NS>;
   static bool attr = false;  // per process; the attribute is per device function
   if (!attr) {
-    cudaError_t e = cudaFuncSetAttribute(k_conv3x3<CIN, COUT, TY, EPI>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         C::SMEM);
+    cudaError_t e = cudaFuncSetAttribute(k_conv3x3<CIN, COUT, TY, NS, EPI>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, C::SMEM);
     if (e != cudaSuccess) return e;
     attr = true;
   }
-  dim3 grid((W + kTX - 1) / kTX, (H + TY - 1) / TY, B);
-  k_conv3x3<CIN, COUT, TY, EPI><<<grid, kThreads, C::SMEM, st>>>(
+  dim3 grid((W + kTX - 1) / kTX, (H + TY - 1) / TY, B * C::NSPLIT);
+  k_conv3x3<CIN, COUT, TY, NS, EPI><<<grid, kThreads, C::SMEM, st>>>(
       static_cast<const uint4*>(in), static_cast<const uint4*>(w), bias, out, H, W, err);
   return cudaGetLastError();
 }
@@ -270,15 +330,16 @@ static cudaError_t launch_t(const void* in, const void* w, const float* bias, vo
 template <int EPI>
 static cudaError_t dispatch(int cin, int cout, const void* in, const void* w, const float* bias, void* out, int B,
                             int H, int W, int* err, cudaStream_t st) {
-#define FS_CONV(ci, co, ty) \
-  if (cin == ci && cout == co) return launch_t<ci, co, ty, EPI>(in, w, bias, out, B, H, W, err, st);
-  FS_CONV(16, 16, 8)
-  FS_CONV(16, 32, 8)
-  FS_CONV(32, 16, 8)
-  FS_CONV(32, 64, 4)
-  FS_CONV(64, 32, 4)
-  FS_CONV(64, 128, 2)
-  FS_CONV(128, 64, 2)
+// (c_in, c_out, rows per CTA, output channels per CTA)
+#define FS_CONV(ci, co, ty, ns) \
+  if (cin == ci && cout == co) return launch_t<ci, co, ty, ns, EPI>(in, w, bias, out, B, H, W, err, st);
+  FS_CONV(16, 16, 2, 16)
+  FS_CONV(16, 32, 4, 32)
+  FS_CONV(32, 16, 2, 16)
+  FS_CONV(32, 64, 2, 32)
+  FS_CONV(64, 32, 4, 32)
+  FS_CONV(64, 128, 2, 128)
+  FS_CONV(128, 64, 2, 64)
 #undef FS_CONV
   return cudaErrorInvalidValue;
 }
@@ -319,7 +380,7 @@ extern "C" FS_API int fs_conv3x3_bf16(const void* d_in, const void* d_wpacked, c
                                       int32_t epilogue, int32_t* d_err, void* stream) {
   if (!d_in || !d_wpacked || !d_bias || !d_out || !d_err)
     return conv_fail(FS_ERR_INVALID_ARGUMENT, "fs_conv3x3_bf16: NULL pointer");
-  if (batch < 1 || h < 1 || w < 1 || epilogue < 0 || epilogue > 2)
+  if (batch < 1 || batch > 8192 || h < 1 || w < 1 || epilogue < 0 || epilogue > 2)
     return conv_fail(FS_ERR_INVALID_ARGUMENT, "fs_conv3x3_bf16: bad shape or epilogue");
   if (!conv::supported(c_in, c_out) || (epilogue == 2 && c_out != 16))
     return conv_fail(FS_ERR_UNSUPPORTED, "fs_conv3x3_bf16: channel pair " + std::to_string(c_in) + "->" +

@@ -27,6 +27,7 @@
 #include <stdio.h>
 
 #include <algorithm>
+#include <cmath>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -79,11 +80,13 @@ struct Net {
   int* err = nullptr;
   double* acc = nullptr;  // loss: per-sample mean error [B], loss [B]; guess: sum of squares
   int64_t adam_t = 0;
+  double w_p = 1.0, w_r = 0.0;  // loss weights: pressure error, residual (lap of the error)
   int capB = 0, capH = 0, capW = 0;
   bf* buf[NBUF] = {};
   float* out = nullptr;     // [B][H][W]
   float* gin = nullptr;     // solver path: h^2 d at net resolution
   float* gmask = nullptr;   // solver path: mask at net resolution
+  float* res = nullptr;     // loss: lap(out - target), [B][H][W]
   float* corr_part = nullptr;
   int64_t corr_cap = 0;
   int64_t launches = 0;
@@ -113,18 +116,19 @@ __device__ __forceinline__ uint4 pack8(const float* f) {
 }
 
 #define GRID_STRIDE(k, n) for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < (n); k += (int64_t)gridDim.x * blockDim.x)
+// element loops of the network's buffers (all below 2^31 elements, checked on the host)
+#define GRID_STRIDE32(k, n) for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < (n); k += gridDim.x * blockDim.x)
 
 // average 2x2 (out dims Ho x Wo); C8 = channels / 8
 __global__ void k_pool(const uint4* __restrict__ in, uint4* __restrict__ out, int B, int Ho, int Wo, int C8) {
-  const int64_t n = (int64_t)B * Ho * Wo * C8;
-  GRID_STRIDE(k, n) {
-    int c = (int)(k % C8);
-    int64_t r = k / C8;
-    int x = (int)(r % Wo), y = (int)((r / Wo) % Ho), b = (int)(r / ((int64_t)Wo * Ho));
+  const int n = B * Ho * Wo * C8;
+  GRID_STRIDE32(k, n) {
+    int c = k % C8, r = k / C8;
+    int x = r % Wo, t2 = r / Wo, y = t2 % Ho, b = t2 / Ho;
     float s[8] = {}, t[8];
 #pragma unroll
     for (int q = 0; q < 4; q++) {
-      int64_t src = (((int64_t)b * 2 * Ho + 2 * y + (q >> 1)) * 2 * Wo + 2 * x + (q & 1)) * C8 + c;
+      int src = ((b * 2 * Ho + 2 * y + (q >> 1)) * 2 * Wo + 2 * x + (q & 1)) * C8 + c;
       unpack8(in[src], t);
 #pragma unroll
       for (int e = 0; e < 8; e++) s[e] += t[e];
@@ -139,13 +143,12 @@ __global__ void k_pool(const uint4* __restrict__ in, uint4* __restrict__ out, in
 // skip += scale * up(coarse)
 __global__ void k_upadd(const uint4* __restrict__ coarse, const uint4* skip, uint4* out, int B, int H, int W, int C8,
                         float scale) {
-  const int64_t n = (int64_t)B * H * W * C8;
-  GRID_STRIDE(k, n) {
-    int c = (int)(k % C8);
-    int64_t r = k / C8;
-    int x = (int)(r % W), y = (int)((r / W) % H), b = (int)(r / ((int64_t)W * H));
+  const int n = B * H * W * C8;
+  GRID_STRIDE32(k, n) {
+    int c = k % C8, r = k / C8;
+    int x = r % W, t2 = r / W, y = t2 % H, b = t2 / H;
     float a[8], s[8];
-    unpack8(coarse[(((int64_t)b * (H >> 1) + (y >> 1)) * (W >> 1) + (x >> 1)) * C8 + c], a);
+    unpack8(coarse[((b * (H >> 1) + (y >> 1)) * (W >> 1) + (x >> 1)) * C8 + c], a);
     unpack8(skip[k], s);
 #pragma unroll
     for (int e = 0; e < 8; e++) s[e] = __fmaf_rn(scale, a[e], s[e]);
@@ -155,15 +158,14 @@ __global__ void k_upadd(const uint4* __restrict__ coarse, const uint4* skip, uin
 
 // coarse = sum over each 2x2 block of fine (the adjoint of nearest upsampling)
 __global__ void k_poolsum(const uint4* __restrict__ in, uint4* __restrict__ out, int B, int Ho, int Wo, int C8) {
-  const int64_t n = (int64_t)B * Ho * Wo * C8;
-  GRID_STRIDE(k, n) {
-    int c = (int)(k % C8);
-    int64_t r = k / C8;
-    int x = (int)(r % Wo), y = (int)((r / Wo) % Ho), b = (int)(r / ((int64_t)Wo * Ho));
+  const int n = B * Ho * Wo * C8;
+  GRID_STRIDE32(k, n) {
+    int c = k % C8, r = k / C8;
+    int x = r % Wo, t2 = r / Wo, y = t2 % Ho, b = t2 / Ho;
     float s[8] = {}, t[8];
 #pragma unroll
     for (int q = 0; q < 4; q++) {
-      int64_t src = (((int64_t)b * 2 * Ho + 2 * y + (q >> 1)) * 2 * Wo + 2 * x + (q & 1)) * C8 + c;
+      int src = ((b * 2 * Ho + 2 * y + (q >> 1)) * 2 * Wo + 2 * x + (q & 1)) * C8 + c;
       unpack8(in[src], t);
 #pragma unroll
       for (int e = 0; e < 8; e++) s[e] += t[e];
@@ -173,8 +175,8 @@ __global__ void k_poolsum(const uint4* __restrict__ in, uint4* __restrict__ out,
 }
 
 // g = a > 0 ? g : 0 (the ReLU's derivative, from its output)
-__global__ void k_relu_mask(uint4* __restrict__ g, const uint4* __restrict__ a, int64_t n8) {
-  GRID_STRIDE(k, n8) {
+__global__ void k_relu_mask(uint4* __restrict__ g, const uint4* __restrict__ a, int n8) {
+  GRID_STRIDE32(k, n8) {
     float gv[8], av[8];
     unpack8(g[k], gv);
     unpack8(a[k], av);
@@ -184,15 +186,24 @@ __global__ void k_relu_mask(uint4* __restrict__ g, const uint4* __restrict__ a, 
   }
 }
 
-// x0[p] = (div, mask, 0, ..., 0)
-__global__ void k_prep(const float* __restrict__ div, const float* __restrict__ mask, uint4* __restrict__ x0,
-                       int64_t npix, const double* __restrict__ sumsq, int64_t nnorm) {
-  float inv = 1.f;
-  if (sumsq) {
-    double rms = sqrt(sumsq[0] / (double)nnorm);
-    inv = rms > 0.0 ? (float)(1.0 / rms) : 1.f;
+// sigma = RMS from a sum of squares (1 when it is 0), computed by one thread
+// of the block: FP64 runs at 1/54 of the FP32 rate on this part, so it is not
+// evaluated per element
+__device__ __forceinline__ float block_sigma(const double* __restrict__ sumsq, int64_t nnorm) {
+  __shared__ float sig;
+  if (threadIdx.x == 0) {
+    double r = sqrt(sumsq[0] / (double)nnorm);
+    sig = r > 0.0 ? (float)r : 1.f;
   }
-  GRID_STRIDE(p, npix) {
+  __syncthreads();
+  return sig;
+}
+
+// x0[p] = (div / sigma, mask, 0, ..., 0); sigma = 1 without a sum of squares
+__global__ void k_prep(const float* __restrict__ div, const float* __restrict__ mask, uint4* __restrict__ x0,
+                       int npix, const double* __restrict__ sumsq, int64_t nnorm) {
+  const float inv = sumsq ? 1.f / block_sigma(sumsq, nnorm) : 1.f;
+  GRID_STRIDE32(p, npix) {
     float f[8] = {div[p] * inv, mask ? mask[p] : 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
     float z[8] = {};
     x0[2 * p] = pack8(f);
@@ -218,17 +229,60 @@ __global__ void k_loss_mean(const float* __restrict__ out, const float* __restri
   }
 }
 
-// seed gradient dL/dout = 2 (e - mean_b e) / (B N) into channel 0 of gJ, loss into acc[B]
-__global__ void k_loss_seed(const float* __restrict__ out, const float* __restrict__ tgt, double* __restrict__ acc,
-                            uint4* __restrict__ gJ, int64_t npix, int B) {
+__device__ __forceinline__ int64_t wrap_idx(int b, int y, int x, int H, int W) {
+  y = y < 0 ? y + H : (y >= H ? y - H : y);
+  x = x < 0 ? x + W : (x >= W ? x - W : x);
+  return ((int64_t)b * H + y) * W + x;
+}
+
+// res = lap(out - target) (periodic 5-point, unscaled); w_r sum res^2 / (B N) into acc[B]
+__global__ void k_loss_res(const float* __restrict__ out, const float* __restrict__ tgt, float* __restrict__ res,
+                           double* __restrict__ acc, int H, int W, int B, double w_r) {
   const int b = blockIdx.y;
+  const int64_t npix = (int64_t)H * W;
+  double s = 0.0;
+  for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < npix; p += (int64_t)gridDim.x * blockDim.x) {
+    const int pi = (int)p, y = pi / W, x = pi - y * W;
+    auto e = [&](int yy, int xx) {
+      int64_t q = wrap_idx(b, yy, xx, H, W);
+      return (double)out[q] - (double)tgt[q];
+    };
+    double r = e(y, x - 1) + e(y, x + 1) + e(y - 1, x) + e(y + 1, x) - 4.0 * e(y, x);
+    res[b * npix + p] = (float)r;
+    s += r * r;
+  }
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  __shared__ double sm[8];
+  if ((threadIdx.x & 31) == 0) sm[threadIdx.x >> 5] = s;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); w++) t += sm[w];
+    atomicAdd(&acc[B], w_r * t / ((double)B * npix));
+  }
+}
+
+// seed gradient dL/dout = (w_p 2 (e - mean_b e) + w_r 2 lap(res)) / (B N) into
+// channel 0 of gJ; w_p sum (e - mean)^2 / (B N) into acc[B]
+__global__ void k_loss_seed(const float* __restrict__ out, const float* __restrict__ tgt,
+                            const float* __restrict__ res, double* __restrict__ acc, uint4* __restrict__ gJ, int H,
+                            int W, int B, double w_p, double w_r) {
+  const int b = blockIdx.y;
+  const int64_t npix = (int64_t)H * W;
   const double mean = acc[b] / (double)npix, scale = 2.0 / ((double)B * npix);
   double s = 0.0;
   for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < npix; p += (int64_t)gridDim.x * blockDim.x) {
     int64_t q = b * npix + p;
     double ec = (double)out[q] - (double)tgt[q] - mean;
     s += ec * ec;
-    float f[8] = {(float)(scale * ec), 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    double g = w_p * ec;
+    if (res) {
+      const int pi = (int)p, y = pi / W, x = pi - y * W;
+      double lr = (double)res[wrap_idx(b, y, x - 1, H, W)] + res[wrap_idx(b, y, x + 1, H, W)] +
+                  res[wrap_idx(b, y - 1, x, H, W)] + res[wrap_idx(b, y + 1, x, H, W)] - 4.0 * res[q];
+      g += w_r * lr;
+    }
+    float f[8] = {(float)(scale * g), 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
     float z[8] = {};
     gJ[2 * q] = pack8(f);
     gJ[2 * q + 1] = pack8(z);
@@ -240,7 +294,7 @@ __global__ void k_loss_seed(const float* __restrict__ out, const float* __restri
   if (threadIdx.x == 0) {
     double t = 0.0;
     for (int w = 0; w < (int)(blockDim.x >> 5); w++) t += sm[w];
-    atomicAdd(&acc[B], t / ((double)B * npix));
+    atomicAdd(&acc[B], w_p * t / ((double)B * npix));
   }
 }
 
@@ -421,7 +475,8 @@ static cudaError_t ensure_capacity(Net* g, int B, int H, int W) {
   if (g->out) cudaFree(g->out);
   if (g->gin) cudaFree(g->gin);
   if (g->gmask) cudaFree(g->gmask);
-  g->out = g->gin = g->gmask = nullptr;
+  if (g->res) cudaFree(g->res);
+  g->out = g->gin = g->gmask = g->res = nullptr;
   cudaError_t e;
   for (int k = 0; k < NBUF; k++) {
     size_t bytes = (size_t)level_pixels(g, nB, nH, nW, kBufLevel[k]) * kBufCh[k] * 2;
@@ -431,6 +486,7 @@ static cudaError_t ensure_capacity(Net* g, int B, int H, int W) {
   if ((e = cudaMalloc(&g->out, npix * 4))) return e;
   if ((e = cudaMalloc(&g->gin, npix * 4))) return e;
   if ((e = cudaMalloc(&g->gmask, npix * 4))) return e;
+  if ((e = cudaMalloc(&g->res, npix * 4))) return e;
   g->capB = nB;
   g->capH = nH;
   g->capW = nW;
@@ -480,7 +536,7 @@ static cudaError_t upadd(const Ctx& c, Buf coarse, Buf skip, Buf out, int B, int
   return cudaGetLastError();
 }
 static cudaError_t relu_mask(const Ctx& c, Buf gbuf, Buf abuf, int B, int H, int W) {
-  int64_t n8 = level_pixels(c.g, B, H, W, kBufLevel[gbuf]) * kBufCh[gbuf] / 8;
+  int n8 = (int)(level_pixels(c.g, B, H, W, kBufLevel[gbuf]) * kBufCh[gbuf] / 8);
   GL(c, "guess_relu_mask", n8 * 48.0,
      k_relu_mask<<<blocks_for(n8), 256, 0, c.st>>>((uint4*)c.g->buf[gbuf], (const uint4*)c.g->buf[abuf], n8));
   return cudaGetLastError();
@@ -549,8 +605,13 @@ static cudaError_t backward(const Ctx& c, const float* target, int B, int H, int
   int lb = (int)((npix + 255) / 256);
   if (lb > 256) lb = 256;
   GL(c, "guess_loss", npix * B * 8.0, k_loss_mean<<<dim3(lb, B), 256, 0, c.st>>>(g->out, target, g->acc, npix));
+  const bool with_res = g->w_r != 0.0;
+  if (with_res)
+    GL(c, "guess_loss", npix * B * 12.0,
+       k_loss_res<<<dim3(lb, B), 256, 0, c.st>>>(g->out, target, g->res, g->acc, H, W, B, g->w_r));
   GL(c, "guess_loss", npix * B * 40.0,
-     k_loss_seed<<<dim3(lb, B), 256, 0, c.st>>>(g->out, target, g->acc, (uint4*)b[GJ], npix, B));
+     k_loss_seed<<<dim3(lb, B), 256, 0, c.st>>>(g->out, target, with_res ? g->res : nullptr, g->acc,
+                                                (uint4*)b[GJ], H, W, B, g->w_p, g->w_r));
   CK(cudaGetLastError());
   CK(wgrad(c, LJ, I0, GJ, B, H, W));
   CK(conv(c, LJ, true, b[GJ], b[DI0], B, H, W, 0));
@@ -633,24 +694,22 @@ static void init_params(std::vector<float>& th, const Net* g, uint64_t seed) {
 }  // namespace guess
 
 // ---------------------------------------------------------- solver hooks
-// h^2 * (d averaged over 2x2 fine cells) at net resolution, the solid mask at
-// the net cell centres, and the sum of squares of the former (for sigma).
-struct GuessDisk {
-  float x, y, r;
-};
+// The network runs at 1/f of the grid resolution (f = 1 or 2).
+// h^2 * (d averaged over f x f fine cells) at net resolution, the solid mask
+// at the net cell centres, and the sum of squares of the former (for sigma).
 __global__ void __launch_bounds__(256)
-    k_guess_in(const float* __restrict__ dh, const float* __restrict__ dl, int nx, int ny, float h2, float* gin,
-               float* gmask, const float* __restrict__ disks, int ndisk, float dxn, float dyn, float lx, float ly,
-               float width, RedCtx ctx) {
-  const int Wn = nx >> 1, Hn = ny >> 1;
-  const int64_t n = (int64_t)Wn * Hn;
+    k_guess_in(const float* __restrict__ dh, const float* __restrict__ dl, int nx, int ny, int f, float h2,
+               float* gin, float* gmask, const float* __restrict__ disks, int ndisk, float dxn, float dyn, float lx,
+               float ly, float width, RedCtx ctx) {
+  const int Wn = nx / f, Hn = ny / f;
+  const int n = Wn * Hn;  // grids are capped at 2^30 cells
   double s2 = 0.0;
-  GRID_STRIDE(k, n) {
-    int I = (int)(k % Wn), J = (int)(k / Wn);
-    int64_t c = (int64_t)(2 * J) * nx + 2 * I;
+  GRID_STRIDE32(k, n) {
+    int J = k / Wn, I = k - J * Wn;
+    int64_t c = (int64_t)(f * J) * nx + f * I;
     // the divergence is a double-float pair (MIXED) or a plain f32 field (dl == nullptr)
     auto at = [&](int64_t q) { return dl ? __fadd_rn(dh[q], dl[q]) : dh[q]; };
-    float d = 0.25f * (at(c) + at(c + 1) + at(c + nx) + at(c + nx + 1));
+    float d = f == 1 ? at(c) : 0.25f * (at(c) + at(c + 1) + at(c + nx) + at(c + nx + 1));
     float x = h2 * d;
     gin[k] = x;
     s2 += (double)x * x;
@@ -668,39 +727,45 @@ __global__ void __launch_bounds__(256)
   block_sum2_finish(s2, 0.0, ctx);
 }
 
-// pressure guess = sigma * bilinear(out) at the fine cell centres (the
-// multigrid prolongation stencil), pl = 0
+// pressure guess = sigma * out at the fine cells: a copy for f = 1, the
+// bilinear multigrid prolongation stencil for f = 2; pl = 0
 __global__ void __launch_bounds__(256) k_guess_out(const float* __restrict__ out, const double* __restrict__ sumsq,
                                                    int64_t nnorm, float* __restrict__ ph, float* __restrict__ pl,
-                                                   int nx, int ny) {
-  const int Wn = nx >> 1, Hn = ny >> 1;
-  double rms = sqrt(sumsq[0] / (double)nnorm);
-  const float sig = rms > 0.0 ? (float)rms : 1.f;
-  const int64_t n = (int64_t)nx * ny;
-  GRID_STRIDE(k, n) {
-    int i = (int)(k % nx), j = (int)(k / nx);
-    int ci0 = (i & 1) ? (i >> 1) : (i >> 1) - 1, cj0 = (j & 1) ? (j >> 1) : (j >> 1) - 1;
-    float fx = (i & 1) ? 0.25f : 0.75f, fy = (j & 1) ? 0.25f : 0.75f;
-    int x0 = ci0 < 0 ? ci0 + Wn : ci0, x1 = ci0 + 1 >= Wn ? ci0 + 1 - Wn : ci0 + 1;
-    int y0 = cj0 < 0 ? cj0 + Hn : cj0, y1 = cj0 + 1 >= Hn ? cj0 + 1 - Hn : cj0 + 1;
-    float a = out[(int64_t)y0 * Wn + x0], b = out[(int64_t)y0 * Wn + x1];
-    float c = out[(int64_t)y1 * Wn + x0], d = out[(int64_t)y1 * Wn + x1];
-    float v = ((1.f - fy) * ((1.f - fx) * a + fx * b) + fy * ((1.f - fx) * c + fx * d)) * sig;
+                                                   int nx, int ny, int f) {
+  const int Wn = nx / f, Hn = ny / f;
+  const float sig = guess::block_sigma(sumsq, nnorm);
+  const int n = nx * ny;  // grids are capped at 2^30 cells
+  GRID_STRIDE32(k, n) {
+    float v;
+    if (f == 1) {
+      v = out[k] * sig;
+    } else {
+      int j = k / nx, i = k - j * nx;
+      int ci0 = (i & 1) ? (i >> 1) : (i >> 1) - 1, cj0 = (j & 1) ? (j >> 1) : (j >> 1) - 1;
+      float fx = (i & 1) ? 0.25f : 0.75f, fy = (j & 1) ? 0.25f : 0.75f;
+      int x0 = ci0 < 0 ? ci0 + Wn : ci0, x1 = ci0 + 1 >= Wn ? ci0 + 1 - Wn : ci0 + 1;
+      int y0 = cj0 < 0 ? cj0 + Hn : cj0, y1 = cj0 + 1 >= Hn ? cj0 + 1 - Hn : cj0 + 1;
+      float a = out[(int64_t)y0 * Wn + x0], b = out[(int64_t)y0 * Wn + x1];
+      float c = out[(int64_t)y1 * Wn + x0], d = out[(int64_t)y1 * Wn + x1];
+      v = ((1.f - fy) * ((1.f - fx) * a + fx * b) + fy * ((1.f - fx) * c + fx * d)) * sig;
+    }
     ph[k] = v;
     if (pl) pl[k] = 0.f;
   }
 }
 
-bool guess_supported(const Solver* s) {
-  return s->g.nx % 16 == 0 && s->g.ny % 16 == 0 && s->g.nx >= 16 && s->g.ny >= 16;
+bool guess_supported(const Solver* s, int f) {
+  if (f != 1 && f != 2) return false;
+  const int m = 8 * f;
+  return s->g.nx % m == 0 && s->g.ny % m == 0;
 }
 
 // enqueue the guess into (ph, pl) (MIXED) or p32 (F32) on s->stream
-int guess_enqueue(Solver* s, fs_guess* handle) {
+int guess_enqueue(Solver* s, fs_guess* handle, int f) {
   guess::Net* g = reinterpret_cast<guess::Net*>(handle);
   const Grid& gr = s->g;
-  const int Wn = gr.nx >> 1, Hn = gr.ny >> 1;
-  const float h2 = (float)(4.0 * gr.dxd * gr.dxd);
+  const int Wn = gr.nx / f, Hn = gr.ny / f;
+  const float h2 = (float)(f * f * gr.dxd * gr.dxd);
   guess::Ctx c{g, s->stream, s};
   double* gsum = g->acc;
   RedCtx ctx = red_ctx(s, gsum);
@@ -711,8 +776,8 @@ int guess_enqueue(Solver* s, fs_guess* handle) {
   if (blocks > s->red_cap) blocks = s->red_cap;
   FS_LAUNCH(s, "guess_in", (double)s->n * 8,
             k_guess_in<<<blocks, 256, 0, s->stream>>>(s->mixed ? s->dh : s->div32, s->mixed ? s->dl : nullptr,
-                                                      gr.nx, gr.ny, h2, g->gin, g->gmask, dsk, nd,
-                                                      (float)(2 * gr.dxd), (float)(2 * gr.dyd), (float)s->prm.lx,
+                                                      gr.nx, gr.ny, f, h2, g->gin, g->gmask, dsk, nd,
+                                                      (float)(f * gr.dxd), (float)(f * gr.dyd), (float)s->prm.lx,
                                                       (float)s->prm.ly, (float)width, ctx));
   const int64_t npn = (int64_t)Wn * Hn;
   FS_LAUNCH(s, "guess_prep", (double)npn * 40,
@@ -722,13 +787,13 @@ int guess_enqueue(Solver* s, fs_guess* handle) {
   if (e != cudaSuccess) return fail_status(s, FS_ERR_CUDA, std::string("pressure guess: ") + cudaGetErrorString(e));
   FS_LAUNCH(s, "guess_out", (double)s->n * 8,
             k_guess_out<<<guess::blocks_for(s->n), 256, 0, s->stream>>>(
-                g->out, gsum, npn, s->mixed ? s->ph : s->p32, s->mixed ? s->pl : nullptr, gr.nx, gr.ny));
+                g->out, gsum, npn, s->mixed ? s->ph : s->p32, s->mixed ? s->pl : nullptr, gr.nx, gr.ny, f));
   return FS_OK;
 }
 
-int guess_prepare(Solver* s, fs_guess* handle) {
+int guess_prepare(Solver* s, fs_guess* handle, int f) {
   guess::Net* g = reinterpret_cast<guess::Net*>(handle);
-  cudaError_t e = guess::ensure_capacity(g, 1, s->g.ny >> 1, s->g.nx >> 1);
+  cudaError_t e = guess::ensure_capacity(g, 1, s->g.ny / f, s->g.nx / f);
   if (e != cudaSuccess) return fail_status(s, FS_ERR_OUT_OF_MEMORY, std::string("pressure guess buffers: ") + cudaGetErrorString(e));
   return FS_OK;
 }
@@ -878,7 +943,7 @@ extern "C" FS_API void fs_guess_destroy(fs_guess* h) {
   if (g->stream) cudaStreamSynchronize(g->stream);
   for (int k = 0; k < NBUF; k++)
     if (g->buf[k]) cudaFree(g->buf[k]);
-  float* fl[] = {g->theta, g->grad, g->m, g->v, g->zero_bias, g->out, g->gin, g->gmask, g->corr_part};
+  float* fl[] = {g->theta, g->grad, g->m, g->v, g->zero_bias, g->out, g->gin, g->gmask, g->res, g->corr_part};
   for (float* p : fl)
     if (p) cudaFree(p);
   if (g->wpk) cudaFree(g->wpk);
@@ -921,6 +986,8 @@ extern "C" FS_API int fs_guess_set_params(fs_guess* h, const float* host, int64_
 static int check_shape(Net* g, int B, int H, int W, const char* who) {
   if (B < 1 || H < 8 || W < 8 || H % 8 || W % 8)
     return gfail(g, FS_ERR_INVALID_ARGUMENT, std::string(who) + ": batch >= 1 and H, W multiples of 8 (>= 8)");
+  if ((int64_t)B * H * W * 16 >= ((int64_t)1 << 31))
+    return gfail(g, FS_ERR_INVALID_ARGUMENT, std::string(who) + ": batch x H x W x 16 must stay below 2^31");
   return FS_OK;
 }
 
@@ -1007,6 +1074,17 @@ extern "C" FS_API int fs_guess_train_step(fs_guess* h, const float* d_div, const
   if (e == cudaSuccess) e = repack(g, g->stream);
   if (e != cudaSuccess) return gcuda(g, e, "fs_guess_train_step");
   return loss ? read_err(g, "fs_guess_train_step") : FS_OK;
+}
+
+extern "C" FS_API int fs_guess_set_loss(fs_guess* h, double w_pressure, double w_residual) {
+  Net* g = reinterpret_cast<Net*>(h);
+  if (!g) return gfail(g, FS_ERR_INVALID_ARGUMENT, "fs_guess_set_loss: NULL handle");
+  if (!(w_pressure >= 0) || !(w_residual >= 0) || !(w_pressure + w_residual > 0) || !std::isfinite(w_pressure) ||
+      !std::isfinite(w_residual))
+    return gfail(g, FS_ERR_INVALID_ARGUMENT, "fs_guess_set_loss: weights must be finite, >= 0, not both 0");
+  g->w_p = w_pressure;
+  g->w_r = w_residual;
+  return FS_OK;
 }
 
 extern "C" FS_API int fs_guess_sync(fs_guess* h) {

@@ -109,6 +109,7 @@ struct Solver {
   // solids
   std::vector<fs_disk> disks;
   fs_guess* guess = nullptr;    // learned initial pressure (fs_set_guess), not owned
+  int guess_factor = 2;         // the network runs at 1/guess_factor of the grid
   float* imp = nullptr;         // 3 * n impulse field (x, y, torque)
   double* d_impulse = nullptr;  // 3 * disks
   int imp_cap = 0;
@@ -227,9 +228,9 @@ int fail_status(Solver* s, int code, const std::string& msg);
 void record_error(const std::string& msg);
 
 // learned pressure guess (fs_guess.cu)
-bool guess_supported(const Solver* s);
-int guess_prepare(Solver* s, fs_guess* g);   // buffers for this grid (outside any capture)
-int guess_enqueue(Solver* s, fs_guess* g);   // initial pressure from the divergence
+bool guess_supported(const Solver* s, int factor);
+int guess_prepare(Solver* s, fs_guess* g, int factor);  // buffers for this grid (outside any capture)
+int guess_enqueue(Solver* s, fs_guess* g, int factor);  // initial pressure from the divergence
 int dump_pair(Solver* s, int factor, float* div, float* mask, float* p);
 
 }  // namespace fs

@@ -41,20 +41,22 @@ __device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
   asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
 }
 __device__ __forceinline__ void mbar_fence_init() { asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory"); }
+// non-blocking probe: has the phase of the given parity completed?
 __device__ __forceinline__ bool mbar_test(uint64_t* bar, uint32_t parity) {
   uint32_t ok;
   asm volatile(
-      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+      "{\n .reg .pred p;\n mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
       : "=r"(ok)
       : "r"(smem_u32(bar)), "r"(parity)
       : "memory");
   return ok != 0;
 }
-// Waits for the phase of the given parity; gives up after `limit` polls and
-// returns false (the caller records the failure and skips the work that
-// depended on it).  try_wait itself suspends for a hardware-chosen interval,
-// so the limit is a bound of seconds, not a spin count tuned for speed.
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, uint32_t limit = 1u << 22) {
+// Spins on the phase of the given parity; gives up after `limit` probes
+// (about a second) and returns false -- the caller records the failure and
+// skips the work that depended on it.  test_wait returns at once, so the
+// waiting thread sees the completion within one probe (try_wait may suspend
+// the thread for an interval of the hardware's choosing first).
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, uint32_t limit = 1u << 26) {
   for (uint32_t k = 0; k < limit; k++)
     if (mbar_test(bar, parity)) return true;
   return false;

@@ -130,6 +130,10 @@ class PressureGuess:
                                                  C.c_float(lr), C.byref(loss) if want_loss else None))
         return loss.value if want_loss else None
 
+    def set_loss(self, w_pressure: float = 1.0, w_residual: float = 0.0) -> None:
+        """Loss = w_pressure * mean-free MSE + w_residual * mean (lap error)^2."""
+        _lib.check(self._lib.fs_guess_set_loss(self._h, float(w_pressure), float(w_residual)))
+
     def sync(self):
         _lib.check(self._lib.fs_guess_sync(self._h))
 

@@ -242,11 +242,12 @@ class GPUFluidSolver:
         return int(self._lib.fs_launch_count(self._h))
 
     # ------------------------------------------------ learned pressure guess
-    def set_guess(self, guess) -> None:
-        """Seed every projection with a PressureGuess (None detaches it);
-        the cycles still run to pressure_tol."""
+    def set_guess(self, guess, factor: int = 2) -> None:
+        """Seed every projection with a PressureGuess running at 1/factor of
+        the grid resolution (None detaches it); the cycles still run to
+        pressure_tol."""
+        self._chk(self._lib.fs_set_guess(self._h, guess.handle if guess is not None else None, factor))
         self._guess = guess  # keep it alive while attached
-        self._chk(self._lib.fs_set_guess(self._h, guess.handle if guess is not None else None))
 
     def dump_pair(self, factor: int = 1):
         """(div, mask, p) of the last projection averaged over factor x factor

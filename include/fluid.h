@@ -313,7 +313,8 @@ FS_API int fs_guess_get_params(fs_guess* g, float* host, int64_t n);
 FS_API int fs_guess_set_params(fs_guess* g, const float* host, int64_t n);
 FS_API int fs_guess_predict(fs_guess* g, const float* d_div_n, const float* d_mask, int32_t batch, int32_t h,
                             int32_t w, float* d_out);
-/* loss = mean over batch and pixels of (e - mean_b e)^2, e = out - target;
+/* loss = mean over batch and pixels of w_p (e - mean_b e)^2 + w_r (lap e)^2,
+ * e = out - target (weights from fs_guess_set_loss);
  * d_grad (nullable, n floats on the device) receives dloss/dparams */
 FS_API int fs_guess_loss_grad(fs_guess* g, const float* d_div_n, const float* d_mask, const float* d_target,
                               int32_t batch, int32_t h, int32_t w, double* loss, float* d_grad);
@@ -321,12 +322,20 @@ FS_API int fs_guess_loss_grad(fs_guess* g, const float* d_div_n, const float* d_
  * corrected).  With loss == NULL the call does not synchronise. */
 FS_API int fs_guess_train_step(fs_guess* g, const float* d_div_n, const float* d_mask, const float* d_target,
                                int32_t batch, int32_t h, int32_t w, float lr, double* loss);
+/* Loss weights (default 1, 0): w_pressure on the mean-free squared pressure
+ * error, w_residual on the squared periodic 5-point Laplacian of the error
+ * (l + r + b + t - 4c, unscaled), which in the network's units is the initial
+ * residual of the projection the guess seeds. */
+FS_API int fs_guess_set_loss(fs_guess* g, double w_pressure, double w_residual);
 FS_API int fs_guess_sync(fs_guess* g);
 FS_API int64_t fs_guess_launch_count(const fs_guess* g);
 
-/* Attach (or with NULL detach) a guess to a multigrid solver; nx, ny must be
- * multiples of 16.  The solver does not own g; keep g alive while attached. */
-FS_API int fs_set_guess(fs_solver* s, fs_guess* g);
+/* Attach (or with NULL detach) a guess to a multigrid solver.  The network
+ * runs at 1/factor of the grid resolution (factor 1 or 2; nx, ny multiples of
+ * 8 * factor); the divergence is block-averaged in and the output
+ * prolongated back (bilinear, the multigrid stencil) for factor 2.  The
+ * solver does not own g; keep g alive while attached. */
+FS_API int fs_set_guess(fs_solver* s, fs_guess* g, int32_t factor);
 
 /* The training pair of the last projection: divergence, solid mask and
  * pressure averaged over factor x factor cells (mask at the coarse cell

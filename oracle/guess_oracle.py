@@ -13,9 +13,11 @@ gradients can be checked independently.  Both sides use:
   convolution but the last;
 * parameters flattened layer by layer, each layer as w[co][ci][3][3] then
   b[co];
-* the loss: mean over batch and pixels of the squared mean-free error
-  (pressure is defined up to a constant):  e = out - target,
-  L = sum_b sum_p (e - mean_b e)^2 / (B H W).
+* the loss, with e = out - target (pressure is defined up to a constant):
+  L = w_p sum (e - mean_b e)^2 / (B H W) + w_r sum (lap e)^2 / (B H W),
+  lap the periodic 5-point stencil l + r + b + t - 4c (unscaled: in the
+  network's units lap p_n = div_n, so the second term is the initial residual
+  of the projection the guess seeds).
 
 ``rnd`` (optional) rounds a tensor to the device's storage type at each point
 where the device stores one in bf16 -- the convolution weights, every
@@ -167,12 +169,19 @@ def forward(theta, x0, rnd=_id):
     return a["out"], a
 
 
-def loss_and_seed(out, target):
+def lap5(e):
+    return (np.roll(e, 1, 1) + np.roll(e, -1, 1) + np.roll(e, 1, 2) + np.roll(e, -1, 2) - 4 * e)
+
+
+def loss_and_seed(out, target, w_p=1.0, w_r=0.0):
     B = out.shape[0]
     n = out[0].size
     e = out - target
     ec = e - e.reshape(B, -1).mean(axis=1)[:, None, None]
-    return float((ec ** 2).sum() / (B * n)), 2.0 * ec / (B * n)
+    r = lap5(e)
+    L = (w_p * (ec ** 2).sum() + w_r * (r ** 2).sum()) / (B * n)
+    g = (w_p * 2.0 * ec + w_r * 2.0 * lap5(r)) / (B * n)
+    return float(L), g
 
 
 def backward(theta, acts, gout, rnd=_id):
@@ -213,9 +222,9 @@ def backward(theta, acts, gout, rnd=_id):
     return flatten(G)
 
 
-def loss_grad(theta, div_n, mask, target, rnd=_id):
+def loss_grad(theta, div_n, mask, target, rnd=_id, w_p=1.0, w_r=0.0):
     out, acts = forward(theta, make_input(div_n, mask), rnd)
-    L, gout = loss_and_seed(out, target)
+    L, gout = loss_and_seed(out, target, w_p, w_r)
     return L, backward(theta, acts, gout, rnd), out
 
 

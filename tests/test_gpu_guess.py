@@ -61,14 +61,17 @@ def test_forward_matches_oracle(pkg, shape):
     g.close()
 
 
-def test_loss_and_gradient_match_oracle(pkg):
+@pytest.mark.parametrize("w", [(1.0, 0.0), (0.1, 1.0)])
+def test_loss_and_gradient_match_oracle(pkg, w):
     B, H, W = 2, 32, 32
     g = pkg.PressureGuess(seed=12)
+    g.set_loss(*w)
     theta = g.get_params().astype(np.float64)
     div, mask, tgt = _inputs(2, B, H, W)
     loss, grad = g.loss_grad(div, mask, tgt)
     grad = grad.cpu().numpy().astype(np.float64)
-    L, gref, _ = G.loss_grad(theta, div.astype(np.float64), mask.astype(np.float64), tgt.astype(np.float64), rnd)
+    L, gref, _ = G.loss_grad(theta, div.astype(np.float64), mask.astype(np.float64), tgt.astype(np.float64), rnd,
+                             *w)
     assert abs(loss - L) <= 2e-2 * L
     k, errs = 0, {}
     for name, ci, co, _ in G.LAYERS:
@@ -129,21 +132,22 @@ def test_training_reduces_loss(pkg):
     g.close()
 
 
-def _solver(pkg, n, disks, guess=None, tol=1e-8):
+def _solver(pkg, n, disks, guess=None, tol=1e-8, factor=2):
     s = pkg.GPUFluidSolver(n=n, nu=1e-3, advection="maccormack", pressureSolver="multigrid",
                            pressureIterations=1, precision="mixed", pressure_tol=tol, max_cycles=60)
     s.set_solids(disks)
     if guess is not None:
-        s.set_guess(guess)
+        s.set_guess(guess, factor)
     return s
 
 
-def test_solver_with_guess_converges_to_the_same_flow(pkg):
+@pytest.mark.parametrize("factor", [1, 2])
+def test_solver_with_guess_converges_to_the_same_flow(pkg, factor):
     n = 64
     u, v, disks, dt = pkg.workload.make_workload(n, seed=3)
     g = pkg.PressureGuess(seed=15)
     a = _solver(pkg, n, disks)
-    b = _solver(pkg, n, disks, g)
+    b = _solver(pkg, n, disks, g, factor=factor)
     for s in (a, b):
         s.upload_velocity(u, v)
         for _ in range(4):
@@ -186,7 +190,11 @@ def test_set_guess_rejections(pkg):
     g = pkg.PressureGuess(seed=16)
     s = pkg.GPUFluidSolver(n=72, pressureSolver="multigrid", precision="mixed", pressure_tol=1e-6)
     with pytest.raises(pkg.FluidError):
-        s.set_guess(g)
+        s.set_guess(g, 2)  # 72 is not a multiple of 16
+    with pytest.raises(pkg.FluidError):
+        s.set_guess(g, 3)
+    s.set_guess(g, 1)  # 72 = 9 * 8
+    s.set_guess(None)
     s.destroy()
     s = pkg.GPUFluidSolver(n=64, pressureSolver="jacobi", pressureIterations=10)
     with pytest.raises(pkg.FluidError):

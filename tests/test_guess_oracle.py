@@ -31,13 +31,13 @@ def test_layer_table_and_count():
     assert G.num_params() == sum(ci * co * 9 + co for _, ci, co, _ in G.LAYERS)
 
 
-@pytest.mark.parametrize("seed", [0, 1])
-def test_gradient_matches_finite_differences(seed):
+@pytest.mark.parametrize("seed,w", [(0, (1.0, 0.0)), (1, (1.0, 0.0)), (2, (0.3, 1.0))])
+def test_gradient_matches_finite_differences(seed, w):
     """One random direction per parameter block (each layer's w, then b):
     a direction over all ~200k parameters at once moves enough ReLUs across
     their kink for the central difference itself to be off."""
     rng, theta, div, mask, tgt = _problem(seed, B=2 if seed else 1)
-    L, g, _ = G.loss_grad(theta, div, mask, tgt)
+    L, g, _ = G.loss_grad(theta, div, mask, tgt, w_p=w[0], w_r=w[1])
     assert np.isfinite(L) and L > 0
     eps = 1e-6
     k = 0
@@ -46,8 +46,8 @@ def test_gradient_matches_finite_differences(seed):
             d = np.zeros_like(theta)
             d[k:k + size] = rng.standard_normal(size)
             k += size
-            lp = G.loss_grad(theta + eps * d, div, mask, tgt)[0]
-            lm = G.loss_grad(theta - eps * d, div, mask, tgt)[0]
+            lp = G.loss_grad(theta + eps * d, div, mask, tgt, w_p=w[0], w_r=w[1])[0]
+            lm = G.loss_grad(theta - eps * d, div, mask, tgt, w_p=w[0], w_r=w[1])[0]
             fd = (lp - lm) / (2 * eps)
             assert abs(fd - g @ d) <= 1e-6 * max(1.0, abs(fd)), (name, size, fd, g @ d)
 
