@@ -186,10 +186,48 @@ def traffic_from_profiles(kernel: str):
         return None
 
 
+GUESS_WEIGHTS = ROOT / "fluid-sim_gb300" / "weights" / "guess_2048_f2.fsguess"
+GUESS_FACTOR = 2
+
+
 def make_solver(pkg, n, device, guess="zero"):
-    return pkg.GPUFluidSolver(n=n, nu=NU, advection="maccormack", pressure_solver="multigrid",
-                              pressure_iterations=1, precision="mixed", pressure_tol=TOL, max_cycles=60,
-                              warm_start=(guess == "warm"), device=device)
+    """guess: "zero" (the reference's zero initial pressure), "warm" (the
+    previous step's pressure) or "nn" (the trained pressure-guess network at
+    half resolution, weights committed under fluid-sim_gb300/weights/)."""
+    s = pkg.GPUFluidSolver(n=n, nu=NU, advection="maccormack", pressure_solver="multigrid",
+                           pressure_iterations=1, precision="mixed", pressure_tol=TOL, max_cycles=60,
+                           warm_start=(guess == "warm"), device=device)
+    if guess == "nn":
+        g = pkg.PressureGuess(device=device)
+        g.load(GUESS_WEIGHTS)
+        s.set_guess(g, GUESS_FACTOR)
+    return s
+
+
+def step_bytes(cycles: float) -> float:
+    """Algorithmic HBM bytes per cell-step of the whole step: 48 B/cell for
+    advection + diffusion, divergence and gradient subtraction on f32 fields,
+    +48 B/cell for the state carried at 8 B/value, and 98 B/cell per V(2,2)
+    cycle over all levels (4 sweeps, residual, restriction, prolongation)."""
+    return 96.0 + 98.0 * cycles
+
+
+def measure_variant(pkg, n, device, guess, u0, v0, disks, dt, steps, warmup):
+    """ms/step, cycles/step and cell-steps/s of one initial-pressure choice."""
+    s = make_solver(pkg, n, device, guess)
+    s.upload_velocity(u0, v0)
+    s.set_solids(disks)
+    for _ in range(warmup):
+        s.step(dt)
+    ms = s.time_steps(dt, steps)
+    cyc = []
+    for _ in range(5):
+        s.step(dt)
+        cyc.append(s.last_stats()["cycles"])
+    md = s.max_divergence()
+    s.destroy()
+    return {"ms_per_step": ms / steps, "cycles_per_step": float(np.mean(cyc)),
+            "value": float(n) * n * steps / (ms / 1e3), "max_div_after": md}
 
 
 # ------------------------------------------------------------------- GPU arm
@@ -262,6 +300,16 @@ def run_gpu(args):
     lib.fs_host_free(hu)
     lib.fs_host_free(hv)
 
+    # the learned guess and the warm start against the zero initial pressure,
+    # same workload, same tolerance, each timed over the same K steps
+    variants = {}
+    if not args.no_variants:
+        for name, g in (("plain_mg", args.guess), ("nn_guess_mg", "nn"), ("warm_start_mg", "warm")):
+            if name != "plain_mg" and g == args.guess:
+                continue
+            variants[name] = measure_variant(pkg, n, local, g, u0, v0, disks, dt, args.steps, args.warmup)
+            variants[name]["guess"] = g
+
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         cpu = cpu_baseline(n, threads=1, timed_steps=1)
@@ -293,9 +341,17 @@ def run_gpu(args):
                         for k in sorted(prof, key=lambda k: -k["total_ms"])],
             "e2e": {"value": e2e_val, "unit": UNIT, "h2d_bytes_per_step": 2 * nbytes,
                     "d2h_bytes_per_step": 2 * nbytes, "steps": e2e_steps},
+            "step_roofline": {
+                "bytes_per_cell_step": step_bytes(float(np.mean(cyc))),
+                "achieved": value * step_bytes(float(np.mean(cyc))) / 1e9 / max(world, 1),
+                "peak": peak, "unit": "GB/s",
+                "frac": value * step_bytes(float(np.mean(cyc))) / 1e9 / max(world, 1) / peak,
+            },
             "gpu_launches": launches,
             "clocks": clk.summary(),
         }
+        if variants:
+            line["guess_comparison"] = variants
         if cpu is not None:
             line["cpu_baseline"] = cpu
         print(json.dumps(line), flush=True)
@@ -377,7 +433,9 @@ def main():
     ap.add_argument("--warmup", type=int, default=10)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--n", type=int, default=N)
-    ap.add_argument("--guess", default="zero", choices=["zero", "warm"])
+    ap.add_argument("--guess", default="zero", choices=["zero", "warm", "nn"])
+    ap.add_argument("--no-variants", action="store_true",
+                    help="skip timing the learned guess and the warm start beside the headline")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl != "reference":

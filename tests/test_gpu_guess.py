@@ -201,3 +201,33 @@ def test_set_guess_rejections(pkg):
         s.set_guess(g)
     s.destroy()
     g.close()
+
+
+def test_trained_guess_saves_cycles_on_a_held_out_flow(pkg):
+    """The committed network (trained by fluid-sim_gb300/guess_train.py on
+    pairs dumped from 2048^2 runs with seeds 1000-1007) on a seed it never saw:
+    a smaller initial residual and fewer V-cycles per step to the same
+    max|div u| <= 1e-6 than the zero initial pressure."""
+    from pathlib import Path
+
+    weights = Path(pkg.__file__).parent / "weights" / "guess_2048_f2.fsguess"
+    n = 2048
+    u, v, disks, dt = pkg.workload.make_workload(n, seed=77)
+    g = pkg.PressureGuess()
+    g.load(weights)
+    stats = {}
+    for name, guess in (("plain", None), ("nn", g)):
+        s = _solver(pkg, n, disks, guess, tol=1e-6)
+        s.upload_velocity(u, v)
+        cyc, r0 = [], []
+        for _ in range(6):
+            s.step(dt)
+            st = s.last_stats()
+            assert st["converged"]
+            cyc.append(st["cycles"])
+            r0.append(st["residual_initial"])
+        stats[name] = (np.mean(cyc), np.median(r0))
+        s.destroy()
+    g.close()
+    assert stats["nn"][1] < stats["plain"][1] / 1.5, stats
+    assert stats["nn"][0] <= stats["plain"][0] - 0.5, stats
