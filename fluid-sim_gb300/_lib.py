@@ -154,6 +154,15 @@ SIGNATURES = {
     "fs_guess_sync": (I, [VP]),
     "fs_guess_launch_count": (C.c_int64, [VP]),
     "fs_set_guess": (I, [VP, VP, C.c_int32]),
+    "fs_batch_create": (I, [C.POINTER(Params), C.c_int32, C.POINTER(VP)]),
+    "fs_batch_destroy": (None, [VP]),
+    "fs_batch_size": (C.c_int32, [VP]),
+    "fs_batch_member": (VP, [VP, C.c_int32]),
+    "fs_batch_last_error": (C.c_char_p, [VP]),
+    "fs_batch_step": (I, [VP, C.POINTER(D)]),
+    "fs_batch_sync": (I, [VP]),
+    "fs_batch_time_steps": (I, [VP, C.POINTER(D), C.c_int32, C.POINTER(D)]),
+    "fs_batch_launch_count": (C.c_int64, [VP]),
     "fs_dump_pair": (I, [VP, C.c_int32, VP, VP, VP]),
     "fs_write_pair_file": (I, [C.c_char_p, C.c_int32, C.c_int32, D, VP, VP, VP]),
     "fs_read_pair_file": (I, [C.c_char_p, C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.POINTER(D), VP, VP, VP]),

@@ -105,7 +105,11 @@ static void free_all(Solver* s) {
   if (s->graph_exec) cudaGraphExecDestroy(s->graph_exec);
   if (s->h_red) cudaFreeHost(s->h_red);
   if (s->body_stream) cudaStreamDestroy(s->body_stream);
-  if (s->stream) cudaStreamDestroy(s->stream);
+  if (s->own_stream) {
+    cudaStreamDestroy(s->own_stream);  // batch member: s->stream is the batch's
+  } else if (s->stream) {
+    cudaStreamDestroy(s->stream);
+  }
 }
 
 static int sync(Solver* s) {
@@ -494,6 +498,7 @@ static void drop_graph(Solver* s) {
   if (s->graph_exec) cudaGraphExecDestroy(s->graph_exec);
   s->graph_exec = nullptr;
   s->graph_ok = false;
+  s->batch_dirty = true;
 }
 
 // Capture one step into a CUDA graph (the fused multigrid configurations):
@@ -1043,3 +1048,225 @@ FS_API void fs_host_free(void* p) {
 }
 
 }  // extern "C"
+
+// ====================================================================== batch
+// Many independent simulations, uneven sizes, advanced together: one CUDA
+// graph whose branches are the members' captured steps (each with its own
+// conditional tolerance loop), launched once per batch step.  Members are
+// ordinary solvers whose eager work (uploads, read-backs, statistics) runs on
+// the batch's stream, so it is ordered with the batch launches without
+// per-step events; while the batch graph is captured each member's step runs
+// on its own stream, forked from and joined back to the batch stream, so the
+// branches are independent and their kernels overlap on the GPU.
+struct fs_batch {
+  std::vector<fs_solver*> members;
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t fork = nullptr;
+  std::vector<cudaEvent_t> joins;
+  cudaGraphExec_t exec = nullptr;
+  std::vector<double> dts;
+  int64_t replays = 0;
+  std::string err;
+};
+
+namespace fs {
+
+static int bfail(fs_batch* b, int code, const std::string& m) {
+  if (b) b->err = m;
+  g_create_error = m;
+  return code;
+}
+
+static void batch_free(fs_batch* b) {
+  if (!b) return;
+  cudaSetDevice(b->device);
+  if (b->stream) cudaStreamSynchronize(b->stream);
+  if (b->exec) cudaGraphExecDestroy(b->exec);
+  for (fs_solver* h : b->members) {
+    if (!h) continue;
+    for (auto& p : h->s.pending) { cudaEventDestroy(p.a); cudaEventDestroy(p.b); }
+    free_all(&h->s);
+    delete h;
+  }
+  for (cudaEvent_t e : b->joins) cudaEventDestroy(e);
+  if (b->fork) cudaEventDestroy(b->fork);
+  if (b->stream) cudaStreamDestroy(b->stream);
+  delete b;
+}
+
+static int batch_build(fs_batch* b, const double* dt) {
+  if (b->exec) cudaGraphExecDestroy(b->exec);
+  b->exec = nullptr;
+  const int n = (int)b->members.size();
+  std::vector<int64_t> l0(n);
+  cudaError_t e = cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal);
+  if (e != cudaSuccess) return bfail(b, FS_ERR_CUDA, std::string("batch capture: ") + cudaGetErrorString(e));
+  e = cudaEventRecord(b->fork, b->stream);
+  int rc = e == cudaSuccess ? FS_OK : FS_ERR_CUDA;
+  for (int i = 0; i < n && rc == FS_OK; i++) {
+    Solver* s = &b->members[i]->s;
+    std::swap(s->stream, s->own_stream);  // this member's branch
+    if (cudaStreamWaitEvent(s->stream, b->fork, 0) != cudaSuccess) rc = FS_ERR_CUDA;
+    l0[i] = s->launches;
+    if (rc == FS_OK) rc = enqueue_step(s, dt[i], true);
+    if (rc == FS_OK && cudaEventRecord(b->joins[i], s->stream) != cudaSuccess) rc = FS_ERR_CUDA;
+    if (rc == FS_OK && cudaStreamWaitEvent(b->stream, b->joins[i], 0) != cudaSuccess) rc = FS_ERR_CUDA;
+    std::swap(s->stream, s->own_stream);
+    if (rc != FS_OK && !s->err.empty()) b->err = "member " + std::to_string(i) + ": " + s->err;
+  }
+  cudaGraph_t g = nullptr;
+  e = cudaStreamEndCapture(b->stream, &g);
+  if (rc != FS_OK) {
+    if (g) cudaGraphDestroy(g);
+    return bfail(b, rc, b->err.empty() ? std::string("batch capture failed") : b->err);
+  }
+  if (e != cudaSuccess) return bfail(b, FS_ERR_CUDA, std::string("batch capture: ") + cudaGetErrorString(e));
+  e = cudaGraphInstantiate(&b->exec, g, 0);
+  cudaGraphDestroy(g);
+  if (e != cudaSuccess) return bfail(b, FS_ERR_CUDA, std::string("batch instantiate: ") + cudaGetErrorString(e));
+  for (int i = 0; i < n; i++) {
+    Solver* s = &b->members[i]->s;
+    int64_t captured = s->launches - l0[i];
+    s->batch_launches_fixed = captured - (s->prm.pressure_tol > 0 ? s->graph_launches_body : 0);
+    s->launches = l0[i];  // counted when the graph runs
+    s->batch_dirty = false;
+  }
+  b->dts.assign(dt, dt + n);
+  return FS_OK;
+}
+
+}  // namespace fs
+
+FS_API int fs_batch_create(const fs_params* params, int32_t count, fs_batch** out) {
+  if (!out) return bfail(nullptr, FS_ERR_INVALID_ARGUMENT, "out is NULL");
+  *out = nullptr;
+  if (!params || count < 1 || count > 65536) return bfail(nullptr, FS_ERR_INVALID_ARGUMENT, "bad params or count");
+  for (int i = 1; i < count; i++)
+    if (params[i].device != params[0].device)
+      return bfail(nullptr, FS_ERR_INVALID_ARGUMENT, "every member must be on the same device");
+  fs_batch* b = new (std::nothrow) fs_batch();
+  if (!b) return bfail(nullptr, FS_ERR_OUT_OF_MEMORY, "host allocation failed");
+  b->device = params[0].device;
+  b->members.assign(count, nullptr);
+  for (int i = 0; i < count; i++) {
+    fs_solver* h = nullptr;
+    int rc = fs_create(&params[i], &h);
+    if (rc != FS_OK) {
+      std::string m = "member " + std::to_string(i) + ": " + g_create_error;
+      batch_free(b);
+      return bfail(nullptr, rc, m);
+    }
+    b->members[i] = h;
+    if (!h->s.fused) {
+      batch_free(b);
+      return bfail(nullptr, FS_ERR_UNSUPPORTED,
+                   "member " + std::to_string(i) + ": batches need the fused multigrid step (pressure_solver = "
+                   "MULTIGRID, kernel_variant = 0, nx == ny)");
+    }
+  }
+  cudaSetDevice(b->device);
+  cudaError_t e = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming);
+  b->joins.assign(count, nullptr);
+  for (int i = 0; i < count && e == cudaSuccess; i++) e = cudaEventCreateWithFlags(&b->joins[i], cudaEventDisableTiming);
+  if (e != cudaSuccess) {
+    batch_free(b);
+    return bfail(nullptr, FS_ERR_CUDA, std::string("fs_batch_create: ") + cudaGetErrorString(e));
+  }
+  for (fs_solver* h : b->members) {
+    Solver* s = &h->s;
+    cudaStreamSynchronize(s->stream);  // creation work is done before the stream changes hands
+    s->own_stream = s->stream;
+    s->stream = b->stream;
+  }
+  *out = b;
+  return FS_OK;
+}
+
+FS_API void fs_batch_destroy(fs_batch* b) { batch_free(b); }
+
+FS_API int32_t fs_batch_size(const fs_batch* b) { return b ? (int32_t)b->members.size() : 0; }
+
+FS_API fs_solver* fs_batch_member(fs_batch* b, int32_t index) {
+  if (!b || index < 0 || index >= (int32_t)b->members.size()) return nullptr;
+  return b->members[index];
+}
+
+FS_API const char* fs_batch_last_error(const fs_batch* b) { return b ? b->err.c_str() : g_create_error.c_str(); }
+
+FS_API int fs_batch_step(fs_batch* b, const double* dt) {
+  if (!b) return bfail(nullptr, FS_ERR_INVALID_ARGUMENT, "batch is NULL");
+  if (!dt) return bfail(b, FS_ERR_INVALID_ARGUMENT, "dt is NULL");
+  if (cudaSetDevice(b->device) != cudaSuccess) return bfail(b, FS_ERR_CUDA, "cudaSetDevice failed");
+  const int n = (int)b->members.size();
+  bool rebuild = !b->exec;
+  for (int i = 0; i < n; i++) {
+    if (!std::isfinite(dt[i])) return bfail(b, FS_ERR_INVALID_ARGUMENT, "dt must be finite");
+    if (b->members[i]->s.batch_dirty || b->dts.empty() || b->dts[i] != dt[i]) rebuild = true;
+  }
+  if (rebuild) {
+    int rc = batch_build(b, dt);
+    if (rc) return rc;
+  }
+  cudaError_t e = cudaGraphLaunch(b->exec, b->stream);
+  if (e != cudaSuccess) return bfail(b, FS_ERR_CUDA, std::string("batch launch: ") + cudaGetErrorString(e));
+  b->replays++;
+  for (int i = 0; i < n; i++) {
+    Solver* s = &b->members[i]->s;
+    s->stats_on_device = s->prm.pressure_tol > 0;
+    if (!s->stats_on_device) s->stats = fs_step_stats{s->prm.pressure_iterations, 1, -1.0, -1.0};
+    s->t += dt[i];
+    s->steps++;
+  }
+  return FS_OK;
+}
+
+FS_API int fs_batch_sync(fs_batch* b) {
+  if (!b) return bfail(nullptr, FS_ERR_INVALID_ARGUMENT, "batch is NULL");
+  cudaSetDevice(b->device);
+  cudaError_t e = cudaStreamSynchronize(b->stream);
+  return e == cudaSuccess ? FS_OK : bfail(b, FS_ERR_CUDA, std::string("batch: ") + cudaGetErrorString(e));
+}
+
+FS_API int fs_batch_time_steps(fs_batch* b, const double* dt, int32_t nsteps, double* elapsed_ms) {
+  if (!b || !elapsed_ms || nsteps < 0) return bfail(b, FS_ERR_INVALID_ARGUMENT, "bad arguments");
+  cudaSetDevice(b->device);
+  cudaEvent_t a, z;
+  if (cudaEventCreate(&a) != cudaSuccess || cudaEventCreate(&z) != cudaSuccess)
+    return bfail(b, FS_ERR_CUDA, "cudaEventCreate failed");
+  int rc = fs_batch_sync(b);
+  if (rc == FS_OK && nsteps > 0 && (!b->exec || b->dts.size() != b->members.size() ||
+                                    !std::equal(b->dts.begin(), b->dts.end(), dt))) {
+    // capture before the timed region
+    rc = batch_build(b, dt);
+  }
+  cudaEventRecord(a, b->stream);
+  for (int k = 0; k < nsteps && rc == FS_OK; k++) rc = fs_batch_step(b, dt);
+  cudaEventRecord(z, b->stream);
+  cudaEventSynchronize(z);
+  float ms = 0;
+  cudaEventElapsedTime(&ms, a, z);
+  cudaEventDestroy(a);
+  cudaEventDestroy(z);
+  *elapsed_ms = ms;
+  return rc;
+}
+
+// kernels launched by the batch's graph replays so far (synchronises)
+FS_API int64_t fs_batch_launch_count(fs_batch* b) {
+  if (!b) return 0;
+  cudaSetDevice(b->device);
+  cudaStreamSynchronize(b->stream);
+  int64_t n = 0;
+  for (fs_solver* h : b->members) {
+    const Solver* s = &h->s;
+    n += b->replays * s->batch_launches_fixed;
+    if (s->graph_launches_body > 0) {
+      DevState d;
+      if (cudaMemcpy(&d, s->dev, sizeof(DevState), cudaMemcpyDeviceToHost) == cudaSuccess)
+        n += d.total_cycles * s->graph_launches_body;
+    }
+  }
+  return n;
+}

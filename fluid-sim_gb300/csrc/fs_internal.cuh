@@ -127,6 +127,12 @@ struct Solver {
   bool graph_ok = false;        // graph_exec matches the current forcing / solids
   bool stats_on_device = false; // the last projection ran inside a graph
   cudaStream_t body_stream = nullptr;  // captures the body of the tolerance loop
+  // batch membership: eager work goes to the batch's shared stream; own_stream
+  // (the solver's original stream) carries its branch while the batch graph
+  // is captured.  batch_dirty: the captured step no longer matches.
+  cudaStream_t own_stream = nullptr;
+  bool batch_dirty = true;
+  int64_t batch_launches_fixed = 0;
   int64_t graph_launches_fixed = 0;    // kernels per replay outside the loop body
   int64_t graph_launches_body = 0;     // kernels per loop iteration
   int64_t graph_replays = 0;

@@ -27,6 +27,46 @@ def _ptr(a: np.ndarray):
     return C.c_void_p(a.ctypes.data)
 
 
+def make_params(n: int = 256, nx: int | None = None, ny: int | None = None, lx: float = 2 * math.pi,
+                ly: float = 2 * math.pi, nu: float = 0.0, confinement: float = 0.0, advection: str = "maccormack",
+                solid_mask_width: float = 1.5, pressure_solver: str = "jacobi", pressure_iterations: int = 40,
+                precision: str = "f32", pressure_tol: float = 0.0, max_cycles: int = 50, mg_pre_smooth: int = 2,
+                mg_post_smooth: int = 2, mg_coarse_sweeps: int = 40, mg_min_size: int = 8,
+                warm_start: bool = False, device: int = 0, kernel_variant: int = 0, **camel) -> "L.Params":
+    """fs_params from the reference's option names (camelCase accepted);
+    unknown names are rejected (the reference silently defaults)."""
+    solid_mask_width = camel.pop("solidMaskWidth", solid_mask_width)
+    pressure_solver = camel.pop("pressureSolver", pressure_solver)
+    pressure_iterations = camel.pop("pressureIterations", pressure_iterations)
+    if camel:
+        raise TypeError(f"unknown options {sorted(camel)}")
+    lib = L.load()
+    p = L.Params()
+    lib.fs_params_default(C.byref(p))
+    p.nx = nx or n
+    p.ny = ny or n
+    p.lx, p.ly, p.nu, p.confinement = lx, ly, nu, confinement
+    if advection not in ADVECTION:
+        raise L.FluidError(1, f"unknown advection scheme {advection!r}")
+    if pressure_solver not in PRESSURE:
+        raise L.FluidError(1, f"unknown pressure solver {pressure_solver!r}")
+    if precision not in PRECISION:
+        raise L.FluidError(1, f"unknown precision {precision!r}")
+    p.advection = ADVECTION[advection]
+    p.solid_mask_width = solid_mask_width
+    p.pressure_solver = PRESSURE[pressure_solver]
+    p.pressure_iterations = pressure_iterations
+    p.precision = PRECISION[precision]
+    p.pressure_tol = pressure_tol
+    p.max_cycles = max_cycles
+    p.mg_pre_smooth, p.mg_post_smooth = mg_pre_smooth, mg_post_smooth
+    p.mg_coarse_sweeps, p.mg_min_size = mg_coarse_sweeps, mg_min_size
+    p.warm_start = int(bool(warm_start))
+    p.device = device
+    p.kernel_variant = kernel_variant
+    return p
+
+
 class GPUFluidSolver:
     """new GPUFluidSolver(device, {n, nx, ny, lx, ly, nu, confinement, advection,
     solidMaskWidth, pressureSolver, pressureIterations}) -- src/gpu/solver.js:65-98.
@@ -43,57 +83,50 @@ class GPUFluidSolver:
                  pressure_tol: float = 0.0, max_cycles: int = 50, mg_pre_smooth: int = 2,
                  mg_post_smooth: int = 2, mg_coarse_sweeps: int = 40, mg_min_size: int = 8,
                  warm_start: bool = False, device: int = 0, kernel_variant: int = 0, **camel):
-        # accept the reference's camelCase option names too
-        solid_mask_width = camel.pop("solidMaskWidth", solid_mask_width)
-        pressure_solver = camel.pop("pressureSolver", pressure_solver)
-        pressure_iterations = camel.pop("pressureIterations", pressure_iterations)
-        if camel:
-            raise TypeError(f"unknown options {sorted(camel)}")
+        p = make_params(n=n, nx=nx, ny=ny, lx=lx, ly=ly, nu=nu, confinement=confinement, advection=advection,
+                        solid_mask_width=solid_mask_width, pressure_solver=pressure_solver,
+                        pressure_iterations=pressure_iterations, precision=precision, pressure_tol=pressure_tol,
+                        max_cycles=max_cycles, mg_pre_smooth=mg_pre_smooth, mg_post_smooth=mg_post_smooth,
+                        mg_coarse_sweeps=mg_coarse_sweeps, mg_min_size=mg_min_size, warm_start=warm_start,
+                        device=device, kernel_variant=kernel_variant, **camel)
         lib = L.load()
-        p = L.Params()
-        lib.fs_params_default(C.byref(p))
-        p.nx = nx or n
-        p.ny = ny or n
-        p.lx, p.ly, p.nu, p.confinement = lx, ly, nu, confinement
-        # unknown names are rejected here (the reference silently defaults)
-        if advection not in ADVECTION:
-            raise L.FluidError(1, f"unknown advection scheme {advection!r}")
-        if pressure_solver not in PRESSURE:
-            raise L.FluidError(1, f"unknown pressure solver {pressure_solver!r}")
-        if precision not in PRECISION:
-            raise L.FluidError(1, f"unknown precision {precision!r}")
-        p.advection = ADVECTION[advection]
-        p.solid_mask_width = solid_mask_width
-        p.pressure_solver = PRESSURE[pressure_solver]
-        p.pressure_iterations = pressure_iterations
-        p.precision = PRECISION[precision]
-        p.pressure_tol = pressure_tol
-        p.max_cycles = max_cycles
-        p.mg_pre_smooth, p.mg_post_smooth = mg_pre_smooth, mg_post_smooth
-        p.mg_coarse_sweeps, p.mg_min_size = mg_coarse_sweeps, mg_min_size
-        p.warm_start = int(bool(warm_start))
-        p.device = device
-        p.kernel_variant = kernel_variant
         h = C.c_void_p()
         L.check(lib.fs_create(C.byref(p), C.byref(h)), None)
+        self._adopt(lib, h, p, owned=True)
+
+    def _adopt(self, lib, h, p, owned: bool) -> None:
         self._h = h
         self._lib = lib
+        self._owned = owned
         self.params = p
         self.nx, self.ny = p.nx, p.ny
         self.n = p.nx * p.ny
-        self.dx, self.dy = lx / p.nx, ly / p.ny
-        self.nu = nu
-        self.advection = advection
-        self.pressure_solver = pressure_solver
-        self.pressure_iterations = pressure_iterations
-        self.precision = precision
+        self.lx, self.ly = p.lx, p.ly
+        self.dx, self.dy = p.lx / p.nx, p.ly / p.ny
+        self.nu = p.nu
+        self.advection = {v: k for k, v in ADVECTION.items()}[p.advection]
+        self.pressure_solver = {v: k for k, v in PRESSURE.items()}[p.pressure_solver]
+        self.pressure_iterations = p.pressure_iterations
+        self.precision = {v: k for k, v in PRECISION.items()}[p.precision]
         self.solid = None
+
+    @classmethod
+    def _member(cls, lib, handle, keep_alive):
+        """A solver owned by a batch (fs_batch_member): same methods, not destroyed here."""
+        self = cls.__new__(cls)
+        p = L.Params()
+        h = C.c_void_p(handle)
+        L.check(lib.fs_get_params(h, C.byref(p)), None)
+        self._adopt(lib, h, p, owned=False)
+        self._batch = keep_alive
+        return self
 
     # ------------------------------------------------------------ lifecycle
     def destroy(self) -> None:
-        """destroy() (solver.js:898-911)"""
+        """destroy() (solver.js:898-911); a batch member is freed with its batch"""
         if getattr(self, "_h", None):
-            self._lib.fs_destroy(self._h)
+            if getattr(self, "_owned", True):
+                self._lib.fs_destroy(self._h)
             self._h = None
 
     def __del__(self):
@@ -258,3 +291,63 @@ class GPUFluidSolver:
         p = np.empty_like(d)
         self._chk(self._lib.fs_dump_pair(self._h, factor, _ptr(d), _ptr(m), _ptr(p)))
         return d, m, p, self.dx * factor
+
+
+class GPUFluidBatch:
+    """Many independent solvers of uneven sizes advanced by one CUDA graph
+    launch per step (fs_batch_*).  ``configs`` is a list of GPUFluidSolver
+    option dicts; ``members[i]`` are GPUFluidSolver views owned by the batch
+    (upload, read back, set solids, read stats as usual)."""
+
+    def __init__(self, configs: Sequence[dict]):
+        lib = L.load()
+        ps = (L.Params * len(configs))()
+        for i, cfg in enumerate(configs):
+            ps[i] = make_params(**cfg)
+        h = C.c_void_p()
+        st = lib.fs_batch_create(ps, len(configs), C.byref(h))
+        if st != L.FS_OK:
+            raise L.FluidError(st, lib.fs_batch_last_error(None).decode())
+        self._h = h
+        self._lib = lib
+        self.members = [GPUFluidSolver._member(lib, lib.fs_batch_member(h, i), self) for i in range(len(configs))]
+
+    def _chk(self, st: int) -> None:
+        if st != L.FS_OK:
+            raise L.FluidError(st, self._lib.fs_batch_last_error(self._h).decode())
+
+    def _dts(self, dt):
+        n = len(self.members)
+        d = np.broadcast_to(np.asarray(dt, np.float64), (n,)).copy()
+        return d, d.ctypes.data_as(C.POINTER(C.c_double))
+
+    def step(self, dt) -> None:
+        """one step of every member (dt scalar or one per member)"""
+        d, ptr = self._dts(dt)
+        self._chk(self._lib.fs_batch_step(self._h, ptr))
+        self._last = d
+
+    def sync(self) -> None:
+        self._chk(self._lib.fs_batch_sync(self._h))
+
+    def time_steps(self, dt, nsteps: int) -> float:
+        d, ptr = self._dts(dt)
+        ms = C.c_double()
+        self._chk(self._lib.fs_batch_time_steps(self._h, ptr, nsteps, C.byref(ms)))
+        return ms.value
+
+    def launch_count(self) -> int:
+        return int(self._lib.fs_batch_launch_count(self._h))
+
+    def destroy(self) -> None:
+        if getattr(self, "_h", None):
+            for m in self.members:
+                m._h = None
+            self._lib.fs_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.destroy()
+        except Exception:
+            pass

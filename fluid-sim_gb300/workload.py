@@ -44,3 +44,46 @@ def make_workload(n: int = 2048, seed: int = 5):
     umax = float(max(np.abs(u).max(), np.abs(v).max()))
     dt = 0.5 * h / umax
     return np.ascontiguousarray(u.ravel()), np.ascontiguousarray(v.ravel()), disks, dt
+
+
+def vortex_blobs(n: int, seed: int, L: float = 2 * math.pi):
+    """Seeded decaying-vortex initial state: 4-16 Gaussian blobs of radius
+    0.05-0.15 L with circulation ~ N(0, 1), periodic images included; the
+    streamfunction comes from the spectral inversion of the vorticity at the
+    cell corners and the MAC velocity from its differences, so the field is
+    exactly divergence-free on the grid.  Returns (u, v, dt) with dt at CFL 0.5."""
+    rng = np.random.default_rng(seed)
+    h = L / n
+    x = np.arange(n) * h
+    X, Y = np.meshgrid(x, x)  # corners (i h, j h), [j, i]
+    w = np.zeros((n, n))
+    for _ in range(int(rng.integers(4, 17))):
+        r = float(rng.uniform(0.05, 0.15)) * L
+        cx, cy = rng.uniform(0, L, size=2)
+        gam = float(rng.normal())
+        dx = X - cx
+        dy = Y - cy
+        dx -= L * np.round(dx / L)
+        dy -= L * np.round(dy / L)
+        w += gam / (2 * math.pi * r * r) * np.exp(-(dx * dx + dy * dy) / (2 * r * r))
+    w -= w.mean()
+    k = np.fft.fftfreq(n, d=h) * 2 * math.pi
+    KX, KY = np.meshgrid(k, k)
+    k2 = KX * KX + KY * KY
+    k2[0, 0] = 1.0
+    psi_hat = np.fft.fft2(w) / k2
+    psi_hat[0, 0] = 0.0
+    psi = np.real(np.fft.ifft2(psi_hat))
+    u = (np.roll(psi, -1, axis=0) - psi) / h   # (psi[j+1, i] - psi[j, i]) / dy on the left face
+    v = -(np.roll(psi, -1, axis=1) - psi) / h  # -(psi[j, i+1] - psi[j, i]) / dx on the bottom face
+    umax = float(max(np.abs(u).max(), np.abs(v).max(), 1e-12))
+    return np.ascontiguousarray(u.ravel()), np.ascontiguousarray(v.ravel()), 0.5 * h / umax
+
+
+BATCH_SIDES = (64, 128, 192, 256, 384, 512)
+
+
+def batch_sides(count: int, seed: int):
+    """Domain sides of a seeded batch of uneven simulations."""
+    rng = np.random.default_rng(seed)
+    return [int(rng.choice(BATCH_SIDES)) for _ in range(count)]

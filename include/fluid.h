@@ -351,6 +351,32 @@ FS_API int fs_write_pair_file(const char* path, int32_t nx, int32_t ny, double d
 FS_API int fs_read_pair_file(const char* path, int32_t* nx, int32_t* ny, double* dx, float* div, float* mask,
                              float* p);
 
+
+/* ------------------------------------------------------------------------
+ * Batches: many independent simulations of uneven sizes advanced by one CUDA
+ * graph launch per step (each member's step, with its own tolerance loop, is
+ * an independent branch of the graph; the branches overlap on the GPU).  No
+ * reference counterpart (the reference steps one solver per submit).
+ * Members need the fused multigrid step (pressure_solver = MULTIGRID,
+ * kernel_variant = 0, nx == ny).  Member handles are owned by the batch (do
+ * not fs_destroy them); use them for upload / read-back / solids / stats.
+ * Eager calls on members and batch steps share one stream, so they are
+ * ordered without further synchronisation.
+ * ------------------------------------------------------------------------ */
+typedef struct fs_batch fs_batch;
+FS_API int fs_batch_create(const fs_params* params, int32_t count, fs_batch** out);
+FS_API void fs_batch_destroy(fs_batch* b);
+FS_API int32_t fs_batch_size(const fs_batch* b);
+FS_API fs_solver* fs_batch_member(fs_batch* b, int32_t index);
+FS_API const char* fs_batch_last_error(const fs_batch* b);
+/* one step of every member; dt[i] per member.  The graph is re-captured when
+ * a dt changes or a member's forcing / solids / guess changed. */
+FS_API int fs_batch_step(fs_batch* b, const double* dt);
+FS_API int fs_batch_sync(fs_batch* b);
+/* nsteps batch steps between two events on the batch stream (capture first) */
+FS_API int fs_batch_time_steps(fs_batch* b, const double* dt, int32_t nsteps, double* elapsed_ms);
+FS_API int64_t fs_batch_launch_count(fs_batch* b);
+
 #ifdef __cplusplus
 }
 #endif

@@ -1,0 +1,100 @@
+"""Batches of uneven simulations (fs_batch_*): one graph launch per step.
+
+Each member's step is the same captured kernel sequence as a solver stepped
+alone (same kernels, same deterministic reductions), so after K batch steps
+every member must equal an independently stepped solver bit for bit.
+"""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+CFG = dict(nu=1e-3, advection="maccormack", pressure_solver="multigrid", pressure_iterations=1,
+           precision="mixed", pressure_tol=1e-8, max_cycles=60)
+
+
+@pytest.fixture(scope="module")
+def pkg(fs):
+    fs._lib.load()
+    return fs
+
+
+def _members(pkg, sides, seed0=20):
+    states = [pkg.workload.vortex_blobs(n, seed0 + i) for i, n in enumerate(sides)]
+    return states
+
+
+def test_batch_equals_independent_solvers(pkg):
+    sides = [64, 96, 128, 64]
+    states = _members(pkg, sides)
+    b = pkg.GPUFluidBatch([dict(n=n, **CFG) for n in sides])
+    _, _, disks, _ = pkg.workload.make_workload(64, 3)
+    for m, (u, v, _) in zip(b.members, states):
+        m.upload_velocity(u, v)
+    b.members[1].set_solids([(1.0, 2.0, 0.4)])
+    dts = [dt for _, _, dt in states]
+    for _ in range(4):
+        b.step(dts)
+    b.sync()
+    for i, (n, (u, v, dt)) in enumerate(zip(sides, states)):
+        s = pkg.GPUFluidSolver(n=n, **CFG)
+        s.upload_velocity(u, v)
+        if i == 1:
+            s.set_solids([(1.0, 2.0, 0.4)])
+        for _ in range(4):
+            s.step(dt)
+        ua, va = b.members[i].read_velocity()
+        ub, vb = s.read_velocity()
+        assert np.array_equal(ua, ub) and np.array_equal(va, vb), f"member {i} (n={n})"
+        st = b.members[i].last_stats()
+        assert st["converged"] and st["residual_max"] <= 1e-8
+        assert b.members[i].steps == 4
+        s.destroy()
+    assert b.launch_count() > 4 * len(sides) * 10
+    b.destroy()
+
+
+def test_batch_recaptures_on_change(pkg):
+    sides = [64, 128]
+    states = _members(pkg, sides, 40)
+    b = pkg.GPUFluidBatch([dict(n=n, **CFG) for n in sides])
+    for m, (u, v, _) in zip(b.members, states):
+        m.upload_velocity(u, v)
+    dts = [dt for _, _, dt in states]
+    b.step(dts)
+    b.members[0].set_solids([(3.0, 3.0, 0.5)])  # invalidates the captured branch
+    b.step(dts)
+    b.step([0.5 * d for d in dts])  # new dt: another capture
+    s = pkg.GPUFluidSolver(n=64, **CFG)
+    s.upload_velocity(states[0][0], states[0][1])
+    s.step(dts[0])
+    s.set_solids([(3.0, 3.0, 0.5)])
+    s.step(dts[0])
+    s.step(0.5 * dts[0])
+    ua, _ = b.members[0].read_velocity()
+    ub, _ = s.read_velocity()
+    assert np.array_equal(ua, ub)
+    s.destroy()
+    b.destroy()
+
+
+def test_batch_rejects_unfused_members(pkg):
+    with pytest.raises(pkg.FluidError):
+        pkg.GPUFluidBatch([dict(n=64, **CFG), dict(n=64, pressure_solver="jacobi", pressure_iterations=10)])
+
+
+def test_batch_of_uneven_sides_times(pkg):
+    sides = pkg.workload.batch_sides(24, 1)
+    b = pkg.GPUFluidBatch([dict(n=n, **CFG) for n in sides])
+    dts = []
+    for i, (m, n) in enumerate(zip(b.members, sides)):
+        u, v, dt = pkg.workload.vortex_blobs(n, 100 + i)
+        m.upload_velocity(u, v)
+        dts.append(dt)
+    ms = b.time_steps(dts, 5)
+    assert ms > 0
+    for m in b.members:
+        assert m.last_stats()["converged"]
+    b.destroy()
