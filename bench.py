@@ -212,6 +212,37 @@ def step_bytes(cycles: float) -> float:
     return 96.0 + 98.0 * cycles
 
 
+def measure_batch(pkg, device, count, steps, warmup, seed=1):
+    """Batched uneven domains (sides drawn from {64, ..., 512}, seeded vortex
+    blobs, mixed-precision multigrid to 1e-6): cell-steps/s of one graph launch
+    per batch step, against the same members stepped one after another."""
+    sides = pkg.workload.batch_sides(count, seed)
+    cfg = dict(nu=1e-4, advection="maccormack", pressure_solver="multigrid", pressure_iterations=1,
+               precision="mixed", pressure_tol=TOL, max_cycles=60, device=device)
+    b = pkg.GPUFluidBatch([dict(n=n, **cfg) for n in sides])
+    dts = []
+    for i, (m, n) in enumerate(zip(b.members, sides)):
+        u, v, dt = pkg.workload.vortex_blobs(n, 1000 + i)
+        m.upload_velocity(u, v)
+        dts.append(dt)
+    for _ in range(warmup):
+        b.step(dts)
+    ms = b.time_steps(dts, steps)
+    converged = all(m.last_stats()["converged"] for m in b.members)
+    launches = b.launch_count()
+    # the same members, one solver graph after another on the same stream
+    seq_ms = 0.0
+    for m, dt in zip(b.members, dts):
+        m.step(dt)  # captures the member's own graph outside the timed region
+        seq_ms += m.time_steps(dt, 2) / 2
+    cells = float(sum(n * n for n in sides))
+    b.destroy()
+    return {"sims": count, "cells": cells, "sides": {str(k): sides.count(k) for k in sorted(set(sides))},
+            "ms_per_step": ms / steps, "value": cells * steps / (ms / 1e3), "unit": UNIT,
+            "sequential_ms_per_step": seq_ms, "speedup_vs_sequential": seq_ms / (ms / steps),
+            "converged": converged, "gpu_launches_total": launches}
+
+
 def measure_variant(pkg, n, device, guess, u0, v0, disks, dt, steps, warmup):
     """ms/step, cycles/step and cell-steps/s of one initial-pressure choice."""
     s = make_solver(pkg, n, device, guess)
@@ -310,6 +341,10 @@ def run_gpu(args):
             variants[name] = measure_variant(pkg, n, local, g, u0, v0, disks, dt, args.steps, args.warmup)
             variants[name]["guess"] = g
 
+    batch = None
+    if args.batch_sims > 0:
+        batch = measure_batch(pkg, local, args.batch_sims, min(args.steps, 20), min(args.warmup, 3))
+
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         cpu = cpu_baseline(n, threads=1, timed_steps=1)
@@ -352,6 +387,8 @@ def run_gpu(args):
         }
         if variants:
             line["guess_comparison"] = variants
+        if batch is not None:
+            line["batch"] = batch
         if cpu is not None:
             line["cpu_baseline"] = cpu
         print(json.dumps(line), flush=True)
@@ -434,6 +471,8 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--n", type=int, default=N)
     ap.add_argument("--guess", default="zero", choices=["zero", "warm", "nn"])
+    ap.add_argument("--batch-sims", type=int, default=256,
+                    help="also time a batch of this many uneven domains (0 = skip)")
     ap.add_argument("--no-variants", action="store_true",
                     help="skip timing the learned guess and the warm start beside the headline")
     ap.add_argument("--no-cpu-baseline", action="store_true")
