@@ -154,6 +154,8 @@ SIGNATURES = {
     "fs_guess_sync": (I, [VP]),
     "fs_guess_launch_count": (C.c_int64, [VP]),
     "fs_set_guess": (I, [VP, VP, C.c_int32]),
+    "fs_diagnose": (I, [VP, VP]),
+    "fs_energy_spectrum": (I, [VP, VP, VP, C.c_int32, C.POINTER(C.c_int32), VP]),
     "fs_batch_create": (I, [C.POINTER(Params), C.c_int32, C.POINTER(VP)]),
     "fs_batch_destroy": (None, [VP]),
     "fs_batch_size": (C.c_int32, [VP]),

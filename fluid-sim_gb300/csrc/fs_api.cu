@@ -104,6 +104,7 @@ static void free_all(Solver* s) {
   f(s->dev); f(s->d_disks); f(s->d_tiles);
   if (s->graph_exec) cudaGraphExecDestroy(s->graph_exec);
   if (s->h_red) cudaFreeHost(s->h_red);
+  diag_free(s);
   if (s->body_stream) cudaStreamDestroy(s->body_stream);
   if (s->own_stream) {
     cudaStreamDestroy(s->own_stream);  // batch member: s->stream is the batch's
@@ -893,6 +894,22 @@ FS_API int fs_dump_pair(fs_solver* h, int32_t factor, float* div, float* mask, f
   if (factor < 1 || s->g.nx % factor || s->g.ny % factor)
     return fail(s, FS_ERR_INVALID_ARGUMENT, "fs_dump_pair: factor must divide nx and ny");
   return dump_pair(s, factor, div, mask, p);
+}
+
+FS_API int fs_diagnose(fs_solver* h, fs_diagnostics* out) {
+  SOLVER(h);
+  if (!out) return fail(s, FS_ERR_INVALID_ARGUMENT, "out is NULL");
+  return diagnostics(s, out, false);
+}
+
+FS_API int fs_energy_spectrum(fs_solver* h, double* E, int32_t* counts, int32_t cap, int32_t* kmax,
+                              double* parseval) {
+  SOLVER(h);
+  if (!E || !counts) return fail(s, FS_ERR_INVALID_ARGUMENT, "E and counts must be given");
+  int km = 0;
+  int rc = energy_spectrum(s, E, counts, cap, &km, parseval);
+  if (kmax) *kmax = km;
+  return rc;
 }
 
 FS_API int fs_step(fs_solver* h, double dt) {

@@ -109,6 +109,7 @@ struct Solver {
   // solids
   std::vector<fs_disk> disks;
   fs_guess* guess = nullptr;    // learned initial pressure (fs_set_guess), not owned
+  void* diag = nullptr;         // diagnostics buffers (fs_diag.cu), allocated on first use
   int guess_factor = 2;         // the network runs at 1/guess_factor of the grid
   float* imp = nullptr;         // 3 * n impulse field (x, y, torque)
   double* d_impulse = nullptr;  // 3 * disks
@@ -238,5 +239,10 @@ bool guess_supported(const Solver* s, int factor);
 int guess_prepare(Solver* s, fs_guess* g, int factor);  // buffers for this grid (outside any capture)
 int guess_enqueue(Solver* s, fs_guess* g, int factor);  // initial pressure from the divergence
 int dump_pair(Solver* s, int factor, float* div, float* mask, float* p);
+
+// diagnostics (fs_diag.cu)
+void diag_free(Solver* s);
+int diagnostics(Solver* s, fs_diagnostics* out, bool with_centres);
+int energy_spectrum(Solver* s, double* E, int32_t* counts, int cap, int* kmax_out, double* parseval);
 
 }  // namespace fs

@@ -274,6 +274,29 @@ class GPUFluidSolver:
     def launch_count(self) -> int:
         return int(self._lib.fs_launch_count(self._h))
 
+    # ------------------------------------------------------- diagnostics
+    def diagnostics(self) -> dict:
+        """kinetic energy, enstrophy, max and L2 divergence of the state (device reductions)"""
+        out = (C.c_double * 4)()
+        self._chk(self._lib.fs_diagnose(self._h, out))
+        return {"kinetic_energy": out[0], "enstrophy": out[1], "max_divergence": out[2], "l2_divergence": out[3]}
+
+    def kinetic_energy(self) -> float:
+        return self.diagnostics()["kinetic_energy"]
+
+    def enstrophy(self) -> float:
+        return self.diagnostics()["enstrophy"]
+
+    def energy_spectrum(self):
+        """(k, E, counts, (sum E, kinetic energy)) -- shell-averaged spectrum on the device"""
+        kmax = min(self.nx, self.ny) // 2
+        E = np.zeros(kmax + 1)
+        cnt = np.zeros(kmax + 1, np.int32)
+        km = C.c_int32()
+        pv = (C.c_double * 2)()
+        self._chk(self._lib.fs_energy_spectrum(self._h, _ptr(E), _ptr(cnt), kmax + 1, C.byref(km), pv))
+        return np.arange(kmax + 1), E, cnt, (pv[0], pv[1])
+
     # ------------------------------------------------ learned pressure guess
     def set_guess(self, guess, factor: int = 2) -> None:
         """Seed every projection with a PressureGuess running at 1/factor of

@@ -353,6 +353,28 @@ FS_API int fs_read_pair_file(const char* path, int32_t* nx, int32_t* ny, double*
 
 
 /* ------------------------------------------------------------------------
+ * Diagnostics on the device (the reference reads the fields back and loops
+ * on the CPU: src/core/grid.js:280-327, src/core/fft.js:196-254).
+ * ------------------------------------------------------------------------ */
+typedef struct fs_diagnostics {
+  double kinetic_energy; /* 1/2 <cu^2 + cv^2>, velocity at cell centres */
+  double enstrophy;      /* 1/2 <w^2>, w = mean of the 4 corner vorticities */
+  double max_divergence; /* max |div u| */
+  double l2_divergence;  /* sqrt(<div u^2>) */
+} fs_diagnostics;
+/* all four in one reduction kernel, per-cell values in f32 and sums in
+ * double (fs_max_divergence is the double-float-exact divergence check);
+ * synchronises */
+FS_API int fs_diagnose(fs_solver* s, fs_diagnostics* out);
+/* Shell-averaged energy spectrum E[k], k = 0..kmax = n/2 (square power-of-two
+ * grids 8..8192): E[k] = sum over modes with round(|k|) = k of
+ * 1/2 (|U|^2 + |V|^2) / N^2, counts[k] the modes per shell (cap >= kmax + 1).
+ * parseval (nullable, 2 doubles): sum E and the kinetic energy it should
+ * match (modes beyond kmax are dropped, as in the reference).  Synchronises. */
+FS_API int fs_energy_spectrum(fs_solver* s, double* E, int32_t* counts, int32_t cap, int32_t* kmax,
+                              double* parseval);
+
+/* ------------------------------------------------------------------------
  * Batches: many independent simulations of uneven sizes advanced by one CUDA
  * graph launch per step (each member's step, with its own tolerance loop, is
  * an independent branch of the graph; the branches overlap on the GPU).  No
