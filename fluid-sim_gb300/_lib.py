@@ -83,7 +83,8 @@ class Params(C.Structure):
                 ("pressure_iterations", C.c_int32), ("precision", C.c_int32),
                 ("pressure_tol", C.c_double), ("max_cycles", C.c_int32), ("mg_pre_smooth", C.c_int32),
                 ("mg_post_smooth", C.c_int32), ("mg_coarse_sweeps", C.c_int32), ("mg_min_size", C.c_int32),
-                ("warm_start", C.c_int32), ("device", C.c_int32), ("kernel_variant", C.c_int32)]
+                ("warm_start", C.c_int32), ("device", C.c_int32), ("kernel_variant", C.c_int32),
+                ("dye_fade", C.c_double)]
 
 
 class Mode(C.Structure):
@@ -154,6 +155,8 @@ SIGNATURES = {
     "fs_guess_sync": (I, [VP]),
     "fs_guess_launch_count": (C.c_int64, [VP]),
     "fs_set_guess": (I, [VP, VP, C.c_int32]),
+    "fs_upload_dye": (I, [VP, VP]),
+    "fs_read_dye": (I, [VP, VP]),
     "fs_diagnose": (I, [VP, VP]),
     "fs_energy_spectrum": (I, [VP, VP, VP, C.c_int32, C.POINTER(C.c_int32), VP]),
     "fs_batch_create": (I, [C.POINTER(Params), C.c_int32, C.POINTER(VP)]),

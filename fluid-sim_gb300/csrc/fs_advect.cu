@@ -379,4 +379,43 @@ void launch_solids(Solver* s, float* u, float* v, float dt, bool record_impulse)
                 s->d_impulse));
 }
 
+// ------------------------------------------------------------------- dye
+// ADVECT_SCALAR (shaders.js:234-266): RK2 trace from the cell centre through
+// the projected velocity, bilinear sample of the RGBA field (centre grid),
+// fade, clamp to [0, 1].  The centre (i+1/2, j+1/2) is at u-grid index
+// (i+1/2, j) and v-grid index (i, j+1/2).
+__device__ __forceinline__ Home home_c() { return {0.5f, 0.f, 0.f, 0.5f}; }
+
+__global__ void __launch_bounds__(256) k_advect_dye(const float* __restrict__ u, const float* __restrict__ v,
+                                                    const float4* __restrict__ q, float4* __restrict__ out, int nx,
+                                                    int ny, float cx, float cy, float keep) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y;
+  if (i >= nx || j >= ny) return;
+  float dX, dY;
+  trace(u, v, nx, ny, i, j, home_c(), cx, cy, dX, dY);
+  float fo = floorf(dX), go = floorf(dY);
+  float fx = dX - fo, fy = dY - go;
+  int i0 = wrap_idx(i + (int)fo, nx), j0 = wrap_idx(j + (int)go, ny);
+  int i1 = i0 + 1 == nx ? 0 : i0 + 1, j1 = j0 + 1 == ny ? 0 : j0 + 1;
+  float4 a = q[(int64_t)j0 * nx + i0], b = q[(int64_t)j0 * nx + i1];
+  float4 c = q[(int64_t)j1 * nx + i0], d = q[(int64_t)j1 * nx + i1];
+  auto lerp2 = [&](float pa, float pb, float pc, float pd) {
+    float top = pa + (pb - pa) * fx, bot = pc + (pd - pc) * fx;
+    return fminf(fmaxf((top + (bot - top) * fy) * keep, 0.f), 1.f);
+  };
+  out[(int64_t)j * nx + i] = make_float4(lerp2(a.x, b.x, c.x, d.x), lerp2(a.y, b.y, c.y, d.y),
+                                         lerp2(a.z, b.z, c.z, d.z), lerp2(a.w, b.w, c.w, d.w));
+}
+
+void launch_advect_dye(Solver* s, float dt) {
+  const Grid& g = s->g;
+  dim3 b(32, 8);
+  FS_LAUNCH(s, "advect_dye", (double)s->n * 40,
+            k_advect_dye<<<grid2d(g.nx, g.ny, b), b, 0, s->stream>>>(
+                s->u, s->v, static_cast<const float4*>(s->dye), static_cast<float4*>(s->dye2), g.nx, g.ny,
+                (float)(dt * g.idxd), (float)(dt * g.idyd), (float)(1.0 - s->prm.dye_fade)));
+  // the next step reads s->dye again: copy back (a captured step cannot swap pointers)
+  cudaMemcpyAsync(s->dye, s->dye2, (size_t)s->n * 16, cudaMemcpyDeviceToDevice, s->stream);
+}
+
 }  // namespace fs

@@ -101,7 +101,7 @@ static void free_all(Solver* s) {
   for (size_t l = 1; l < s->lev.size(); l++) { f(s->lev[l].x); f(s->lev[l].x2); f(s->lev[l].rhs); }
   f(s->stage);
   f(s->red_partials); f(s->red_out); f(s->modes); f(s->imp); f(s->d_impulse);
-  f(s->dev); f(s->d_disks); f(s->d_tiles);
+  f(s->dev); f(s->d_disks); f(s->d_tiles); f(s->dye); f(s->dye2);
   if (s->graph_exec) cudaGraphExecDestroy(s->graph_exec);
   if (s->h_red) cudaFreeHost(s->h_red);
   diag_free(s);
@@ -135,6 +135,7 @@ static int create(const fs_params* prm, Solver* s) {
   if ((int64_t)P.nx * P.ny > (int64_t)1 << 30) return fail(nullptr, FS_ERR_INVALID_ARGUMENT, "grid larger than 2^30 cells");
   if (!(P.lx > 0) || !(P.ly > 0)) return fail(nullptr, FS_ERR_INVALID_ARGUMENT, "domain size must be positive");
   if (!(P.nu >= 0)) return fail(nullptr, FS_ERR_INVALID_ARGUMENT, "nu must be >= 0");
+  if (!(P.dye_fade >= 0) || !(P.dye_fade <= 1)) return fail(nullptr, FS_ERR_INVALID_ARGUMENT, "dye_fade must be in [0, 1]");
   if (P.confinement != 0)
     return fail(nullptr, FS_ERR_UNSUPPORTED, "vorticity confinement is not part of this path (it must stay off)");
   if (P.advection != FS_ADVECT_SEMI_LAGRANGIAN && P.advection != FS_ADVECT_MACCORMACK)
@@ -491,6 +492,8 @@ static int enqueue_step(Solver* s, double dt, bool capture) {
   if (s->n_modes > 0) launch_forcing(s, cu, cv, fdt);
   if (!s->disks.empty()) launch_solids(s, cu, cv, fdt, false);
   int rc = project_from(s, cu, cv, capture);
+  // dye through the now divergence-free field (solver.js:516, 577-586)
+  if (s->dye) launch_advect_dye(s, fdt);
   launch_step_finish(s, dt);
   return rc;
 }
@@ -665,6 +668,7 @@ FS_API void fs_params_default(fs_params* p) {
   p->warm_start = 0;
   p->device = 0;
   p->kernel_variant = 0;
+  p->dye_fade = 0.0;
 }
 
 FS_API int fs_create(const fs_params* params, fs_solver** out) {
@@ -894,6 +898,29 @@ FS_API int fs_dump_pair(fs_solver* h, int32_t factor, float* div, float* mask, f
   if (factor < 1 || s->g.nx % factor || s->g.ny % factor)
     return fail(s, FS_ERR_INVALID_ARGUMENT, "fs_dump_pair: factor must divide nx and ny");
   return dump_pair(s, factor, div, mask, p);
+}
+
+FS_API int fs_upload_dye(fs_solver* h, const float* rgba) {
+  SOLVER(h);
+  if (!rgba) return fail(s, FS_ERR_INVALID_ARGUMENT, "rgba is NULL");
+  if (!s->dye) {
+    CU(s, cudaStreamSynchronize(s->stream));
+    CU(s, cudaMalloc(&s->dye, (size_t)s->n * 16));
+    CU(s, cudaMalloc(&s->dye2, (size_t)s->n * 16));
+    drop_graph(s);  // the captured step gains the dye pass
+  }
+  CU(s, cudaMemcpyAsync(s->dye, rgba, (size_t)s->n * 16, cudaMemcpyHostToDevice, s->stream));
+  CU(s, cudaStreamSynchronize(s->stream));
+  return FS_OK;
+}
+
+FS_API int fs_read_dye(fs_solver* h, float* rgba) {
+  SOLVER(h);
+  if (!rgba) return fail(s, FS_ERR_INVALID_ARGUMENT, "rgba is NULL");
+  if (!s->dye) return fail(s, FS_ERR_INVALID_ARGUMENT, "no dye uploaded");
+  CU(s, cudaMemcpyAsync(rgba, s->dye, (size_t)s->n * 16, cudaMemcpyDeviceToHost, s->stream));
+  CU(s, cudaStreamSynchronize(s->stream));
+  return FS_OK;
 }
 
 FS_API int fs_diagnose(fs_solver* h, fs_diagnostics* out) {

@@ -110,6 +110,8 @@ struct Solver {
   std::vector<fs_disk> disks;
   fs_guess* guess = nullptr;    // learned initial pressure (fs_set_guess), not owned
   void* diag = nullptr;         // diagnostics buffers (fs_diag.cu), allocated on first use
+  void* dye = nullptr;          // RGBA float4 per cell once uploaded (fs_upload_dye)
+  void* dye2 = nullptr;         // advection target
   int guess_factor = 2;         // the network runs at 1/guess_factor of the grid
   float* imp = nullptr;         // 3 * n impulse field (x, y, torque)
   double* d_impulse = nullptr;  // 3 * disks
@@ -183,6 +185,7 @@ void launch_diffuse(Solver* s, const float* u, const float* v, float* ou, float*
 void launch_forcing(Solver* s, float* u, float* v, float dt);
 int upload_disks(Solver* s);
 void launch_solids(Solver* s, float* u, float* v, float dt, bool record_impulse);
+void launch_advect_dye(Solver* s, float dt);
 
 // fs_pressure.cu
 template <class TV, class TD>

@@ -32,12 +32,14 @@ def make_params(n: int = 256, nx: int | None = None, ny: int | None = None, lx: 
                 solid_mask_width: float = 1.5, pressure_solver: str = "jacobi", pressure_iterations: int = 40,
                 precision: str = "f32", pressure_tol: float = 0.0, max_cycles: int = 50, mg_pre_smooth: int = 2,
                 mg_post_smooth: int = 2, mg_coarse_sweeps: int = 40, mg_min_size: int = 8,
-                warm_start: bool = False, device: int = 0, kernel_variant: int = 0, **camel) -> "L.Params":
+                warm_start: bool = False, device: int = 0, kernel_variant: int = 0, dye_fade: float = 0.0,
+                **camel) -> "L.Params":
     """fs_params from the reference's option names (camelCase accepted);
     unknown names are rejected (the reference silently defaults)."""
     solid_mask_width = camel.pop("solidMaskWidth", solid_mask_width)
     pressure_solver = camel.pop("pressureSolver", pressure_solver)
     pressure_iterations = camel.pop("pressureIterations", pressure_iterations)
+    dye_fade = camel.pop("dyeFade", dye_fade)
     if camel:
         raise TypeError(f"unknown options {sorted(camel)}")
     lib = L.load()
@@ -64,6 +66,7 @@ def make_params(n: int = 256, nx: int | None = None, ny: int | None = None, lx: 
     p.warm_start = int(bool(warm_start))
     p.device = device
     p.kernel_variant = kernel_variant
+    p.dye_fade = dye_fade
     return p
 
 
@@ -82,13 +85,14 @@ class GPUFluidSolver:
                  pressure_solver: str = "jacobi", pressure_iterations: int = 40, precision: str = "f32",
                  pressure_tol: float = 0.0, max_cycles: int = 50, mg_pre_smooth: int = 2,
                  mg_post_smooth: int = 2, mg_coarse_sweeps: int = 40, mg_min_size: int = 8,
-                 warm_start: bool = False, device: int = 0, kernel_variant: int = 0, **camel):
+                 warm_start: bool = False, device: int = 0, kernel_variant: int = 0, dye_fade: float = 0.0,
+                 **camel):
         p = make_params(n=n, nx=nx, ny=ny, lx=lx, ly=ly, nu=nu, confinement=confinement, advection=advection,
                         solid_mask_width=solid_mask_width, pressure_solver=pressure_solver,
                         pressure_iterations=pressure_iterations, precision=precision, pressure_tol=pressure_tol,
                         max_cycles=max_cycles, mg_pre_smooth=mg_pre_smooth, mg_post_smooth=mg_post_smooth,
                         mg_coarse_sweeps=mg_coarse_sweeps, mg_min_size=mg_min_size, warm_start=warm_start,
-                        device=device, kernel_variant=kernel_variant, **camel)
+                        device=device, kernel_variant=kernel_variant, dye_fade=dye_fade, **camel)
         lib = L.load()
         h = C.c_void_p()
         L.check(lib.fs_create(C.byref(p), C.byref(h)), None)
@@ -273,6 +277,19 @@ class GPUFluidSolver:
 
     def launch_count(self) -> int:
         return int(self._lib.fs_launch_count(self._h))
+
+    # ------------------------------------------------------------------ dye
+    def upload_dye(self, rgba) -> None:
+        """uploadDye(rgba) (solver.js:317-323): f32 RGBA per cell, [ny, nx, 4] or flat"""
+        a = np.ascontiguousarray(rgba, dtype=np.float32)
+        if a.size != 4 * self.n:
+            raise ValueError(f"dye needs {4 * self.n} floats")
+        self._chk(self._lib.fs_upload_dye(self._h, _ptr(a)))
+
+    def read_dye(self) -> np.ndarray:
+        out = np.empty((self.ny, self.nx, 4), np.float32)
+        self._chk(self._lib.fs_read_dye(self._h, _ptr(out)))
+        return out
 
     # ------------------------------------------------------- diagnostics
     def diagnostics(self) -> dict:

@@ -127,6 +127,9 @@ typedef struct fs_params {
   int32_t kernel_variant;     /* 0: fused multigrid kernels (default); 1: one kernel per
                                  reference pass (RBGS colour, residual, restriction,
                                  prolongation), kept to cross-check the fused cycle */
+  double dye_fade;            /* dyeFade (solver.js:67,82): dye *= 1 - dye_fade per step
+                                 (default 0); dye advection runs once a dye field is
+                                 uploaded (fs_upload_dye) */
 } fs_params;
 
 /* one forcing mode, as setForcing's {kx, ky, phase} (solver.js:370-385) */
@@ -351,6 +354,15 @@ FS_API int fs_write_pair_file(const char* path, int32_t nx, int32_t ny, double d
 FS_API int fs_read_pair_file(const char* path, int32_t* nx, int32_t* ny, double* dx, float* div, float* mask,
                              float* p);
 
+
+/* ------------------------------------------------------------------------
+ * Dye (uploadDye, solver.js:317-323; ADVECT_SCALAR, shaders.js:234-266): an
+ * RGBA f32 field at the cell centres, [ny][nx][4].  Once uploaded, every step
+ * advects it semi-Lagrangian through the projected velocity, fades it by
+ * dye_fade and clamps it to [0, 1], as the reference does.
+ * ------------------------------------------------------------------------ */
+FS_API int fs_upload_dye(fs_solver* s, const float* rgba);
+FS_API int fs_read_dye(fs_solver* s, float* rgba);
 
 /* ------------------------------------------------------------------------
  * Diagnostics on the device (the reference reads the fields back and loops
