@@ -44,7 +44,9 @@ template <int CIN, int COUT, int TY, int NS>
 struct Cfg {
   static constexpr int KC = CIN / 8;
   static constexpr int NSPLIT = COUT / NS;                   // CTAs sharing one pixel tile
-  static constexpr int PLANE = (TY + 2) * kTW * 16;          // bytes of one chunk plane
+  // bytes of one chunk plane, padded to 64 mod 128 so that the two chunks of
+  // one pixel (stored by neighbouring threads) fall in different banks
+  static constexpr int PLANE = ((TY + 2) * kTW * 16 + 63) / 128 * 128 + 64;
   static constexpr int IN_BYTES = align128(KC * PLANE);
   static constexpr int WTAP = KC * NS * 16;                  // bytes of one tap of this CTA's weights
   static constexpr int W_BYTES = align128(WTAP);

@@ -546,7 +546,7 @@ static void up_t(Solver* s, Level& L, const Level& C, float* acc_h, float* acc_l
   dim3 grid((L.n + T - 1) / T, (L.n + T - 1) / T);
   if (acc_h) {
     double bytes = (double)L.n * L.n * 24.0 + (double)C.n * C.n * 4.0;
-    FS_LAUNCH(s, "mg_up", bytes,
+    FS_LAUNCH(s, "mg_up_acc", bytes,
               k_mg_up<T, H, true><<<grid, kTileBlock, 0, s->stream>>>(L.rhs, L.x, nullptr, C.x, L.n, L.h2,
                                                                       s->prm.mg_post_smooth, acc_h, acc_l));
     return;
