@@ -86,85 +86,179 @@ __device__ __forceinline__ void trace(const TV* __restrict__ u, const TV* __rest
   dY = -cy * v2;
 }
 
-// ADVECT_VELOCITY: each component traced from its own face (shaders.js:126-146)
-template <class TV>
-__global__ void __launch_bounds__(256) k_advect_sl(const TV* __restrict__ u, const TV* __restrict__ v,
-                                                   float* __restrict__ ou, float* __restrict__ ov,
-                                                   int nx, int ny, float cx, float cy) {
-  int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y;
-  if (i >= nx || j >= ny) return;
-  float dX, dY;
-  Home hu = home_u(), hv = home_v();
-  trace(u, v, nx, ny, i, j, hu, cx, cy, dX, dY);
-  float a = bilerp(u, nx, ny, i, j, hu.ux + dX, hu.uy + dY);
-  trace(u, v, nx, ny, i, j, hv, cx, cy, dX, dY);
-  float b = bilerp(v, nx, ny, i, j, hv.vx + dX, hv.vy + dY);
-  int64_t c = (int64_t)j * nx + i;
-  ou[c] = a;
-  ov[c] = b;
+// ------------------------------------------------------ tiled advection
+// The advection kernels are gather-bound: a MacCormack step takes about 20
+// bilinear samples per cell.  A CTA stages its 32x16-cell tile of each field
+// it samples, plus a halo of 3 cells, in shared memory; every sample whose
+// four cells lie in the staged block is read from there with 32-bit tile
+// addressing, anything else (a trace longer than the halo, i.e. a CFL number
+// above ~1.5) falls back to the wrapped global read.  The arithmetic is the
+// same as the global sampler, so the results are too.
+constexpr int kTX = 32, kTY = 16, kHalo = 3;
+constexpr int kSW = kTX + 2 * kHalo, kSH = kTY + 2 * kHalo;
+
+struct TileView {
+  const float* sm;  // kSH x kSW staged block
+  int oi, oj;       // global (unwrapped) index of the block's element (0, 0)
+  const float* g;
+  int nx, ny;
+
+  __device__ __forceinline__ float sample(int bi, int bj, float ox, float oy) const {
+    const float fo = floorf(ox), go = floorf(oy);
+    const float fx = ox - fo, fy = oy - go;
+    const int li = bi + (int)fo - oi, lj = bj + (int)go - oj;
+    if ((unsigned)li < (unsigned)(kSW - 1) && (unsigned)lj < (unsigned)(kSH - 1)) {
+      const float* p = sm + lj * kSW + li;
+      const float a = p[0], b = p[1], c = p[kSW], d = p[kSW + 1];
+      const float top = a + (b - a) * fx;
+      const float bot = c + (d - c) * fx;
+      return top + (bot - top) * fy;
+    }
+    return bilerp(g, nx, ny, bi, bj, ox, oy);
+  }
+  __device__ __forceinline__ void range4(int bi, int bj, float ox, float oy, float& lo, float& hi) const {
+    const int li = bi + (int)floorf(ox) - oi, lj = bj + (int)floorf(oy) - oj;
+    if ((unsigned)li < (unsigned)(kSW - 1) && (unsigned)lj < (unsigned)(kSH - 1)) {
+      const float* p = sm + lj * kSW + li;
+      const float a = p[0], b = p[1], c = p[kSW], d = p[kSW + 1];
+      lo = fminf(fminf(a, b), fminf(c, d));
+      hi = fmaxf(fmaxf(a, b), fmaxf(c, d));
+      return;
+    }
+    bounds4(g, nx, ny, bi, bj, ox, oy, lo, hi);
+  }
+};
+
+// RK2 midpoint backward trace (src/cpu/advect.js:46-54, shaders.js:117-122) in cells
+__device__ __forceinline__ void trace_t(const TileView& u, const TileView& v, int i, int j, Home h, float cx,
+                                        float cy, float& dX, float& dY) {
+  const float u1 = u.sample(i, j, h.ux, h.uy);
+  const float v1 = v.sample(i, j, h.vx, h.vy);
+  const float mx = -0.5f * cx * u1, my = -0.5f * cy * v1;
+  const float u2 = u.sample(i, j, h.ux + mx, h.uy + my);
+  const float v2 = v.sample(i, j, h.vx + mx, h.vy + my);
+  dX = -cx * u2;
+  dY = -cy * v2;
+}
+
+// stage the kSH x kSW block of f whose (0, 0) is global (oi, oj), wrapped
+__device__ __forceinline__ void stage_tile(float* sm, const float* __restrict__ f, int oi, int oj, int nx, int ny) {
+  const int tid = threadIdx.y * blockDim.x + threadIdx.x, nthr = blockDim.x * blockDim.y;
+  for (int k = tid; k < kSW * kSH; k += nthr) {
+    const int lj = k / kSW, li = k - lj * kSW;
+    sm[k] = __ldg(f + (int64_t)wrap_idx(oj + lj, ny) * nx + wrap_idx(oi + li, nx));
+  }
+}
+
+// ADVECT_VELOCITY: each component traced from its own face (shaders.js:126-146).
+// With bounds != nullptr (the forward pass of MacCormack) the min and max of
+// the four cells each sample read -- the limiter's range, src/cpu/advect.js
+// :104-111 -- are written too, planes (lo_u, hi_u, lo_v, hi_v), so the combine
+// pass does not trace forward again.
+__global__ void __launch_bounds__(256) k_advect_sl_t(const float* __restrict__ u, const float* __restrict__ v,
+                                                     float* __restrict__ ou, float* __restrict__ ov, int nx, int ny,
+                                                     float cx, float cy, float* __restrict__ bounds) {
+  __shared__ float su[kSW * kSH], sv[kSW * kSH];
+  const int ti = blockIdx.x * kTX, tj = blockIdx.y * kTY;
+  const int oi = ti - kHalo, oj = tj - kHalo;
+  stage_tile(su, u, oi, oj, nx, ny);
+  stage_tile(sv, v, oi, oj, nx, ny);
+  __syncthreads();
+  const TileView U{su, oi, oj, u, nx, ny}, V{sv, oi, oj, v, nx, ny};
+  const Home hu = home_u(), hv = home_v();
+  const int i = ti + threadIdx.x;
+  if (i >= nx) return;
+  const int64_t n = (int64_t)nx * ny;
+  for (int r = threadIdx.y; r < kTY; r += blockDim.y) {
+    const int j = tj + r;
+    if (j >= ny) break;
+    const int64_t c = (int64_t)j * nx + i;
+    float dX, dY, lo, hi;
+    trace_t(U, V, i, j, hu, cx, cy, dX, dY);
+    ou[c] = U.sample(i, j, hu.ux + dX, hu.uy + dY);
+    if (bounds) {
+      U.range4(i, j, hu.ux + dX, hu.uy + dY, lo, hi);
+      bounds[c] = lo;
+      bounds[n + c] = hi;
+    }
+    trace_t(U, V, i, j, hv, cx, cy, dX, dY);
+    ov[c] = V.sample(i, j, hv.vx + dX, hv.vy + dY);
+    if (bounds) {
+      V.range4(i, j, hv.vx + dX, hv.vy + dY, lo, hi);
+      bounds[2 * n + c] = lo;
+      bounds[3 * n + c] = hi;
+    }
+  }
 }
 
 // MACCORMACK: the backward pass (ADVECT_FIELD_BY with -dt) is evaluated inside
-// the combine kernel at the single point it is needed, then the limited
-// correction (shaders.js:187-231, src/cpu/advect.js:149-185).
-template <class TV>
-__global__ void __launch_bounds__(256)
-    k_mc_combine(const TV* __restrict__ u, const TV* __restrict__ v, const float* __restrict__ fu,
-                 const float* __restrict__ fv, float* __restrict__ ou, float* __restrict__ ov, int nx,
-                 int ny, float cx, float cy) {
-  int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y;
-  if (i >= nx || j >= ny) return;
-  int64_t c = (int64_t)j * nx + i;
-  Home hu = home_u(), hv = home_v();
-  float dX, dY, lo, hi;
-  // u component
-  trace(u, v, nx, ny, i, j, hu, -cx, -cy, dX, dY);  // backward: trace with -dt
-  float bu = bilerp(fu, nx, ny, i, j, hu.ux + dX, hu.uy + dY);
-  float cu = __ldg(fu + c) + 0.5f * ((float)__ldg(u + c) - bu);
-  trace(u, v, nx, ny, i, j, hu, cx, cy, dX, dY);
-  bounds4(u, nx, ny, i, j, hu.ux + dX, hu.uy + dY, lo, hi);
-  cu = cu < lo ? lo : cu > hi ? hi : cu;
-  // v component
-  trace(u, v, nx, ny, i, j, hv, -cx, -cy, dX, dY);
-  float bv = bilerp(fv, nx, ny, i, j, hv.vx + dX, hv.vy + dY);
-  float cv = __ldg(fv + c) + 0.5f * ((float)__ldg(v + c) - bv);
-  trace(u, v, nx, ny, i, j, hv, cx, cy, dX, dY);
-  bounds4(v, nx, ny, i, j, hv.vx + dX, hv.vy + dY, lo, hi);
-  cv = cv < lo ? lo : cv > hi ? hi : cv;
-  ou[c] = cu;
-  ov[c] = cv;
+// the combine kernel at the single point it is needed, then the correction
+// limited to the forward pass's range (shaders.js:187-231, src/cpu/advect.js:149-185).
+__global__ void __launch_bounds__(256) k_mc_combine_t(const float* __restrict__ u, const float* __restrict__ v,
+                                                      const float* __restrict__ fu, const float* __restrict__ fv,
+                                                      const float* __restrict__ bounds, float* __restrict__ ou,
+                                                      float* __restrict__ ov, int nx, int ny, float cx, float cy) {
+  __shared__ float su[kSW * kSH], sv[kSW * kSH], sfu[kSW * kSH], sfv[kSW * kSH];
+  const int ti = blockIdx.x * kTX, tj = blockIdx.y * kTY;
+  const int oi = ti - kHalo, oj = tj - kHalo;
+  stage_tile(su, u, oi, oj, nx, ny);
+  stage_tile(sv, v, oi, oj, nx, ny);
+  stage_tile(sfu, fu, oi, oj, nx, ny);
+  stage_tile(sfv, fv, oi, oj, nx, ny);
+  __syncthreads();
+  const TileView U{su, oi, oj, u, nx, ny}, V{sv, oi, oj, v, nx, ny};
+  const TileView FU{sfu, oi, oj, fu, nx, ny}, FV{sfv, oi, oj, fv, nx, ny};
+  const Home hu = home_u(), hv = home_v();
+  const int i = ti + threadIdx.x;
+  if (i >= nx) return;
+  const int64_t n = (int64_t)nx * ny;
+  for (int r = threadIdx.y; r < kTY; r += blockDim.y) {
+    const int j = tj + r;
+    if (j >= ny) break;
+    const int64_t c = (int64_t)j * nx + i;
+    const int lc = (r + kHalo) * kSW + threadIdx.x + kHalo;  // this cell in the staged block
+    float dX, dY;
+    // u component
+    trace_t(U, V, i, j, hu, -cx, -cy, dX, dY);  // backward: trace with -dt
+    const float bu = FU.sample(i, j, hu.ux + dX, hu.uy + dY);
+    float cu = sfu[lc] + 0.5f * (su[lc] - bu);
+    float lo = __ldg(bounds + c), hi = __ldg(bounds + n + c);
+    cu = cu < lo ? lo : cu > hi ? hi : cu;
+    // v component
+    trace_t(U, V, i, j, hv, -cx, -cy, dX, dY);
+    const float bv = FV.sample(i, j, hv.vx + dX, hv.vy + dY);
+    float cv = sfv[lc] + 0.5f * (sv[lc] - bv);
+    lo = __ldg(bounds + 2 * n + c);
+    hi = __ldg(bounds + 3 * n + c);
+    cv = cv < lo ? lo : cv > hi ? hi : cv;
+    ou[c] = cu;
+    ov[c] = cv;
+  }
 }
 
 static const dim3 kBlock(32, 8);
 
-template <class TV>
-void launch_advect_sl(Solver* s, const TV* u, const TV* v, float* ou, float* ov, float dt) {
+static dim3 tile_grid(const Grid& g) { return dim3((g.nx + kTX - 1) / kTX, (g.ny + kTY - 1) / kTY); }
+
+template <>
+void launch_advect_sl<float>(Solver* s, const float* u, const float* v, float* ou, float* ov, float dt) {
   const Grid& g = s->g;
   float cx = (float)((double)dt / g.dxd), cy = (float)((double)dt / g.dyd);
-  FS_LAUNCH(s, "advect_sl", (double)s->n * (2 * sizeof(TV) + 8),
-            k_advect_sl<TV><<<grid2d(g.nx, g.ny, kBlock), kBlock, 0, s->stream>>>(u, v, ou, ov, g.nx,
-                                                                                   g.ny, cx, cy));
+  FS_LAUNCH(s, "advect_sl", (double)s->n * 16,
+            k_advect_sl_t<<<tile_grid(g), kBlock, 0, s->stream>>>(u, v, ou, ov, g.nx, g.ny, cx, cy, nullptr));
 }
 
-template <class TV>
-void launch_advect_mc(Solver* s, const TV* u, const TV* v, float* fu, float* fv, float* ou,
-                      float* ov, float dt) {
+template <>
+void launch_advect_mc<float>(Solver* s, const float* u, const float* v, float* fu, float* fv, float* ou,
+                             float* ov, float dt) {
   const Grid& g = s->g;
   float cx = (float)((double)dt / g.dxd), cy = (float)((double)dt / g.dyd);
-  FS_LAUNCH(s, "advect_sl", (double)s->n * (2 * sizeof(TV) + 8),
-            k_advect_sl<TV><<<grid2d(g.nx, g.ny, kBlock), kBlock, 0, s->stream>>>(u, v, fu, fv, g.nx,
-                                                                                   g.ny, cx, cy));
-  FS_LAUNCH(s, "mc_combine", (double)s->n * (2 * sizeof(TV) + 8 + 8),
-            k_mc_combine<TV><<<grid2d(g.nx, g.ny, kBlock), kBlock, 0, s->stream>>>(
-                u, v, fu, fv, ou, ov, g.nx, g.ny, cx, cy));
+  FS_LAUNCH(s, "advect_sl", (double)s->n * 32,
+            k_advect_sl_t<<<tile_grid(g), kBlock, 0, s->stream>>>(u, v, fu, fv, g.nx, g.ny, cx, cy, s->mc_bounds));
+  FS_LAUNCH(s, "mc_combine", (double)s->n * 40,
+            k_mc_combine_t<<<tile_grid(g), kBlock, 0, s->stream>>>(u, v, fu, fv, s->mc_bounds, ou, ov, g.nx, g.ny,
+                                                                   cx, cy));
 }
-
-template void launch_advect_sl<float>(Solver*, const float*, const float*, float*, float*, float);
-template void launch_advect_sl<double>(Solver*, const double*, const double*, float*, float*, float);
-template void launch_advect_mc<float>(Solver*, const float*, const float*, float*, float*, float*,
-                                      float*, float);
-template void launch_advect_mc<double>(Solver*, const double*, const double*, float*, float*,
-                                       float*, float*, float);
 
 // DIFFUSE (shaders.js:401-425; src/cpu/solver.js:56-68 operand order)
 __global__ void __launch_bounds__(256) k_diffuse(const float* __restrict__ u, const float* __restrict__ v,

@@ -95,7 +95,7 @@ static int dalloc(Solver* s, T** p, size_t count) {
 static void free_all(Solver* s) {
   auto f = [](void* p) { if (p) cudaFree(p); };
   f(s->u); f(s->v); f(s->wu); f(s->wv); f(s->tu); f(s->tv); f(s->fu); f(s->fv);
-  f(s->ulo); f(s->vlo);
+  f(s->ulo); f(s->vlo); f(s->mc_bounds);
   f(s->p32); f(s->p32b); f(s->div32); f(s->ph); f(s->pl); f(s->pbh); f(s->pbl); f(s->dh); f(s->dl);
   f(s->r32); f(s->e32); f(s->e32b); f(s->scratch);
   for (size_t l = 1; l < s->lev.size(); l++) { f(s->lev[l].x); f(s->lev[l].x2); f(s->lev[l].rhs); }
@@ -208,7 +208,11 @@ static int create(const fs_params* prm, Solver* s) {
     A(s->p32, float, n); A(s->p32b, float, n); A(s->div32, float, n);
   }
   A(s->wu, float, n); A(s->wv, float, n); A(s->tu, float, n); A(s->tv, float, n);
-  if (P.advection == FS_ADVECT_MACCORMACK) { A(s->fu, float, n); A(s->fv, float, n); }
+  if (P.advection == FS_ADVECT_MACCORMACK) {
+    A(s->fu, float, n);
+    A(s->fv, float, n);
+    A(s->mc_bounds, float, 4 * n);
+  }
   if (!s->lev.empty()) {
     A(s->scratch, float, n);
     s->lev[0].x = s->mixed ? s->e32 : s->p32;

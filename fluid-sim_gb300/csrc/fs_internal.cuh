@@ -77,6 +77,7 @@ struct Solver {
   float* tv = nullptr;
   float* fu = nullptr;  // MacCormack forward field
   float* fv = nullptr;
+  float* mc_bounds = nullptr;  // MacCormack limiter range per face: lo_u, hi_u, lo_v, hi_v planes
 
   // pressure: F32 -> p32/div32 are the Poisson unknown/rhs.
   //           MIXED -> (ph, pl) and (dh, dl) hold the double-float pressure and

@@ -407,6 +407,45 @@ __global__ void __launch_bounds__(256)
   block_max_finish(m, ctx);
 }
 
+// The same residual, four consecutive cells per thread (nx a multiple of 4):
+// float4 loads of the three pressure rows, the left / right neighbours of the
+// group from the adjacent words, so each cell costs ~1/3 of the loads and
+// index arithmetic of the one-cell form.  Same arithmetic, same results.
+__global__ void __launch_bounds__(256)
+    k_refine_init4(const float* __restrict__ dh, const float* __restrict__ dl, const float* __restrict__ ph,
+                   const float* __restrict__ pl, float* __restrict__ r32, int nx, int ny, LapScale ks, RedCtx ctx) {
+  float m = 0.f;
+  const int nq = nx >> 2;  // quads per row
+  // tiles of 32 quads x 8 rows walked by the capped 2-D grid
+  for (int ty = blockIdx.y, nty = (ny + 7) >> 3; ty < nty; ty += gridDim.y)
+    for (int tx = blockIdx.x, ntx = (nq + 31) >> 5; tx < ntx; tx += gridDim.x) {
+      const int q = tx * 32 + threadIdx.x, j = ty * 8 + threadIdx.y;
+      if (q >= nq || j >= ny) continue;
+      const int i0 = q << 2;
+      const int jm = j == 0 ? ny - 1 : j - 1, jp = j + 1 == ny ? 0 : j + 1;
+      const int64_t r = (int64_t)j * nx, rm = (int64_t)jm * nx, rp = (int64_t)jp * nx;
+      const int il = i0 == 0 ? nx - 1 : i0 - 1, ir = i0 + 4 == nx ? 0 : i0 + 4;
+      const float4 ch = __ldg(reinterpret_cast<const float4*>(ph + r + i0));
+      const float4 cl = __ldg(reinterpret_cast<const float4*>(pl + r + i0));
+      const float4 bh = __ldg(reinterpret_cast<const float4*>(ph + rm + i0));
+      const float4 bl = __ldg(reinterpret_cast<const float4*>(pl + rm + i0));
+      const float4 th = __ldg(reinterpret_cast<const float4*>(ph + rp + i0));
+      const float4 tl = __ldg(reinterpret_cast<const float4*>(pl + rp + i0));
+      const float4 d4h = __ldg(reinterpret_cast<const float4*>(dh + r + i0));
+      const float4 d4l = __ldg(reinterpret_cast<const float4*>(dl + r + i0));
+      const df lft = {__ldg(ph + r + il), __ldg(pl + r + il)}, rgt = {__ldg(ph + r + ir), __ldg(pl + r + ir)};
+      const df c0 = {ch.x, cl.x}, c1 = {ch.y, cl.y}, c2 = {ch.z, cl.z}, c3 = {ch.w, cl.w};
+      float4 out;
+      out.x = residual_df(df{d4h.x, d4l.x}, c0, lft, c1, df{bh.x, bl.x}, df{th.x, tl.x}, ks);
+      out.y = residual_df(df{d4h.y, d4l.y}, c1, c0, c2, df{bh.y, bl.y}, df{th.y, tl.y}, ks);
+      out.z = residual_df(df{d4h.z, d4l.z}, c2, c1, c3, df{bh.z, bl.z}, df{th.z, tl.z}, ks);
+      out.w = residual_df(df{d4h.w, d4l.w}, c3, c2, rgt, df{bh.w, bl.w}, df{th.w, tl.w}, ks);
+      *reinterpret_cast<float4*>(r32 + r + i0) = out;
+      m = fmaxf(fmaxf(m, fmaxf(absnanf(out.x), absnanf(out.y))), fmaxf(absnanf(out.z), absnanf(out.w)));
+    }
+  block_max_finish(m, ctx);
+}
+
 // p' = p + e; r = d - lap(p') in df; r32 = (float) r; max|r| reduced
 __global__ void __launch_bounds__(256)
     k_refine_update(const float* __restrict__ ph, const float* __restrict__ pl, const float* __restrict__ e,
@@ -439,8 +478,13 @@ void launch_refine_init(Solver* s, const float* dh, const float* dl, const float
                         float* r32, bool zero_p) {
   const Grid& g = s->g;
   FS_LAUNCH(s, "refine_init", (double)s->n * (zero_p ? 12 : 20),
-            k_refine_init<<<red_grid2(g.nx, g.ny), kBlock, 0, s->stream>>>(
-                dh, dl, ph, pl, r32, g.nx, g.ny, lap_scale(g), zero_p ? 1 : 0, red_ctx(s, s->red_out)));
+            if (!zero_p && g.nx % 4 == 0) {
+              k_refine_init4<<<red_grid2(g.nx / 4, g.ny), kBlock, 0, s->stream>>>(
+                  dh, dl, ph, pl, r32, g.nx, g.ny, lap_scale(g), red_ctx(s, s->red_out));
+            } else {
+              k_refine_init<<<red_grid2(g.nx, g.ny), kBlock, 0, s->stream>>>(
+                  dh, dl, ph, pl, r32, g.nx, g.ny, lap_scale(g), zero_p ? 1 : 0, red_ctx(s, s->red_out));
+            });
 }
 
 void launch_refine_update(Solver* s, const float* ph, const float* pl, const float* e, const float* dh,
