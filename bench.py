@@ -166,6 +166,12 @@ def allsum(dist, x: float) -> float:
     return float(t.item())
 
 
+def aggregate(dist, cells_local: float, ms_local: float):
+    """Whole-job throughput of N replicas: all ranks' cells over the slowest rank's time."""
+    ms = allmax(dist, ms_local)
+    return allsum(dist, cells_local) / (ms / 1e3), ms
+
+
 def measured_peaks():
     p = ROOT / "MEASURED_PEAKS.json"
     if p.exists():
@@ -287,9 +293,7 @@ def run_gpu(args):
     launches = s.launch_count() - launches0
     st = s.last_stats()
     md = s.max_divergence()
-    ms_max = allmax(dist, ms)
-    cells = allsum(dist, float(n) * n * args.steps)
-    value = cells / (ms_max / 1e3)
+    value, ms_max = aggregate(dist, float(n) * n * args.steps, ms)
 
     # per-kernel profile (events around every launch), a few steps after the timed region
     prof = s.profile_step(dt, 3)
