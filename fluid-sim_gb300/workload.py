@@ -87,3 +87,28 @@ def batch_sides(count: int, seed: int):
     """Domain sides of a seeded batch of uneven simulations."""
     rng = np.random.default_rng(seed)
     return [int(rng.choice(BATCH_SIDES)) for _ in range(count)]
+
+
+def decaying_turbulence(n: int, seed: int, L: float = 2 * math.pi, k0: float = 16.0):
+    """Seeded decaying-turbulence state: random-phase streamfunction whose
+    shell spectrum is E(k) ~ k^4 exp(-(k/k0)^2) (|psi_k|^2 ~ k exp(-(k/k0)^2)
+    since E ~ k^3 |psi_k|^2 in 2-D), sampled at the cell corners so the MAC
+    velocity from its differences is exactly divergence-free, normalised to
+    kinetic energy 1/2 <u^2 + v^2> = 1.  Returns (u, v, dt) with dt at CFL 0.5."""
+    rng = np.random.default_rng(seed)
+    h = L / n
+    kk = np.fft.fftfreq(n, d=1.0 / n)
+    KX, KY = np.meshgrid(kk, kk)
+    k = np.hypot(KX, KY)
+    amp = np.sqrt(k * np.exp(-(k / k0) ** 2))
+    amp[0, 0] = 0.0
+    psi_hat = amp * np.exp(2j * math.pi * rng.random((n, n)))
+    psi = np.real(np.fft.ifft2(psi_hat)) * n * n
+    u = (np.roll(psi, -1, axis=0) - psi) / h
+    v = -(np.roll(psi, -1, axis=1) - psi) / h
+    ke = 0.5 * np.mean(u * u + v * v)
+    s = 1.0 / math.sqrt(ke)
+    u *= s
+    v *= s
+    umax = float(max(np.abs(u).max(), np.abs(v).max()))
+    return np.ascontiguousarray(u.ravel()), np.ascontiguousarray(v.ravel()), 0.5 * h / umax
