@@ -927,6 +927,13 @@ FS_API int fs_read_dye(fs_solver* h, float* rgba) {
   return FS_OK;
 }
 
+FS_API int fs_render(fs_solver* h, int32_t mode, double exposure, float* rgba) {
+  SOLVER(h);
+  if (!rgba) return fail(s, FS_ERR_INVALID_ARGUMENT, "rgba is NULL");
+  if (!std::isfinite(exposure)) return fail(s, FS_ERR_INVALID_ARGUMENT, "exposure must be finite");
+  return render(s, mode, (float)exposure, rgba);
+}
+
 FS_API int fs_diagnose(fs_solver* h, fs_diagnostics* out) {
   SOLVER(h);
   if (!out) return fail(s, FS_ERR_INVALID_ARGUMENT, "out is NULL");

@@ -35,13 +35,13 @@ struct DiagBuffers {
   float2* fv = nullptr;
   double* E = nullptr;
   int* counts = nullptr;
-  int64_t n_cells = 0;
+  float4* rgba = nullptr;   // render target
 };
 
 void diag_free(Solver* s) {
   DiagBuffers* d = static_cast<DiagBuffers*>(s->diag);
   if (!d) return;
-  void* ptrs[] = {d->part, d->counter, d->out, d->cu, d->cv, d->fu, d->fv, d->E, d->counts};
+  void* ptrs[] = {d->part, d->counter, d->out, d->cu, d->cv, d->fu, d->fv, d->E, d->counts, d->rgba};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   delete d;
@@ -314,6 +314,85 @@ int energy_spectrum(Solver* s, double* E, int32_t* counts, int cap, int* kmax_ou
     parseval[0] = tot;
     parseval[1] = dg.kinetic_energy;
   }
+  return FS_OK;
+}
+
+// ------------------------------------------------------------------ render
+// The arithmetic of the reference's RENDER pass (src/gpu/shaders.js:677-768)
+// into a device buffer instead of a swapchain texture: centre vorticity from
+// the four corner curls, a two-sided neon ramp in tanh(w * exposure) (or in
+// speed for mode 1), a white-hot speed term scaled by the same exposure, and
+// a dim dye lift.  Colours are linear RGBA f32 (the reference writes
+// rgba16float); non-finite colours become black.
+__device__ __forceinline__ float smoothstep_f(float e0, float e1, float x) {
+  const float t = fminf(fmaxf((x - e0) / (e1 - e0), 0.f), 1.f);
+  return t * t * (3.f - 2.f * t);
+}
+__device__ __forceinline__ float3 mix3(float3 a, float3 b, float t) {
+  return make_float3(a.x * (1.f - t) + b.x * t, a.y * (1.f - t) + b.y * t, a.z * (1.f - t) + b.z * t);
+}
+__device__ __forceinline__ float3 scale3(float3 a, float k) { return make_float3(a.x * k, a.y * k, a.z * k); }
+
+__global__ void __launch_bounds__(256) k_render(Face u, Face v, const float4* __restrict__ dye, int nx, int ny,
+                                                float idx, float idy, float exposure, int mode,
+                                                float4* __restrict__ out) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y;
+  if (i >= nx || j >= ny) return;
+  const int ip = i + 1 == nx ? 0 : i + 1, im = i == 0 ? nx - 1 : i - 1;
+  const int jp = j + 1 == ny ? 0 : j + 1, jm = j == 0 ? ny - 1 : j - 1;
+  const int64_t r = (int64_t)j * nx, rp = (int64_t)jp * nx, rm = (int64_t)jm * nx;
+  const float w00 = v.diff(r + i, r + im) * idx - u.diff(r + i, rm + i) * idy;
+  const float w10 = v.diff(r + ip, r + i) * idx - u.diff(r + ip, rm + ip) * idy;
+  const float w01 = v.diff(rp + i, rp + im) * idx - u.diff(rp + i, r + i) * idy;
+  const float w11 = v.diff(rp + ip, rp + i) * idx - u.diff(rp + ip, r + ip) * idy;
+  const float w = 0.25f * (w00 + w10 + w01 + w11);
+  const float cu = u.val(r + i), cv = v.val(r + i);
+  const float speed = sqrtf(cu * cu + cv * cv);
+  const float3 MAGENTA = make_float3(1.00f, 0.10f, 0.62f), CYAN = make_float3(0.10f, 0.92f, 1.00f);
+  const float3 VIOLET = make_float3(0.16f, 0.03f, 0.42f), VOID_ = make_float3(0.004f, 0.003f, 0.016f);
+  float3 col;
+  if (mode == 0) {
+    const float sig = tanhf(fminf(fmaxf(w * exposure, -12.f), 12.f));
+    const float mag = fabsf(sig);
+    const float3 hue = sig >= 0.f ? MAGENTA : CYAN;
+    const float3 ramp = mix3(mix3(VOID_, VIOLET, smoothstep_f(0.f, 0.22f, mag)), hue, smoothstep_f(0.12f, 0.62f, mag));
+    col = scale3(ramp, 0.30f + 4.6f * mag * mag);
+  } else {
+    const float t = tanhf(fminf(fmaxf(speed * exposure, -12.f), 12.f));
+    const float3 hue = mix3(VIOLET, CYAN, smoothstep_f(0.15f, 0.95f, t));
+    col = scale3(mix3(VOID_, hue, smoothstep_f(0.f, 0.6f, t)), 0.35f + 2.9f * t * t);
+  }
+  const float sp = tanhf(fminf(fmaxf(speed * exposure * 0.45f, 0.f), 12.f));
+  const float sp2 = sp * sp, hot = sp2 * sp2 * sp * 0.85f;
+  col = make_float3(col.x + 0.55f * hot, col.y + 0.78f * hot, col.z + 1.0f * hot);
+  if (dye) {
+    const float4 d = dye[r + i];
+    const float lum = d.x * 0.2126f + d.y * 0.7152f + d.z * 0.0722f;
+    col = make_float3(col.x + col.x * lum * 1.5f + d.x * 0.20f, col.y + col.y * lum * 1.5f + d.y * 0.20f,
+                      col.z + col.z * lum * 1.5f + d.z * 0.20f);
+  }
+  col = make_float3(col.x == col.x ? col.x : 0.f, col.y == col.y ? col.y : 0.f, col.z == col.z ? col.z : 0.f);
+  out[r + i] = make_float4(col.x, col.y, col.z, 1.f);
+}
+
+int render(Solver* s, int mode, float exposure, float* host_rgba) {
+  if (mode != 0 && mode != 1) return fail_status(s, FS_ERR_INVALID_ARGUMENT, "render: mode is 0 (vorticity) or 1 (speed)");
+  int rc = diag_alloc(s, false);
+  if (rc) return rc;
+  DiagBuffers* d = static_cast<DiagBuffers*>(s->diag);
+  cudaError_t e = cudaSuccess;
+  if (!d->rgba) e = cudaMalloc(&d->rgba, s->n * 16);
+  if (e != cudaSuccess) return fail_status(s, FS_ERR_OUT_OF_MEMORY, "render buffer");
+  Face u, v;
+  state_faces(s, &u, &v);
+  dim3 b(32, 8), g((s->g.nx + 31) / 32, (s->g.ny + 7) / 8);
+  k_render<<<g, b, 0, s->stream>>>(u, v, static_cast<const float4*>(s->dye), s->g.nx, s->g.ny, (float)s->g.idxd,
+                                   (float)s->g.idyd, exposure, mode, d->rgba);
+  s->launches++;
+  e = cudaGetLastError();
+  if (e == cudaSuccess) e = cudaMemcpyAsync(host_rgba, d->rgba, s->n * 16, cudaMemcpyDeviceToHost, s->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
+  if (e != cudaSuccess) return fail_status(s, FS_ERR_CUDA, std::string("render: ") + cudaGetErrorString(e));
   return FS_OK;
 }
 

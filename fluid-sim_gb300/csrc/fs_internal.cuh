@@ -248,5 +248,6 @@ int dump_pair(Solver* s, int factor, float* div, float* mask, float* p);
 void diag_free(Solver* s);
 int diagnostics(Solver* s, fs_diagnostics* out, bool with_centres);
 int energy_spectrum(Solver* s, double* E, int32_t* counts, int cap, int* kmax_out, double* parseval);
+int render(Solver* s, int mode, float exposure, float* host_rgba);
 
 }  // namespace fs

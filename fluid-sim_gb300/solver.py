@@ -291,6 +291,21 @@ class GPUFluidSolver:
         self._chk(self._lib.fs_read_dye(self._h, _ptr(out)))
         return out
 
+    def render(self, mode: str = "vorticity", exposure: float = 1.0) -> np.ndarray:
+        """RENDER arithmetic (shaders.js:677-768) into an [ny, nx, 4] f32 array"""
+        out = np.empty((self.ny, self.nx, 4), np.float32)
+        self._chk(self._lib.fs_render(self._h, {"vorticity": 0, "speed": 1}[mode], float(exposure), _ptr(out)))
+        return out
+
+    @staticmethod
+    def save_ppm(path, rgba: np.ndarray) -> None:
+        """Write a render as a binary PPM (Reinhard tone map, gamma 2.2, row 0 at the bottom)."""
+        c = np.asarray(rgba, np.float64)[..., :3]
+        c = (c / (1.0 + c)) ** (1 / 2.2)
+        img = np.clip(np.round(c[::-1] * 255), 0, 255).astype(np.uint8)
+        with open(path, "wb") as f:
+            f.write(f"P6 {img.shape[1]} {img.shape[0]} 255\n".encode() + img.tobytes())
+
     # ------------------------------------------------------- diagnostics
     def diagnostics(self) -> dict:
         """kinetic energy, enstrophy, max and L2 divergence of the state (device reductions)"""

@@ -364,6 +364,14 @@ FS_API int fs_read_pair_file(const char* path, int32_t* nx, int32_t* ny, double*
 FS_API int fs_upload_dye(fs_solver* s, const float* rgba);
 FS_API int fs_read_dye(fs_solver* s, float* rgba);
 
+/* The arithmetic of the reference's RENDER pass (shaders.js:677-768) into a
+ * buffer instead of a swapchain (no graphics API): linear RGBA f32 per cell,
+ * [ny][nx][4], host array.  mode 0 colours the centre vorticity
+ * tanh(w * exposure) on a magenta / cyan ramp, mode 1 the speed; both add the
+ * exposure-scaled speed glow and, if uploaded, the dim dye lift.  exposure is
+ * the reference's param_a.  Synchronises. */
+FS_API int fs_render(fs_solver* s, int32_t mode, double exposure, float* rgba);
+
 /* ------------------------------------------------------------------------
  * Diagnostics on the device (the reference reads the fields back and loops
  * on the CPU: src/core/grid.js:280-327, src/core/fft.js:196-254).
