@@ -1055,6 +1055,120 @@ FS_API int fs_time_steps(fs_solver* h, double dt, int nsteps, double* elapsed_ms
   return rc;
 }
 
+FS_API int fs_set_mg_sweeps(fs_solver* h, int32_t pre, int32_t post) {
+  SOLVER(h);
+  if (s->prm.pressure_solver != FS_PRESSURE_MULTIGRID) return fail(s, FS_ERR_UNSUPPORTED, "multigrid only");
+  if (pre < 1 || pre > 8 || post < 1 || post > 8) return fail(s, FS_ERR_INVALID_ARGUMENT, "sweeps in 1..8");
+  CU(s, cudaStreamSynchronize(s->stream));
+  const fs_params old = s->prm;
+  s->prm.mg_pre_smooth = pre;
+  s->prm.mg_post_smooth = post;
+  if (s->fused && !mg_fused_supported(s)) {  // the fused tile kernels take 1..3
+    s->prm = old;
+    return fail(s, FS_ERR_UNSUPPORTED, "the fused multigrid kernels take 1 to 3 sweeps");
+  }
+  drop_graph(s);
+  return FS_OK;
+}
+
+// Autotuner of the multigrid sweep counts: every (pre, post) pair the fused
+// kernels take is timed over `nsteps` steps from the same state (the state,
+// dye, time and pressure are saved on the device and restored between
+// candidates and at the end), and the fastest is kept.  Ties in time go to
+// fewer sweeps.  Returns the choice and its ms per step.
+FS_API int fs_autotune(fs_solver* h, double dt, int32_t nsteps, int32_t* pre_out, int32_t* post_out,
+                       double* ms_out) {
+  SOLVER(h);
+  if (s->prm.pressure_solver != FS_PRESSURE_MULTIGRID || !s->fused)
+    return fail(s, FS_ERR_UNSUPPORTED, "fs_autotune tunes the fused multigrid step");
+  if (nsteps < 1 || !std::isfinite(dt)) return fail(s, FS_ERR_INVALID_ARGUMENT, "bad dt or nsteps");
+  CU(s, cudaStreamSynchronize(s->stream));
+  // planes that a step changes and the next step reads
+  std::vector<std::pair<void*, size_t>> planes = {{s->u, 4}, {s->v, 4}};
+  if (s->mixed) {
+    planes.push_back({s->ulo, 4});
+    planes.push_back({s->vlo, 4});
+    planes.push_back({s->ph, 4});
+    planes.push_back({s->pl, 4});
+  } else {
+    planes.push_back({s->p32, 4});
+  }
+  if (s->dye) planes.push_back({s->dye, 16});
+  size_t total = sizeof(DevState);
+  for (auto& p : planes) total += p.second * (size_t)s->n;
+  char* save = nullptr;
+  CU(s, cudaMalloc(&save, total));
+  auto copy = [&](bool to_save) -> cudaError_t {
+    size_t off = 0;
+    for (auto& p : planes) {
+      size_t b = p.second * (size_t)s->n;
+      cudaError_t e = to_save ? cudaMemcpyAsync(save + off, p.first, b, cudaMemcpyDeviceToDevice, s->stream)
+                              : cudaMemcpyAsync(p.first, save + off, b, cudaMemcpyDeviceToDevice, s->stream);
+      if (e != cudaSuccess) return e;
+      off += b;
+    }
+    return to_save ? cudaMemcpyAsync(save + off, s->dev, sizeof(DevState), cudaMemcpyDeviceToDevice, s->stream)
+                   : cudaMemcpyAsync(s->dev, save + off, sizeof(DevState), cudaMemcpyDeviceToDevice, s->stream);
+  };
+  const double t0 = s->t;
+  const int64_t steps0 = s->steps, l0 = s->launches, r0 = s->graph_replays;
+  const fs_params orig = s->prm;
+  int best_pre = orig.mg_pre_smooth, best_post = orig.mg_post_smooth, rc = FS_OK;
+  double best = 1e300;
+  cudaError_t e = copy(true);
+  cudaEvent_t a = nullptr, b = nullptr;
+  if (e == cudaSuccess) e = cudaEventCreate(&a);
+  if (e == cudaSuccess) e = cudaEventCreate(&b);
+  for (int pre = 1; pre <= 3 && e == cudaSuccess && rc == FS_OK; pre++) {
+    for (int post = 1; post <= 3 && e == cudaSuccess && rc == FS_OK; post++) {
+      s->prm.mg_pre_smooth = pre;
+      s->prm.mg_post_smooth = post;
+      drop_graph(s);
+      rc = step(s, dt);  // captures the graph for this candidate outside the timing
+      if (rc == FS_OK) e = copy(false);
+      if (e != cudaSuccess || rc != FS_OK) break;
+      e = cudaEventRecord(a, s->stream);
+      for (int k = 0; k < nsteps && rc == FS_OK; k++) rc = step(s, dt);
+      if (e == cudaSuccess) e = cudaEventRecord(b, s->stream);
+      if (e == cudaSuccess) e = cudaEventSynchronize(b);
+      float ms = 0;
+      if (e == cudaSuccess) cudaEventElapsedTime(&ms, a, b);
+      fs_step_stats st;
+      if (rc == FS_OK && s->stats_on_device) {
+        DevState d;
+        e = cudaMemcpy(&d, s->dev, sizeof d, cudaMemcpyDeviceToHost);
+        if (e == cudaSuccess && (!d.converged || d.nonfinite)) ms = 1e30f;  // must still meet the tolerance
+      }
+      (void)st;
+      const double per = ms / nsteps;
+      if (per < best * 0.999) {
+        best = per;
+        best_pre = pre;
+        best_post = post;
+      }
+      if (e == cudaSuccess) e = copy(false);
+    }
+  }
+  if (a) cudaEventDestroy(a);
+  if (b) cudaEventDestroy(b);
+  cudaStreamSynchronize(s->stream);
+  cudaFree(save);
+  s->t = t0;
+  s->steps = steps0;
+  s->launches = l0;
+  s->graph_replays = r0;
+  s->prm = orig;
+  s->prm.mg_pre_smooth = best_pre;
+  s->prm.mg_post_smooth = best_post;
+  drop_graph(s);
+  if (rc != FS_OK) return rc;
+  if (e != cudaSuccess) return fail(s, FS_ERR_CUDA, std::string("fs_autotune: ") + cudaGetErrorString(e));
+  if (pre_out) *pre_out = best_pre;
+  if (post_out) *post_out = best_post;
+  if (ms_out) *ms_out = best;
+  return FS_OK;
+}
+
 FS_API int fs_profile_step(fs_solver* h, double dt, int nsteps, fs_kernel_time* out, int cap, int* count) {
   SOLVER(h);
   if (nsteps < 0 || cap < 0 || (cap > 0 && !out)) return fail(s, FS_ERR_INVALID_ARGUMENT, "bad arguments");

@@ -291,6 +291,17 @@ class GPUFluidSolver:
         self._chk(self._lib.fs_read_dye(self._h, _ptr(out)))
         return out
 
+    def set_mg_sweeps(self, pre: int, post: int) -> None:
+        self._chk(self._lib.fs_set_mg_sweeps(self._h, pre, post))
+        self.params.mg_pre_smooth, self.params.mg_post_smooth = pre, post
+
+    def autotune(self, dt: float, nsteps: int = 5) -> dict:
+        """time every (pre, post) sweep pair from the current state, keep the fastest"""
+        pre, post, ms = C.c_int32(), C.c_int32(), C.c_double()
+        self._chk(self._lib.fs_autotune(self._h, dt, nsteps, C.byref(pre), C.byref(post), C.byref(ms)))
+        self.params.mg_pre_smooth, self.params.mg_post_smooth = pre.value, post.value
+        return {"pre": pre.value, "post": post.value, "ms_per_step": ms.value}
+
     def render(self, mode: str = "vorticity", exposure: float = 1.0) -> np.ndarray:
         """RENDER arithmetic (shaders.js:677-768) into an [ny, nx, 4] f32 array"""
         out = np.empty((self.ny, self.nx, 4), np.float32)

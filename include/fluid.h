@@ -372,6 +372,14 @@ FS_API int fs_read_dye(fs_solver* s, float* rgba);
  * the reference's param_a.  Synchronises. */
 FS_API int fs_render(fs_solver* s, int32_t mode, double exposure, float* rgba);
 
+/* Multigrid sweep counts of an existing solver (drops the captured step). */
+FS_API int fs_set_mg_sweeps(fs_solver* s, int32_t pre, int32_t post);
+/* Autotuner: times nsteps steps of dt for every (pre, post) sweep pair the
+ * fused kernels take (1..3 each), from the same saved state each time, and
+ * keeps the fastest that still meets pressure_tol; the state, dye, time and
+ * pressure are restored afterwards.  No reference counterpart. */
+FS_API int fs_autotune(fs_solver* s, double dt, int32_t nsteps, int32_t* pre, int32_t* post, double* ms_per_step);
+
 /* ------------------------------------------------------------------------
  * Diagnostics on the device (the reference reads the fields back and loops
  * on the CPU: src/core/grid.js:280-327, src/core/fft.js:196-254).
