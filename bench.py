@@ -236,6 +236,12 @@ def measure_batch(pkg, device, count, steps, warmup, seed=1):
     ms = b.time_steps(dts, steps)
     converged = all(m.last_stats()["converged"] for m in b.members)
     launches = b.launch_count()
+    # sweep counts per domain size picked by the autotuner, then the same timing
+    picks = b.autotune(dts, 3)
+    for _ in range(warmup):
+        b.step(dts)
+    ms_tuned = b.time_steps(dts, steps)
+    converged = converged and all(m.last_stats()["converged"] for m in b.members)
     # the same members, one solver graph after another on the same stream
     seq_ms = 0.0
     for m, dt in zip(b.members, dts):
@@ -246,6 +252,8 @@ def measure_batch(pkg, device, count, steps, warmup, seed=1):
     return {"sims": count, "cells": cells, "sides": {str(k): sides.count(k) for k in sorted(set(sides))},
             "ms_per_step": ms / steps, "value": cells * steps / (ms / 1e3), "unit": UNIT,
             "sequential_ms_per_step": seq_ms, "speedup_vs_sequential": seq_ms / (ms / steps),
+            "autotuned_sweeps": {f"{k[0]}": list(v) for k, v in sorted(picks.items())},
+            "autotuned_ms_per_step": ms_tuned / steps, "autotuned_value": cells * steps / (ms_tuned / 1e3),
             "converged": converged, "gpu_launches_total": launches}
 
 

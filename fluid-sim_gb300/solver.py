@@ -405,6 +405,21 @@ class GPUFluidBatch:
     def launch_count(self) -> int:
         return int(self._lib.fs_batch_launch_count(self._h))
 
+    def autotune(self, dt, nsteps: int = 3) -> dict:
+        """Sweep counts per domain size: the first member of each size is tuned
+        (fs_autotune, its state restored afterwards) and its choice is applied
+        to every member of that size.  Returns {(nx, ny): (pre, post)}."""
+        d, _ = self._dts(dt)
+        picks = {}
+        for m, dtm in zip(self.members, d):
+            key = (m.nx, m.ny)
+            if key not in picks:
+                r = m.autotune(float(dtm), nsteps)
+                picks[key] = (r["pre"], r["post"])
+            else:
+                m.set_mg_sweeps(*picks[key])
+        return picks
+
     def destroy(self) -> None:
         if getattr(self, "_h", None):
             for m in self.members:
