@@ -168,40 +168,82 @@ __global__ void __launch_bounds__(256) k_mg_up(const float* __restrict__ rhs, co
   const int par0 = (gi0 + gj0) & 1;
   const int tid = threadIdx.y * blockDim.x + threadIdx.x, nthr = blockDim.x * blockDim.y;
   const int nc = n >> 1;
-  for (int k = tid; k < R * R; k += nthr) {
-    int lj = k / R, li = k - lj * R;
-    int gi = wrap1(gi0 + li, n), gj = wrap1(gj0 + lj, n);
-    int64_t g = (int64_t)gj * n + gi;
-    // PROLONG (multigrid.js:99-131): sample at ((i+1/2)/2 - 1/2, (j+1/2)/2 - 1/2)
-    int ci0 = (gi & 1) ? (gi >> 1) : (gi >> 1) - 1;
-    int cj0 = (gj & 1) ? (gj >> 1) : (gj >> 1) - 1;
-    float fx = (gi & 1) ? 0.25f : 0.75f, fy = (gj & 1) ? 0.25f : 0.75f;
-    int x0 = ci0 < 0 ? ci0 + nc : ci0, x1 = ci0 + 1 >= nc ? ci0 + 1 - nc : ci0 + 1;
-    int y0 = cj0 < 0 ? cj0 + nc : cj0, y1 = cj0 + 1 >= nc ? cj0 + 1 - nc : cj0 + 1;
-    float p = prolong_val(__ldg(xc + (int64_t)y0 * nc + x0), __ldg(xc + (int64_t)y0 * nc + x1),
-                          __ldg(xc + (int64_t)y1 * nc + x0), __ldg(xc + (int64_t)y1 * nc + x1), fx, fy);
-    int q = CK::at(li, lj, par0);
-    xs[q] = __fadd_rn(__ldg(xin + g), p);
-    rs[q] = __ldg(rhs + g);
+  // staging: two cells' loads (fine x, rhs, four coarse values each) in flight
+  // per thread before the prolongation arithmetic and the stores
+  constexpr int U = 2;
+  for (int k0 = tid; k0 < R * R; k0 += U * nthr) {
+    float vx[U], vr[U], c00[U], c10[U], c01[U], c11[U], fx[U], fy[U];
+    int q[U];
+#pragma unroll
+    for (int u = 0; u < U; u++) {
+      const int k = k0 + u * nthr;
+      q[u] = -1;
+      if (k < R * R) {
+        const int lj = k / R, li = k - lj * R;
+        const int gi = wrap1(gi0 + li, n), gj = wrap1(gj0 + lj, n);
+        const int64_t g = (int64_t)gj * n + gi;
+        // PROLONG (multigrid.js:99-131): sample at ((i+1/2)/2 - 1/2, (j+1/2)/2 - 1/2)
+        const int ci0 = (gi & 1) ? (gi >> 1) : (gi >> 1) - 1;
+        const int cj0 = (gj & 1) ? (gj >> 1) : (gj >> 1) - 1;
+        fx[u] = (gi & 1) ? 0.25f : 0.75f;
+        fy[u] = (gj & 1) ? 0.25f : 0.75f;
+        const int x0 = ci0 < 0 ? ci0 + nc : ci0, x1 = ci0 + 1 >= nc ? ci0 + 1 - nc : ci0 + 1;
+        const int y0 = cj0 < 0 ? cj0 + nc : cj0, y1 = cj0 + 1 >= nc ? cj0 + 1 - nc : cj0 + 1;
+        c00[u] = __ldg(xc + (int64_t)y0 * nc + x0);
+        c10[u] = __ldg(xc + (int64_t)y0 * nc + x1);
+        c01[u] = __ldg(xc + (int64_t)y1 * nc + x0);
+        c11[u] = __ldg(xc + (int64_t)y1 * nc + x1);
+        vx[u] = __ldg(xin + g);
+        vr[u] = __ldg(rhs + g);
+        q[u] = CK::at(li, lj, par0);
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < U; u++)
+      if (q[u] >= 0) {
+        xs[q[u]] = __fadd_rn(vx[u], prolong_val(c00[u], c10[u], c01[u], c11[u], fx[u], fy[u]));
+        rs[q[u]] = vr[u];
+      }
   }
   __syncthreads();
   for (int s = 0; s < 2 * post; s++) {
     rb_half_smem<R>(xs, rs, s & 1, par0, h2);
     __syncthreads();
   }
-  for (int k = tid; k < T * T; k += nthr) {
-    int y = k / T, x = k - y * T;
-    int gi = i0 + x, gj = j0 + y;
-    if (gi < n && gj < n) {
-      int64_t g = (int64_t)gj * n + gi;
-      float e = xs[CK::at(H + x, H + y, par0)];
-      if (ACC) {
-        df p = df_add_f(df{ph[g], pl[g]}, e);
-        ph[g] = p.hi;
-        pl[g] = p.lo;
-      } else {
-        xout[g] = e;
+  if constexpr (ACC) {
+    // four cells' double-float pressure loads in flight per thread
+    constexpr int V = 4;
+    for (int k0 = tid; k0 < T * T; k0 += V * nthr) {
+      float hv[V], lv[V], ev[V];
+      int64_t gv[V];
+#pragma unroll
+      for (int u = 0; u < V; u++) {
+        const int k = k0 + u * nthr;
+        gv[u] = -1;
+        if (k < T * T) {
+          const int y = k / T, x = k - y * T;
+          const int gi = i0 + x, gj = j0 + y;
+          if (gi < n && gj < n) {
+            gv[u] = (int64_t)gj * n + gi;
+            hv[u] = ph[gv[u]];
+            lv[u] = pl[gv[u]];
+            ev[u] = xs[CK::at(H + x, H + y, par0)];
+          }
+        }
       }
+#pragma unroll
+      for (int u = 0; u < V; u++)
+        if (gv[u] >= 0) {
+          const df p = df_add_f(df{hv[u], lv[u]}, ev[u]);
+          ph[gv[u]] = p.hi;
+          pl[gv[u]] = p.lo;
+        }
+    }
+  } else {
+    for (int k = tid; k < T * T; k += nthr) {
+      const int y = k / T, x = k - y * T;
+      const int gi = i0 + x, gj = j0 + y;
+      if (gi < n && gj < n) xout[(int64_t)gj * n + gi] = xs[CK::at(H + x, H + y, par0)];
     }
   }
 }
