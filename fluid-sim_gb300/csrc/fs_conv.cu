@@ -22,6 +22,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <atomic>
 #include <string>
 
 #include "../../include/fluid.h"
@@ -316,12 +317,17 @@ template <int CIN, int COUT, int TY, int NS, int EPI>
 static cudaError_t launch_t(const void* in, const void* w, const float* bias, void* out, int B, int H, int W,
                             int* err, cudaStream_t st) {
   using C = Cfg<CIN, COUT, TY, NS>;
-  static bool attr = false;  // per process; the attribute is per device function
-  if (!attr) {
+  // the dynamic shared-memory limit is an attribute of the function on each device
+  static std::atomic<uint64_t> attr_set{0};
+  int dev = 0;
+  cudaError_t e0 = cudaGetDevice(&dev);
+  if (e0 != cudaSuccess) return e0;
+  const uint64_t bit = 1ull << (dev & 63);
+  if (!(attr_set.load() & bit)) {
     cudaError_t e = cudaFuncSetAttribute(k_conv3x3<CIN, COUT, TY, NS, EPI>,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize, C::SMEM);
     if (e != cudaSuccess) return e;
-    attr = true;
+    attr_set.fetch_or(bit);
   }
   dim3 grid((W + kTX - 1) / kTX, (H + TY - 1) / TY, B * C::NSPLIT);
   k_conv3x3<CIN, COUT, TY, NS, EPI><<<grid, kThreads, C::SMEM, st>>>(
