@@ -264,14 +264,12 @@ def measure_variant(pkg, n, device, guess, u0, v0, disks, dt, steps, warmup):
     s.set_solids(disks)
     for _ in range(warmup):
         s.step(dt)
+    c0 = s.total_cycles()
     ms = s.time_steps(dt, steps)
-    cyc = []
-    for _ in range(5):
-        s.step(dt)
-        cyc.append(s.last_stats()["cycles"])
+    cyc = (s.total_cycles() - c0) / steps
     md = s.max_divergence()
     s.destroy()
-    return {"ms_per_step": ms / steps, "cycles_per_step": float(np.mean(cyc)),
+    return {"ms_per_step": ms / steps, "cycles_per_step": cyc,
             "value": float(n) * n * steps / (ms / 1e3), "max_div_after": md}
 
 
@@ -294,11 +292,13 @@ def run_gpu(args):
     s.sync()
     # timed region: K steps, device events on the solver's stream
     launches0 = s.launch_count()
+    cycles0 = s.total_cycles()
     barrier(dist)
     with ClockSampler(local) as clk:
         ms = s.time_steps(dt, args.steps)
     barrier(dist)
     launches = s.launch_count() - launches0
+    cycles_timed = (s.total_cycles() - cycles0) / max(args.steps, 1)
     st = s.last_stats()
     md = s.max_divergence()
     value, ms_max = aggregate(dist, float(n) * n * args.steps, ms)
@@ -312,12 +312,6 @@ def run_gpu(args):
     peak, peak_src = measured_peaks()
     achieved = bytes_per_launch / (per_launch_ms / 1e3) / 1e9
     traffic = traffic_from_profiles(top["name"])
-
-    # cycles per step over the timed steps (from a separate short run of stats)
-    cyc = []
-    for _ in range(5):
-        s.step(dt)
-        cyc.append(s.last_stats()["cycles"])
 
     # e2e: host upload + step + host read-back per step through the C ABI
     lib = pkg.load()
@@ -374,7 +368,7 @@ def run_gpu(args):
                 "n": n, "disks": len(disks), "dt": dt, "tol": TOL, "guess": args.guess,
                 "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
                 "l2": "working set ~0.35 GB > 129 MB L2; no flush between steps",
-                "cycles_per_step": float(np.mean(cyc)),
+                "cycles_per_step": cycles_timed,
                 "max_div_after": md, "converged": bool(st["converged"]),
             },
             "roofline": {
@@ -389,10 +383,10 @@ def run_gpu(args):
             "e2e": {"value": e2e_val, "unit": UNIT, "h2d_bytes_per_step": 2 * nbytes,
                     "d2h_bytes_per_step": 2 * nbytes, "steps": e2e_steps},
             "step_roofline": {
-                "bytes_per_cell_step": step_bytes(float(np.mean(cyc))),
-                "achieved": value * step_bytes(float(np.mean(cyc))) / 1e9 / max(world, 1),
+                "bytes_per_cell_step": step_bytes(cycles_timed),
+                "achieved": value * step_bytes(cycles_timed) / 1e9 / max(world, 1),
                 "peak": peak, "unit": "GB/s",
-                "frac": value * step_bytes(float(np.mean(cyc))) / 1e9 / max(world, 1) / peak,
+                "frac": value * step_bytes(cycles_timed) / 1e9 / max(world, 1) / peak,
             },
             "gpu_launches": launches,
             "clocks": clk.summary(),

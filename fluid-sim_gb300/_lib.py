@@ -159,6 +159,7 @@ SIGNATURES = {
     "fs_read_dye": (I, [VP, VP]),
     "fs_render": (I, [VP, C.c_int32, D, VP]),
     "fs_set_mg_sweeps": (I, [VP, C.c_int32, C.c_int32]),
+    "fs_total_cycles": (I, [VP, C.POINTER(C.c_int64)]),
     "fs_autotune": (I, [VP, D, C.c_int32, C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.POINTER(D)]),
     "fs_diagnose": (I, [VP, VP]),
     "fs_energy_spectrum": (I, [VP, VP, VP, C.c_int32, C.POINTER(C.c_int32), VP]),

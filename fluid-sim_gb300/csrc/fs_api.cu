@@ -1191,6 +1191,16 @@ FS_API int fs_profile_step(fs_solver* h, double dt, int nsteps, fs_kernel_time* 
   return rc;
 }
 
+FS_API int fs_total_cycles(fs_solver* h, int64_t* cycles) {
+  SOLVER(h);
+  if (!cycles) return fail(s, FS_ERR_INVALID_ARGUMENT, "cycles is NULL");
+  CU(s, cudaStreamSynchronize(s->stream));
+  DevState d;
+  CU(s, cudaMemcpy(&d, s->dev, sizeof d, cudaMemcpyDeviceToHost));
+  *cycles = d.total_cycles;
+  return FS_OK;
+}
+
 FS_API int64_t fs_launch_count(const fs_solver* h) {
   if (!h) return 0;
   const Solver* s = &h->s;

@@ -291,6 +291,12 @@ class GPUFluidSolver:
         self._chk(self._lib.fs_read_dye(self._h, _ptr(out)))
         return out
 
+    def total_cycles(self) -> int:
+        """refinement cycles run by all projections so far (device counter)"""
+        c = C.c_int64()
+        self._chk(self._lib.fs_total_cycles(self._h, C.byref(c)))
+        return c.value
+
     def set_mg_sweeps(self, pre: int, post: int) -> None:
         self._chk(self._lib.fs_set_mg_sweeps(self._h, pre, post))
         self.params.mg_pre_smooth, self.params.mg_post_smooth = pre, post

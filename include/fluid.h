@@ -374,6 +374,9 @@ FS_API int fs_render(fs_solver* s, int32_t mode, double exposure, float* rgba);
 
 /* Multigrid sweep counts of an existing solver (drops the captured step). */
 FS_API int fs_set_mg_sweeps(fs_solver* s, int32_t pre, int32_t post);
+/* refinement cycles run by every projection of the tolerance loop since
+ * creation (a device counter; synchronises) */
+FS_API int fs_total_cycles(fs_solver* s, int64_t* cycles);
 /* Autotuner: times nsteps steps of dt for every (pre, post) sweep pair the
  * fused kernels take (1..3 each), from the same saved state each time, and
  * keeps the fastest that still meets pressure_tol; the state, dye, time and

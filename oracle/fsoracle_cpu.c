@@ -753,7 +753,7 @@ int fso_diffuse(const fso_grid* g, const double* field, double* out, double nu, 
   }
   /* CG on (I - nu dt lap), warm-started from the field */
   double k = nu * dt;
-  double* r = (double*)malloc(sizeof(double) * n);
+  double* r = (double*)calloc((size_t)n, sizeof(double));
   double* Ap = (double*)malloc(sizeof(double) * n);
   double* d = (double*)malloc(sizeof(double) * n);
   memcpy(out, field, sizeof(double) * n);

@@ -425,6 +425,21 @@ def test_graph_step_equals_eager_step(G, O, precision):
     assert np.array_equal(outs[0][0], outs[1][0]) and np.array_equal(outs[0][1], outs[1][1])
 
 
+def test_total_cycles_counts_every_projection(G, O):
+    """fs_total_cycles is the sum of the per-step cycle counts of fs_last_stats."""
+    n = 128
+    u0, v0 = O.lcg_uv(31, n * n)
+    s = G.GPUFluidSolver(n=n, nu=1e-3, advection="maccormack", pressure_solver="multigrid",
+                         pressure_iterations=1, precision="mixed", pressure_tol=1e-6, max_cycles=40)
+    s.upload_velocity(u0, v0)
+    c0 = s.total_cycles()
+    per_step = []
+    for _ in range(4):
+        s.step(0.01)
+        per_step.append(s.last_stats()["cycles"])
+    assert s.total_cycles() - c0 == sum(per_step) and min(per_step) >= 1
+
+
 def test_graph_step_reports_tolerance_failure(G, O):
     n = 128
     u0, v0 = O.lcg_uv(8, n * n)
