@@ -84,7 +84,8 @@ class Params(C.Structure):
                 ("pressure_tol", C.c_double), ("max_cycles", C.c_int32), ("mg_pre_smooth", C.c_int32),
                 ("mg_post_smooth", C.c_int32), ("mg_coarse_sweeps", C.c_int32), ("mg_min_size", C.c_int32),
                 ("warm_start", C.c_int32), ("device", C.c_int32), ("kernel_variant", C.c_int32),
-                ("dye_fade", C.c_double)]
+                ("dye_fade", C.c_double),
+                ("relax", C.c_double)]
 
 
 class Mode(C.Structure):

@@ -136,6 +136,7 @@ static int create(const fs_params* prm, Solver* s) {
   if (!(P.lx > 0) || !(P.ly > 0)) return fail(nullptr, FS_ERR_INVALID_ARGUMENT, "domain size must be positive");
   if (!(P.nu >= 0)) return fail(nullptr, FS_ERR_INVALID_ARGUMENT, "nu must be >= 0");
   if (!(P.dye_fade >= 0) || !(P.dye_fade <= 1)) return fail(nullptr, FS_ERR_INVALID_ARGUMENT, "dye_fade must be in [0, 1]");
+  if (!(P.relax > 0) || !(P.relax < 2)) return fail(nullptr, FS_ERR_INVALID_ARGUMENT, "relax must be in (0, 2)");
   if (P.confinement != 0)
     return fail(nullptr, FS_ERR_UNSUPPORTED, "vorticity confinement is not part of this path (it must stay off)");
   if (P.advection != FS_ADVECT_SEMI_LAGRANGIAN && P.advection != FS_ADVECT_MACCORMACK)
@@ -673,6 +674,7 @@ FS_API void fs_params_default(fs_params* p) {
   p->device = 0;
   p->kernel_variant = 0;
   p->dye_fade = 0.0;
+  p->relax = 1.0;
 }
 
 FS_API int fs_create(const fs_params* params, fs_solver** out) {

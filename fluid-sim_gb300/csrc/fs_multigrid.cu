@@ -70,7 +70,7 @@ struct Checker {
 // left/right pair and its up neighbour one of row lj+1's, so a row costs two
 // new loads of the other colour (plus the cell and its rhs) instead of four.
 template <int R>
-__device__ __forceinline__ void rb_half_smem(float* xs, const float* rs, int c, int par0, float h2) {
+__device__ __forceinline__ void rb_half_smem(float* xs, const float* rs, int c, int par0, float h2, float w) {
   using CK = Checker<R>;
   constexpr int S = CK::S;
   constexpr int SW = S - 1;              // cells of one colour per row inside [1, R-2]
@@ -93,7 +93,7 @@ __device__ __forceinline__ void rb_half_smem(float* xs, const float* rs, int c, 
   for (; lj < lend; lj++) {
     float nl = xo[base + S], nr = xo[base + S + 1];  // row lj + 1
     int k = base + b;
-    xc[k] = gs_update(xc[k], cl, cr, b ? pr : pl, b ? nr : nl, rc[k], h2);
+    xc[k] = gs_update(xc[k], cl, cr, b ? pr : pl, b ? nr : nl, rc[k], h2, w);
     pl = cl; pr = cr; cl = nl; cr = nr;
     base += S;
     b ^= 1;
@@ -106,7 +106,7 @@ __device__ __forceinline__ void rb_half_smem(float* xs, const float* rs, int c, 
 template <int T, int H>
 __global__ void __launch_bounds__(256) k_mg_down(const float* __restrict__ rhs, const float* __restrict__ xin,
                                                  float* __restrict__ xout, float* __restrict__ crhs, int n,
-                                                 float h2, int pre) {
+                                                 float h2, int pre, float w) {
   constexpr int R = T + 2 * H;
   using CK = Checker<R>;
   __shared__ float xs[CK::STRIDE + CK::N];
@@ -124,7 +124,7 @@ __global__ void __launch_bounds__(256) k_mg_down(const float* __restrict__ rhs, 
   }
   __syncthreads();
   for (int s = 0; s < 2 * pre; s++) {
-    rb_half_smem<R>(xs, rs, s & 1, par0, h2);
+    rb_half_smem<R>(xs, rs, s & 1, par0, h2, w);
     __syncthreads();
   }
   for (int k = tid; k < T * T; k += nthr) {
@@ -169,7 +169,7 @@ template <int T, int H, bool ACC>
 __global__ void __launch_bounds__(256) k_mg_up(const float* __restrict__ rhs, const float* __restrict__ xin,
                                                float* __restrict__ xout, const float* __restrict__ xc, int n,
                                                float h2, int post, float* __restrict__ ph,
-                                               float* __restrict__ pl) {
+                                               float* __restrict__ pl, float w) {
   constexpr int R = T + 2 * H;
   using CK = Checker<R>;
   __shared__ float xs[CK::STRIDE + CK::N];
@@ -218,7 +218,7 @@ __global__ void __launch_bounds__(256) k_mg_up(const float* __restrict__ rhs, co
   }
   __syncthreads();
   for (int s = 0; s < 2 * post; s++) {
-    rb_half_smem<R>(xs, rs, s & 1, par0, h2);
+    rb_half_smem<R>(xs, rs, s & 1, par0, h2, w);
     __syncthreads();
   }
   if constexpr (ACC) {
@@ -269,6 +269,7 @@ struct BottomLevels {
   int n[8];
   float h2[8];
   int off_x[8], off_x2[8], off_r[8];  // float offsets into dynamic smem (-1: none)
+  float w;                            // relaxation factor of every sweep
 };
 
 // A thread group: the whole CTA, or warp 0 alone (levels <= 16).
@@ -295,7 +296,7 @@ __device__ void bottom_smooth(float* sm, const BottomLevels& L, int l, int sweep
         if (((i + j) & 1) != c) continue;
         int im = i == 0 ? n - 1 : i - 1, ip = i + 1 == n ? 0 : i + 1;
         int jm = j == 0 ? n - 1 : j - 1, jp = j + 1 == n ? 0 : j + 1;
-        x[k] = gs_update(x[k], x[j * n + im], x[j * n + ip], x[jm * n + i], x[jp * n + i], r[k], h2);
+        x[k] = gs_update(x[k], x[j * n + im], x[j * n + ip], x[jm * n + i], x[jp * n + i], r[k], h2, L.w);
       }
     } else {
       for (int k = G.tid; k < n * n; k += G.nthr) {
@@ -304,7 +305,7 @@ __device__ void bottom_smooth(float* sm, const BottomLevels& L, int l, int sweep
         if (((i + j) & 1) != c) { x2[k] = cur; continue; }
         int im = i == 0 ? n - 1 : i - 1, ip = i + 1 == n ? 0 : i + 1;
         int jm = j == 0 ? n - 1 : j - 1, jp = j + 1 == n ? 0 : j + 1;
-        x2[k] = gs_update(cur, x[j * n + im], x[j * n + ip], x[jm * n + i], x[jp * n + i], r[k], h2);
+        x2[k] = gs_update(cur, x[j * n + im], x[j * n + ip], x[jm * n + i], x[jp * n + i], r[k], h2, L.w);
       }
       G.sync();
       float* t = x; x = x2; x2 = t;  // two swaps per sweep: x is back in off_x at the end
@@ -426,6 +427,7 @@ __global__ void __launch_bounds__(1024) k_mg_bottom(const float* __restrict__ rh
 // arithmetic (fs_stencil.cuh) and order as the generic kernel above.
 struct BottomH2 {
   float h2[4];
+  float w;  // relaxation factor of every sweep
 };
 
 template <int N>
@@ -440,7 +442,7 @@ __device__ __forceinline__ void p2_sync() {
 }
 
 template <int N, bool WARP>
-__device__ void p2_smooth(float* x, const float* r, float h2, int sweeps) {
+__device__ void p2_smooth(float* x, const float* r, float h2, int sweeps, float w) {
   constexpr int HALF = N / 2, LH = ilog2<HALF>();
   const int tid = WARP ? (int)(threadIdx.x & 31) : (int)threadIdx.x;
   const int nthr = WARP ? 32 : (int)blockDim.x;
@@ -452,7 +454,7 @@ __device__ void p2_smooth(float* x, const float* r, float h2, int sweeps) {
       int row = j * N, k = row + i;
       int rm = ((j - 1) & (N - 1)) * N, rp = ((j + 1) & (N - 1)) * N;
       x[k] = gs_update(x[k], x[row + ((i - 1) & (N - 1))], x[row + ((i + 1) & (N - 1))], x[rm + i], x[rp + i], r[k],
-                       h2);
+                       h2, w);
     }
     p2_sync<N, WARP>();
   }
@@ -504,9 +506,9 @@ __device__ void p2_cycle(float* const* X, float* const* R, const BottomH2& H, in
                          int coarse) {
   constexpr bool W = N <= 16;
   if constexpr (N == 8) {
-    p2_smooth<8, true>(X[lvl], R[lvl], H.h2[lvl], coarse);
+    p2_smooth<8, true>(X[lvl], R[lvl], H.h2[lvl], coarse, H.w);
   } else {
-    p2_smooth<N, W>(X[lvl], R[lvl], H.h2[lvl], pre);
+    p2_smooth<N, W>(X[lvl], R[lvl], H.h2[lvl], pre, H.w);
     p2_restrict<N, W>(X[lvl], R[lvl], H.h2[lvl], R[lvl + 1], X[lvl + 1]);
     if constexpr (!W && N / 2 <= 16) {
       if (threadIdx.x < 32) p2_cycle<N / 2>(X, R, H, lvl + 1, pre, post, coarse);
@@ -515,7 +517,7 @@ __device__ void p2_cycle(float* const* X, float* const* R, const BottomH2& H, in
       p2_cycle<N / 2>(X, R, H, lvl + 1, pre, post, coarse);
     }
     p2_prolong<N, W>(X[lvl], X[lvl + 1]);
-    p2_smooth<N, W>(X[lvl], R[lvl], H.h2[lvl], post);
+    p2_smooth<N, W>(X[lvl], R[lvl], H.h2[lvl], post, H.w);
   }
 }
 
@@ -581,7 +583,7 @@ static void down_t(Solver* s, Level& L, const Level& C, bool has_x) {
   float* out = has_x ? L.x2 : L.x;
   FS_LAUNCH(s, "mg_down", bytes,
             k_mg_down<T, H><<<grid, kTileBlock, 0, s->stream>>>(L.rhs, has_x ? L.x : nullptr, out, C.rhs, L.n,
-                                                                L.h2, s->prm.mg_pre_smooth));
+                                                                L.h2, s->prm.mg_pre_smooth, (float)s->prm.relax));
   if (has_x) std::swap(L.x, L.x2);
 }
 
@@ -601,13 +603,15 @@ static void up_t(Solver* s, Level& L, const Level& C, float* acc_h, float* acc_l
     double bytes = (double)L.n * L.n * 24.0 + (double)C.n * C.n * 4.0;
     FS_LAUNCH(s, "mg_up_acc", bytes,
               k_mg_up<T, H, true><<<grid, kTileBlock, 0, s->stream>>>(L.rhs, L.x, nullptr, C.x, L.n, L.h2,
-                                                                      s->prm.mg_post_smooth, acc_h, acc_l));
+                                                                      s->prm.mg_post_smooth, acc_h, acc_l,
+                                                                      (float)s->prm.relax));
     return;
   }
   double bytes = (double)L.n * L.n * 12.0 + (double)C.n * C.n * 4.0;
   FS_LAUNCH(s, "mg_up", bytes,
             k_mg_up<T, H, false><<<grid, kTileBlock, 0, s->stream>>>(L.rhs, L.x, L.x2, C.x, L.n, L.h2,
-                                                                     s->prm.mg_post_smooth, nullptr, nullptr));
+                                                                     s->prm.mg_post_smooth, nullptr, nullptr,
+                                                                     (float)s->prm.relax));
   std::swap(L.x, L.x2);
 }
 
@@ -652,6 +656,7 @@ static size_t bottom_layout(const Solver* s, BottomLevels* B) {
   int lb = bottom_first_level(s);
   int nl = (int)s->lev.size();
   B->count = nl - lb;
+  B->w = (float)s->prm.relax;
   int off = 0;
   for (int k = 0; k < B->count; k++) {
     const Level& L = s->lev[lb + k];
@@ -690,6 +695,7 @@ void mg_vcycle_fused(Solver* s, bool first_has_x, float* acc_h, float* acc_l) {
   if (p2) {
     BottomH2 H{};
     for (int k = 0; k < (int)L.size() - lb && k < 4; k++) H.h2[k] = L[lb + k].h2;
+    H.w = (float)P.relax;
 #define FS_P2(N0)                                                                                               FS_LAUNCH(s, "mg_bottom", bytes,                                                                                        k_mg_bottom_p2<N0><<<1, 256, 0, s->stream>>>(L[lb].rhs, L[lb].x, hx ? 1 : 0, H, P.mg_pre_smooth,                                                           P.mg_post_smooth, P.mg_coarse_sweeps, bah, bal))
     switch (nb) {
       case 64: FS_P2(64); break;

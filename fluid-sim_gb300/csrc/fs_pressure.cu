@@ -72,26 +72,27 @@ void launch_subtract_gradient_f32(Solver* s, const float* wu, const float* wv, c
                                                                                 g.ny, g.idx, g.idy));
 }
 // ----------------------------------------------------------------- smoothers
-// damped Jacobi, omega = 1 (shaders.js:302-325)
+// damped Jacobi, relaxation factor w (shaders.js:302-325)
 __global__ void __launch_bounds__(256) k_jacobi(const float* __restrict__ p, const float* __restrict__ d,
-                                                float* __restrict__ o, int nx, int ny, float h2) {
+                                                float* __restrict__ o, int nx, int ny, float h2, float w) {
   int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y;
   if (i >= nx || j >= ny) return;
   int im = i == 0 ? nx - 1 : i - 1, ip = i + 1 == nx ? 0 : i + 1;
   int jm = j == 0 ? ny - 1 : j - 1, jp = j + 1 == ny ? 0 : j + 1;
   int64_t r = (int64_t)j * nx;
   o[r + i] = gs_update(__ldg(p + r + i), __ldg(p + r + im), __ldg(p + r + ip), __ldg(p + (int64_t)jm * nx + i),
-                       __ldg(p + (int64_t)jp * nx + i), __ldg(d + r + i), h2);
+                       __ldg(p + (int64_t)jp * nx + i), __ldg(d + r + i), h2, w);
 }
 
 void launch_jacobi(Solver* s, const float* p, const float* d, float* out, float h2, int nx, int ny) {
   FS_LAUNCH(s, "jacobi", (double)nx * ny * 12,
-            k_jacobi<<<grid2d(nx, ny, kBlock), kBlock, 0, s->stream>>>(p, d, out, nx, ny, h2));
+            k_jacobi<<<grid2d(nx, ny, kBlock), kBlock, 0, s->stream>>>(p, d, out, nx, ny, h2,
+                                                                        (float)s->prm.relax));
 }
 
-// one red-black colour (shaders.js:340-372, omega = 1); dst may equal src on even grids
+// one red-black colour (shaders.js:340-372, relaxation factor w); dst may equal src on even grids
 __global__ void __launch_bounds__(256) k_rb_half(const float* src, const float* __restrict__ d, float* dst,
-                                                 int nx, int ny, float h2, int colour) {
+                                                 int nx, int ny, float h2, int colour, float w) {
   int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y;
   if (i >= nx || j >= ny) return;
   int64_t r = (int64_t)j * nx;
@@ -103,13 +104,14 @@ __global__ void __launch_bounds__(256) k_rb_half(const float* src, const float* 
   int im = i == 0 ? nx - 1 : i - 1, ip = i + 1 == nx ? 0 : i + 1;
   int jm = j == 0 ? ny - 1 : j - 1, jp = j + 1 == ny ? 0 : j + 1;
   dst[r + i] = gs_update(cur, src[r + im], src[r + ip], src[(int64_t)jm * nx + i], src[(int64_t)jp * nx + i],
-                         __ldg(d + r + i), h2);
+                         __ldg(d + r + i), h2, w);
 }
 
 void launch_rb_half(Solver* s, const float* src, const float* d, float* dst, float h2, int colour,
                     int nx, int ny) {
   FS_LAUNCH(s, "rb_half", (double)nx * ny * (src == dst ? 6 : 12),
-            k_rb_half<<<grid2d(nx, ny, kBlock), kBlock, 0, s->stream>>>(src, d, dst, nx, ny, h2, colour));
+            k_rb_half<<<grid2d(nx, ny, kBlock), kBlock, 0, s->stream>>>(src, d, dst, nx, ny, h2, colour,
+                                                                         (float)s->prm.relax));
 }
 
 // ------------------------------------------------------- multigrid transfers

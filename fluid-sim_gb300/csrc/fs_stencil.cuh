@@ -17,10 +17,13 @@ __device__ __forceinline__ float sum4(float l, float r, float b, float t) {
   return __fadd_rn(__fadd_rn(__fadd_rn(l, r), b), t);
 }
 
-// Gauss-Seidel / Jacobi point update with omega = 1: cur + ((sum - h2 d)/4 - cur)
-__device__ __forceinline__ float gs_update(float cur, float l, float r, float b, float t, float d, float h2) {
+// Gauss-Seidel / Jacobi point update with relaxation factor w (param_a of
+// JACOBI / RED_BLACK_GS): cur + w ((sum - h2 d)/4 - cur).  w = 1 multiplies
+// exactly, so that case rounds like the plain update the reference runs.
+__device__ __forceinline__ float gs_update(float cur, float l, float r, float b, float t, float d, float h2,
+                                           float w) {
   float gs = __fmul_rn(__fmaf_rn(-h2, d, sum4(l, r, b, t)), 0.25f);
-  return __fadd_rn(cur, __fsub_rn(gs, cur));
+  return __fadd_rn(cur, __fmul_rn(w, __fsub_rn(gs, cur)));
 }
 
 // rhs - (l + r + b + t - 4c) / h2

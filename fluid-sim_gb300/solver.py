@@ -33,7 +33,7 @@ def make_params(n: int = 256, nx: int | None = None, ny: int | None = None, lx: 
                 precision: str = "f32", pressure_tol: float = 0.0, max_cycles: int = 50, mg_pre_smooth: int = 2,
                 mg_post_smooth: int = 2, mg_coarse_sweeps: int = 40, mg_min_size: int = 8,
                 warm_start: bool = False, device: int = 0, kernel_variant: int = 0, dye_fade: float = 0.0,
-                **camel) -> "L.Params":
+                relax: float = 1.0, **camel) -> "L.Params":
     """fs_params from the reference's option names (camelCase accepted);
     unknown names are rejected (the reference silently defaults)."""
     solid_mask_width = camel.pop("solidMaskWidth", solid_mask_width)
@@ -67,6 +67,7 @@ def make_params(n: int = 256, nx: int | None = None, ny: int | None = None, lx: 
     p.device = device
     p.kernel_variant = kernel_variant
     p.dye_fade = dye_fade
+    p.relax = relax
     return p
 
 
@@ -76,7 +77,9 @@ class GPUFluidSolver:
 
     Extra options: ``precision`` ("f32" | "mixed"), ``pressure_tol`` (> 0 runs
     cycles until max|div u| <= tol), ``max_cycles``, ``warm_start``, the
-    multigrid sweep counts and ``device`` (CUDA ordinal).
+    multigrid sweep counts, ``relax`` (the relaxation factor of every sweep,
+    param_a of the reference's smoother shaders; 1.0 as the reference) and
+    ``device`` (CUDA ordinal).
     """
 
     def __init__(self, n: int = 256, nx: int | None = None, ny: int | None = None, lx: float = 2 * math.pi,
@@ -86,13 +89,14 @@ class GPUFluidSolver:
                  pressure_tol: float = 0.0, max_cycles: int = 50, mg_pre_smooth: int = 2,
                  mg_post_smooth: int = 2, mg_coarse_sweeps: int = 40, mg_min_size: int = 8,
                  warm_start: bool = False, device: int = 0, kernel_variant: int = 0, dye_fade: float = 0.0,
-                 **camel):
+                 relax: float = 1.0, **camel):
         p = make_params(n=n, nx=nx, ny=ny, lx=lx, ly=ly, nu=nu, confinement=confinement, advection=advection,
                         solid_mask_width=solid_mask_width, pressure_solver=pressure_solver,
                         pressure_iterations=pressure_iterations, precision=precision, pressure_tol=pressure_tol,
                         max_cycles=max_cycles, mg_pre_smooth=mg_pre_smooth, mg_post_smooth=mg_post_smooth,
                         mg_coarse_sweeps=mg_coarse_sweeps, mg_min_size=mg_min_size, warm_start=warm_start,
-                        device=device, kernel_variant=kernel_variant, dye_fade=dye_fade, **camel)
+                        device=device, kernel_variant=kernel_variant, dye_fade=dye_fade, relax=relax,
+                        **camel)
         lib = L.load()
         h = C.c_void_p()
         L.check(lib.fs_create(C.byref(p), C.byref(h)), None)

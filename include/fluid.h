@@ -130,6 +130,12 @@ typedef struct fs_params {
   double dye_fade;            /* dyeFade (solver.js:67,82): dye *= 1 - dye_fade per step
                                  (default 0); dye advection runs once a dye field is
                                  uploaded (fs_upload_dye) */
+  double relax;               /* relaxation factor w of every Jacobi / red-black sweep,
+                                 including the multigrid smoothers: cur + w (gs - cur),
+                                 param_a of JACOBI / RED_BLACK_GS (shaders.js:322,368).
+                                 Default 1.0, the value the reference's callers pass
+                                 (solver.js:716,729, multigrid.js:261); w = 1 rounds
+                                 exactly like the plain update.  Must lie in (0, 2). */
 } fs_params;
 
 /* one forcing mode, as setForcing's {kx, ky, phase} (solver.js:370-385) */

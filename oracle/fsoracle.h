@@ -190,6 +190,7 @@ void fso_set_threads(int n);
                              double vy, double omega, double r);                            \
   void fsw_##SUF##_read_impulse(fsw_solver_##SUF* s, double* fx, double* fy, double* tq);  \
   void fsw_##SUF##_set_iterations(fsw_solver_##SUF* s, int iterations);                    \
+  void fsw_##SUF##_set_relax(fsw_solver_##SUF* s, double relax);                           \
   void fsw_##SUF##_step(fsw_solver_##SUF* s, double dt);                                   \
   void fsw_##SUF##_stage(fsw_solver_##SUF* s, int stage, double dt);                       \
   double fsw_##SUF##_poisson_residual_after(fsw_solver_##SUF* s, int iterations, double dt);\

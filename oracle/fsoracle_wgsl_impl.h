@@ -37,6 +37,7 @@ struct ST {
   int nx, ny;
   double dx, dy, nu, mask_width;
   int advection, solver, iterations;
+  double relax; /* param_a of every JACOBI / RED_BLACK_GS dispatch (1.0 as the reference) */
   REAL *u, *v, *un, *vn, *fu, *fv, *bu, *bv;
   REAL *p, *pn, *div;
   int n_modes;
@@ -352,6 +353,7 @@ ST* FN(create)(int nx, int ny, double lx, double ly, double nu, int advection, i
   int64_t n = (int64_t)nx * ny;
   s->nx = nx; s->ny = ny; s->dx = lx / nx; s->dy = ly / ny; s->nu = nu;
   s->advection = advection; s->solver = pressure_solver; s->iterations = iterations;
+  s->relax = 1.0;
   s->mask_width = solid_mask_width;
   s->u = ALLOC(n); s->v = ALLOC(n); s->un = ALLOC(n); s->vn = ALLOC(n);
   s->fu = ALLOC(n); s->fv = ALLOC(n); s->bu = ALLOC(n); s->bv = ALLOC(n);
@@ -410,6 +412,9 @@ void FN(read_impulse)(ST* s, double* fx, double* fy, double* tq) {
   for (int64_t i = 0; i < n; i++) { fx[i] = s->imp_x[i]; fy[i] = s->imp_y[i]; tq[i] = s->imp_t[i]; }
 }
 void FN(set_iterations)(ST* s, int iterations) { s->iterations = iterations; }
+/* the relaxation factor the reference's callers fix at 1.0 (solver.js:716,729,
+   multigrid.js:261), applied to every sweep including the coarsest level's */
+void FN(set_relax)(ST* s, double relax) { s->relax = relax; }
 
 /* setForcing, solver.js:370-385 */
 void FN(set_forcing)(ST* s, const double* modes, int m, double amp, double drag, double drift) {
@@ -477,10 +482,10 @@ static void K(do_divergence)(ST* s, double dt) {
 }
 
 /* Multigrid._smooth, multigrid.js:256-270 */
-static void K(mg_smooth)(LEV* lv, const REAL* rhs, int sweeps) {
+static void K(mg_smooth)(LEV* lv, const REAL* rhs, int sweeps, double relax) {
   for (int k = 0; k < sweeps; k++)
     for (int colour = 0; colour < 2; colour++) {
-      PRM P = K(level_params)(lv, 1.0, colour);
+      PRM P = K(level_params)(lv, relax, colour);
       K(red_black)(&P, lv->x[lv->xi], rhs, lv->x[1 - lv->xi]);
       lv->xi = 1 - lv->xi;
     }
@@ -494,7 +499,7 @@ static void K(vcycle)(ST* s, REAL* rhs) {
   for (int i = 0; i < nl - 1; i++) {
     LEV* lv = &L[i];
     LEV* nx = &L[i + 1];
-    K(mg_smooth)(lv, lv->rhs, 2);
+    K(mg_smooth)(lv, lv->rhs, 2, s->relax);
     PRM P = K(level_params)(lv, 0, 0);
     K(residual)(&P, lv->x[lv->xi], lv->rhs, lv->res);
     PRM Pc = K(level_params)(nx, 0, 0);
@@ -503,14 +508,14 @@ static void K(vcycle)(ST* s, REAL* rhs) {
     memset(nx->x[1 - nx->xi], 0, sizeof(REAL) * (size_t)nx->n * nx->n);
   }
   LEV* last = &L[nl - 1];
-  K(mg_smooth)(last, last->rhs, 40);
+  K(mg_smooth)(last, last->rhs, 40, s->relax);
   for (int i = nl - 2; i >= 0; i--) {
     LEV* lv = &L[i];
     LEV* below = &L[i + 1];
     PRM P = K(level_params)(lv, 0, 0);
     K(prolong)(&P, below->x[below->xi], lv->x[lv->xi], lv->x[1 - lv->xi]);
     lv->xi = 1 - lv->xi;
-    K(mg_smooth)(lv, lv->rhs, 2);
+    K(mg_smooth)(lv, lv->rhs, 2, s->relax);
   }
   L[0].rhs = NULL;
 }
@@ -529,14 +534,14 @@ static void K(do_poisson)(ST* s, double dt, int iterations) {
   if (s->solver == FSW_RED_BLACK) {
     for (int k = 0; k < iterations; k++)
       for (int colour = 0; colour < 2; colour++) {
-        PRM P = K(params)(s, dt, 1.0, colour);
+        PRM P = K(params)(s, dt, s->relax, colour);
         K(red_black)(&P, s->p, s->div, s->pn);
         K(swappres)(s);
       }
     return;
   }
   for (int k = 0; k < iterations; k++) {
-    PRM P = K(params)(s, dt, 1.0, 0);
+    PRM P = K(params)(s, dt, s->relax, 0);
     K(jacobi)(&P, s->p, s->div, s->pn);
     K(swappres)(s);
   }

@@ -145,6 +145,7 @@ def lib():
                 f"fsw_{suf}_set_forcing": (None, [VP, DP, I, D, D, D]),
                 f"fsw_{suf}_set_solid": (None, [VP, I, D, D, D, D, D, D]),
                 f"fsw_{suf}_set_iterations": (None, [VP, I]),
+                f"fsw_{suf}_set_relax": (None, [VP, D]),
                 f"fsw_{suf}_step": (None, [VP, D]),
                 f"fsw_{suf}_stage": (None, [VP, I, D]),
                 f"fsw_{suf}_poisson_residual_after": (D, [VP, I, D]),
@@ -508,6 +509,10 @@ class RefGpuSolver:
 
     def set_iterations(self, it):
         self._f("set_iterations")(self._h, it)
+
+    def set_relax(self, relax):
+        """param_a of every Jacobi / red-black sweep (the reference passes 1.0)"""
+        self._f("set_relax")(self._h, relax)
 
     def set_forcing(self, modes, amplitude=1.0, drag=0.0, phase_drift=0.3):
         flat = np.ascontiguousarray(np.asarray(modes, dtype=np.float64).reshape(-1))

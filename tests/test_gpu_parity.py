@@ -194,6 +194,59 @@ def test_f32_solver_matches_same_iteration_in_f64(G, O, solver, iters, n):
     assert max(O.rel_l2(u, ru), O.rel_l2(v, rv)) < 1e-5
 
 
+@pytest.mark.parametrize("solver,iters,relax", [("jacobi", 60, 0.8), ("red-black", 30, 1.5), ("multigrid", 3, 1.2)])
+@pytest.mark.parametrize("n", [64, 72])
+def test_relaxed_sweeps_match_same_iteration_in_f64(G, O, solver, iters, relax, n):
+    """The relaxation factor (param_a of JACOBI / RED_BLACK_GS, 1.0 in the
+    reference's calls) applied to every sweep, multigrid smoothers and
+    coarsest level included, against the f64 restatement with the same
+    factor: 3 SL steps as above."""
+    dt = 0.01
+    g = O.grid(n)
+    u0, v0 = O.tg_init(g)
+    nu_u, nu_v = O.lcg_uv(4711, n * n)
+    u0 += 0.1 * nu_u
+    v0 += 0.1 * nu_v
+    ref = O.RefGpuSolver(n=n, nu=1e-3, advection="semi-lagrangian", pressure_solver=solver,
+                         pressure_iterations=iters, precision="f64")
+    ref.set_relax(relax)
+    ref.upload_velocity(u0, v0)
+    s = G.GPUFluidSolver(n=n, nu=1e-3, advection="semi-lagrangian", pressure_solver=solver,
+                         pressure_iterations=iters, relax=relax)
+    s.upload_velocity(u0, v0)
+    for _ in range(3):
+        ref.step(dt)
+        s.step(dt)
+    ru, rv = ref.read_velocity()
+    u, v = s.read_velocity()
+    assert max(O.rel_l2(u, ru), O.rel_l2(v, rv)) < 1e-5
+
+
+def test_over_relaxed_multigrid_meets_tolerance_in_fewer_cycles(G, O):
+    """Mixed-precision V-cycles to max|div u| <= 1e-6 on a 512^2 random field:
+    relax = 1.2 needs fewer cycles than the reference's 1.0 and still meets
+    the tolerance (the result is checked by fs_max_divergence in f64)."""
+    n = 512
+    u0, v0 = O.lcg_uv(99, n * n)
+    cyc = {}
+    for relax in (1.0, 1.2):
+        s = G.GPUFluidSolver(n=n, nu=1e-4, advection="maccormack", pressure_solver="multigrid",
+                             pressure_iterations=1, precision="mixed", pressure_tol=1e-6, max_cycles=40,
+                             relax=relax)
+        s.upload_velocity(u0, v0)
+        s.step(0.002)
+        st = s.last_stats()
+        assert st["converged"] and s.max_divergence() <= 1e-6
+        cyc[relax] = st["cycles"]
+    assert cyc[1.2] < cyc[1.0], cyc
+
+
+@pytest.mark.parametrize("relax", [0.0, 2.0, -1.0, float("nan")])
+def test_relax_out_of_range_is_rejected(G, O, relax):
+    with pytest.raises(G.FluidError):
+        G.GPUFluidSolver(n=32, pressure_solver="multigrid", relax=relax)
+
+
 @pytest.mark.parametrize("solver", ["jacobi", "red-black"])
 def test_odd_and_nonsquare_grids(G, O, solver):
     """Flat smoothers on 33 x 33 and 40 x 24 grids against the f64 restatement."""
@@ -365,19 +418,21 @@ def test_bitwise_repeatable(G, O):
 
 # ---------------------------------------------------- fused multigrid cycle
 @pytest.mark.parametrize("precision", ["f32", "mixed"])
-@pytest.mark.parametrize("n", [64, 200, 256, 320, 1056])
-def test_fused_vcycle_bitwise_equals_one_pass_kernels(G, O, precision, n):
+@pytest.mark.parametrize("n,relax", [(64, 1.0), (200, 1.0), (256, 1.0), (320, 1.0), (1056, 1.0), (64, 1.2),
+                                     (200, 1.2), (256, 1.2)])
+def test_fused_vcycle_bitwise_equals_one_pass_kernels(G, O, precision, n, relax):
     """The fused V-cycle (tile kernels + one-CTA bottom solve) evaluates the same
     expressions in the same order as the one-kernel-per-pass path, so the two
-    agree bit for bit.  n = 64 runs entirely in the power-of-two bottom kernel
-    (with a non-zero initial x on V-cycles 2 and 3 in F32); n = 200 has partial
-    16-cell tiles and a 50 -> 25 generic bottom with an odd coarsest level;
-    n = 1056 has partial 64-, 32- and 16-cell tiles and an odd 33 bottom."""
+    agree bit for bit, over-relaxed sweeps included.  n = 64 runs entirely in
+    the power-of-two bottom kernel (with a non-zero initial x on V-cycles 2
+    and 3 in F32); n = 200 has partial 16-cell tiles and a 50 -> 25 generic
+    bottom with an odd coarsest level; n = 1056 has partial 64-, 32- and
+    16-cell tiles and an odd 33 bottom."""
     u0, v0 = O.lcg_uv(4242, n * n)
     out = []
     for variant in (0, 1):
         s = G.GPUFluidSolver(n=n, nu=1e-3, advection="maccormack", pressure_solver="multigrid",
-                             pressure_iterations=3, precision=precision, kernel_variant=variant)
+                             pressure_iterations=3, precision=precision, kernel_variant=variant, relax=relax)
         s.upload_velocity(u0, v0)
         s.advance(0.01, 2)
         u, v = s.read_velocity()

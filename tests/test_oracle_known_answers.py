@@ -268,3 +268,20 @@ def test_lcg_matches_reference_fixture(O):
         s = int(math.fmod(t, 4294967296.0)) & 0x7FFFFFFF
         exp.append(s / 0x7FFFFFFF - 0.5)
     assert list(x) == exp
+
+
+def test_relaxation_factor_in_reference_gpu_restatement(O):
+    """param_a of RED_BLACK_GS (shaders.js:368): 1.0 set explicitly gives the
+    reference's curve bit for bit; 1.2 on every multigrid sweep lowers the
+    residual after the same V-cycles (64^2, seed 777)."""
+    n = 64
+    u0, v0 = O.lcg_uv(777, n * n)
+    res = {}
+    for relax in (None, 1.0, 1.2):
+        r = O.RefGpuSolver(n=n, nu=0.0, pressure_solver="multigrid", precision="f64")
+        if relax is not None:
+            r.set_relax(relax)
+        r.upload_velocity(u0, v0)
+        res[relax] = [r.poisson_residual_after(k) for k in (1, 2, 3)]
+    assert res[None] == res[1.0]
+    assert all(a < b for a, b in zip(res[1.2], res[1.0]))
