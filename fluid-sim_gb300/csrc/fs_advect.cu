@@ -89,49 +89,62 @@ __device__ __forceinline__ void trace(const TV* __restrict__ u, const TV* __rest
 // ------------------------------------------------------ tiled advection
 // The advection kernels are gather-bound: a MacCormack step takes about 20
 // bilinear samples per cell.  A CTA stages its 32x16-cell tile of each field
-// it samples, plus a halo of 3 cells, in shared memory; every sample whose
-// four cells lie in the staged block is read from there with 32-bit tile
-// addressing, anything else (a trace longer than the halo, i.e. a CFL number
-// above ~1.5) falls back to the wrapped global read.  The arithmetic is the
-// same as the global sampler, so the results are too.
-constexpr int kTX = 32, kTY = 16, kHalo = 3;
+// it samples, plus a halo of 4 cells, in shared memory.  When the largest
+// displacement any trace of the tile can reach is at most 3 cells (checked
+// once per CTA on the staged velocities, below) every sample lies in the
+// staged block and is read from there unchecked; otherwise each sample is
+// checked and one whose four cells leave the block falls back to the wrapped
+// global read.  The arithmetic of the three ways is the same, so the results
+// are too.
+constexpr int kTX = 32, kTY = 16, kHalo = 4;
 constexpr int kSW = kTX + 2 * kHalo, kSH = kTY + 2 * kHalo;
+// largest |u| dt/dx (cells) for which every trace stays in the staged block:
+// a sample at home + (h + d), |h| <= 1/2, reads cells floor(h + d) .. +1,
+// inside [-kHalo, kTX - 1 + kHalo] while |d| < kHalo - 1/2; the midpoint of
+// the RK2 trace moves half as far and interpolates staged values only, so
+// its velocity is bounded by the staged maximum too.
+constexpr float kFastDisp = 3.0f;
 
+template <bool FAST>
 struct TileView {
   const float* sm;  // kSH x kSW staged block
   int oi, oj;       // global (unwrapped) index of the block's element (0, 0)
   const float* g;
   int nx, ny;
 
-  __device__ __forceinline__ float sample(int bi, int bj, float ox, float oy) const {
+  // bilinear sample at (bi + ox, bj + oy); with lo/hi also the range of the
+  // four cells it read (src/cpu/advect.js:104-111)
+  template <bool RANGE = false>
+  __device__ __forceinline__ float sample(int bi, int bj, float ox, float oy, float* lo = nullptr,
+                                          float* hi = nullptr) const {
     const float fo = floorf(ox), go = floorf(oy);
     const float fx = ox - fo, fy = oy - go;
     const int li = bi + (int)fo - oi, lj = bj + (int)go - oj;
-    if ((unsigned)li < (unsigned)(kSW - 1) && (unsigned)lj < (unsigned)(kSH - 1)) {
+    float a, b, c, d;
+    if (FAST || ((unsigned)li < (unsigned)(kSW - 1) && (unsigned)lj < (unsigned)(kSH - 1))) {
       const float* p = sm + lj * kSW + li;
-      const float a = p[0], b = p[1], c = p[kSW], d = p[kSW + 1];
-      const float top = a + (b - a) * fx;
-      const float bot = c + (d - c) * fx;
-      return top + (bot - top) * fy;
+      a = p[0]; b = p[1]; c = p[kSW]; d = p[kSW + 1];
+    } else {
+      const int i0 = wrap_idx(bi + (int)fo, nx), j0 = wrap_idx(bj + (int)go, ny);
+      const int i1 = i0 + 1 == nx ? 0 : i0 + 1;
+      const int j1 = j0 + 1 == ny ? 0 : j0 + 1;
+      const int64_t r0 = (int64_t)j0 * nx, r1 = (int64_t)j1 * nx;
+      a = __ldg(g + r0 + i0); b = __ldg(g + r0 + i1); c = __ldg(g + r1 + i0); d = __ldg(g + r1 + i1);
     }
-    return bilerp(g, nx, ny, bi, bj, ox, oy);
-  }
-  __device__ __forceinline__ void range4(int bi, int bj, float ox, float oy, float& lo, float& hi) const {
-    const int li = bi + (int)floorf(ox) - oi, lj = bj + (int)floorf(oy) - oj;
-    if ((unsigned)li < (unsigned)(kSW - 1) && (unsigned)lj < (unsigned)(kSH - 1)) {
-      const float* p = sm + lj * kSW + li;
-      const float a = p[0], b = p[1], c = p[kSW], d = p[kSW + 1];
-      lo = fminf(fminf(a, b), fminf(c, d));
-      hi = fmaxf(fmaxf(a, b), fmaxf(c, d));
-      return;
+    if (RANGE) {
+      *lo = fminf(fminf(a, b), fminf(c, d));
+      *hi = fmaxf(fmaxf(a, b), fmaxf(c, d));
     }
-    bounds4(g, nx, ny, bi, bj, ox, oy, lo, hi);
+    const float top = a + (b - a) * fx;
+    const float bot = c + (d - c) * fx;
+    return top + (bot - top) * fy;
   }
 };
 
 // RK2 midpoint backward trace (src/cpu/advect.js:46-54, shaders.js:117-122) in cells
-__device__ __forceinline__ void trace_t(const TileView& u, const TileView& v, int i, int j, Home h, float cx,
-                                        float cy, float& dX, float& dY) {
+template <bool FAST>
+__device__ __forceinline__ void trace_t(const TileView<FAST>& u, const TileView<FAST>& v, int i, int j, Home h,
+                                        float cx, float cy, float& dX, float& dY) {
   const float u1 = u.sample(i, j, h.ux, h.uy);
   const float v1 = v.sample(i, j, h.vx, h.vy);
   const float mx = -0.5f * cx * u1, my = -0.5f * cy * v1;
@@ -141,13 +154,38 @@ __device__ __forceinline__ void trace_t(const TileView& u, const TileView& v, in
   dY = -cy * v2;
 }
 
-// stage the kSH x kSW block of f whose (0, 0) is global (oi, oj), wrapped
-__device__ __forceinline__ void stage_tile(float* sm, const float* __restrict__ f, int oi, int oj, int nx, int ny) {
-  const int tid = threadIdx.y * blockDim.x + threadIdx.x, nthr = blockDim.x * blockDim.y;
-  for (int k = tid; k < kSW * kSH; k += nthr) {
-    const int lj = k / kSW, li = k - lj * kSW;
-    sm[k] = __ldg(f + (int64_t)wrap_idx(oj + lj, ny) * nx + wrap_idx(oi + li, nx));
+// Stage the kSH x kSW blocks of F fields whose (0, 0) is global (oi, oj),
+// wrapped, one row per warp at a time; returns max |value| of the first two
+// fields (the velocities), NaN counted as infinite.
+template <int F>
+__device__ __forceinline__ void stage_tiles(float* const (&sm)[F], const float* const (&f)[F], int oi, int oj,
+                                            int nx, int ny, float& umax, float& vmax) {
+  const int lane = threadIdx.x, warp = threadIdx.y, nwarp = blockDim.y;
+  const bool interior = oi >= 0 && oj >= 0 && oi + kSW <= nx && oj + kSH <= ny;
+  uint32_t mu = 0, mv = 0;  // bit patterns of non-negative floats order like the floats
+  for (int lj = warp; lj < kSH; lj += nwarp) {
+    const int gj = interior ? oj + lj : wrap_idx(oj + lj, ny);
+    const int64_t row = (int64_t)gj * nx;
+    for (int li = lane; li < kSW; li += 32) {
+      const int gi = interior ? oi + li : wrap_idx(oi + li, nx);
+      const int k = lj * kSW + li;
+#pragma unroll
+      for (int q = 0; q < F; q++) {
+        const float x = __ldg(f[q] + row + gi);
+        sm[q][k] = x;
+        if (q == 0) mu = max(mu, __float_as_uint(fabsf(x)));
+        if (q == 1) mv = max(mv, __float_as_uint(fabsf(x)));
+      }
+    }
   }
+  umax = __uint_as_float(mu);
+  vmax = __uint_as_float(mv);
+}
+
+// one CTA-wide decision after staging (and the barrier the staging needs)
+__device__ __forceinline__ bool fast_tile(float umax, float vmax, float cx, float cy) {
+  const bool ok = umax * fabsf(cx) <= kFastDisp && vmax * fabsf(cy) <= kFastDisp;  // false for NaN / inf
+  return __syncthreads_and(ok) != 0;
 }
 
 // ADVECT_VELOCITY: each component traced from its own face (shaders.js:126-146).
@@ -155,16 +193,10 @@ __device__ __forceinline__ void stage_tile(float* sm, const float* __restrict__ 
 // the four cells each sample read -- the limiter's range, src/cpu/advect.js
 // :104-111 -- are written too, planes (lo_u, hi_u, lo_v, hi_v), so the combine
 // pass does not trace forward again.
-__global__ void __launch_bounds__(256) k_advect_sl_t(const float* __restrict__ u, const float* __restrict__ v,
-                                                     float* __restrict__ ou, float* __restrict__ ov, int nx, int ny,
-                                                     float cx, float cy, float* __restrict__ bounds) {
-  __shared__ float su[kSW * kSH], sv[kSW * kSH];
-  const int ti = blockIdx.x * kTX, tj = blockIdx.y * kTY;
-  const int oi = ti - kHalo, oj = tj - kHalo;
-  stage_tile(su, u, oi, oj, nx, ny);
-  stage_tile(sv, v, oi, oj, nx, ny);
-  __syncthreads();
-  const TileView U{su, oi, oj, u, nx, ny}, V{sv, oi, oj, v, nx, ny};
+template <bool FAST>
+__device__ __forceinline__ void advect_rows(const TileView<FAST>& U, const TileView<FAST>& V, float* __restrict__ ou,
+                                            float* __restrict__ ov, int nx, int ny, int ti, int tj, float cx,
+                                            float cy, float* __restrict__ bounds) {
   const Home hu = home_u(), hv = home_v();
   const int i = ti + threadIdx.x;
   if (i >= nx) return;
@@ -175,39 +207,54 @@ __global__ void __launch_bounds__(256) k_advect_sl_t(const float* __restrict__ u
     const int64_t c = (int64_t)j * nx + i;
     float dX, dY, lo, hi;
     trace_t(U, V, i, j, hu, cx, cy, dX, dY);
-    ou[c] = U.sample(i, j, hu.ux + dX, hu.uy + dY);
     if (bounds) {
-      U.range4(i, j, hu.ux + dX, hu.uy + dY, lo, hi);
+      ou[c] = U.template sample<true>(i, j, hu.ux + dX, hu.uy + dY, &lo, &hi);
       bounds[c] = lo;
       bounds[n + c] = hi;
+    } else {
+      ou[c] = U.sample(i, j, hu.ux + dX, hu.uy + dY);
     }
     trace_t(U, V, i, j, hv, cx, cy, dX, dY);
-    ov[c] = V.sample(i, j, hv.vx + dX, hv.vy + dY);
     if (bounds) {
-      V.range4(i, j, hv.vx + dX, hv.vy + dY, lo, hi);
+      ov[c] = V.template sample<true>(i, j, hv.vx + dX, hv.vy + dY, &lo, &hi);
       bounds[2 * n + c] = lo;
       bounds[3 * n + c] = hi;
+    } else {
+      ov[c] = V.sample(i, j, hv.vx + dX, hv.vy + dY);
     }
+  }
+}
+
+__global__ void __launch_bounds__(256) k_advect_sl_t(const float* __restrict__ u, const float* __restrict__ v,
+                                                     float* __restrict__ ou, float* __restrict__ ov, int nx, int ny,
+                                                     float cx, float cy, float* __restrict__ bounds) {
+  __shared__ float su[kSW * kSH], sv[kSW * kSH];
+  const int ti = blockIdx.x * kTX, tj = blockIdx.y * kTY;
+  const int oi = ti - kHalo, oj = tj - kHalo;
+  float umax, vmax;
+  {
+    float* const sm[2] = {su, sv};
+    const float* const f[2] = {u, v};
+    stage_tiles<2>(sm, f, oi, oj, nx, ny, umax, vmax);
+  }
+  if (fast_tile(umax, vmax, cx, cy)) {
+    const TileView<true> U{su, oi, oj, u, nx, ny}, V{sv, oi, oj, v, nx, ny};
+    advect_rows(U, V, ou, ov, nx, ny, ti, tj, cx, cy, bounds);
+  } else {
+    const TileView<false> U{su, oi, oj, u, nx, ny}, V{sv, oi, oj, v, nx, ny};
+    advect_rows(U, V, ou, ov, nx, ny, ti, tj, cx, cy, bounds);
   }
 }
 
 // MACCORMACK: the backward pass (ADVECT_FIELD_BY with -dt) is evaluated inside
 // the combine kernel at the single point it is needed, then the correction
 // limited to the forward pass's range (shaders.js:187-231, src/cpu/advect.js:149-185).
-__global__ void __launch_bounds__(256) k_mc_combine_t(const float* __restrict__ u, const float* __restrict__ v,
-                                                      const float* __restrict__ fu, const float* __restrict__ fv,
-                                                      const float* __restrict__ bounds, float* __restrict__ ou,
-                                                      float* __restrict__ ov, int nx, int ny, float cx, float cy) {
-  __shared__ float su[kSW * kSH], sv[kSW * kSH], sfu[kSW * kSH], sfv[kSW * kSH];
-  const int ti = blockIdx.x * kTX, tj = blockIdx.y * kTY;
-  const int oi = ti - kHalo, oj = tj - kHalo;
-  stage_tile(su, u, oi, oj, nx, ny);
-  stage_tile(sv, v, oi, oj, nx, ny);
-  stage_tile(sfu, fu, oi, oj, nx, ny);
-  stage_tile(sfv, fv, oi, oj, nx, ny);
-  __syncthreads();
-  const TileView U{su, oi, oj, u, nx, ny}, V{sv, oi, oj, v, nx, ny};
-  const TileView FU{sfu, oi, oj, fu, nx, ny}, FV{sfv, oi, oj, fv, nx, ny};
+template <bool FAST>
+__device__ __forceinline__ void combine_rows(const TileView<FAST>& U, const TileView<FAST>& V,
+                                             const TileView<FAST>& FU, const TileView<FAST>& FV,
+                                             const float* __restrict__ bounds, float* __restrict__ ou,
+                                             float* __restrict__ ov, int nx, int ny, int ti, int tj, float cx,
+                                             float cy) {
   const Home hu = home_u(), hv = home_v();
   const int i = ti + threadIdx.x;
   if (i >= nx) return;
@@ -217,22 +264,45 @@ __global__ void __launch_bounds__(256) k_mc_combine_t(const float* __restrict__ 
     if (j >= ny) break;
     const int64_t c = (int64_t)j * nx + i;
     const int lc = (r + kHalo) * kSW + threadIdx.x + kHalo;  // this cell in the staged block
+    const float lou = __ldg(bounds + c), hiu = __ldg(bounds + n + c);
+    const float lov = __ldg(bounds + 2 * n + c), hiv = __ldg(bounds + 3 * n + c);
     float dX, dY;
     // u component
     trace_t(U, V, i, j, hu, -cx, -cy, dX, dY);  // backward: trace with -dt
     const float bu = FU.sample(i, j, hu.ux + dX, hu.uy + dY);
-    float cu = sfu[lc] + 0.5f * (su[lc] - bu);
-    float lo = __ldg(bounds + c), hi = __ldg(bounds + n + c);
-    cu = cu < lo ? lo : cu > hi ? hi : cu;
+    float cu = FU.sm[lc] + 0.5f * (U.sm[lc] - bu);
+    cu = cu < lou ? lou : cu > hiu ? hiu : cu;
     // v component
     trace_t(U, V, i, j, hv, -cx, -cy, dX, dY);
     const float bv = FV.sample(i, j, hv.vx + dX, hv.vy + dY);
-    float cv = sfv[lc] + 0.5f * (sv[lc] - bv);
-    lo = __ldg(bounds + 2 * n + c);
-    hi = __ldg(bounds + 3 * n + c);
-    cv = cv < lo ? lo : cv > hi ? hi : cv;
+    float cv = FV.sm[lc] + 0.5f * (V.sm[lc] - bv);
+    cv = cv < lov ? lov : cv > hiv ? hiv : cv;
     ou[c] = cu;
     ov[c] = cv;
+  }
+}
+
+__global__ void __launch_bounds__(256) k_mc_combine_t(const float* __restrict__ u, const float* __restrict__ v,
+                                                      const float* __restrict__ fu, const float* __restrict__ fv,
+                                                      const float* __restrict__ bounds, float* __restrict__ ou,
+                                                      float* __restrict__ ov, int nx, int ny, float cx, float cy) {
+  __shared__ float su[kSW * kSH], sv[kSW * kSH], sfu[kSW * kSH], sfv[kSW * kSH];
+  const int ti = blockIdx.x * kTX, tj = blockIdx.y * kTY;
+  const int oi = ti - kHalo, oj = tj - kHalo;
+  float umax, vmax;
+  {
+    float* const sm[4] = {su, sv, sfu, sfv};
+    const float* const f[4] = {u, v, fu, fv};
+    stage_tiles<4>(sm, f, oi, oj, nx, ny, umax, vmax);
+  }
+  if (fast_tile(umax, vmax, cx, cy)) {
+    const TileView<true> U{su, oi, oj, u, nx, ny}, V{sv, oi, oj, v, nx, ny};
+    const TileView<true> FU{sfu, oi, oj, fu, nx, ny}, FV{sfv, oi, oj, fv, nx, ny};
+    combine_rows(U, V, FU, FV, bounds, ou, ov, nx, ny, ti, tj, cx, cy);
+  } else {
+    const TileView<false> U{su, oi, oj, u, nx, ny}, V{sv, oi, oj, v, nx, ny};
+    const TileView<false> FU{sfu, oi, oj, fu, nx, ny}, FV{sfv, oi, oj, fv, nx, ny};
+    combine_rows(U, V, FU, FV, bounds, ou, ov, nx, ny, ti, tj, cx, cy);
   }
 }
 

@@ -50,15 +50,39 @@ def test_advection_stage_matches_oracle(G, O, scheme):
 
 
 @pytest.mark.parametrize("precision", ["f32", "mixed"])
-def test_advection_random_field_large_cfl(G, O, precision):
-    """A random field (seed 4242) at CFL ~ 3: traces leave the home cell by
-    several cells and wrap across the periodic edges."""
-    n, dt = 48, 0.5
+@pytest.mark.parametrize("dt", [0.5, 1.5])
+def test_advection_random_field_large_cfl(G, O, precision, dt):
+    """A random field (seed 4242) at CFL ~ 2 and ~ 6: traces leave the home
+    cell by several cells and wrap across the periodic edges; at CFL ~ 6 they
+    also leave the staged tile and its halo (the checked sampling path)."""
+    n = 48
     g = O.grid(n)
     u0, v0 = O.lcg_uv(4242, n * n)
     for scheme in ("semi-lagrangian", "maccormack"):
         cu, cv = O.advect_velocity(g, u0, v0, dt, scheme)
         s = G.GPUFluidSolver(n=n, advection=scheme, pressure_iterations=0, precision=precision)
+        s.upload_velocity(u0, v0)
+        s.run_stage("advect", dt)
+        u, v = s.read_velocity()
+        assert max(O.rel_l2(u, cu), O.rel_l2(v, cv)) < 2e-6, scheme
+
+
+def test_advection_mixed_fast_and_checked_tiles(G, O):
+    """A slow field with one fast spot on a 96 x 80 grid: the tiles whose
+    staged block holds the spot sample with per-sample checks and global
+    fallback, the rest unchecked; both match the f64 scheme."""
+    nx, ny, dt = 96, 80, 0.05
+    g = O.grid(nx, ny)
+    u0, v0 = O.lcg_uv(77, nx * ny)
+    u0 *= 0.2
+    v0 *= 0.2
+    j, i = np.divmod(np.arange(nx * ny), nx)
+    spot = (np.abs(i - 60) < 4) & (np.abs(j - 30) < 4)
+    u0[spot] *= 150.0
+    v0[spot] *= 150.0
+    for scheme in ("semi-lagrangian", "maccormack"):
+        cu, cv = O.advect_velocity(g, u0, v0, dt, scheme)
+        s = G.GPUFluidSolver(nx=nx, ny=ny, advection=scheme, pressure_iterations=0)
         s.upload_velocity(u0, v0)
         s.run_stage("advect", dt)
         u, v = s.read_velocity()
