@@ -22,6 +22,7 @@
 // Shared-memory layout: each tile row is split into its even and odd columns
 // so that the lanes of a warp, which update cells of one colour in one row
 // (stride 2 in the row), hit consecutive words.
+#include <atomic>
 #include <utility>
 
 #include "fs_df.cuh"
@@ -40,6 +41,19 @@ __device__ __forceinline__ int wrap_n(int i, int n) {
 }
 
 constexpr int kTileThreads = 256;  // threads of a tile kernel (32 x 8)
+
+// 4-byte asynchronous global -> shared copies (no register round trip, all of
+// a thread's copies in flight at once); wait_all before the barrier that
+// publishes them.
+__device__ __forceinline__ void cp_async4(float* sdst, const float* gsrc) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"((uint32_t)__cvta_generic_to_shared(sdst)),
+               "l"((size_t)__cvta_generic_to_global(gsrc))
+               : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
+__device__ __forceinline__ void prefetch_l2(const void* p) {
+  asm volatile("prefetch.global.L2 [%0];" ::"l"((size_t)__cvta_generic_to_global(p)));
+}
 
 // i in (-n, 2n): one correction wraps it (halo offsets are far below n)
 __device__ __forceinline__ int wrap1(int i, int n) { return i < 0 ? i + n : (i >= n ? i - n : i); }
@@ -119,9 +133,11 @@ __global__ void __launch_bounds__(256) k_mg_down(const float* __restrict__ rhs, 
     int lj = k / R, li = k - lj * R;
     int64_t g = (int64_t)wrap1(gj0 + lj, n) * n + wrap1(gi0 + li, n);
     int q = CK::at(li, lj, par0);
-    rs[q] = __ldg(rhs + g);
-    xs[q] = xin ? __ldg(xin + g) : 0.f;
+    cp_async4(&rs[q], rhs + g);
+    if (xin) cp_async4(&xs[q], xin + g);
+    else xs[q] = 0.f;
   }
+  cp_async_wait_all();
   __syncthreads();
   for (int s = 0; s < 2 * pre; s++) {
     rb_half_smem<R>(xs, rs, s & 1, par0, h2, w);
@@ -172,49 +188,55 @@ __global__ void __launch_bounds__(256) k_mg_up(const float* __restrict__ rhs, co
                                                float* __restrict__ pl, float w) {
   constexpr int R = T + 2 * H;
   using CK = Checker<R>;
-  __shared__ float xs[CK::STRIDE + CK::N];
-  __shared__ float rs[CK::STRIDE + CK::N];
+  static_assert(T % 2 == 0 && H % 2 == 0, "the up kernel's region starts on an even index");
+  extern __shared__ float up_smem[];  // xs, rs (checkerboard), cs (coarse block)
+  float* const xs = up_smem;
+  float* const rs = up_smem + (CK::STRIDE + CK::N);
+  float* const cs = up_smem + 2 * (CK::STRIDE + CK::N);
   const int i0 = blockIdx.x * T, j0 = blockIdx.y * T;
   const int gi0 = i0 - H, gj0 = j0 - H;
   const int par0 = (gi0 + gj0) & 1;
   const int tid = threadIdx.y * blockDim.x + threadIdx.x, nthr = blockDim.x * blockDim.y;
   const int nc = n >> 1;
-  // staging: two cells' loads (fine x, rhs, four coarse values each) in flight
-  // per thread before the prolongation arithmetic and the stores
-  constexpr int U = 2;
-  for (int k0 = tid; k0 < R * R; k0 += U * nthr) {
-    float vx[U], vr[U], c00[U], c10[U], c01[U], c11[U], fx[U], fy[U];
-    int q[U];
-#pragma unroll
-    for (int u = 0; u < U; u++) {
-      const int k = k0 + u * nthr;
-      q[u] = -1;
-      if (k < R * R) {
-        const int lj = k / R, li = k - lj * R;
-        const int gi = wrap1(gi0 + li, n), gj = wrap1(gj0 + lj, n);
-        const int64_t g = (int64_t)gj * n + gi;
-        // PROLONG (multigrid.js:99-131): sample at ((i+1/2)/2 - 1/2, (j+1/2)/2 - 1/2)
-        const int ci0 = (gi & 1) ? (gi >> 1) : (gi >> 1) - 1;
-        const int cj0 = (gj & 1) ? (gj >> 1) : (gj >> 1) - 1;
-        fx[u] = (gi & 1) ? 0.25f : 0.75f;
-        fy[u] = (gj & 1) ? 0.25f : 0.75f;
-        const int x0 = ci0 < 0 ? ci0 + nc : ci0, x1 = ci0 + 1 >= nc ? ci0 + 1 - nc : ci0 + 1;
-        const int y0 = cj0 < 0 ? cj0 + nc : cj0, y1 = cj0 + 1 >= nc ? cj0 + 1 - nc : cj0 + 1;
-        c00[u] = __ldg(xc + (int64_t)y0 * nc + x0);
-        c10[u] = __ldg(xc + (int64_t)y0 * nc + x1);
-        c01[u] = __ldg(xc + (int64_t)y1 * nc + x0);
-        c11[u] = __ldg(xc + (int64_t)y1 * nc + x1);
-        vx[u] = __ldg(xin + g);
-        vr[u] = __ldg(rhs + g);
-        q[u] = CK::at(li, lj, par0);
+  if constexpr (ACC) {
+    // the tile's double-float pressure, read and written after the sweeps:
+    // start its DRAM reads now (one 128-byte line per thread and array)
+    constexpr int LPR = (T + 31) / 32;  // 128-byte lines per tile row
+    for (int k = tid; k < T * LPR; k += nthr) {
+      const int y = k / LPR, x = (k - y * LPR) * 32;
+      const int gi = i0 + x, gj = j0 + y;
+      if (gi < n && gj < n) {
+        prefetch_l2(ph + (int64_t)gj * n + gi);
+        prefetch_l2(pl + (int64_t)gj * n + gi);
       }
     }
-#pragma unroll
-    for (int u = 0; u < U; u++)
-      if (q[u] >= 0) {
-        xs[q[u]] = __fadd_rn(vx[u], prolong_val(c00[u], c10[u], c01[u], c11[u], fx[u], fy[u]));
-        rs[q[u]] = vr[u];
-      }
+  }
+  // staging, all asynchronous: the fine iterate and rhs of the R x R region
+  // and the RC x RC coarse block its prolongation reads.  gi0 is even (T and
+  // H are), so fine local column li samples coarse local columns
+  // (li + 1) / 2 and (li + 1) / 2 + 1 with weight 1/4 or 3/4 on the first
+  // (PROLONG, multigrid.js:99-131: sample at ((i+1/2)/2 - 1/2, (j+1/2)/2 - 1/2)).
+  constexpr int RC = R / 2 + 2;
+  const int cgi0 = (gi0 >> 1) - 1, cgj0 = (gj0 >> 1) - 1;
+  for (int k = tid; k < RC * RC; k += nthr) {
+    const int lj = k / RC, li = k - lj * RC;
+    cp_async4(&cs[k], xc + (int64_t)wrap1(cgj0 + lj, nc) * nc + wrap1(cgi0 + li, nc));
+  }
+  for (int k = tid; k < R * R; k += nthr) {
+    const int lj = k / R, li = k - lj * R;
+    const int64_t g = (int64_t)wrap1(gj0 + lj, n) * n + wrap1(gi0 + li, n);
+    const int q = CK::at(li, lj, par0);
+    cp_async4(&xs[q], xin + g);
+    cp_async4(&rs[q], rhs + g);
+  }
+  cp_async_wait_all();
+  __syncthreads();
+  for (int k = tid; k < R * R; k += nthr) {
+    const int lj = k / R, li = k - lj * R;
+    const int q = CK::at(li, lj, par0);
+    const float* c = cs + ((lj + 1) >> 1) * RC + ((li + 1) >> 1);
+    const float fx = (li & 1) ? 0.25f : 0.75f, fy = (lj & 1) ? 0.25f : 0.75f;
+    xs[q] = __fadd_rn(xs[q], prolong_val(c[0], c[1], c[RC], c[RC + 1], fx, fy));
   }
   __syncthreads();
   for (int s = 0; s < 2 * post; s++) {
@@ -596,22 +618,47 @@ static void down(Solver* s, Level& L, const Level& C, bool has_x) {
   }
 }
 
+// dynamic shared memory of k_mg_up<T, H, *>: two checkerboard arrays and the coarse block
+template <int T, int H>
+constexpr size_t up_smem_bytes() {
+  using CK = Checker<T + 2 * H>;
+  constexpr int RC = (T + 2 * H) / 2 + 2;
+  return (2 * (size_t)(CK::STRIDE + CK::N) + (size_t)RC * RC) * sizeof(float);
+}
+
+// the dynamic shared-memory limit is an attribute of the function on each device
+template <int T, int H, bool ACC>
+static void up_smem_attr(Solver* s) {
+  constexpr size_t bytes = up_smem_bytes<T, H>();
+  if (bytes <= 48 * 1024) return;
+  static std::atomic<uint64_t> attr_set{0};
+  const uint64_t bit = 1ull << (s->prm.device & 63);
+  if (!(attr_set.load() & bit)) {
+    if (cudaFuncSetAttribute(k_mg_up<T, H, ACC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes) ==
+        cudaSuccess)
+      attr_set.fetch_or(bit);
+  }
+}
+
 template <int T, int H>
 static void up_t(Solver* s, Level& L, const Level& C, float* acc_h, float* acc_l) {
   dim3 grid((L.n + T - 1) / T, (L.n + T - 1) / T);
+  constexpr size_t smem = up_smem_bytes<T, H>();
   if (acc_h) {
+    up_smem_attr<T, H, true>(s);
     double bytes = (double)L.n * L.n * 24.0 + (double)C.n * C.n * 4.0;
     FS_LAUNCH(s, "mg_up_acc", bytes,
-              k_mg_up<T, H, true><<<grid, kTileBlock, 0, s->stream>>>(L.rhs, L.x, nullptr, C.x, L.n, L.h2,
-                                                                      s->prm.mg_post_smooth, acc_h, acc_l,
-                                                                      (float)s->prm.relax));
+              k_mg_up<T, H, true><<<grid, kTileBlock, smem, s->stream>>>(L.rhs, L.x, nullptr, C.x, L.n, L.h2,
+                                                                         s->prm.mg_post_smooth, acc_h, acc_l,
+                                                                         (float)s->prm.relax));
     return;
   }
+  up_smem_attr<T, H, false>(s);
   double bytes = (double)L.n * L.n * 12.0 + (double)C.n * C.n * 4.0;
   FS_LAUNCH(s, "mg_up", bytes,
-            k_mg_up<T, H, false><<<grid, kTileBlock, 0, s->stream>>>(L.rhs, L.x, L.x2, C.x, L.n, L.h2,
-                                                                     s->prm.mg_post_smooth, nullptr, nullptr,
-                                                                     (float)s->prm.relax));
+            k_mg_up<T, H, false><<<grid, kTileBlock, smem, s->stream>>>(L.rhs, L.x, L.x2, C.x, L.n, L.h2,
+                                                                        s->prm.mg_post_smooth, nullptr, nullptr,
+                                                                        (float)s->prm.relax));
   std::swap(L.x, L.x2);
 }
 
