@@ -23,6 +23,7 @@
 // so that the lanes of a warp, which update cells of one colour in one row
 // (stride 2 in the row), hit consecutive words.
 #include <atomic>
+#include <string>
 #include <utility>
 
 #include "fs_df.cuh"
@@ -598,12 +599,17 @@ static int tile_for(int n) {
   return 16;
 }
 
+// profile name of a tile kernel: one entry per level ("mg_down_l0", ...)
+static std::string level_name(const Solver* s, const Level& L, const char* base) {
+  return std::string(base) + "_l" + std::to_string(&L - s->lev.data());
+}
+
 template <int T, int H>
 static void down_t(Solver* s, Level& L, const Level& C, bool has_x) {
   dim3 grid((L.n + T - 1) / T, (L.n + T - 1) / T);
   double bytes = (double)L.n * L.n * (has_x ? 12.0 : 8.0) + (double)C.n * C.n * 4.0;
   float* out = has_x ? L.x2 : L.x;
-  FS_LAUNCH(s, "mg_down", bytes,
+  FS_LAUNCH(s, level_name(s, L, "mg_down").c_str(), bytes,
             k_mg_down<T, H><<<grid, kTileBlock, 0, s->stream>>>(L.rhs, has_x ? L.x : nullptr, out, C.rhs, L.n,
                                                                 L.h2, s->prm.mg_pre_smooth, (float)s->prm.relax));
   if (has_x) std::swap(L.x, L.x2);
@@ -655,7 +661,7 @@ static void up_t(Solver* s, Level& L, const Level& C, float* acc_h, float* acc_l
   }
   up_smem_attr<T, H, false>(s);
   double bytes = (double)L.n * L.n * 12.0 + (double)C.n * C.n * 4.0;
-  FS_LAUNCH(s, "mg_up", bytes,
+  FS_LAUNCH(s, level_name(s, L, "mg_up").c_str(), bytes,
             k_mg_up<T, H, false><<<grid, kTileBlock, smem, s->stream>>>(L.rhs, L.x, L.x2, C.x, L.n, L.h2,
                                                                         s->prm.mg_post_smooth, nullptr, nullptr,
                                                                         (float)s->prm.relax));

@@ -50,7 +50,16 @@ __device__ __forceinline__ void block_max_finish(float m, RedCtx ctx) {
   if (!commit_partial_is_last(ctx)) return;
   int nblk = gridDim.x * gridDim.y;
   float t = 0.f;
-  for (int k = tid; k < nblk; k += nthr) t = fmaxf(t, ((volatile float*)ctx.fpartials)[k]);
+  // L2 reads (the partials of the other blocks), eight in flight per thread
+  int k = tid;
+  for (; k + 7 * nthr < nblk; k += 8 * nthr) {
+    float v[8];
+#pragma unroll
+    for (int u = 0; u < 8; u++) v[u] = __ldcg(ctx.fpartials + k + u * nthr);
+#pragma unroll
+    for (int u = 0; u < 8; u++) t = fmaxf(t, v[u]);
+  }
+  for (; k < nblk; k += nthr) t = fmaxf(t, __ldcg(ctx.fpartials + k));
   for (int o = 16; o > 0; o >>= 1) t = fmaxf(t, __shfl_xor_sync(0xffffffffu, t, o));
   __syncthreads();
   if (lane == 0) sm[warp] = t;

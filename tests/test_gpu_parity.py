@@ -442,8 +442,8 @@ def test_bitwise_repeatable(G, O):
 
 # ---------------------------------------------------- fused multigrid cycle
 @pytest.mark.parametrize("precision", ["f32", "mixed"])
-@pytest.mark.parametrize("n,relax", [(64, 1.0), (200, 1.0), (256, 1.0), (320, 1.0), (1056, 1.0), (64, 1.2),
-                                     (200, 1.2), (256, 1.2)])
+@pytest.mark.parametrize("n,relax", [(64, 1.0), (200, 1.0), (256, 1.0), (320, 1.0), (528, 1.0), (1056, 1.0),
+                                     (64, 1.2), (200, 1.2), (256, 1.2), (1024, 1.2)])
 def test_fused_vcycle_bitwise_equals_one_pass_kernels(G, O, precision, n, relax):
     """The fused V-cycle (tile kernels + one-CTA bottom solve) evaluates the same
     expressions in the same order as the one-kernel-per-pass path, so the two
@@ -451,7 +451,8 @@ def test_fused_vcycle_bitwise_equals_one_pass_kernels(G, O, precision, n, relax)
     the power-of-two bottom kernel (with a non-zero initial x on V-cycles 2
     and 3 in F32); n = 200 has partial 16-cell tiles and a 50 -> 25 generic
     bottom with an odd coarsest level; n = 1056 has partial 64-, 32- and
-    16-cell tiles and an odd 33 bottom."""
+    16-cell tiles and an odd 33 bottom; n = 528 and 1024 have 32- and
+    64-cell tiles at level 0 (the last one partial at 528)."""
     u0, v0 = O.lcg_uv(4242, n * n)
     out = []
     for variant in (0, 1):
@@ -478,13 +479,13 @@ def test_fused_tolerance_loop_f32(G, O):
 
 
 # ------------------------------------------------------------ CUDA graphs
-@pytest.mark.parametrize("precision", ["f32", "mixed"])
-def test_graph_step_equals_eager_step(G, O, precision):
+@pytest.mark.parametrize("precision,n", [("f32", 256), ("mixed", 256), ("mixed", 528)])
+def test_graph_step_equals_eager_step(G, O, precision, n):
     """fs_step captures the fused configuration into a CUDA graph whose tolerance
     loop is a conditional node; fs_profile_step runs the same kernels eagerly
     with the host reading the residual.  Fields and cycle counts agree bit for
-    bit after three steps with solids and forcing."""
-    n = 256
+    bit after three steps with solids and forcing (n = 528: 32-cell tiles at
+    level 0, the last one partial)."""
     u0, v0 = O.lcg_uv(123, n * n)
     outs, cycles = [], []
     for graph in (True, False):
