@@ -317,23 +317,25 @@ def run_gpu(args):
     achieved = bytes_per_launch / (per_launch_ms / 1e3) / 1e9
     traffic = traffic_from_profiles(top["name"])
 
-    # e2e: host upload + step + host read-back per step through the C ABI
+    # e2e: host upload + step + host read-back per step through the C ABI, with
+    # f32 host arrays: the element type the reference's uploadVelocity stores
+    # and its readVelocity returns (Float32Array, src/gpu/solver.js:300-362)
     lib = pkg.load()
-    nbytes = n * n * 8
+    nbytes = n * n * 4
     hu = lib.fs_host_alloc(nbytes)
     hv = lib.fs_host_alloc(nbytes)
-    au = np.ctypeslib.as_array(C.cast(hu, C.POINTER(C.c_double)), shape=(n * n,))
-    av = np.ctypeslib.as_array(C.cast(hv, C.POINTER(C.c_double)), shape=(n * n,))
+    au = np.ctypeslib.as_array(C.cast(hu, C.POINTER(C.c_float)), shape=(n * n,))
+    av = np.ctypeslib.as_array(C.cast(hv, C.POINTER(C.c_float)), shape=(n * n,))
     au[:] = u0
     av[:] = v0
-    e2e_steps = max(3, min(args.steps, 20))
+    e2e_steps = max(3, min(args.steps, 100))
     s.sync()
     barrier(dist)
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
-        pkg._lib.check(lib.fs_upload_velocity(s._h, hu, hv, 1), s._h)
+        pkg._lib.check(lib.fs_upload_velocity(s._h, hu, hv, 0), s._h)
         pkg._lib.check(lib.fs_step(s._h, dt), s._h)
-        pkg._lib.check(lib.fs_read_velocity(s._h, hu, hv, 1), s._h)
+        pkg._lib.check(lib.fs_read_velocity(s._h, hu, hv, 0), s._h)
     e2e_s = time.perf_counter() - t0
     barrier(dist)
     e2e_s = allmax(dist, e2e_s)
@@ -390,7 +392,7 @@ def run_gpu(args):
                          "gbs": (k["bytes"] / (k["total_ms"] / 1e3) / 1e9) if k["total_ms"] > 0 else None}
                         for k in sorted(prof, key=lambda k: -k["total_ms"])],
             "e2e": {"value": e2e_val, "unit": UNIT, "h2d_bytes_per_step": 2 * nbytes,
-                    "d2h_bytes_per_step": 2 * nbytes, "steps": e2e_steps},
+                    "d2h_bytes_per_step": 2 * nbytes, "steps": e2e_steps, "host_dtype": "f32"},
             "step_roofline": {
                 "bytes_per_cell_step": step_bytes(cycles_timed),
                 "achieved": value * step_bytes(cycles_timed) / 1e9 / max(world, 1),

@@ -759,8 +759,9 @@ static int upload_to(Solver* s, const void* src, int dtype, float* hi, float* lo
   return check_launch(s);
 }
 
-// device field -> host array (synchronises)
-static int download_from(Solver* s, const float* hi, const float* lo, void* dst, int dtype) {
+// device field -> host array (synchronises unless sync is false; later work on
+// the stream may reuse the staging buffer, the stream orders it after the copy)
+static int download_from(Solver* s, const float* hi, const float* lo, void* dst, int dtype, bool sync = true) {
   if (dtype != FS_DTYPE_F32 && dtype != FS_DTYPE_F64) return fail(s, FS_ERR_INVALID_ARGUMENT, "unknown dtype");
   const size_t n = (size_t)s->n;
   if (dtype == FS_DTYPE_F32 && !lo) {
@@ -777,7 +778,7 @@ static int download_from(Solver* s, const float* hi, const float* lo, void* dst,
       CU(s, cudaMemcpyAsync(dst, st, n * 8, cudaMemcpyDeviceToHost, s->stream));
     }
   }
-  CU(s, cudaStreamSynchronize(s->stream));
+  if (sync) CU(s, cudaStreamSynchronize(s->stream));
   return check_launch(s);
 }
 
@@ -792,7 +793,7 @@ FS_API int fs_upload_velocity(fs_solver* h, const void* u, const void* v, int dt
 FS_API int fs_read_velocity(fs_solver* h, void* u, void* v, int dtype) {
   SOLVER(h);
   if (!u || !v) return fail(s, FS_ERR_INVALID_ARGUMENT, "u or v is NULL");
-  int rc = download_from(s, s->u, s->ulo, u, dtype);
+  int rc = download_from(s, s->u, s->ulo, u, dtype, false);  // one synchronisation for both
   if (rc) return rc;
   return download_from(s, s->v, s->vlo, v, dtype);
 }
