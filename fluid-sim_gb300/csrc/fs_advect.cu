@@ -11,11 +11,15 @@
 // keep full f32 precision at any grid size.  The reference forms x = i*dx in
 // f32 and divides by dx again, which at n = 2048 quantises the weights to
 // ~2e-4 of a cell; the mathematics is otherwise identical.
+#include <cuda.h>
+#include <cudaTypedefs.h>
 #include <math.h>
 
+#include <utility>
 #include <vector>
 
 #include "fs_internal.cuh"
+#include "fs_tc.cuh"
 
 namespace fs {
 
@@ -182,6 +186,40 @@ __device__ __forceinline__ void stage_tiles(float* const (&sm)[F], const float* 
   vmax = __uint_as_float(mv);
 }
 
+// max |value| (NaN counted as infinite) over a staged block, this thread's share
+__device__ __forceinline__ uint32_t smem_absmax_bits(const float* sm) {
+  const int tid = threadIdx.y * blockDim.x + threadIdx.x, nthr = blockDim.x * blockDim.y;
+  uint32_t m = 0;
+  for (int k = tid; k < kSW * kSH; k += nthr) m = max(m, __float_as_uint(fabsf(sm[k])));
+  return m;
+}
+
+// TMA staging of F kSH x kSW blocks (tiles whose block lies inside the grid):
+// thread 0 arms the barrier and issues the copies, every thread waits (bounded).
+// Returns false on every thread if the wait gave up (after waiting once more
+// for the copies in flight and raising *err); the caller then skips the tile.
+template <int F>
+__device__ __forceinline__ bool tma_stage(float* const (&sm)[F], const CUtensorMap* const (&tm)[F], int oi, int oj,
+                                          uint64_t* bar, int* err) {
+  const int tid = threadIdx.y * blockDim.x + threadIdx.x;
+  if (tid == 0) {
+    tc::mbar_init(bar, 1);
+    tc::mbar_fence_init();
+  }
+  __syncthreads();
+  if (tid == 0) {
+    tc::mbar_arrive_expect_tx(bar, (uint32_t)(F * kSW * kSH * sizeof(float)));
+#pragma unroll
+    for (int q = 0; q < F; q++) tc::tma_load_2d(sm[q], tm[q], oi, oj, bar);
+  }
+  const bool ok = __syncthreads_and(tc::mbar_wait(bar, 0)) != 0;
+  if (!ok) {
+    if (tid == 0) atomicExch(err, 1);
+    tc::mbar_wait(bar, 0);
+  }
+  return ok;
+}
+
 // one CTA-wide decision after staging (and the barrier the staging needs)
 __device__ __forceinline__ bool fast_tile(float umax, float vmax, float cx, float cy) {
   const bool ok = umax * fabsf(cx) <= kFastDisp && vmax * fabsf(cy) <= kFastDisp;  // false for NaN / inf
@@ -225,17 +263,30 @@ __device__ __forceinline__ void advect_rows(const TileView<FAST>& U, const TileV
   }
 }
 
+// Tiles whose staged block lies inside the grid are staged by TMA when the
+// tensor maps are valid (tma != 0); the others by the wrapped loads.
 __global__ void __launch_bounds__(256) k_advect_sl_t(const float* __restrict__ u, const float* __restrict__ v,
                                                      float* __restrict__ ou, float* __restrict__ ov, int nx, int ny,
-                                                     float cx, float cy, float* __restrict__ bounds) {
-  __shared__ float su[kSW * kSH], sv[kSW * kSH];
+                                                     float cx, float cy, float* __restrict__ bounds,
+                                                     const __grid_constant__ CUtensorMap tm_u,
+                                                     const __grid_constant__ CUtensorMap tm_v, int tma, int* err) {
+  __shared__ __align__(128) float su[kSW * kSH];
+  __shared__ __align__(128) float sv[kSW * kSH];
+  __shared__ uint64_t bar;
   const int ti = blockIdx.x * kTX, tj = blockIdx.y * kTY;
   const int oi = ti - kHalo, oj = tj - kHalo;
   float umax, vmax;
   {
     float* const sm[2] = {su, sv};
-    const float* const f[2] = {u, v};
-    stage_tiles<2>(sm, f, oi, oj, nx, ny, umax, vmax);
+    if (tma && oi >= 0 && oj >= 0 && oi + kSW <= nx && oj + kSH <= ny) {
+      const CUtensorMap* const tm[2] = {&tm_u, &tm_v};
+      if (!tma_stage<2>(sm, tm, oi, oj, &bar, err)) return;
+      umax = __uint_as_float(smem_absmax_bits(su));
+      vmax = __uint_as_float(smem_absmax_bits(sv));
+    } else {
+      const float* const f[2] = {u, v};
+      stage_tiles<2>(sm, f, oi, oj, nx, ny, umax, vmax);
+    }
   }
   if (fast_tile(umax, vmax, cx, cy)) {
     const TileView<true> U{su, oi, oj, u, nx, ny}, V{sv, oi, oj, v, nx, ny};
@@ -285,15 +336,30 @@ __device__ __forceinline__ void combine_rows(const TileView<FAST>& U, const Tile
 __global__ void __launch_bounds__(256) k_mc_combine_t(const float* __restrict__ u, const float* __restrict__ v,
                                                       const float* __restrict__ fu, const float* __restrict__ fv,
                                                       const float* __restrict__ bounds, float* __restrict__ ou,
-                                                      float* __restrict__ ov, int nx, int ny, float cx, float cy) {
-  __shared__ float su[kSW * kSH], sv[kSW * kSH], sfu[kSW * kSH], sfv[kSW * kSH];
+                                                      float* __restrict__ ov, int nx, int ny, float cx, float cy,
+                                                      const __grid_constant__ CUtensorMap tm_u,
+                                                      const __grid_constant__ CUtensorMap tm_v,
+                                                      const __grid_constant__ CUtensorMap tm_fu,
+                                                      const __grid_constant__ CUtensorMap tm_fv, int tma, int* err) {
+  __shared__ __align__(128) float su[kSW * kSH];
+  __shared__ __align__(128) float sv[kSW * kSH];
+  __shared__ __align__(128) float sfu[kSW * kSH];
+  __shared__ __align__(128) float sfv[kSW * kSH];
+  __shared__ uint64_t bar;
   const int ti = blockIdx.x * kTX, tj = blockIdx.y * kTY;
   const int oi = ti - kHalo, oj = tj - kHalo;
   float umax, vmax;
   {
     float* const sm[4] = {su, sv, sfu, sfv};
-    const float* const f[4] = {u, v, fu, fv};
-    stage_tiles<4>(sm, f, oi, oj, nx, ny, umax, vmax);
+    if (tma && oi >= 0 && oj >= 0 && oi + kSW <= nx && oj + kSH <= ny) {
+      const CUtensorMap* const tm[4] = {&tm_u, &tm_v, &tm_fu, &tm_fv};
+      if (!tma_stage<4>(sm, tm, oi, oj, &bar, err)) return;
+      umax = __uint_as_float(smem_absmax_bits(su));
+      vmax = __uint_as_float(smem_absmax_bits(sv));
+    } else {
+      const float* const f[4] = {u, v, fu, fv};
+      stage_tiles<4>(sm, f, oi, oj, nx, ny, umax, vmax);
+    }
   }
   if (fast_tile(umax, vmax, cx, cy)) {
     const TileView<true> U{su, oi, oj, u, nx, ny}, V{sv, oi, oj, v, nx, ny};
@@ -310,12 +376,55 @@ static const dim3 kBlock(32, 8);
 
 static dim3 tile_grid(const Grid& g) { return dim3((g.nx + kTX - 1) / kTX, (g.ny + kTY - 1) / kTY); }
 
+// Tensor map of one f32 field for the advection tiles (box kSW x kSH), kept
+// per device pointer.  TMA needs the row pitch a multiple of 16 bytes (nx % 4
+// == 0) and a 16-byte-aligned base; otherwise, or if the driver lacks the
+// encoder, every tile uses the wrapped loads.
+static PFN_cuTensorMapEncodeTiled_v12000 tmap_encoder() {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = [] {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess)
+      p = nullptr;
+    return reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+  }();
+  return fn;
+}
+
+static bool tile_tmap(Solver* s, const float* f, CUtensorMap* out) {
+  const Grid& g = s->g;
+  if (g.nx % 4 != 0 || ((uintptr_t)f & 15) != 0 || g.nx < kSW || g.ny < kSH) return false;
+  for (auto& e : s->tmaps)
+    if (e.first == f) {
+      *out = e.second;
+      return true;
+    }
+  PFN_cuTensorMapEncodeTiled_v12000 enc = tmap_encoder();
+  if (!enc) return false;
+  CUtensorMap m;
+  const cuuint64_t dims[2] = {(cuuint64_t)g.nx, (cuuint64_t)g.ny};
+  const cuuint64_t pitch[1] = {(cuuint64_t)g.nx * sizeof(float)};
+  const cuuint32_t box[2] = {(cuuint32_t)kSW, (cuuint32_t)kSH};
+  const cuuint32_t estr[2] = {1, 1};
+  if (enc(&m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<float*>(f), dims, pitch, box, estr,
+          CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+          CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+    return false;
+  s->tmaps.emplace_back(f, m);
+  *out = m;
+  return true;
+}
+
 template <>
 void launch_advect_sl<float>(Solver* s, const float* u, const float* v, float* ou, float* ov, float dt) {
   const Grid& g = s->g;
   float cx = (float)((double)dt / g.dxd), cy = (float)((double)dt / g.dyd);
+  CUtensorMap tu{}, tv{};
+  const int tma = tile_tmap(s, u, &tu) && tile_tmap(s, v, &tv) ? 1 : 0;
   FS_LAUNCH(s, "advect_sl", (double)s->n * 16,
-            k_advect_sl_t<<<tile_grid(g), kBlock, 0, s->stream>>>(u, v, ou, ov, g.nx, g.ny, cx, cy, nullptr));
+            k_advect_sl_t<<<tile_grid(g), kBlock, 0, s->stream>>>(u, v, ou, ov, g.nx, g.ny, cx, cy, nullptr, tu, tv,
+                                                                  tma, &s->dev->async_err));
 }
 
 template <>
@@ -323,11 +432,16 @@ void launch_advect_mc<float>(Solver* s, const float* u, const float* v, float* f
                              float* ov, float dt) {
   const Grid& g = s->g;
   float cx = (float)((double)dt / g.dxd), cy = (float)((double)dt / g.dyd);
+  CUtensorMap tu{}, tv{}, tfu{}, tfv{};
+  const int tma =
+      tile_tmap(s, u, &tu) && tile_tmap(s, v, &tv) && tile_tmap(s, fu, &tfu) && tile_tmap(s, fv, &tfv) ? 1 : 0;
   FS_LAUNCH(s, "advect_sl", (double)s->n * 32,
-            k_advect_sl_t<<<tile_grid(g), kBlock, 0, s->stream>>>(u, v, fu, fv, g.nx, g.ny, cx, cy, s->mc_bounds));
+            k_advect_sl_t<<<tile_grid(g), kBlock, 0, s->stream>>>(u, v, fu, fv, g.nx, g.ny, cx, cy, s->mc_bounds, tu,
+                                                                  tv, tma, &s->dev->async_err));
   FS_LAUNCH(s, "mc_combine", (double)s->n * 40,
             k_mc_combine_t<<<tile_grid(g), kBlock, 0, s->stream>>>(u, v, fu, fv, s->mc_bounds, ou, ov, g.nx, g.ny,
-                                                                   cx, cy));
+                                                                   cx, cy, tu, tv, tfu, tfv, tma,
+                                                                   &s->dev->async_err));
 }
 
 // DIFFUSE (shaders.js:401-425; src/cpu/solver.js:56-68 operand order)

@@ -979,10 +979,11 @@ FS_API int fs_last_stats(fs_solver* h, fs_step_stats* out) {
   if (!out) return fail(s, FS_ERR_INVALID_ARGUMENT, "out is NULL");
   int rc = sync(s);
   if (rc) return rc;
+  DevState d;
+  CU(s, cudaMemcpy(&d, s->dev, sizeof(DevState), cudaMemcpyDeviceToHost));
+  if (d.async_err) return fail(s, FS_ERR_CUDA, "an asynchronous tile copy did not complete (bounded wait)");
   if (s->stats_on_device) {
     // the last projection's loop ran inside a captured step
-    DevState d;
-    CU(s, cudaMemcpy(&d, s->dev, sizeof(DevState), cudaMemcpyDeviceToHost));
     s->stats = fs_step_stats{d.cycles, d.converged, d.res_max, d.res_initial};
     *out = s->stats;
     if (d.nonfinite) return fail(s, FS_ERR_NONFINITE, "non-finite Poisson residual in the last step");

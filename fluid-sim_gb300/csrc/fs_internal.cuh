@@ -6,10 +6,12 @@
 // arrays move a quarter of the bytes for p, div and the multigrid levels).
 #pragma once
 
+#include <cuda.h>  // CUtensorMap (types only; the encoder is looked up at run time)
 #include <cuda_runtime.h>
 #include <stdint.h>
 
 #include <string>
+#include <utility>
 #include <vector>
 
 #include "../../include/fluid.h"
@@ -45,7 +47,7 @@ struct DevState {
   int cycles;          // cycles the last projection ran
   int converged;
   int nonfinite;
-  int pad;
+  int async_err;  // a bounded wait for an asynchronous (TMA) copy gave up
 };
 
 struct KernelStat {
@@ -95,6 +97,8 @@ struct Solver {
   void* stage = nullptr;     // n doubles: host I/O conversion staging
 
   std::vector<Level> lev;
+  // TMA tensor maps of the advected fields, by device pointer (fs_advect.cu)
+  std::vector<std::pair<const void*, CUtensorMap>> tmaps;
 
   // reductions: per-block partials and the final words
   double* red_partials = nullptr;  // 2 * red_cap doubles

@@ -62,6 +62,23 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, uint32
   return false;
 }
 
+// -------------------------------------------------------------- TMA loads
+// one arrival on the barrier that also expects `bytes` of asynchronous copies
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+// 2-D tiled tensor copy global -> shared: the box of the tensor map whose
+// first element is (x, y) (x innermost; x * element size a multiple of 16
+// bytes), completion counted on bar.  tmap is the address of a CUtensorMap
+// kernel parameter (__grid_constant__).
+__device__ __forceinline__ void tma_load_2d(void* dst, const void* tmap, int x, int y, uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(
+          smem_u32(dst)),
+      "l"(reinterpret_cast<uint64_t>(tmap)), "r"(x), "r"(y), "r"(smem_u32(bar))
+      : "memory");
+}
+
 // ---------------------------------------------------------------- the MMA
 // Shared-memory matrix descriptor, no swizzle: start address, LBO and SBO in
 // 16-byte units, bit 46 = the descriptor version for this architecture.
