@@ -782,12 +782,17 @@ static int download_from(Solver* s, const float* hi, const float* lo, void* dst,
   return check_launch(s);
 }
 
+// Uploads return once the caller's arrays have been read, as the reference's
+// writeTexture copies them at the call (src/gpu/solver.js:300-315): a copy from
+// page-locked memory is asynchronous, so the stream is synchronised.
 FS_API int fs_upload_velocity(fs_solver* h, const void* u, const void* v, int dtype) {
   SOLVER(h);
   if (!u || !v) return fail(s, FS_ERR_INVALID_ARGUMENT, "u or v is NULL");
   int rc = upload_to(s, u, dtype, s->u, s->ulo);
   if (rc) return rc;
-  return upload_to(s, v, dtype, s->v, s->vlo);
+  if ((rc = upload_to(s, v, dtype, s->v, s->vlo))) return rc;
+  CU(s, cudaStreamSynchronize(s->stream));
+  return FS_OK;
 }
 
 FS_API int fs_read_velocity(fs_solver* h, void* u, void* v, int dtype) {
@@ -822,7 +827,10 @@ FS_API int fs_upload_field(fs_solver* h, int field, const void* data, int dtype)
   SOLVER(h);
   if (!data) return fail(s, FS_ERR_INVALID_ARGUMENT, "data is NULL");
   if (field != FS_FIELD_PRESSURE) return fail(s, FS_ERR_INVALID_ARGUMENT, "only the pressure can be uploaded");
-  return s->mixed ? upload_to(s, data, dtype, s->ph, s->pl) : upload_to(s, data, dtype, s->p32, nullptr);
+  int rc = s->mixed ? upload_to(s, data, dtype, s->ph, s->pl) : upload_to(s, data, dtype, s->p32, nullptr);
+  if (rc) return rc;
+  CU(s, cudaStreamSynchronize(s->stream));
+  return FS_OK;
 }
 
 FS_API int fs_set_forcing(fs_solver* h, const fs_mode* modes, int count, double amplitude, double drag,

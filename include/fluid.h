@@ -177,7 +177,9 @@ FS_API const char* fs_status_string(int status);
 FS_API int fs_get_params(const fs_solver* s, fs_params* out);
 
 /* -------------------------------------------------------------- field I/O */
-/* uploadVelocity(u, v) (solver.js:301-315); dtype selects f32 or f64 input */
+/* uploadVelocity(u, v) (solver.js:301-315); dtype selects f32 or f64 input.
+ * Returns once u and v have been read (the caller may reuse them), as the
+ * reference copies them at the call. */
 FS_API int fs_upload_velocity(fs_solver* s, const void* u, const void* v, int dtype);
 /* readVelocity() (solver.js:356-362); synchronises */
 FS_API int fs_read_velocity(fs_solver* s, void* u, void* v, int dtype);
