@@ -378,7 +378,7 @@ static dim3 tile_grid(const Grid& g) { return dim3((g.nx + kTX - 1) / kTX, (g.ny
 
 // Tensor map of one f32 field for the advection tiles (box kSW x kSH), kept
 // per device pointer.  TMA needs the row pitch a multiple of 16 bytes (nx % 4
-// == 0) and a 16-byte-aligned base; otherwise, or if the driver lacks the
+// == 0) and a 16-byte-aligned base; otherwise, or if the CUDA driver lacks the
 // encoder, every tile uses the wrapped loads.
 static PFN_cuTensorMapEncodeTiled_v12000 tmap_encoder() {
   static PFN_cuTensorMapEncodeTiled_v12000 fn = [] {

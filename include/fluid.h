@@ -304,7 +304,7 @@ FS_API int fs_tc_gemm_check(const void* d_a, const void* d_b, float* d_d, int32_
  * the divergence and the solid mask at half the grid resolution to an
  * initial pressure.  With a guess attached, the multigrid projection starts
  * from it instead of zero and still iterates to pressure_tol, so plain
- * multigrid stays both the fallback and the judge.  No reference counterpart.
+ * multigrid stays both the fallback and the yardstick.  No reference counterpart.
  *
  * Network inputs at its own resolution H x W (multiples of 8):
  *   div_n = h^2 d / sigma, sigma = RMS(h^2 d) per sample (h = grid spacing),
