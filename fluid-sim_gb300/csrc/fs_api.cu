@@ -410,7 +410,7 @@ static int capture_tolerance_loop(Solver* s) {
 //    max|div u| <= tol or max_cycles.  In a captured step the loop is a
 //    conditional node evaluated on the device; otherwise the host reads the
 //    residual after every cycle.
-static int pressure_solve(Solver* s, bool capture) {
+static int pressure_solve(Solver* s, bool capture, bool defer = false) {
   const fs_params& P = s->prm;
   const int iters = P.pressure_iterations;
   const bool tol = P.pressure_tol > 0;
@@ -446,6 +446,12 @@ static int pressure_solve(Solver* s, bool capture) {
   }
   if (capture) {
     s->stats_on_device = true;
+    if (defer) {
+      // a batch runs the loop for a whole size class (batch_build): only the
+      // statistics of the initial residual are set here
+      launch_cond_init(s, 0, false);
+      return check_launch(s);
+    }
     return capture_tolerance_loop(s);
   }
   double m;
@@ -468,13 +474,19 @@ static int pressure_solve(Solver* s, bool capture) {
 }
 
 // divergence of (wu, wv) -> solve -> state velocity = w - grad p
-static int project_from(Solver* s, const float* wu, const float* wv, bool capture) {
-  if (s->mixed) launch_div_df(s, wu, nullptr, wv, nullptr, s->dh, s->dl);
-  else launch_divergence<float, float>(s, wu, wv, s->div32);
-  int rc = pressure_solve(s, capture);
+static int project_finish(Solver* s, const float* wu, const float* wv) {
   if (s->mixed) launch_subgrad_df(s, wu, nullptr, wv, nullptr, s->ph, s->pl, s->u, s->ulo, s->v, s->vlo);
   else launch_subtract_gradient_f32(s, wu, wv, s->p32, s->u, s->v);
-  int rc2 = check_launch(s);
+  return check_launch(s);
+}
+
+// defer: stop after the start of the pressure solve (see pressure_solve)
+static int project_from(Solver* s, const float* wu, const float* wv, bool capture, bool defer = false) {
+  if (s->mixed) launch_div_df(s, wu, nullptr, wv, nullptr, s->dh, s->dl);
+  else launch_divergence<float, float>(s, wu, wv, s->div32);
+  int rc = pressure_solve(s, capture, defer);
+  if (defer) return rc;
+  int rc2 = project_finish(s, wu, wv);
   return rc ? rc : rc2;
 }
 
@@ -485,8 +497,17 @@ static void advect_into(Solver* s, float dt, float* ou, float* ov) {
   else launch_advect_sl<float>(s, s->u, s->v, ou, ov, dt);
 }
 
-// step(dt), solver.js:518-591, enqueued on s->stream (eagerly or under capture)
-static int enqueue_step(Solver* s, double dt, bool capture) {
+// A step split around its tolerance loop (batched size classes): the velocity
+// the gradient subtraction reads.
+struct StepSplit {
+  const float* wu = nullptr;
+  const float* wv = nullptr;
+};
+
+// step(dt), solver.js:518-591, enqueued on s->stream (eagerly or under capture).
+// With split, it stops where the tolerance loop would start; the rest is
+// enqueue_step_back.
+static int enqueue_step(Solver* s, double dt, bool capture, StepSplit* split = nullptr) {
   float fdt = (float)dt;
   advect_into(s, fdt, s->wu, s->wv);
   float *cu = s->wu, *cv = s->wv;
@@ -496,9 +517,21 @@ static int enqueue_step(Solver* s, double dt, bool capture) {
   }
   if (s->n_modes > 0) launch_forcing(s, cu, cv, fdt);
   if (!s->disks.empty()) launch_solids(s, cu, cv, fdt, false);
-  int rc = project_from(s, cu, cv, capture);
+  int rc = project_from(s, cu, cv, capture, split != nullptr);
+  if (split) {
+    split->wu = cu;
+    split->wv = cv;
+    return rc;
+  }
   // dye through the now divergence-free field (solver.js:516, 577-586)
   if (s->dye) launch_advect_dye(s, fdt);
+  launch_step_finish(s, dt);
+  return rc;
+}
+
+static int enqueue_step_back(Solver* s, double dt, const StepSplit& split) {
+  int rc = project_finish(s, split.wu, split.wv);
+  if (s->dye) launch_advect_dye(s, (float)dt);
   launch_step_finish(s, dt);
   return rc;
 }
@@ -1249,15 +1282,33 @@ FS_API void fs_host_free(void* p) {
 // per-step events; while the batch graph is captured each member's step runs
 // on its own stream, forked from and joined back to the batch stream, so the
 // branches are independent and their kernels overlap on the GPU.
+// Members that run the MIXED tolerance loop of the fused multigrid step with the
+// same grid and multigrid settings form a size class: their refinement cycles
+// run as batched launches inside one conditional loop per class (up to
+// kClassMax members per class; a larger group is split).
+struct BatchClass {
+  std::vector<int> idx;  // member indices
+  int body_launches = 0;  // launches of one loop iteration
+};
+
 struct fs_batch {
   std::vector<fs_solver*> members;
   int device = 0;
   cudaStream_t stream = nullptr;
+  cudaStream_t body_stream = nullptr;        // captures the class loop bodies
+  std::vector<cudaStream_t> class_streams;   // one per class, grown as needed
   cudaEvent_t fork = nullptr;
   std::vector<cudaEvent_t> joins;
+  std::vector<cudaEvent_t> class_done;
+  std::vector<BatchClass> classes;
+  long long* d_iters = nullptr;  // device: loop iterations per class since the last capture
+  int iters_cap = 0;
+  int64_t launches_done = 0;     // class launches of graphs replaced since
+  int64_t fixed_per_replay = 0;  // launches of one replay outside the class loops
   cudaGraphExec_t exec = nullptr;
   std::vector<double> dts;
   int64_t replays = 0;
+  int64_t replays_at_build = 0;
   std::string err;
 };
 
@@ -1281,31 +1332,177 @@ static void batch_free(fs_batch* b) {
     delete h;
   }
   for (cudaEvent_t e : b->joins) cudaEventDestroy(e);
+  for (cudaEvent_t e : b->class_done) cudaEventDestroy(e);
+  for (cudaStream_t c : b->class_streams) cudaStreamDestroy(c);
+  if (b->body_stream) cudaStreamDestroy(b->body_stream);
+  if (b->d_iters) cudaFree(b->d_iters);
   if (b->fork) cudaEventDestroy(b->fork);
   if (b->stream) cudaStreamDestroy(b->stream);
   delete b;
 }
 
+// a member that can run its loop in a size class, and the settings a class shares
+static bool class_eligible(const Solver* s) {
+  return s->mixed && s->fused && s->prm.pressure_tol > 0 && !s->guess && s->g.nx == s->g.ny;
+}
+static bool same_class(const Solver* a, const Solver* b) {
+  const fs_params &p = a->prm, &q = b->prm;
+  return a->g.nx == b->g.nx && a->g.ny == b->g.ny && p.mg_pre_smooth == q.mg_pre_smooth &&
+         p.mg_post_smooth == q.mg_post_smooth && p.mg_coarse_sweeps == q.mg_coarse_sweeps &&
+         p.mg_min_size == q.mg_min_size && p.relax == q.relax && p.max_cycles == q.max_cycles &&
+         a->lev.size() == b->lev.size();
+}
+
+// the class's conditional loop on cs (already part of the batch capture):
+// k_cond_class sets the condition from the members' initial statistics, the
+// body is one batched refinement cycle plus k_cond_class's bookkeeping
+static int capture_class_loop(fs_batch* b, BatchClass& c, cudaStream_t cs, long long* iters) {
+  std::vector<Solver*> ms;
+  for (int i : c.idx) ms.push_back(&b->members[i]->s);
+  const int count = (int)ms.size();
+  cudaStreamCaptureStatus cst;
+  cudaGraph_t cg = nullptr;
+  const cudaGraphNode_t* deps = nullptr;
+  size_t nd = 0;
+  cudaError_t e = cudaStreamGetCaptureInfo(cs, &cst, nullptr, &cg, &deps, nullptr, &nd);
+  cudaGraphConditionalHandle h = 0;
+  if (e == cudaSuccess) e = cudaGraphConditionalHandleCreate(&h, cg, 0, 0);
+  if (e != cudaSuccess) return bfail(b, FS_ERR_CUDA, std::string("batch loop: ") + cudaGetErrorString(e));
+  launch_cond_class(ms.data(), count, cs, h, true, iters);
+  e = cudaStreamGetCaptureInfo(cs, &cst, nullptr, &cg, &deps, nullptr, &nd);
+  cudaGraphNodeParams cp = {};
+  cp.type = cudaGraphNodeTypeConditional;
+  cp.conditional.handle = h;
+  cp.conditional.type = cudaGraphCondTypeWhile;
+  cp.conditional.size = 1;
+  cudaGraphNode_t node;
+  if (e == cudaSuccess) e = cudaGraphAddNode(&node, cg, deps, nullptr, nd, &cp);
+  if (e == cudaSuccess)
+    e = cudaStreamUpdateCaptureDependencies(cs, &node, nullptr, 1, cudaStreamSetCaptureDependencies);
+  if (e == cudaSuccess)
+    e = cudaStreamBeginCaptureToGraph(b->body_stream, cp.conditional.phGraph_out[0], nullptr, nullptr, 0,
+                                      cudaStreamCaptureModeThreadLocal);
+  if (e != cudaSuccess) return bfail(b, FS_ERR_CUDA, std::string("batch loop: ") + cudaGetErrorString(e));
+  c.body_launches = mg_vcycle_class(ms.data(), count, b->body_stream);
+  launch_refine_class(ms.data(), count, b->body_stream);
+  launch_cond_class(ms.data(), count, b->body_stream, h, false, iters);
+  c.body_launches += 2;
+  cudaGraph_t tmp = nullptr;
+  cudaError_t e2 = cudaGetLastError();
+  e = cudaStreamEndCapture(b->body_stream, &tmp);
+  if (e2 != cudaSuccess) e = e2;
+  return e == cudaSuccess ? FS_OK : bfail(b, FS_ERR_CUDA, std::string("batch loop: ") + cudaGetErrorString(e));
+}
+
 static int batch_build(fs_batch* b, const double* dt) {
+  const int n = (int)b->members.size();
+  // the class launches of the graph being replaced, before its counters reset
+  if (b->exec && b->d_iters && !b->classes.empty()) {
+    std::vector<long long> it(b->classes.size());
+    if (cudaStreamSynchronize(b->stream) == cudaSuccess &&
+        cudaMemcpy(it.data(), b->d_iters, it.size() * sizeof(long long), cudaMemcpyDeviceToHost) == cudaSuccess)
+      for (size_t c = 0; c < it.size(); c++) b->launches_done += it[c] * b->classes[c].body_launches;
+  }
+  b->launches_done += (b->replays - b->replays_at_build) * b->fixed_per_replay;
   if (b->exec) cudaGraphExecDestroy(b->exec);
   b->exec = nullptr;
-  const int n = (int)b->members.size();
+
+  // size classes
+  b->classes.clear();
+  std::vector<int> cls(n, -1);
+  for (int i = 0; i < n; i++) {
+    const Solver* s = &b->members[i]->s;
+    if (!class_eligible(s)) continue;
+    for (size_t c = 0; c < b->classes.size() && cls[i] < 0; c++) {
+      const Solver* r = &b->members[b->classes[c].idx[0]]->s;
+      if (same_class(s, r) && (int)b->classes[c].idx.size() < kClassMax) cls[i] = (int)c;
+    }
+    if (cls[i] < 0) {
+      cls[i] = (int)b->classes.size();
+      b->classes.emplace_back();
+    }
+    b->classes[cls[i]].idx.push_back(i);
+  }
+  const int nc = (int)b->classes.size();
+  // streams, events and counters for the classes (outside the capture)
+  while ((int)b->class_streams.size() < nc) {
+    cudaStream_t cs = nullptr;
+    cudaEvent_t ev = nullptr;
+    if (cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&ev, cudaEventDisableTiming) != cudaSuccess)
+      return bfail(b, FS_ERR_CUDA, "batch: stream creation failed");
+    b->class_streams.push_back(cs);
+    b->class_done.push_back(ev);
+  }
+  if (nc > b->iters_cap) {
+    if (b->d_iters) cudaFree(b->d_iters);
+    b->d_iters = nullptr;
+    if (cudaMalloc(&b->d_iters, (size_t)nc * sizeof(long long)) != cudaSuccess)
+      return bfail(b, FS_ERR_OUT_OF_MEMORY, "batch: counter allocation failed");
+    b->iters_cap = nc;
+  }
+  if (nc > 0 && cudaMemset(b->d_iters, 0, (size_t)nc * sizeof(long long)) != cudaSuccess)
+    return bfail(b, FS_ERR_CUDA, "batch: counter reset failed");
+
   std::vector<int64_t> l0(n);
+  std::vector<StepSplit> split(n);
   cudaError_t e = cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal);
   if (e != cudaSuccess) return bfail(b, FS_ERR_CUDA, std::string("batch capture: ") + cudaGetErrorString(e));
   e = cudaEventRecord(b->fork, b->stream);
   int rc = e == cudaSuccess ? FS_OK : FS_ERR_CUDA;
+  auto member_err = [&](int i) {
+    Solver* s = &b->members[i]->s;
+    if (!s->err.empty()) b->err = "member " + std::to_string(i) + ": " + s->err;
+  };
+  // members outside a class: their whole captured step as one branch, joined
+  // at the end
   for (int i = 0; i < n && rc == FS_OK; i++) {
+    if (cls[i] >= 0) continue;
     Solver* s = &b->members[i]->s;
     std::swap(s->stream, s->own_stream);  // this member's branch
     if (cudaStreamWaitEvent(s->stream, b->fork, 0) != cudaSuccess) rc = FS_ERR_CUDA;
     l0[i] = s->launches;
     if (rc == FS_OK) rc = enqueue_step(s, dt[i], true);
     if (rc == FS_OK && cudaEventRecord(b->joins[i], s->stream) != cudaSuccess) rc = FS_ERR_CUDA;
-    if (rc == FS_OK && cudaStreamWaitEvent(b->stream, b->joins[i], 0) != cudaSuccess) rc = FS_ERR_CUDA;
     std::swap(s->stream, s->own_stream);
-    if (rc != FS_OK && !s->err.empty()) b->err = "member " + std::to_string(i) + ": " + s->err;
+    if (rc != FS_OK) member_err(i);
   }
+  // The classes one after another (measured: six size classes run together
+  // took twice the sum of their times alone).  Each class: the members' steps
+  // up to their loops as branches, the class loop on the class stream, then
+  // the members' remaining steps as branches.
+  for (int c = 0; c < nc && rc == FS_OK; c++) {
+    cudaStream_t cs = b->class_streams[c];
+    if (c > 0 && cudaEventRecord(b->fork, b->stream) != cudaSuccess) rc = FS_ERR_CUDA;  // after class c - 1
+    if (cudaStreamWaitEvent(cs, b->fork, 0) != cudaSuccess) rc = FS_ERR_CUDA;
+    for (int i : b->classes[c].idx) {
+      if (rc != FS_OK) break;
+      Solver* s = &b->members[i]->s;
+      std::swap(s->stream, s->own_stream);
+      if (cudaStreamWaitEvent(s->stream, b->fork, 0) != cudaSuccess) rc = FS_ERR_CUDA;
+      l0[i] = s->launches;
+      if (rc == FS_OK) rc = enqueue_step(s, dt[i], true, &split[i]);
+      if (rc == FS_OK && cudaEventRecord(b->joins[i], s->stream) != cudaSuccess) rc = FS_ERR_CUDA;
+      if (rc == FS_OK && cudaStreamWaitEvent(cs, b->joins[i], 0) != cudaSuccess) rc = FS_ERR_CUDA;
+      std::swap(s->stream, s->own_stream);
+      if (rc != FS_OK) member_err(i);
+    }
+    if (rc == FS_OK) rc = capture_class_loop(b, b->classes[c], cs, b->d_iters + c);
+    if (rc == FS_OK && cudaEventRecord(b->class_done[c], cs) != cudaSuccess) rc = FS_ERR_CUDA;
+    for (int i : b->classes[c].idx) {
+      if (rc != FS_OK) break;
+      Solver* s = &b->members[i]->s;
+      std::swap(s->stream, s->own_stream);
+      if (cudaStreamWaitEvent(s->stream, b->class_done[c], 0) != cudaSuccess) rc = FS_ERR_CUDA;
+      if (rc == FS_OK) rc = enqueue_step_back(s, dt[i], split[i]);
+      if (rc == FS_OK && cudaEventRecord(b->joins[i], s->stream) != cudaSuccess) rc = FS_ERR_CUDA;
+      if (rc == FS_OK && cudaStreamWaitEvent(b->stream, b->joins[i], 0) != cudaSuccess) rc = FS_ERR_CUDA;
+      std::swap(s->stream, s->own_stream);
+      if (rc != FS_OK) member_err(i);
+    }
+  }
+  for (int i = 0; i < n && rc == FS_OK; i++)
+    if (cls[i] < 0 && cudaStreamWaitEvent(b->stream, b->joins[i], 0) != cudaSuccess) rc = FS_ERR_CUDA;
   cudaGraph_t g = nullptr;
   e = cudaStreamEndCapture(b->stream, &g);
   if (rc != FS_OK) {
@@ -1316,13 +1513,17 @@ static int batch_build(fs_batch* b, const double* dt) {
   e = cudaGraphInstantiate(&b->exec, g, 0);
   cudaGraphDestroy(g);
   if (e != cudaSuccess) return bfail(b, FS_ERR_CUDA, std::string("batch instantiate: ") + cudaGetErrorString(e));
+  b->fixed_per_replay = nc;  // the class loops' initial condition kernels
   for (int i = 0; i < n; i++) {
     Solver* s = &b->members[i]->s;
     int64_t captured = s->launches - l0[i];
-    s->batch_launches_fixed = captured - (s->prm.pressure_tol > 0 ? s->graph_launches_body : 0);
+    const bool own_loop = cls[i] < 0 && s->prm.pressure_tol > 0;
+    s->batch_launches_fixed = captured - (own_loop ? s->graph_launches_body : 0);
+    s->in_class = cls[i] >= 0;
     s->launches = l0[i];  // counted when the graph runs
     s->batch_dirty = false;
   }
+  b->replays_at_build = b->replays;
   b->dts.assign(dt, dt + n);
   return FS_OK;
 }
@@ -1358,6 +1559,7 @@ FS_API int fs_batch_create(const fs_params* params, int32_t count, fs_batch** ou
   }
   cudaSetDevice(b->device);
   cudaError_t e = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&b->body_stream, cudaStreamNonBlocking);
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming);
   b->joins.assign(count, nullptr);
   for (int i = 0; i < count && e == cudaSuccess; i++) e = cudaEventCreateWithFlags(&b->joins[i], cudaEventDisableTiming);
@@ -1449,15 +1651,20 @@ FS_API int64_t fs_batch_launch_count(fs_batch* b) {
   if (!b) return 0;
   cudaSetDevice(b->device);
   cudaStreamSynchronize(b->stream);
-  int64_t n = 0;
+  int64_t n = b->launches_done + (b->replays - b->replays_at_build) * b->fixed_per_replay;
   for (fs_solver* h : b->members) {
     const Solver* s = &h->s;
     n += b->replays * s->batch_launches_fixed;
-    if (s->graph_launches_body > 0) {
+    if (!s->in_class && s->graph_launches_body > 0) {
       DevState d;
       if (cudaMemcpy(&d, s->dev, sizeof(DevState), cudaMemcpyDeviceToHost) == cudaSuccess)
         n += d.total_cycles * s->graph_launches_body;
     }
+  }
+  if (!b->classes.empty() && b->d_iters) {
+    std::vector<long long> it(b->classes.size());
+    if (cudaMemcpy(it.data(), b->d_iters, it.size() * sizeof(long long), cudaMemcpyDeviceToHost) == cudaSuccess)
+      for (size_t c = 0; c < it.size(); c++) n += it[c] * b->classes[c].body_launches;
   }
   return n;
 }

@@ -141,6 +141,7 @@ struct Solver {
   cudaStream_t own_stream = nullptr;
   bool batch_dirty = true;
   int64_t batch_launches_fixed = 0;
+  bool in_class = false;  // its batch runs the tolerance loop for its size class
   int64_t graph_launches_fixed = 0;    // kernels per replay outside the loop body
   int64_t graph_launches_body = 0;     // kernels per loop iteration
   int64_t graph_replays = 0;
@@ -178,6 +179,9 @@ void prof_end(Solver* s, int slot, cudaEvent_t a);
   } while (0)
 
 inline dim3 grid2d(int nx, int ny, dim3 b) { return dim3((nx + b.x - 1) / b.x, (ny + b.y - 1) / b.y); }
+
+// members of one batched launch (a size class of a batch; larger classes are split)
+constexpr int kClassMax = 64;
 
 // --------------------------------------------------------- kernel launchers
 // fs_advect.cu
@@ -237,6 +241,11 @@ void mg_vcycle(Solver* s);
 // double-float pressure (acc_h, acc_l) in place instead of writing lev[0].x2
 void mg_vcycle_fused(Solver* s, bool first_has_x, float* acc_h = nullptr, float* acc_l = nullptr);
 bool mg_fused_supported(const Solver* s);
+// batched refinement cycle of one size class of a batch (fs_multigrid.cu, fs_pressure.cu)
+int mg_vcycle_class(Solver* const* ms, int count, cudaStream_t st);
+void launch_refine_class(Solver* const* ms, int count, cudaStream_t st);
+void launch_cond_class(Solver* const* ms, int count, cudaStream_t st, cudaGraphConditionalHandle h, bool init,
+                       long long* iterations);
 
 // errors (fs_api.cu): message into the handle (or the thread's last error)
 int fail_status(Solver* s, int code, const std::string& msg);

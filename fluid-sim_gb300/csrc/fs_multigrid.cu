@@ -119,9 +119,9 @@ __device__ __forceinline__ void rb_half_smem(float* xs, const float* rs, int c, 
 // H = 2 * pre + 1.  xin == nullptr means the level starts from zero; otherwise
 // xin and xout must differ (the halo of a tile is another tile's interior).
 template <int T, int H>
-__global__ void __launch_bounds__(256) k_mg_down(const float* __restrict__ rhs, const float* __restrict__ xin,
-                                                 float* __restrict__ xout, float* __restrict__ crhs, int n,
-                                                 float h2, int pre, float w) {
+__device__ __forceinline__ void mg_down_body(const float* __restrict__ rhs, const float* __restrict__ xin,
+                                             float* __restrict__ xout, float* __restrict__ crhs, int n, float h2,
+                                             int pre, float w) {
   constexpr int R = T + 2 * H;
   using CK = Checker<R>;
   __shared__ float xs[CK::STRIDE + CK::N];
@@ -176,6 +176,13 @@ __global__ void __launch_bounds__(256) k_mg_down(const float* __restrict__ rhs, 
   }
 }
 
+template <int T, int H>
+__global__ void __launch_bounds__(256) k_mg_down(const float* __restrict__ rhs, const float* __restrict__ xin,
+                                                 float* __restrict__ xout, float* __restrict__ crhs, int n,
+                                                 float h2, int pre, float w) {
+  mg_down_body<T, H>(rhs, xin, xout, crhs, n, h2, pre, w);
+}
+
 // -------------------------------------------------------------------- up
 // H = 2 * post.  x += P(coarse) on the region, then the post sweeps.  xin and
 // xout must differ: the halo of a tile is another tile's interior.  With ACC
@@ -183,10 +190,9 @@ __global__ void __launch_bounds__(256) k_mg_down(const float* __restrict__ rhs, 
 // double-float pressure (ph, pl) in place instead of being written to xout:
 // each cell is read and written by its own tile only.
 template <int T, int H, bool ACC>
-__global__ void __launch_bounds__(256) k_mg_up(const float* __restrict__ rhs, const float* __restrict__ xin,
-                                               float* __restrict__ xout, const float* __restrict__ xc, int n,
-                                               float h2, int post, float* __restrict__ ph,
-                                               float* __restrict__ pl, float w) {
+__device__ __forceinline__ void mg_up_body(const float* __restrict__ rhs, const float* __restrict__ xin,
+                                           float* __restrict__ xout, const float* __restrict__ xc, int n, float h2,
+                                           int post, float* __restrict__ ph, float* __restrict__ pl, float w) {
   constexpr int R = T + 2 * H;
   using CK = Checker<R>;
   static_assert(T % 2 == 0 && H % 2 == 0, "the up kernel's region starts on an even index");
@@ -282,6 +288,14 @@ __global__ void __launch_bounds__(256) k_mg_up(const float* __restrict__ rhs, co
   }
 }
 
+template <int T, int H, bool ACC>
+__global__ void __launch_bounds__(256) k_mg_up(const float* __restrict__ rhs, const float* __restrict__ xin,
+                                               float* __restrict__ xout, const float* __restrict__ xc, int n,
+                                               float h2, int post, float* __restrict__ ph,
+                                               float* __restrict__ pl, float w) {
+  mg_up_body<T, H, ACC>(rhs, xin, xout, xc, n, h2, post, ph, pl, w);
+}
+
 // ---------------------------------------------------------------- bottom
 // Levels 0..count-1 of the bottom (each n <= 64), all in shared memory.  Per
 // level: x, rhs and, for odd n, a ping-pong partner (red-black on an odd
@@ -375,9 +389,9 @@ __device__ void bottom_prolong(float* sm, const BottomLevels& L, int l, Group G)
   G.sync();
 }
 
-__global__ void __launch_bounds__(1024) k_mg_bottom(const float* __restrict__ rhs_top, float* __restrict__ x_top,
-                                                    int has_x, BottomLevels L, int pre, int post, int coarse,
-                                                    float* __restrict__ acc_h, float* __restrict__ acc_l) {
+__device__ __forceinline__ void mg_bottom_body(const float* __restrict__ rhs_top, float* __restrict__ x_top,
+                                               int has_x, const BottomLevels& L, int pre, int post, int coarse,
+                                               float* __restrict__ acc_h, float* __restrict__ acc_l) {
   extern __shared__ float sm[];
   const int tid = threadIdx.x;
   const Group CTA{tid, (int)blockDim.x, false};
@@ -439,6 +453,12 @@ __global__ void __launch_bounds__(1024) k_mg_bottom(const float* __restrict__ rh
       }
     }
   }
+}
+
+__global__ void __launch_bounds__(1024) k_mg_bottom(const float* __restrict__ rhs_top, float* __restrict__ x_top,
+                                                    int has_x, BottomLevels L, int pre, int post, int coarse,
+                                                    float* __restrict__ acc_h, float* __restrict__ acc_l) {
+  mg_bottom_body(rhs_top, x_top, has_x, L, pre, post, coarse, acc_h, acc_l);
 }
 
 // ------------------------------------------------- bottom, power-of-two levels
@@ -545,9 +565,9 @@ __device__ void p2_cycle(float* const* X, float* const* R, const BottomH2& H, in
 }
 
 template <int N0>
-__global__ void __launch_bounds__(256) k_mg_bottom_p2(const float* __restrict__ rhs_top, float* __restrict__ x_top,
-                                                      int has_x, BottomH2 H, int pre, int post, int coarse,
-                                                      float* __restrict__ acc_h, float* __restrict__ acc_l) {
+__device__ __forceinline__ void mg_bottom_p2_body(const float* __restrict__ rhs_top, float* __restrict__ x_top,
+                                                  int has_x, const BottomH2& H, int pre, int post, int coarse,
+                                                  float* __restrict__ acc_h, float* __restrict__ acc_l) {
   constexpr int L = ilog2<N0>() - 2;  // levels N0 .. 8
   constexpr int SZ = (N0 * N0 * 4 - 64) / 3 + 64;  // N0^2 + N0^2/4 + ... + 64
   __shared__ float sx[SZ], sr[SZ];
@@ -584,6 +604,84 @@ __global__ void __launch_bounds__(256) k_mg_bottom_p2(const float* __restrict__ 
       x_top[k] = e;
     }
   }
+}
+
+template <int N0>
+__global__ void __launch_bounds__(256) k_mg_bottom_p2(const float* __restrict__ rhs_top, float* __restrict__ x_top,
+                                                      int has_x, BottomH2 H, int pre, int post, int coarse,
+                                                      float* __restrict__ acc_h, float* __restrict__ acc_l) {
+  mg_bottom_p2_body<N0>(rhs_top, x_top, has_x, H, pre, post, coarse, acc_h, acc_l);
+}
+
+// ------------------------------------------------- batched (one size class)
+// The members of a batch with the same grid and multigrid settings run each
+// kernel of their refinement cycles as one launch, member = blockIdx.z, with
+// their pointers in a table passed by value among the kernel parameters.  A
+// member whose tolerance loop has ended (the per-member condition the
+// class-wide loop kernel keeps in its DevState) leaves the launch at once, so
+// every member runs exactly the cycles it would run alone.
+__device__ __forceinline__ bool member_active(const DevState* st, int max_cycles) {
+  return !st->converged && !st->nonfinite && st->cycles < max_cycles;
+}
+
+struct DownTab {
+  struct {
+    const float* rhs;
+    float* xout;
+    float* crhs;
+    const DevState* st;
+  } m[kClassMax];
+};
+struct UpTab {
+  struct {
+    const float* rhs;
+    const float* xin;
+    float* xout;
+    const float* xc;
+    float* ph;
+    float* pl;
+    const DevState* st;
+  } m[kClassMax];
+};
+struct BottomTab {
+  struct {
+    const float* rhs;
+    float* x;
+    float* acc_h;
+    float* acc_l;
+    const DevState* st;
+  } m[kClassMax];
+};
+
+template <int T, int H>
+__global__ void __launch_bounds__(256) k_mg_down_class(const DownTab tab, int n, float h2, int pre, float w,
+                                                       int max_cycles) {
+  const auto& a = tab.m[blockIdx.z];
+  if (!member_active(a.st, max_cycles)) return;
+  mg_down_body<T, H>(a.rhs, nullptr, a.xout, a.crhs, n, h2, pre, w);
+}
+
+template <int T, int H, bool ACC>
+__global__ void __launch_bounds__(256) k_mg_up_class(const UpTab tab, int n, float h2, int post, float w,
+                                                     int max_cycles) {
+  const auto& a = tab.m[blockIdx.z];
+  if (!member_active(a.st, max_cycles)) return;
+  mg_up_body<T, H, ACC>(a.rhs, a.xin, a.xout, a.xc, n, h2, post, a.ph, a.pl, w);
+}
+
+template <int N0>
+__global__ void __launch_bounds__(256) k_mg_bottom_p2_class(const BottomTab tab, BottomH2 H, int pre, int post,
+                                                            int coarse, int max_cycles) {
+  const auto& a = tab.m[blockIdx.z];
+  if (!member_active(a.st, max_cycles)) return;
+  mg_bottom_p2_body<N0>(a.rhs, a.x, 0, H, pre, post, coarse, a.acc_h, a.acc_l);
+}
+
+__global__ void __launch_bounds__(1024) k_mg_bottom_class(const BottomTab tab, BottomLevels L, int pre, int post,
+                                                          int coarse, int max_cycles) {
+  const auto& a = tab.m[blockIdx.z];
+  if (!member_active(a.st, max_cycles)) return;
+  mg_bottom_body(a.rhs, a.x, 0, L, pre, post, coarse, a.acc_h, a.acc_l);
 }
 
 // ------------------------------------------------------------------ host
@@ -776,4 +874,120 @@ void mg_vcycle_fused(Solver* s, bool first_has_x, float* acc_h, float* acc_l) {
   }
 }
 
+
+// ------------------------------------------------------- batched V-cycle
+// mg_vcycle_fused(s, false, ph, pl) of a MIXED refinement cycle for every
+// member of one size class (same grid and multigrid settings), one launch per
+// level and phase; the level pointers of each member move exactly as in the
+// single-solver cycle.  Returns the number of launches it recorded.
+template <int T, int H>
+static void down_class_t(Solver* const* ms, int count, int l, cudaStream_t st) {
+  const Level& L0 = ms[0]->lev[l];
+  DownTab tab{};
+  for (int i = 0; i < count; i++) {
+    Level& L = ms[i]->lev[l];
+    tab.m[i] = {L.rhs, L.x, ms[i]->lev[l + 1].rhs, ms[i]->dev};
+  }
+  dim3 grid((L0.n + T - 1) / T, (L0.n + T - 1) / T, count);
+  k_mg_down_class<T, H><<<grid, kTileBlock, 0, st>>>(tab, L0.n, L0.h2, ms[0]->prm.mg_pre_smooth,
+                                                      (float)ms[0]->prm.relax, ms[0]->prm.max_cycles);
+}
+
+template <int H>
+static void down_class(Solver* const* ms, int count, int l, cudaStream_t st) {
+  switch (tile_for(ms[0]->lev[l].n)) {
+    case 64: down_class_t<64, H>(ms, count, l, st); break;
+    case 32: down_class_t<32, H>(ms, count, l, st); break;
+    default: down_class_t<16, H>(ms, count, l, st); break;
+  }
+}
+
+template <int T, int H, bool ACC>
+static void up_class_t(Solver* const* ms, int count, int l, cudaStream_t st) {
+  const Level& L0 = ms[0]->lev[l];
+  UpTab tab{};
+  for (int i = 0; i < count; i++) {
+    Solver* s = ms[i];
+    Level& L = s->lev[l];
+    tab.m[i] = {L.rhs, L.x, ACC ? nullptr : L.x2, s->lev[l + 1].x, ACC ? s->ph : nullptr, ACC ? s->pl : nullptr,
+                s->dev};
+    if (!ACC) std::swap(L.x, L.x2);
+  }
+  constexpr size_t smem = up_smem_bytes<T, H>();
+  if constexpr (smem > 48 * 1024) {
+    static std::atomic<uint64_t> attr_set{0};
+    const uint64_t bit = 1ull << (ms[0]->prm.device & 63);
+    if (!(attr_set.load() & bit) &&
+        cudaFuncSetAttribute(k_mg_up_class<T, H, ACC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) ==
+            cudaSuccess)
+      attr_set.fetch_or(bit);
+  }
+  dim3 grid((L0.n + T - 1) / T, (L0.n + T - 1) / T, count);
+  k_mg_up_class<T, H, ACC><<<grid, kTileBlock, smem, st>>>(tab, L0.n, L0.h2, ms[0]->prm.mg_post_smooth,
+                                                            (float)ms[0]->prm.relax, ms[0]->prm.max_cycles);
+}
+
+template <int H>
+static void up_class(Solver* const* ms, int count, int l, cudaStream_t st) {
+  const bool acc = l == 0;
+  switch (tile_for(ms[0]->lev[l].n)) {
+    case 64: acc ? up_class_t<64, H, true>(ms, count, l, st) : up_class_t<64, H, false>(ms, count, l, st); break;
+    case 32: acc ? up_class_t<32, H, true>(ms, count, l, st) : up_class_t<32, H, false>(ms, count, l, st); break;
+    default: acc ? up_class_t<16, H, true>(ms, count, l, st) : up_class_t<16, H, false>(ms, count, l, st); break;
+  }
+}
+
+int mg_vcycle_class(Solver* const* ms, int count, cudaStream_t st) {
+  Solver* s0 = ms[0];
+  for (int i = 0; i < count; i++) {  // level 0 is the correction of the refinement cycle
+    ms[i]->lev[0].x = ms[i]->e32;
+    ms[i]->lev[0].x2 = ms[i]->e32b;
+  }
+  const std::vector<Level>& L = s0->lev;
+  const int lb = bottom_first_level(s0);
+  const fs_params& P = s0->prm;
+  int launches = 0;
+  for (int l = 0; l < lb; l++, launches++) {
+    switch (P.mg_pre_smooth) {
+      case 1: down_class<3>(ms, count, l, st); break;
+      case 2: down_class<5>(ms, count, l, st); break;
+      default: down_class<7>(ms, count, l, st); break;
+    }
+  }
+  const int nb = L[lb].n;
+  BottomTab tab{};
+  for (int i = 0; i < count; i++) {
+    Solver* s = ms[i];
+    tab.m[i] = {s->lev[lb].rhs, s->lev[lb].x, lb == 0 ? s->ph : nullptr, lb == 0 ? s->pl : nullptr, s->dev};
+  }
+  const bool p2 = (nb & (nb - 1)) == 0 && nb >= 8 && nb <= 64 && L.back().n == 8 &&
+                  (int)L.size() - lb == ilog2_host(nb) - 2;
+  if (p2) {
+    BottomH2 H{};
+    for (int k = 0; k < (int)L.size() - lb && k < 4; k++) H.h2[k] = L[lb + k].h2;
+    H.w = (float)P.relax;
+    const dim3 grid(1, 1, count);
+    switch (nb) {
+      case 64: k_mg_bottom_p2_class<64><<<grid, 256, 0, st>>>(tab, H, P.mg_pre_smooth, P.mg_post_smooth, P.mg_coarse_sweeps, P.max_cycles); break;
+      case 32: k_mg_bottom_p2_class<32><<<grid, 256, 0, st>>>(tab, H, P.mg_pre_smooth, P.mg_post_smooth, P.mg_coarse_sweeps, P.max_cycles); break;
+      case 16: k_mg_bottom_p2_class<16><<<grid, 256, 0, st>>>(tab, H, P.mg_pre_smooth, P.mg_post_smooth, P.mg_coarse_sweeps, P.max_cycles); break;
+      default: k_mg_bottom_p2_class<8><<<grid, 256, 0, st>>>(tab, H, P.mg_pre_smooth, P.mg_post_smooth, P.mg_coarse_sweeps, P.max_cycles); break;
+    }
+  } else {
+    BottomLevels B;
+    const size_t smem = bottom_layout(s0, &B);
+    const int threads = std::min(1024, std::max(32, ((nb * nb / 4 + 31) / 32) * 32));
+    k_mg_bottom_class<<<dim3(1, 1, count), threads, smem, st>>>(tab, B, P.mg_pre_smooth, P.mg_post_smooth,
+                                                                 P.mg_coarse_sweeps, P.max_cycles);
+  }
+  launches++;
+  for (int l = lb - 1; l >= 0; l--, launches++) {
+    switch (P.mg_post_smooth) {
+      case 1: up_class<2>(ms, count, l, st); break;
+      case 2: up_class<4>(ms, count, l, st); break;
+      default: up_class<6>(ms, count, l, st); break;
+    }
+  }
+  return launches;
+}
 }  // namespace fs

@@ -381,10 +381,10 @@ __device__ __forceinline__ float residual_df(df d, df pc, df pl, df pr, df pb, d
 }
 
 // r = d - lap(p) (or r = d when zero_p); r32 = (float) r; max|r| reduced
-__global__ void __launch_bounds__(256)
-    k_refine_init(const float* __restrict__ dh, const float* __restrict__ dl, const float* __restrict__ ph,
-                  const float* __restrict__ pl, float* __restrict__ r32, int nx, int ny, LapScale ks,
-                  int zero_p, RedCtx ctx) {
+__device__ __forceinline__ void refine_init_body(const float* __restrict__ dh, const float* __restrict__ dl,
+                                                 const float* __restrict__ ph, const float* __restrict__ pl,
+                                                 float* __restrict__ r32, int nx, int ny, const LapScale& ks,
+                                                 int zero_p, const RedCtx& ctx) {
   float m = 0.f;
   FOR_RED_TILES(nx, ny) {
     int i = tx * 32 + threadIdx.x, j = ty * 8 + threadIdx.y;
@@ -409,13 +409,21 @@ __global__ void __launch_bounds__(256)
   block_max_finish(m, ctx);
 }
 
+__global__ void __launch_bounds__(256)
+    k_refine_init(const float* __restrict__ dh, const float* __restrict__ dl, const float* __restrict__ ph,
+                  const float* __restrict__ pl, float* __restrict__ r32, int nx, int ny, LapScale ks,
+                  int zero_p, RedCtx ctx) {
+  refine_init_body(dh, dl, ph, pl, r32, nx, ny, ks, zero_p, ctx);
+}
+
 // The same residual, four consecutive cells per thread (nx a multiple of 4):
 // float4 loads of the three pressure rows, the left / right neighbours of the
 // group from the adjacent words, so each cell costs ~1/3 of the loads and
 // index arithmetic of the one-cell form.  Same arithmetic, same results.
-__global__ void __launch_bounds__(256)
-    k_refine_init4(const float* __restrict__ dh, const float* __restrict__ dl, const float* __restrict__ ph,
-                   const float* __restrict__ pl, float* __restrict__ r32, int nx, int ny, LapScale ks, RedCtx ctx) {
+__device__ __forceinline__ void refine_init4_body(const float* __restrict__ dh, const float* __restrict__ dl,
+                                                  const float* __restrict__ ph, const float* __restrict__ pl,
+                                                  float* __restrict__ r32, int nx, int ny, const LapScale& ks,
+                                                  const RedCtx& ctx) {
   float m = 0.f;
   const int nq = nx >> 2;  // quads per row
   // tiles of 32 quads x 8 rows walked by the capped 2-D grid
@@ -446,6 +454,12 @@ __global__ void __launch_bounds__(256)
       m = fmaxf(fmaxf(m, fmaxf(absnanf(out.x), absnanf(out.y))), fmaxf(absnanf(out.z), absnanf(out.w)));
     }
   block_max_finish(m, ctx);
+}
+
+__global__ void __launch_bounds__(256)
+    k_refine_init4(const float* __restrict__ dh, const float* __restrict__ dl, const float* __restrict__ ph,
+                   const float* __restrict__ pl, float* __restrict__ r32, int nx, int ny, LapScale ks, RedCtx ctx) {
+  refine_init4_body(dh, dl, ph, pl, r32, nx, ny, ks, ctx);
 }
 
 // p' = p + e; r = d - lap(p') in df; r32 = (float) r; max|r| reduced
@@ -584,6 +598,93 @@ void launch_cond_step(Solver* s, cudaGraphConditionalHandle h, bool graph) {
 }
 void launch_step_finish(Solver* s, double dt) {
   FS_LAUNCH(s, "step_finish", 0.0, k_step_finish<<<1, 1, 0, s->stream>>>(s->dev, dt));
+}
+
+// ------------------------------------------- batched refinement bookkeeping
+// One size class of a batch (see fs_multigrid.cu): the refinement residual of
+// every member still in its loop as one launch (member = blockIdx.z, each with
+// its own reduction), and one kernel that does k_cond's bookkeeping for every
+// member and sets the class loop's condition to "any member continues".
+__device__ __forceinline__ bool member_in_loop(const DevState* st, int max_cycles) {
+  return !st->converged && !st->nonfinite && st->cycles < max_cycles;
+}
+
+struct RefineTab {
+  struct {
+    const float* dh;
+    const float* dl;
+    const float* ph;
+    const float* pl;
+    float* r32;
+    RedCtx ctx;
+    const DevState* st;
+  } m[kClassMax];
+};
+
+struct CondTab {
+  struct {
+    const double* red;
+    DevState* st;
+    double tol;
+  } m[kClassMax];
+};
+
+__global__ void __launch_bounds__(256) k_refine_class(const RefineTab tab, int nx, int ny, LapScale ks,
+                                                      int max_cycles, int quad) {
+  const auto& a = tab.m[blockIdx.z];
+  if (!member_in_loop(a.st, max_cycles)) return;
+  if (quad) refine_init4_body(a.dh, a.dl, a.ph, a.pl, a.r32, nx, ny, ks, a.ctx);
+  else refine_init_body(a.dh, a.dl, a.ph, a.pl, a.r32, nx, ny, ks, 0, a.ctx);
+}
+
+// one block of kClassMax threads; init = 1 before the loop (the members' own
+// k_cond has set their statistics), 0 after each cycle
+__global__ void __launch_bounds__(kClassMax) k_cond_class(const CondTab tab, int count, int max_cycles,
+                                                          cudaGraphConditionalHandle h, int init,
+                                                          long long* iterations) {
+  const int z = threadIdx.x;
+  int again = 0;
+  if (z < count) {
+    DevState* st = tab.m[z].st;
+    if (init) {
+      again = member_in_loop(st, max_cycles);
+    } else if (member_in_loop(st, max_cycles)) {  // this member ran the cycle
+      const double m = tab.m[z].red[0];
+      st->cycles += 1;
+      st->total_cycles += 1;
+      st->res_max = m;
+      const bool finite = isfinite(m);
+      st->nonfinite = finite ? 0 : 1;
+      st->converged = (finite && m <= tab.m[z].tol) ? 1 : 0;
+      again = finite && m > tab.m[z].tol && st->cycles < max_cycles;
+    }
+  }
+  again = __syncthreads_or(again);
+  if (threadIdx.x == 0) {
+    if (!init) *iterations += 1;
+    cudaGraphSetConditional(h, again ? 1u : 0u);
+  }
+}
+
+void launch_refine_class(Solver* const* ms, int count, cudaStream_t st) {
+  Solver* s0 = ms[0];
+  const Grid& g = s0->g;
+  RefineTab tab{};
+  for (int i = 0; i < count; i++) {
+    Solver* s = ms[i];
+    tab.m[i] = {s->dh, s->dl, s->ph, s->pl, s->r32, red_ctx(s, s->red_out), s->dev};
+  }
+  const bool quad = g.nx % 4 == 0;
+  dim3 grid = quad ? red_grid2(g.nx / 4, g.ny) : red_grid2(g.nx, g.ny);
+  grid.z = count;
+  k_refine_class<<<grid, kBlock, 0, st>>>(tab, g.nx, g.ny, lap_scale(g), s0->prm.max_cycles, quad ? 1 : 0);
+}
+
+void launch_cond_class(Solver* const* ms, int count, cudaStream_t st, cudaGraphConditionalHandle h, bool init,
+                       long long* iterations) {
+  CondTab tab{};
+  for (int i = 0; i < count; i++) tab.m[i] = {ms[i]->red_out, ms[i]->dev, ms[i]->prm.pressure_tol};
+  k_cond_class<<<1, kClassMax, 0, st>>>(tab, count, ms[0]->prm.max_cycles, h, init ? 1 : 0, iterations);
 }
 
 // ---------------------------------------------------------------- conversion
