@@ -461,13 +461,14 @@ __global__ void __launch_bounds__(1024) k_mg_bottom(const float* __restrict__ rh
   mg_bottom_body(rhs_top, x_top, has_x, L, pre, post, coarse, acc_h, acc_l);
 }
 
-// ------------------------------------------------- bottom, power-of-two levels
-// The common case (n a power of two, coarsest level 8): the bottom levels are
-// N0, N0/2, ..., 8 with N0 <= 64, all sizes known at compile time, so cell
-// indices are shifts and masks.  Levels >= 32 run on the whole CTA (256
-// threads), levels <= 16 -- including the coarse sweeps -- on warp 0 alone,
-// where one lane updates one cell of the 8x8 level per half-sweep.  Same
-// arithmetic (fs_stencil.cuh) and order as the generic kernel above.
+// ------------------------------------------------ bottom, compile-time chains
+// The common cases: the bottom levels are N0, N0/2, ..., NMIN with every size
+// but the coarsest even and N0 <= 64 -- the power-of-two chains down to 8 and
+// the 48 -> 24 -> 12 chain of grids of 3 * 2^k cells -- all sizes known at
+// compile time, so cell indices use constant divisors.  Levels >= 32 run on
+// the whole CTA (256 threads), levels <= 16 -- including the coarse sweeps --
+// on warp 0 alone.  Same arithmetic (fs_stencil.cuh) and order as the generic
+// kernel above.
 struct BottomH2 {
   float h2[4];
   float w;  // relaxation factor of every sweep
@@ -476,6 +477,15 @@ struct BottomH2 {
 template <int N>
 constexpr int ilog2() {
   return N <= 1 ? 0 : 1 + ilog2<N / 2>();
+}
+// levels and floats of the chain N0, N0/2, ..., NMIN
+template <int N0, int NMIN>
+constexpr int chain_levels() {
+  return N0 == NMIN ? 1 : 1 + chain_levels<N0 / 2, NMIN>();
+}
+template <int N0, int NMIN>
+constexpr int chain_floats() {
+  return N0 == NMIN ? N0 * N0 : N0 * N0 + chain_floats<N0 / 2, NMIN>();
 }
 
 template <int N, bool WARP>
@@ -486,18 +496,18 @@ __device__ __forceinline__ void p2_sync() {
 
 template <int N, bool WARP>
 __device__ void p2_smooth(float* x, const float* r, float h2, int sweeps, float w) {
-  constexpr int HALF = N / 2, LH = ilog2<HALF>();
+  constexpr int HALF = N / 2;
   const int tid = WARP ? (int)(threadIdx.x & 31) : (int)threadIdx.x;
   const int nthr = WARP ? 32 : (int)blockDim.x;
   for (int s = 0; s < 2 * sweeps; s++) {
     const int c = s & 1;
     for (int idx = tid; idx < N * HALF; idx += nthr) {
-      int j = idx >> LH, m = idx & (HALF - 1);
-      int i = 2 * m + ((j + c) & 1);
-      int row = j * N, k = row + i;
-      int rm = ((j - 1) & (N - 1)) * N, rp = ((j + 1) & (N - 1)) * N;
-      x[k] = gs_update(x[k], x[row + ((i - 1) & (N - 1))], x[row + ((i + 1) & (N - 1))], x[rm + i], x[rp + i], r[k],
-                       h2, w);
+      const int j = idx / HALF, m = idx - j * HALF;
+      const int i = 2 * m + ((j + c) & 1);
+      const int row = j * N, k = row + i;
+      const int rm = (j == 0 ? N - 1 : j - 1) * N, rp = (j + 1 == N ? 0 : j + 1) * N;
+      const int im = i == 0 ? N - 1 : i - 1, ip = i + 1 == N ? 0 : i + 1;
+      x[k] = gs_update(x[k], x[row + im], x[row + ip], x[rm + i], x[rp + i], r[k], h2, w);
     }
     p2_sync<N, WARP>();
   }
@@ -506,19 +516,19 @@ __device__ void p2_smooth(float* x, const float* r, float h2, int sweeps, float 
 // residual of level N restricted into (cr, cx = 0) of level N/2
 template <int N, bool WARP>
 __device__ void p2_restrict(const float* x, const float* r, float h2, float* cr, float* cx) {
-  constexpr int NC = N / 2, LC = ilog2<NC>();
+  constexpr int NC = N / 2;
   const int tid = WARP ? (int)(threadIdx.x & 31) : (int)threadIdx.x;
   const int nthr = WARP ? 32 : (int)blockDim.x;
   for (int k = tid; k < NC * NC; k += nthr) {
-    int cj = k >> LC, ci = k & (NC - 1);
+    const int cj = k / NC, ci = k - cj * NC;
     float r4[4];
 #pragma unroll
     for (int q = 0; q < 4; q++) {
-      int i = 2 * ci + (q & 1), j = 2 * cj + (q >> 1);
-      int row = j * N;
-      int rm = ((j - 1) & (N - 1)) * N, rp = ((j + 1) & (N - 1)) * N;
-      r4[q] = residual_at(x[row + i], x[row + ((i - 1) & (N - 1))], x[row + ((i + 1) & (N - 1))], x[rm + i], x[rp + i],
-                          r[row + i], h2);
+      const int i = 2 * ci + (q & 1), j = 2 * cj + (q >> 1);
+      const int row = j * N;
+      const int rm = (j == 0 ? N - 1 : j - 1) * N, rp = (j + 1 == N ? 0 : j + 1) * N;
+      const int im = i == 0 ? N - 1 : i - 1, ip = i + 1 == N ? 0 : i + 1;
+      r4[q] = residual_at(x[row + i], x[row + im], x[row + ip], x[rm + i], x[rp + i], r[row + i], h2);
     }
     cr[k] = restrict4(r4[0], r4[1], r4[2], r4[3]);
     cx[k] = 0.f;
@@ -529,47 +539,50 @@ __device__ void p2_restrict(const float* x, const float* r, float h2, float* cr,
 // x (level N) += bilinear prolongation of c (level N/2)
 template <int N, bool WARP>
 __device__ void p2_prolong(float* x, const float* c) {
-  constexpr int NC = N / 2, LN = ilog2<N>();
+  constexpr int NC = N / 2;
   const int tid = WARP ? (int)(threadIdx.x & 31) : (int)threadIdx.x;
   const int nthr = WARP ? 32 : (int)blockDim.x;
   for (int k = tid; k < N * N; k += nthr) {
-    int j = k >> LN, i = k & (N - 1);
-    int ci0 = (i & 1) ? (i >> 1) : (i >> 1) - 1;
-    int cj0 = (j & 1) ? (j >> 1) : (j >> 1) - 1;
-    float fx = (i & 1) ? 0.25f : 0.75f, fy = (j & 1) ? 0.25f : 0.75f;
-    int x0 = ci0 & (NC - 1), x1 = (ci0 + 1) & (NC - 1), y0 = (cj0 & (NC - 1)) * NC, y1 = ((cj0 + 1) & (NC - 1)) * NC;
+    const int j = k / N, i = k - j * N;
+    const int ci0 = (i & 1) ? (i >> 1) : (i >> 1) - 1;
+    const int cj0 = (j & 1) ? (j >> 1) : (j >> 1) - 1;
+    const float fx = (i & 1) ? 0.25f : 0.75f, fy = (j & 1) ? 0.25f : 0.75f;
+    const int x0 = ci0 < 0 ? ci0 + NC : ci0, x1 = ci0 + 1 >= NC ? ci0 + 1 - NC : ci0 + 1;
+    const int y0 = (cj0 < 0 ? cj0 + NC : cj0) * NC, y1 = (cj0 + 1 >= NC ? cj0 + 1 - NC : cj0 + 1) * NC;
     x[k] = __fadd_rn(x[k], prolong_val(c[y0 + x0], c[y0 + x1], c[y1 + x0], c[y1 + x1], fx, fy));
   }
   p2_sync<N, WARP>();
 }
 
-// sub-cycle from level N down to 8 and back; levels <= 16 are called by warp 0 only
-template <int N>
+// sub-cycle from level N down to NMIN and back; levels <= 16 are called by warp 0 only
+template <int N, int NMIN>
 __device__ void p2_cycle(float* const* X, float* const* R, const BottomH2& H, int lvl, int pre, int post,
                          int coarse) {
   constexpr bool W = N <= 16;
-  if constexpr (N == 8) {
-    p2_smooth<8, true>(X[lvl], R[lvl], H.h2[lvl], coarse, H.w);
+  if constexpr (N == NMIN) {
+    p2_smooth<N, W>(X[lvl], R[lvl], H.h2[lvl], coarse, H.w);
   } else {
+    static_assert(N % 2 == 0, "every level above the coarsest is even");
     p2_smooth<N, W>(X[lvl], R[lvl], H.h2[lvl], pre, H.w);
     p2_restrict<N, W>(X[lvl], R[lvl], H.h2[lvl], R[lvl + 1], X[lvl + 1]);
     if constexpr (!W && N / 2 <= 16) {
-      if (threadIdx.x < 32) p2_cycle<N / 2>(X, R, H, lvl + 1, pre, post, coarse);
+      if (threadIdx.x < 32) p2_cycle<N / 2, NMIN>(X, R, H, lvl + 1, pre, post, coarse);
       __syncthreads();
     } else {
-      p2_cycle<N / 2>(X, R, H, lvl + 1, pre, post, coarse);
+      p2_cycle<N / 2, NMIN>(X, R, H, lvl + 1, pre, post, coarse);
     }
     p2_prolong<N, W>(X[lvl], X[lvl + 1]);
     p2_smooth<N, W>(X[lvl], R[lvl], H.h2[lvl], post, H.w);
   }
 }
 
-template <int N0>
-__device__ __forceinline__ void mg_bottom_p2_body(const float* __restrict__ rhs_top, float* __restrict__ x_top,
-                                                  int has_x, const BottomH2& H, int pre, int post, int coarse,
-                                                  float* __restrict__ acc_h, float* __restrict__ acc_l) {
-  constexpr int L = ilog2<N0>() - 2;  // levels N0 .. 8
-  constexpr int SZ = (N0 * N0 * 4 - 64) / 3 + 64;  // N0^2 + N0^2/4 + ... + 64
+template <int N0, int NMIN>
+__device__ __forceinline__ void mg_bottom_chain_body(const float* __restrict__ rhs_top, float* __restrict__ x_top,
+                                                     int has_x, const BottomH2& H, int pre, int post, int coarse,
+                                                     float* __restrict__ acc_h, float* __restrict__ acc_l) {
+  constexpr int L = chain_levels<N0, NMIN>();
+  constexpr int SZ = chain_floats<N0, NMIN>();
+  static_assert(L <= 4 && NMIN % 2 == 0, "chains of at most four even levels");
   __shared__ float sx[SZ], sr[SZ];
   float* X[4];
   float* R[4];
@@ -589,10 +602,10 @@ __device__ __forceinline__ void mg_bottom_p2_body(const float* __restrict__ rhs_
   }
   __syncthreads();
   if constexpr (N0 <= 16) {
-    if (tid < 32) p2_cycle<N0>(X, R, H, 0, pre, post, coarse);
+    if (tid < 32) p2_cycle<N0, NMIN>(X, R, H, 0, pre, post, coarse);
     __syncthreads();
   } else {
-    p2_cycle<N0>(X, R, H, 0, pre, post, coarse);
+    p2_cycle<N0, NMIN>(X, R, H, 0, pre, post, coarse);
   }
   for (int k = tid; k < N0 * N0; k += blockDim.x) {
     float e = X[0][k];
@@ -606,11 +619,12 @@ __device__ __forceinline__ void mg_bottom_p2_body(const float* __restrict__ rhs_
   }
 }
 
-template <int N0>
-__global__ void __launch_bounds__(256) k_mg_bottom_p2(const float* __restrict__ rhs_top, float* __restrict__ x_top,
-                                                      int has_x, BottomH2 H, int pre, int post, int coarse,
-                                                      float* __restrict__ acc_h, float* __restrict__ acc_l) {
-  mg_bottom_p2_body<N0>(rhs_top, x_top, has_x, H, pre, post, coarse, acc_h, acc_l);
+template <int N0, int NMIN>
+__global__ void __launch_bounds__(256) k_mg_bottom_chain(const float* __restrict__ rhs_top,
+                                                         float* __restrict__ x_top, int has_x, BottomH2 H, int pre,
+                                                         int post, int coarse, float* __restrict__ acc_h,
+                                                         float* __restrict__ acc_l) {
+  mg_bottom_chain_body<N0, NMIN>(rhs_top, x_top, has_x, H, pre, post, coarse, acc_h, acc_l);
 }
 
 // ------------------------------------------------- batched (one size class)
@@ -669,12 +683,12 @@ __global__ void __launch_bounds__(256) k_mg_up_class(const UpTab tab, int n, flo
   mg_up_body<T, H, ACC>(a.rhs, a.xin, a.xout, a.xc, n, h2, post, a.ph, a.pl, w);
 }
 
-template <int N0>
-__global__ void __launch_bounds__(256) k_mg_bottom_p2_class(const BottomTab tab, BottomH2 H, int pre, int post,
-                                                            int coarse, int max_cycles) {
+template <int N0, int NMIN>
+__global__ void __launch_bounds__(256) k_mg_bottom_chain_class(const BottomTab tab, BottomH2 H, int pre, int post,
+                                                               int coarse, int max_cycles) {
   const auto& a = tab.m[blockIdx.z];
   if (!member_active(a.st, max_cycles)) return;
-  mg_bottom_p2_body<N0>(a.rhs, a.x, 0, H, pre, post, coarse, a.acc_h, a.acc_l);
+  mg_bottom_chain_body<N0, NMIN>(a.rhs, a.x, 0, H, pre, post, coarse, a.acc_h, a.acc_l);
 }
 
 __global__ void __launch_bounds__(1024) k_mg_bottom_class(const BottomTab tab, BottomLevels L, int pre, int post,
@@ -775,12 +789,6 @@ static void up(Solver* s, Level& L, const Level& C, float* acc_h, float* acc_l) 
   }
 }
 
-static int ilog2_host(int n) {
-  int l = 0;
-  while (n > 1) { n >>= 1; l++; }
-  return l;
-}
-
 // first level of the bottom solve: every level from there down is <= 64
 int bottom_first_level(const Solver* s) {
   int nl = (int)s->lev.size();
@@ -823,6 +831,26 @@ static size_t bottom_layout(const Solver* s, BottomLevels* B) {
   return (size_t)off * sizeof(float);
 }
 
+// The compile-time chain kernel for the bottom levels from lb, identified by
+// its first size (64, 32, 16, 8 down to 8; 48, 24, 12 down to 12), or 0 when
+// the levels form another chain (odd sizes, other coarsest sizes).
+static int bottom_chain(const Solver* s, int lb) {
+  const std::vector<Level>& L = s->lev;
+  for (size_t k = lb; k + 1 < L.size(); k++)
+    if ((L[k].n & 1) || L[k + 1].n * 2 != L[k].n) return 0;
+  const int nb = L[lb].n, nmin = L.back().n;
+  if (nmin == 8 && (nb == 64 || nb == 32 || nb == 16 || nb == 8)) return nb;
+  if (nmin == 12 && (nb == 48 || nb == 24 || nb == 12)) return nb;
+  return 0;
+}
+
+static BottomH2 bottom_h2(const Solver* s, int lb) {
+  BottomH2 H{};
+  for (int k = 0; k < (int)s->lev.size() - lb && k < 4; k++) H.h2[k] = s->lev[lb + k].h2;
+  H.w = (float)s->prm.relax;
+  return H;
+}
+
 void mg_vcycle_fused(Solver* s, bool first_has_x, float* acc_h, float* acc_l) {
   std::vector<Level>& L = s->lev;
   const int lb = bottom_first_level(s);
@@ -840,21 +868,25 @@ void mg_vcycle_fused(Solver* s, bool first_has_x, float* acc_h, float* acc_l) {
   float* bah = lb == 0 ? acc_h : nullptr;
   float* bal = lb == 0 ? acc_l : nullptr;
   double bytes = (double)nb * nb * (hx ? 12.0 : 8.0);
-  // power-of-two bottom N0 .. 8 (N0 <= 64): the compile-time-size kernel
-  bool p2 = (nb & (nb - 1)) == 0 && nb >= 8 && nb <= 64 && L.back().n == 8 &&
-            (int)L.size() - lb == ilog2_host(nb) - 2;
-  if (p2) {
-    BottomH2 H{};
-    for (int k = 0; k < (int)L.size() - lb && k < 4; k++) H.h2[k] = L[lb + k].h2;
-    H.w = (float)P.relax;
-#define FS_P2(N0)                                                                                               FS_LAUNCH(s, "mg_bottom", bytes,                                                                                        k_mg_bottom_p2<N0><<<1, 256, 0, s->stream>>>(L[lb].rhs, L[lb].x, hx ? 1 : 0, H, P.mg_pre_smooth,                                                           P.mg_post_smooth, P.mg_coarse_sweeps, bah, bal))
-    switch (nb) {
-      case 64: FS_P2(64); break;
-      case 32: FS_P2(32); break;
-      case 16: FS_P2(16); break;
-      default: FS_P2(8); break;
+  // a chain of levels known at compile time: the specialised kernel
+  const int chain = bottom_chain(s, lb);
+  if (chain) {
+    const BottomH2 H = bottom_h2(s, lb);
+#define FS_CHAIN(N0, NM)                                                                                     \
+  FS_LAUNCH(s, "mg_bottom", bytes,                                                                           \
+            k_mg_bottom_chain<N0, NM><<<1, 256, 0, s->stream>>>(L[lb].rhs, L[lb].x, hx ? 1 : 0, H,            \
+                                                                 P.mg_pre_smooth, P.mg_post_smooth,            \
+                                                                 P.mg_coarse_sweeps, bah, bal))
+    switch (chain) {
+      case 64: FS_CHAIN(64, 8); break;
+      case 32: FS_CHAIN(32, 8); break;
+      case 16: FS_CHAIN(16, 8); break;
+      case 8: FS_CHAIN(8, 8); break;
+      case 48: FS_CHAIN(48, 12); break;
+      case 24: FS_CHAIN(24, 12); break;
+      default: FS_CHAIN(12, 12); break;
     }
-#undef FS_P2
+#undef FS_CHAIN
   } else {
     BottomLevels B;
     size_t smem = bottom_layout(s, &B);
@@ -960,19 +992,23 @@ int mg_vcycle_class(Solver* const* ms, int count, cudaStream_t st) {
     Solver* s = ms[i];
     tab.m[i] = {s->lev[lb].rhs, s->lev[lb].x, lb == 0 ? s->ph : nullptr, lb == 0 ? s->pl : nullptr, s->dev};
   }
-  const bool p2 = (nb & (nb - 1)) == 0 && nb >= 8 && nb <= 64 && L.back().n == 8 &&
-                  (int)L.size() - lb == ilog2_host(nb) - 2;
-  if (p2) {
-    BottomH2 H{};
-    for (int k = 0; k < (int)L.size() - lb && k < 4; k++) H.h2[k] = L[lb + k].h2;
-    H.w = (float)P.relax;
+  const int chain = bottom_chain(s0, lb);
+  if (chain) {
+    const BottomH2 H = bottom_h2(s0, lb);
     const dim3 grid(1, 1, count);
-    switch (nb) {
-      case 64: k_mg_bottom_p2_class<64><<<grid, 256, 0, st>>>(tab, H, P.mg_pre_smooth, P.mg_post_smooth, P.mg_coarse_sweeps, P.max_cycles); break;
-      case 32: k_mg_bottom_p2_class<32><<<grid, 256, 0, st>>>(tab, H, P.mg_pre_smooth, P.mg_post_smooth, P.mg_coarse_sweeps, P.max_cycles); break;
-      case 16: k_mg_bottom_p2_class<16><<<grid, 256, 0, st>>>(tab, H, P.mg_pre_smooth, P.mg_post_smooth, P.mg_coarse_sweeps, P.max_cycles); break;
-      default: k_mg_bottom_p2_class<8><<<grid, 256, 0, st>>>(tab, H, P.mg_pre_smooth, P.mg_post_smooth, P.mg_coarse_sweeps, P.max_cycles); break;
+#define FS_CHAIN(N0, NM)                                                                                        \
+  k_mg_bottom_chain_class<N0, NM><<<grid, 256, 0, st>>>(tab, H, P.mg_pre_smooth, P.mg_post_smooth,             \
+                                                         P.mg_coarse_sweeps, P.max_cycles)
+    switch (chain) {
+      case 64: FS_CHAIN(64, 8); break;
+      case 32: FS_CHAIN(32, 8); break;
+      case 16: FS_CHAIN(16, 8); break;
+      case 8: FS_CHAIN(8, 8); break;
+      case 48: FS_CHAIN(48, 12); break;
+      case 24: FS_CHAIN(24, 12); break;
+      default: FS_CHAIN(12, 12); break;
     }
+#undef FS_CHAIN
   } else {
     BottomLevels B;
     const size_t smem = bottom_layout(s0, &B);

@@ -461,7 +461,7 @@ def test_bitwise_repeatable(G, O):
 # ---------------------------------------------------- fused multigrid cycle
 @pytest.mark.parametrize("precision", ["f32", "mixed"])
 @pytest.mark.parametrize("n,relax", [(64, 1.0), (200, 1.0), (256, 1.0), (320, 1.0), (528, 1.0), (1056, 1.0),
-                                     (64, 1.2), (200, 1.2), (256, 1.2), (1024, 1.2)])
+                                     (64, 1.2), (200, 1.2), (256, 1.2), (1024, 1.2), (192, 1.0), (384, 1.2)])
 def test_fused_vcycle_bitwise_equals_one_pass_kernels(G, O, precision, n, relax):
     """The fused V-cycle (tile kernels + one-CTA bottom solve) evaluates the same
     expressions in the same order as the one-kernel-per-pass path, so the two
@@ -470,7 +470,8 @@ def test_fused_vcycle_bitwise_equals_one_pass_kernels(G, O, precision, n, relax)
     and 3 in F32); n = 200 has partial 16-cell tiles and a 50 -> 25 generic
     bottom with an odd coarsest level; n = 1056 has partial 64-, 32- and
     16-cell tiles and an odd 33 bottom; n = 528 and 1024 have 32- and
-    64-cell tiles at level 0 (the last one partial at 528)."""
+    64-cell tiles at level 0 (the last one partial at 528); n = 192 and 384
+    end in the 48 -> 24 -> 12 bottom chain."""
     u0, v0 = O.lcg_uv(4242, n * n)
     out = []
     for variant in (0, 1):
