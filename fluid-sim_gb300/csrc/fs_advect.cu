@@ -372,9 +372,84 @@ __global__ void __launch_bounds__(256) k_mc_combine_t(const float* __restrict__ 
   }
 }
 
+// ------------------------------------------------- batched (one size class)
+// The steps of the members of one batch size class (fs_api.cu batch_build),
+// one launch per kernel, member = blockIdx.z, pointers and per-member step
+// factors in a table passed by value; staging by the wrapped loads (the same
+// values the TMA copies deliver).
+struct AdvTab {
+  struct {
+    const float* u;
+    const float* v;
+    const float* fu;  // combine: the forward field
+    const float* fv;
+    float* ou;
+    float* ov;
+    float* bounds;
+    float cx, cy;
+  } m[kClassMax];
+};
+struct DiffTab {
+  struct {
+    const float* u;
+    const float* v;
+    float* ou;
+    float* ov;
+    float a, b;
+  } m[kClassMax];
+};
+
+__global__ void __launch_bounds__(256) k_advect_sl_class(const AdvTab tab, int nx, int ny) {
+  const auto& a = tab.m[blockIdx.z];
+  __shared__ __align__(128) float su[kSW * kSH];
+  __shared__ __align__(128) float sv[kSW * kSH];
+  const int ti = blockIdx.x * kTX, tj = blockIdx.y * kTY;
+  const int oi = ti - kHalo, oj = tj - kHalo;
+  float umax, vmax;
+  {
+    float* const sm[2] = {su, sv};
+    const float* const f[2] = {a.u, a.v};
+    stage_tiles<2>(sm, f, oi, oj, nx, ny, umax, vmax);
+  }
+  if (fast_tile(umax, vmax, a.cx, a.cy)) {
+    const TileView<true> U{su, oi, oj, a.u, nx, ny}, V{sv, oi, oj, a.v, nx, ny};
+    advect_rows(U, V, a.ou, a.ov, nx, ny, ti, tj, a.cx, a.cy, a.bounds);
+  } else {
+    const TileView<false> U{su, oi, oj, a.u, nx, ny}, V{sv, oi, oj, a.v, nx, ny};
+    advect_rows(U, V, a.ou, a.ov, nx, ny, ti, tj, a.cx, a.cy, a.bounds);
+  }
+}
+
+__global__ void __launch_bounds__(256) k_mc_combine_class(const AdvTab tab, int nx, int ny) {
+  const auto& a = tab.m[blockIdx.z];
+  __shared__ __align__(128) float su[kSW * kSH];
+  __shared__ __align__(128) float sv[kSW * kSH];
+  __shared__ __align__(128) float sfu[kSW * kSH];
+  __shared__ __align__(128) float sfv[kSW * kSH];
+  const int ti = blockIdx.x * kTX, tj = blockIdx.y * kTY;
+  const int oi = ti - kHalo, oj = tj - kHalo;
+  float umax, vmax;
+  {
+    float* const sm[4] = {su, sv, sfu, sfv};
+    const float* const f[4] = {a.u, a.v, a.fu, a.fv};
+    stage_tiles<4>(sm, f, oi, oj, nx, ny, umax, vmax);
+  }
+  if (fast_tile(umax, vmax, a.cx, a.cy)) {
+    const TileView<true> U{su, oi, oj, a.u, nx, ny}, V{sv, oi, oj, a.v, nx, ny};
+    const TileView<true> FU{sfu, oi, oj, a.fu, nx, ny}, FV{sfv, oi, oj, a.fv, nx, ny};
+    combine_rows(U, V, FU, FV, a.bounds, a.ou, a.ov, nx, ny, ti, tj, a.cx, a.cy);
+  } else {
+    const TileView<false> U{su, oi, oj, a.u, nx, ny}, V{sv, oi, oj, a.v, nx, ny};
+    const TileView<false> FU{sfu, oi, oj, a.fu, nx, ny}, FV{sfv, oi, oj, a.fv, nx, ny};
+    combine_rows(U, V, FU, FV, a.bounds, a.ou, a.ov, nx, ny, ti, tj, a.cx, a.cy);
+  }
+}
+
 static const dim3 kBlock(32, 8);
 
 static dim3 tile_grid(const Grid& g) { return dim3((g.nx + kTX - 1) / kTX, (g.ny + kTY - 1) / kTY); }
+
+
 
 // Tensor map of one f32 field for the advection tiles (box kSW x kSH), kept
 // per device pointer.  TMA needs the row pitch a multiple of 16 bytes (nx % 4
@@ -445,9 +520,9 @@ void launch_advect_mc<float>(Solver* s, const float* u, const float* v, float* f
 }
 
 // DIFFUSE (shaders.js:401-425; src/cpu/solver.js:56-68 operand order)
-__global__ void __launch_bounds__(256) k_diffuse(const float* __restrict__ u, const float* __restrict__ v,
-                                                 float* __restrict__ ou, float* __restrict__ ov,
-                                                 int nx, int ny, float a, float b) {
+__device__ __forceinline__ void diffuse_body(const float* __restrict__ u, const float* __restrict__ v,
+                                             float* __restrict__ ou, float* __restrict__ ov, int nx, int ny, float a,
+                                             float b) {
   int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y;
   if (i >= nx || j >= ny) return;
   int im = i == 0 ? nx - 1 : i - 1, ip = i + 1 == nx ? 0 : i + 1;
@@ -461,6 +536,12 @@ __global__ void __launch_bounds__(256) k_diffuse(const float* __restrict__ u, co
               b * (__ldg(v + rm + i) - 2.f * c + __ldg(v + rp + i));
 }
 
+__global__ void __launch_bounds__(256) k_diffuse(const float* __restrict__ u, const float* __restrict__ v,
+                                                 float* __restrict__ ou, float* __restrict__ ov,
+                                                 int nx, int ny, float a, float b) {
+  diffuse_body(u, v, ou, ov, nx, ny, a, b);
+}
+
 void launch_diffuse(Solver* s, const float* u, const float* v, float* ou, float* ov, float dt) {
   const Grid& g = s->g;
   float a = (float)(s->prm.nu * dt / (g.dxd * g.dxd));
@@ -468,6 +549,47 @@ void launch_diffuse(Solver* s, const float* u, const float* v, float* ou, float*
   FS_LAUNCH(s, "diffuse", (double)s->n * 16,
             k_diffuse<<<grid2d(g.nx, g.ny, kBlock), kBlock, 0, s->stream>>>(u, v, ou, ov, g.nx, g.ny,
                                                                             a, b));
+}
+
+__global__ void __launch_bounds__(256) k_diffuse_class(const DiffTab tab, int nx, int ny) {
+  const auto& a = tab.m[blockIdx.z];
+  diffuse_body(a.u, a.v, a.ou, a.ov, nx, ny, a.a, a.b);
+}
+
+// advection (and diffusion) of every member of a class into (wu, wv), or
+// (tu, tv) after the diffusion; the velocity the projection reads
+void launch_front_advect_class(Solver* const* ms, int count, const double* dts, cudaStream_t st) {
+  Solver* s0 = ms[0];
+  const Grid& g = s0->g;
+  const bool mc = s0->prm.advection == FS_ADVECT_MACCORMACK;
+  AdvTab fwd{}, comb{};
+  for (int i = 0; i < count; i++) {
+    Solver* s = ms[i];
+    const float dt = (float)dts[i];
+    const float cx = (float)((double)dt / s->g.dxd), cy = (float)((double)dt / s->g.dyd);
+    if (mc) {
+      fwd.m[i] = {s->u, s->v, nullptr, nullptr, s->fu, s->fv, s->mc_bounds, cx, cy};
+      comb.m[i] = {s->u, s->v, s->fu, s->fv, s->wu, s->wv, s->mc_bounds, cx, cy};
+    } else {
+      fwd.m[i] = {s->u, s->v, nullptr, nullptr, s->wu, s->wv, nullptr, cx, cy};
+    }
+  }
+  dim3 grid = tile_grid(g);
+  grid.z = count;
+  k_advect_sl_class<<<grid, kBlock, 0, st>>>(fwd, g.nx, g.ny);
+  if (mc) k_mc_combine_class<<<grid, kBlock, 0, st>>>(comb, g.nx, g.ny);
+  if (s0->prm.nu > 0) {
+    DiffTab dt{};
+    for (int i = 0; i < count; i++) {
+      Solver* s = ms[i];
+      const float a = (float)(s->prm.nu * (float)dts[i] / (s->g.dxd * s->g.dxd));
+      const float b = (float)(s->prm.nu * (float)dts[i] / (s->g.dyd * s->g.dyd));
+      dt.m[i] = {s->wu, s->wv, s->tu, s->tv, a, b};
+    }
+    dim3 g2 = grid2d(g.nx, g.ny, kBlock);
+    g2.z = count;
+    k_diffuse_class<<<g2, kBlock, 0, st>>>(dt, g.nx, g.ny);
+  }
 }
 
 // FORCING + drag, in place (shaders.js:532-566): u <- u*exp(-drag dt) + amp dt/sqrt(M) sum_m

@@ -1341,6 +1341,19 @@ static void batch_free(fs_batch* b) {
   delete b;
 }
 
+// a class whose members' whole steps can run as batched launches: nothing
+// but advection, diffusion and the projection from zero pressure
+static bool class_plain(const fs_batch* b, const BatchClass& c) {
+  const Solver* r = &b->members[c.idx[0]]->s;
+  for (int i : c.idx) {
+    const Solver* s = &b->members[i]->s;
+    if (s->n_modes > 0 || !s->disks.empty() || s->dye || s->guess || s->prm.warm_start ||
+        s->prm.advection != r->prm.advection || (s->prm.nu > 0) != (r->prm.nu > 0))
+      return false;
+  }
+  return true;
+}
+
 // a member that can run its loop in a size class, and the settings a class shares
 static bool class_eligible(const Solver* s) {
   return s->mixed && s->fused && s->prm.pressure_tol > 0 && !s->guess && s->g.nx == s->g.ny;
@@ -1356,7 +1369,7 @@ static bool same_class(const Solver* a, const Solver* b) {
 // the class's conditional loop on cs (already part of the batch capture):
 // k_cond_class sets the condition from the members' initial statistics, the
 // body is one batched refinement cycle plus k_cond_class's bookkeeping
-static int capture_class_loop(fs_batch* b, BatchClass& c, cudaStream_t cs, long long* iters) {
+static int capture_class_loop(fs_batch* b, BatchClass& c, cudaStream_t cs, long long* iters, int init_mode) {
   std::vector<Solver*> ms;
   for (int i : c.idx) ms.push_back(&b->members[i]->s);
   const int count = (int)ms.size();
@@ -1368,7 +1381,7 @@ static int capture_class_loop(fs_batch* b, BatchClass& c, cudaStream_t cs, long 
   cudaGraphConditionalHandle h = 0;
   if (e == cudaSuccess) e = cudaGraphConditionalHandleCreate(&h, cg, 0, 0);
   if (e != cudaSuccess) return bfail(b, FS_ERR_CUDA, std::string("batch loop: ") + cudaGetErrorString(e));
-  launch_cond_class(ms.data(), count, cs, h, true, iters);
+  launch_cond_class(ms.data(), count, cs, h, init_mode, iters);
   e = cudaStreamGetCaptureInfo(cs, &cst, nullptr, &cg, &deps, nullptr, &nd);
   cudaGraphNodeParams cp = {};
   cp.type = cudaGraphNodeTypeConditional;
@@ -1385,7 +1398,7 @@ static int capture_class_loop(fs_batch* b, BatchClass& c, cudaStream_t cs, long 
   if (e != cudaSuccess) return bfail(b, FS_ERR_CUDA, std::string("batch loop: ") + cudaGetErrorString(e));
   c.body_launches = mg_vcycle_class(ms.data(), count, b->body_stream);
   launch_refine_class(ms.data(), count, b->body_stream);
-  launch_cond_class(ms.data(), count, b->body_stream, h, false, iters);
+  launch_cond_class(ms.data(), count, b->body_stream, h, 0, iters);
   c.body_launches += 2;
   cudaGraph_t tmp = nullptr;
   cudaError_t e2 = cudaGetLastError();
@@ -1471,10 +1484,38 @@ static int batch_build(fs_batch* b, const double* dt) {
   // took twice the sum of their times alone).  Each class: the members' steps
   // up to their loops as branches, the class loop on the class stream, then
   // the members' remaining steps as branches.
+  int64_t class_fixed = 0;  // launches per replay of the batched plain classes
   for (int c = 0; c < nc && rc == FS_OK; c++) {
     cudaStream_t cs = b->class_streams[c];
     if (c > 0 && cudaEventRecord(b->fork, b->stream) != cudaSuccess) rc = FS_ERR_CUDA;  // after class c - 1
     if (cudaStreamWaitEvent(cs, b->fork, 0) != cudaSuccess) rc = FS_ERR_CUDA;
+    if (rc == FS_OK && class_plain(b, b->classes[c])) {
+      // the whole class step as batched launches on the class stream
+      std::vector<Solver*> ms;
+      std::vector<const float*> wu, wv;
+      std::vector<double> cdt;
+      for (int i : b->classes[c].idx) {
+        Solver* s = &b->members[i]->s;
+        ms.push_back(s);
+        const bool diff = s->prm.nu > 0;
+        wu.push_back(diff ? s->tu : s->wu);
+        wv.push_back(diff ? s->tv : s->wv);
+        cdt.push_back(dt[i]);
+        s->stats = fs_step_stats{0, 1, -1.0, -1.0};
+        s->stats_on_device = true;
+        l0[i] = s->launches;
+      }
+      const int count = (int)ms.size();
+      launch_front_advect_class(ms.data(), count, cdt.data(), cs);
+      launch_front_project_class(ms.data(), count, wu.data(), wv.data(), cdt.data(), cs);
+      rc = capture_class_loop(b, b->classes[c], cs, b->d_iters + c, 2);
+      if (rc == FS_OK) launch_back_class(ms.data(), count, wu.data(), wv.data(), cdt.data(), cs);
+      class_fixed += (ms[0]->prm.advection == FS_ADVECT_MACCORMACK ? 2 : 1) + (ms[0]->prm.nu > 0 ? 1 : 0) + 3 + 2;
+      if (rc == FS_OK && cudaGetLastError() != cudaSuccess) rc = bfail(b, FS_ERR_CUDA, "batch: class launch failed");
+      if (rc == FS_OK && cudaEventRecord(b->class_done[c], cs) != cudaSuccess) rc = FS_ERR_CUDA;
+      if (rc == FS_OK && cudaStreamWaitEvent(b->stream, b->class_done[c], 0) != cudaSuccess) rc = FS_ERR_CUDA;
+      continue;
+    }
     for (int i : b->classes[c].idx) {
       if (rc != FS_OK) break;
       Solver* s = &b->members[i]->s;
@@ -1487,7 +1528,7 @@ static int batch_build(fs_batch* b, const double* dt) {
       std::swap(s->stream, s->own_stream);
       if (rc != FS_OK) member_err(i);
     }
-    if (rc == FS_OK) rc = capture_class_loop(b, b->classes[c], cs, b->d_iters + c);
+    if (rc == FS_OK) rc = capture_class_loop(b, b->classes[c], cs, b->d_iters + c, 1);
     if (rc == FS_OK && cudaEventRecord(b->class_done[c], cs) != cudaSuccess) rc = FS_ERR_CUDA;
     for (int i : b->classes[c].idx) {
       if (rc != FS_OK) break;
@@ -1513,7 +1554,7 @@ static int batch_build(fs_batch* b, const double* dt) {
   e = cudaGraphInstantiate(&b->exec, g, 0);
   cudaGraphDestroy(g);
   if (e != cudaSuccess) return bfail(b, FS_ERR_CUDA, std::string("batch instantiate: ") + cudaGetErrorString(e));
-  b->fixed_per_replay = nc;  // the class loops' initial condition kernels
+  b->fixed_per_replay = nc + class_fixed;  // the class loops' initial condition kernels, batched steps
   for (int i = 0; i < n; i++) {
     Solver* s = &b->members[i]->s;
     int64_t captured = s->launches - l0[i];

@@ -244,8 +244,14 @@ bool mg_fused_supported(const Solver* s);
 // batched refinement cycle of one size class of a batch (fs_multigrid.cu, fs_pressure.cu)
 int mg_vcycle_class(Solver* const* ms, int count, cudaStream_t st);
 void launch_refine_class(Solver* const* ms, int count, cudaStream_t st);
-void launch_cond_class(Solver* const* ms, int count, cudaStream_t st, cudaGraphConditionalHandle h, bool init,
+void launch_cond_class(Solver* const* ms, int count, cudaStream_t st, cudaGraphConditionalHandle h, int init,
                        long long* iterations);
+// the rest of the step of a class whose members are plain (fs_advect.cu, fs_pressure.cu)
+void launch_front_advect_class(Solver* const* ms, int count, const double* dts, cudaStream_t st);
+void launch_front_project_class(Solver* const* ms, int count, const float* const* wu, const float* const* wv,
+                                const double* dts, cudaStream_t st);
+void launch_back_class(Solver* const* ms, int count, const float* const* wu, const float* const* wv,
+                       const double* dts, cudaStream_t st);
 
 // errors (fs_api.cu): message into the handle (or the thread's last error)
 int fail_status(Solver* s, int code, const std::string& msg);

@@ -925,9 +925,19 @@ static void down_class_t(Solver* const* ms, int count, int l, cudaStream_t st) {
                                                       (float)ms[0]->prm.relax, ms[0]->prm.max_cycles);
 }
 
+// tile side for a level of a class: like tile_for, counting the CTAs of all
+// members (the tiles give the same values whatever their size)
+static int tile_for_class(int n, int count) {
+  for (int t : {64, 32}) {
+    int c = (n + t - 1) / t;
+    if (c * c * count >= 256) return t;
+  }
+  return 16;
+}
+
 template <int H>
 static void down_class(Solver* const* ms, int count, int l, cudaStream_t st) {
-  switch (tile_for(ms[0]->lev[l].n)) {
+  switch (tile_for_class(ms[0]->lev[l].n, count)) {
     case 64: down_class_t<64, H>(ms, count, l, st); break;
     case 32: down_class_t<32, H>(ms, count, l, st); break;
     default: down_class_t<16, H>(ms, count, l, st); break;
@@ -962,7 +972,7 @@ static void up_class_t(Solver* const* ms, int count, int l, cudaStream_t st) {
 template <int H>
 static void up_class(Solver* const* ms, int count, int l, cudaStream_t st) {
   const bool acc = l == 0;
-  switch (tile_for(ms[0]->lev[l].n)) {
+  switch (tile_for_class(ms[0]->lev[l].n, count)) {
     case 64: acc ? up_class_t<64, H, true>(ms, count, l, st) : up_class_t<64, H, false>(ms, count, l, st); break;
     case 32: acc ? up_class_t<32, H, true>(ms, count, l, st) : up_class_t<32, H, false>(ms, count, l, st); break;
     default: acc ? up_class_t<16, H, true>(ms, count, l, st) : up_class_t<16, H, false>(ms, count, l, st); break;

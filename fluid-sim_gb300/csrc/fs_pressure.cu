@@ -269,10 +269,10 @@ void launch_poisson_norms(Solver* s, const float* p, const float* d, float h2f, 
 
 // divergence of (hi + lo) faces, lo planes optional (nullptr = 0):
 // d = (uR - uL)/dx + (vT - vB)/dy with every operation error-free or df
-__global__ void __launch_bounds__(256)
-    k_div_df(const float* __restrict__ uh, const float* __restrict__ ul, const float* __restrict__ vh,
-             const float* __restrict__ vl, float* __restrict__ dh, float* __restrict__ dl, int nx, int ny, df idx,
-             df idy) {
+__device__ __forceinline__ void div_df_body(const float* __restrict__ uh, const float* __restrict__ ul,
+                                            const float* __restrict__ vh, const float* __restrict__ vl,
+                                            float* __restrict__ dh, float* __restrict__ dl, int nx, int ny, df idx,
+                                            df idy) {
   int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y;
   if (i >= nx || j >= ny) return;
   int ip = i + 1 == nx ? 0 : i + 1, jp = j + 1 == ny ? 0 : j + 1;
@@ -286,6 +286,13 @@ __global__ void __launch_bounds__(256)
   dl[c] = d.lo;
 }
 
+__global__ void __launch_bounds__(256)
+    k_div_df(const float* __restrict__ uh, const float* __restrict__ ul, const float* __restrict__ vh,
+             const float* __restrict__ vl, float* __restrict__ dh, float* __restrict__ dl, int nx, int ny, df idx,
+             df idy) {
+  div_df_body(uh, ul, vh, vl, dh, dl, nx, ny, idx, idy);
+}
+
 void launch_div_df(Solver* s, const float* uh, const float* ul, const float* vh, const float* vl, float* dh,
                    float* dl) {
   const Grid& g = s->g;
@@ -295,11 +302,11 @@ void launch_div_df(Solver* s, const float* uh, const float* ul, const float* vh,
 }
 
 // u = w - (p_i - p_{i-1})/dx, v = w - (p_j - p_{j-1})/dy in df; w lo planes optional
-__global__ void __launch_bounds__(256)
-    k_subgrad_df(const float* __restrict__ wuh, const float* __restrict__ wul, const float* __restrict__ wvh,
-                 const float* __restrict__ wvl, const float* __restrict__ ph, const float* __restrict__ pl,
-                 float* __restrict__ uh, float* __restrict__ ul, float* __restrict__ vh, float* __restrict__ vl,
-                 int nx, int ny, df idx, df idy) {
+__device__ __forceinline__ void subgrad_df_body(const float* __restrict__ wuh, const float* __restrict__ wul,
+                                                const float* __restrict__ wvh, const float* __restrict__ wvl,
+                                                const float* __restrict__ ph, const float* __restrict__ pl,
+                                                float* __restrict__ uh, float* __restrict__ ul, float* __restrict__ vh,
+                                                float* __restrict__ vl, int nx, int ny, df idx, df idy) {
   int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y;
   if (i >= nx || j >= ny) return;
   int im = i == 0 ? nx - 1 : i - 1, jm = j == 0 ? ny - 1 : j - 1;
@@ -312,6 +319,14 @@ __global__ void __launch_bounds__(256)
   df u = df_sub(wu, gx), v = df_sub(wv, gy);
   uh[c] = u.hi; ul[c] = u.lo;
   vh[c] = v.hi; vl[c] = v.lo;
+}
+
+__global__ void __launch_bounds__(256)
+    k_subgrad_df(const float* __restrict__ wuh, const float* __restrict__ wul, const float* __restrict__ wvh,
+                 const float* __restrict__ wvl, const float* __restrict__ ph, const float* __restrict__ pl,
+                 float* __restrict__ uh, float* __restrict__ ul, float* __restrict__ vh, float* __restrict__ vl,
+                 int nx, int ny, df idx, df idy) {
+  subgrad_df_body(wuh, wul, wvh, wvl, ph, pl, uh, ul, vh, vl, nx, ny, idx, idy);
 }
 
 void launch_subgrad_df(Solver* s, const float* wuh, const float* wul, const float* wvh, const float* wvl,
@@ -637,8 +652,9 @@ __global__ void __launch_bounds__(256) k_refine_class(const RefineTab tab, int n
   else refine_init_body(a.dh, a.dl, a.ph, a.pl, a.r32, nx, ny, ks, 0, a.ctx);
 }
 
-// one block of kClassMax threads; init = 1 before the loop (the members' own
-// k_cond has set their statistics), 0 after each cycle
+// one block of kClassMax threads; init = 1 before the loop when the members'
+// own k_cond has set their statistics, 2 before the loop doing that here
+// (k_cond's init arithmetic), 0 after each cycle
 __global__ void __launch_bounds__(kClassMax) k_cond_class(const CondTab tab, int count, int max_cycles,
                                                           cudaGraphConditionalHandle h, int init,
                                                           long long* iterations) {
@@ -646,7 +662,16 @@ __global__ void __launch_bounds__(kClassMax) k_cond_class(const CondTab tab, int
   int again = 0;
   if (z < count) {
     DevState* st = tab.m[z].st;
-    if (init) {
+    if (init == 2) {
+      const double m = tab.m[z].red[0];
+      st->cycles = 0;
+      st->res_initial = m;
+      st->res_max = m;
+      const bool finite = isfinite(m);
+      st->nonfinite = finite ? 0 : 1;
+      st->converged = (finite && m <= tab.m[z].tol) ? 1 : 0;
+      again = finite && m > tab.m[z].tol && 0 < max_cycles;
+    } else if (init) {
       again = member_in_loop(st, max_cycles);
     } else if (member_in_loop(st, max_cycles)) {  // this member ran the cycle
       const double m = tab.m[z].red[0];
@@ -680,12 +705,103 @@ void launch_refine_class(Solver* const* ms, int count, cudaStream_t st) {
   k_refine_class<<<grid, kBlock, 0, st>>>(tab, g.nx, g.ny, lap_scale(g), s0->prm.max_cycles, quad ? 1 : 0);
 }
 
-void launch_cond_class(Solver* const* ms, int count, cudaStream_t st, cudaGraphConditionalHandle h, bool init,
+void launch_cond_class(Solver* const* ms, int count, cudaStream_t st, cudaGraphConditionalHandle h, int init,
                        long long* iterations) {
   CondTab tab{};
   for (int i = 0; i < count; i++) tab.m[i] = {ms[i]->red_out, ms[i]->dev, ms[i]->prm.pressure_tol};
-  k_cond_class<<<1, kClassMax, 0, st>>>(tab, count, ms[0]->prm.max_cycles, h, init ? 1 : 0, iterations);
+  k_cond_class<<<1, kClassMax, 0, st>>>(tab, count, ms[0]->prm.max_cycles, h, init, iterations);
 }
+
+// ---- the rest of a plain class member's step, batched: the divergence of the
+// (advected, diffused) velocity, the initial residual from zero pressure, the
+// zeroed pressure, and after the loop the gradient subtraction and the step
+// finish (k_div_df, k_refine_init with zero_p, launch_fill, k_subgrad_df,
+// k_step_finish, one launch each for the whole class)
+struct ProjTab {
+  struct {
+    const float* wu;  // the velocity the projection reads
+    const float* wv;
+    float* uh;
+    float* ul;
+    float* vh;
+    float* vl;
+    float* dh;
+    float* dl;
+    float* ph;
+    float* pl;
+    float* r32;
+    RedCtx ctx;
+    DevState* st;
+    df idx, idy;
+    double dt;
+  } m[kClassMax];
+};
+
+__global__ void __launch_bounds__(256) k_div_class(const ProjTab tab, int nx, int ny) {
+  const auto& a = tab.m[blockIdx.z];
+  div_df_body(a.wu, nullptr, a.wv, nullptr, a.dh, a.dl, nx, ny, a.idx, a.idy);
+}
+
+__global__ void __launch_bounds__(256) k_refine_zero_class(const ProjTab tab, int nx, int ny, LapScale ks) {
+  const auto& a = tab.m[blockIdx.z];
+  refine_init_body(a.dh, a.dl, a.ph, a.pl, a.r32, nx, ny, ks, 1, a.ctx);
+}
+
+__global__ void k_zero_p_class(const ProjTab tab, int64_t n) {
+  const auto& a = tab.m[blockIdx.z];
+  for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x) {
+    a.ph[k] = 0.f;
+    a.pl[k] = 0.f;
+  }
+}
+
+__global__ void __launch_bounds__(256) k_subgrad_class(const ProjTab tab, int nx, int ny) {
+  const auto& a = tab.m[blockIdx.z];
+  subgrad_df_body(a.wu, nullptr, a.wv, nullptr, a.ph, a.pl, a.uh, a.ul, a.vh, a.vl, nx, ny, a.idx, a.idy);
+}
+
+__global__ void k_finish_class(const ProjTab tab, int count) {
+  const int z = threadIdx.x;
+  if (z < count) tab.m[z].st->t += tab.m[z].dt;
+}
+
+static ProjTab proj_tab(Solver* const* ms, int count, const float* const* wu, const float* const* wv,
+                        const double* dts) {
+  ProjTab tab{};
+  for (int i = 0; i < count; i++) {
+    Solver* s = ms[i];
+    tab.m[i] = {wu[i],  wv[i],  s->u,  s->ulo, s->v,   s->vlo, s->dh,
+                s->dl,  s->ph,  s->pl, s->r32, red_ctx(s, s->red_out), s->dev,
+                df_host(s->g.idxd), df_host(s->g.idyd), dts[i]};
+  }
+  return tab;
+}
+
+// before the loop: divergence, initial residual (zero pressure), zeroed pressure
+void launch_front_project_class(Solver* const* ms, int count, const float* const* wu, const float* const* wv,
+                                const double* dts, cudaStream_t st) {
+  const Grid& g = ms[0]->g;
+  const ProjTab tab = proj_tab(ms, count, wu, wv, dts);
+  dim3 g2 = grid2d(g.nx, g.ny, kBlock);
+  g2.z = count;
+  k_div_class<<<g2, kBlock, 0, st>>>(tab, g.nx, g.ny);
+  dim3 gr = red_grid2(g.nx, g.ny);
+  gr.z = count;
+  k_refine_zero_class<<<gr, kBlock, 0, st>>>(tab, g.nx, g.ny, lap_scale(g));
+  k_zero_p_class<<<dim3(fill_blocks(ms[0]->n), 1, count), 256, 0, st>>>(tab, ms[0]->n);
+}
+
+// after the loop: gradient subtraction and the step finish
+void launch_back_class(Solver* const* ms, int count, const float* const* wu, const float* const* wv,
+                       const double* dts, cudaStream_t st) {
+  const Grid& g = ms[0]->g;
+  const ProjTab tab = proj_tab(ms, count, wu, wv, dts);
+  dim3 g2 = grid2d(g.nx, g.ny, kBlock);
+  g2.z = count;
+  k_subgrad_class<<<g2, kBlock, 0, st>>>(tab, g.nx, g.ny);
+  k_finish_class<<<1, kClassMax, 0, st>>>(tab, count);
+}
+
 
 // ---------------------------------------------------------------- conversion
 __global__ void k_convert(const void* src, int sf64, void* dst, int df64, int64_t n) {
