@@ -1286,6 +1286,12 @@ FS_API void fs_host_free(void* p) {
 // same grid and multigrid settings form a size class: their refinement cycles
 // run as batched launches inside one conditional loop per class (up to
 // kClassMax members per class; a larger group is split).
+// chains of size classes that run side by side within one batch step.  With
+// the classes' steps batched, running them side by side pays: the 256-member
+// benchmark batch (six classes) took 4.47 / 3.97 / 3.76 / 3.56 / 3.29 ms per
+// step with 1 / 2 / 3 / 4 / 6 chains.
+constexpr int kBatchLanes = 8;
+
 struct BatchClass {
   std::vector<int> idx;  // member indices
   int body_launches = 0;  // launches of one loop iteration
@@ -1480,15 +1486,32 @@ static int batch_build(fs_batch* b, const double* dt) {
     std::swap(s->stream, s->own_stream);
     if (rc != FS_OK) member_err(i);
   }
-  // The classes one after another (measured: six size classes run together
-  // took twice the sum of their times alone).  Each class: the members' steps
-  // up to their loops as branches, the class loop on the class stream, then
-  // the members' remaining steps as branches.
+  // The classes run in kBatchLanes chains, each class after the previous one
+  // of its lane; a class goes to the lane with the fewest cells so far,
+  // largest classes first.  Each class: the members' steps up to their
+  // loops, the class loop on the class stream, then the members' remaining
+  // steps; the class's completion is recorded on its stream.
+  std::vector<int> order(nc), lane_prev(kBatchLanes, -1), prev_class(nc, -1);
+  std::vector<double> lane_cells(kBatchLanes, 0.0), class_cells(nc, 0.0);
+  for (int c = 0; c < nc; c++) {
+    order[c] = c;
+    for (int i : b->classes[c].idx) class_cells[c] += (double)b->members[i]->s.n;
+  }
+  std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return class_cells[x] > class_cells[y]; });
+  for (int c : order) {
+    int lane = 0;
+    for (int k = 1; k < kBatchLanes; k++)
+      if (lane_cells[k] < lane_cells[lane]) lane = k;
+    prev_class[c] = lane_prev[lane];
+    lane_prev[lane] = c;
+    lane_cells[lane] += class_cells[c];
+  }
   int64_t class_fixed = 0;  // launches per replay of the batched plain classes
-  for (int c = 0; c < nc && rc == FS_OK; c++) {
+  for (int oc = 0; oc < nc && rc == FS_OK; oc++) {
+    const int c = order[oc];
     cudaStream_t cs = b->class_streams[c];
-    if (c > 0 && cudaEventRecord(b->fork, b->stream) != cudaSuccess) rc = FS_ERR_CUDA;  // after class c - 1
-    if (cudaStreamWaitEvent(cs, b->fork, 0) != cudaSuccess) rc = FS_ERR_CUDA;
+    cudaEvent_t after = prev_class[c] < 0 ? b->fork : b->class_done[prev_class[c]];
+    if (cudaStreamWaitEvent(cs, after, 0) != cudaSuccess) rc = FS_ERR_CUDA;
     if (rc == FS_OK && class_plain(b, b->classes[c])) {
       // the whole class step as batched launches on the class stream
       std::vector<Solver*> ms;
@@ -1520,7 +1543,7 @@ static int batch_build(fs_batch* b, const double* dt) {
       if (rc != FS_OK) break;
       Solver* s = &b->members[i]->s;
       std::swap(s->stream, s->own_stream);
-      if (cudaStreamWaitEvent(s->stream, b->fork, 0) != cudaSuccess) rc = FS_ERR_CUDA;
+      if (cudaStreamWaitEvent(s->stream, after, 0) != cudaSuccess) rc = FS_ERR_CUDA;
       l0[i] = s->launches;
       if (rc == FS_OK) rc = enqueue_step(s, dt[i], true, &split[i]);
       if (rc == FS_OK && cudaEventRecord(b->joins[i], s->stream) != cudaSuccess) rc = FS_ERR_CUDA;
@@ -1537,10 +1560,12 @@ static int batch_build(fs_batch* b, const double* dt) {
       if (cudaStreamWaitEvent(s->stream, b->class_done[c], 0) != cudaSuccess) rc = FS_ERR_CUDA;
       if (rc == FS_OK) rc = enqueue_step_back(s, dt[i], split[i]);
       if (rc == FS_OK && cudaEventRecord(b->joins[i], s->stream) != cudaSuccess) rc = FS_ERR_CUDA;
-      if (rc == FS_OK && cudaStreamWaitEvent(b->stream, b->joins[i], 0) != cudaSuccess) rc = FS_ERR_CUDA;
+      if (rc == FS_OK && cudaStreamWaitEvent(cs, b->joins[i], 0) != cudaSuccess) rc = FS_ERR_CUDA;
       std::swap(s->stream, s->own_stream);
       if (rc != FS_OK) member_err(i);
     }
+    if (rc == FS_OK && cudaEventRecord(b->class_done[c], cs) != cudaSuccess) rc = FS_ERR_CUDA;
+    if (rc == FS_OK && cudaStreamWaitEvent(b->stream, b->class_done[c], 0) != cudaSuccess) rc = FS_ERR_CUDA;
   }
   for (int i = 0; i < n && rc == FS_OK; i++)
     if (cls[i] < 0 && cudaStreamWaitEvent(b->stream, b->joins[i], 0) != cudaSuccess) rc = FS_ERR_CUDA;
