@@ -98,3 +98,39 @@ def test_batch_of_uneven_sides_times(pkg):
     for m in b.members:
         assert m.last_stats()["converged"]
     b.destroy()
+
+
+def test_batch_mixed_paths_equal_independent_solvers(pkg):
+    """Three ways a member steps inside a batch, each bit for bit equal to the
+    same solver stepped alone: two 64^2 members in one size class of which one
+    has forcing (the class loop is batched, their other kernels run as member
+    branches), an F32 member with a tolerance (outside every class: its own
+    captured step), and a plain 128^2 class (its whole step batched)."""
+    f32 = dict(CFG, precision="f32", pressure_tol=1e-4)
+    cfgs = [dict(n=64, **CFG), dict(n=64, **CFG), dict(n=64, **f32), dict(n=128, **CFG)]
+    states = _members(pkg, [c["n"] for c in cfgs], 60)
+    modes = [(3.0, 1.0, 0.2), (0.0, 4.0, 1.0)]
+
+    def setup(s, i, u, v):
+        s.upload_velocity(u, v)
+        if i == 1:
+            s.set_forcing(modes, amplitude=0.5, drag=0.1)
+
+    b = pkg.GPUFluidBatch(cfgs)
+    for i, (m, (u, v, _)) in enumerate(zip(b.members, states)):
+        setup(m, i, u, v)
+    dts = [dt for _, _, dt in states]
+    for _ in range(3):
+        b.step(dts)
+    b.sync()
+    for i, (cfg, (u, v, dt)) in enumerate(zip(cfgs, states)):
+        s = pkg.GPUFluidSolver(**cfg)
+        setup(s, i, u, v)
+        for _ in range(3):
+            s.step(dt)
+        ua, va = b.members[i].read_velocity()
+        ub, vb = s.read_velocity()
+        assert np.array_equal(ua, ub) and np.array_equal(va, vb), f"member {i}"
+        assert b.members[i].last_stats()["cycles"] == s.last_stats()["cycles"]
+        s.destroy()
+    b.destroy()
