@@ -240,8 +240,10 @@ def measure_batch(pkg, device, count, steps, warmup, seed=1, relax=RELAX):
     ms = b.time_steps(dts, steps)
     converged = all(m.last_stats()["converged"] for m in b.members)
     launches = b.launch_count()
-    # sweep counts per domain size picked by the autotuner, then the same timing
+    # sweep counts per domain size, then tile sides per size class and level,
+    # picked by the autotuners; then the same timing
     picks = b.autotune(dts, 3)
+    tiles = b.autotune_tiles(dts, 5)["tiles"]
     for _ in range(warmup):
         b.step(dts)
     ms_tuned = b.time_steps(dts, steps)
@@ -257,6 +259,7 @@ def measure_batch(pkg, device, count, steps, warmup, seed=1, relax=RELAX):
             "ms_per_step": ms / steps, "value": cells * steps / (ms / 1e3), "unit": UNIT,
             "sequential_ms_per_step": seq_ms, "speedup_vs_sequential": seq_ms / (ms / steps),
             "autotuned_sweeps": {f"{k[0]}": list(v) for k, v in sorted(picks.items())},
+            "autotuned_tiles": {f"{k[0]}": list(v) for k, v in sorted(tiles.items())},
             "autotuned_ms_per_step": ms_tuned / steps, "autotuned_value": cells * steps / (ms_tuned / 1e3),
             "converged": converged, "gpu_launches_total": launches}
 

@@ -162,6 +162,10 @@ SIGNATURES = {
     "fs_set_mg_sweeps": (I, [VP, C.c_int32, C.c_int32]),
     "fs_total_cycles": (I, [VP, C.POINTER(C.c_int64)]),
     "fs_autotune": (I, [VP, D, C.c_int32, C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.POINTER(D)]),
+    "fs_set_mg_tiles": (I, [VP, C.POINTER(C.c_int32), C.c_int32]),
+    "fs_get_mg_tiles": (I, [VP, C.POINTER(C.c_int32), C.c_int32, C.POINTER(C.c_int32)]),
+    "fs_autotune_tiles": (I, [VP, D, C.c_int32, C.POINTER(C.c_int32), C.c_int32, C.POINTER(C.c_int32),
+                              C.POINTER(D)]),
     "fs_diagnose": (I, [VP, VP]),
     "fs_energy_spectrum": (I, [VP, VP, VP, C.c_int32, C.POINTER(C.c_int32), VP]),
     "fs_batch_create": (I, [C.POINTER(Params), C.c_int32, C.POINTER(VP)]),
@@ -173,6 +177,8 @@ SIGNATURES = {
     "fs_batch_sync": (I, [VP]),
     "fs_batch_time_steps": (I, [VP, C.POINTER(D), C.c_int32, C.POINTER(D)]),
     "fs_batch_launch_count": (C.c_int64, [VP]),
+    "fs_batch_autotune_tiles": (I, [VP, C.POINTER(D), C.c_int32, C.POINTER(D)]),
+    "fs_batch_autotune": (I, [VP, C.POINTER(D), C.c_int32, C.POINTER(D)]),
     "fs_dump_pair": (I, [VP, C.c_int32, VP, VP, VP]),
     "fs_write_pair_file": (I, [C.c_char_p, C.c_int32, C.c_int32, D, VP, VP, VP]),
     "fs_read_pair_file": (I, [C.c_char_p, C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.POINTER(D), VP, VP, VP]),

@@ -1121,87 +1121,123 @@ FS_API int fs_set_mg_sweeps(fs_solver* h, int32_t pre, int32_t post) {
 // dye, time and pressure are saved on the device and restored between
 // candidates and at the end), and the fastest is kept.  Ties in time go to
 // fewer sweeps.  Returns the choice and its ms per step.
+// ------------------------------------------------------------- autotuning
+// A solver's step-changing state saved on the device, so that every candidate
+// setting is timed from the same state, and the timing of one candidate.
+struct TuneState {
+  Solver* s = nullptr;
+  std::vector<std::pair<void*, size_t>> planes;  // device plane, bytes per cell
+  char* save = nullptr;
+  cudaEvent_t a = nullptr, b = nullptr;
+  double t0 = 0;
+  int64_t steps0 = 0, l0 = 0, r0 = 0;
+};
+
+static cudaError_t tune_copy(TuneState& T, bool to_save) {
+  Solver* s = T.s;
+  size_t off = 0;
+  for (auto& p : T.planes) {
+    const size_t b = p.second * (size_t)s->n;
+    cudaError_t e = to_save ? cudaMemcpyAsync(T.save + off, p.first, b, cudaMemcpyDeviceToDevice, s->stream)
+                            : cudaMemcpyAsync(p.first, T.save + off, b, cudaMemcpyDeviceToDevice, s->stream);
+    if (e != cudaSuccess) return e;
+    off += b;
+  }
+  return to_save ? cudaMemcpyAsync(T.save + off, s->dev, sizeof(DevState), cudaMemcpyDeviceToDevice, s->stream)
+                 : cudaMemcpyAsync(s->dev, T.save + off, sizeof(DevState), cudaMemcpyDeviceToDevice, s->stream);
+}
+
+static cudaError_t tune_begin(Solver* s, TuneState& T) {
+  T.s = s;
+  T.planes = {{s->u, 4}, {s->v, 4}};
+  if (s->mixed) {
+    T.planes.push_back({s->ulo, 4});
+    T.planes.push_back({s->vlo, 4});
+    T.planes.push_back({s->ph, 4});
+    T.planes.push_back({s->pl, 4});
+  } else {
+    T.planes.push_back({s->p32, 4});
+  }
+  if (s->dye) T.planes.push_back({s->dye, 16});
+  size_t total = sizeof(DevState);
+  for (auto& p : T.planes) total += p.second * (size_t)s->n;
+  T.t0 = s->t;
+  T.steps0 = s->steps;
+  T.l0 = s->launches;
+  T.r0 = s->graph_replays;
+  cudaError_t e = cudaStreamSynchronize(s->stream);
+  if (e == cudaSuccess) e = cudaMalloc(&T.save, total);
+  if (e == cudaSuccess) e = cudaEventCreate(&T.a);
+  if (e == cudaSuccess) e = cudaEventCreate(&T.b);
+  if (e == cudaSuccess) e = tune_copy(T, true);
+  return e;
+}
+
+// restores the saved state and the host-side counters
+static void tune_end(TuneState& T) {
+  Solver* s = T.s;
+  if (T.save) tune_copy(T, false);
+  cudaStreamSynchronize(s->stream);
+  if (T.a) cudaEventDestroy(T.a);
+  if (T.b) cudaEventDestroy(T.b);
+  if (T.save) cudaFree(T.save);
+  T.save = nullptr;
+  s->t = T.t0;
+  s->steps = T.steps0;
+  s->launches = T.l0;
+  s->graph_replays = T.r0;
+}
+
+// ms per step of nsteps steps of the current settings from the saved state
+// (the graph is captured before the timing); 1e30 if the tolerance was missed
+static int tune_time(TuneState& T, double dt, int nsteps, double* per, cudaError_t* err) {
+  Solver* s = T.s;
+  drop_graph(s);
+  int rc = step(s, dt);
+  cudaError_t e = cudaSuccess;
+  if (rc == FS_OK) e = tune_copy(T, false);
+  if (rc == FS_OK && e == cudaSuccess) e = cudaEventRecord(T.a, s->stream);
+  for (int k = 0; k < nsteps && rc == FS_OK && e == cudaSuccess; k++) rc = step(s, dt);
+  if (e == cudaSuccess) e = cudaEventRecord(T.b, s->stream);
+  if (e == cudaSuccess) e = cudaEventSynchronize(T.b);
+  float ms = 0;
+  if (e == cudaSuccess) cudaEventElapsedTime(&ms, T.a, T.b);
+  if (rc == FS_OK && e == cudaSuccess && s->stats_on_device) {
+    DevState d;
+    e = cudaMemcpy(&d, s->dev, sizeof d, cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess && (!d.converged || d.nonfinite)) ms = 1e30f;  // must still meet the tolerance
+  }
+  if (e == cudaSuccess) e = tune_copy(T, false);
+  *per = ms / nsteps;
+  *err = e;
+  return rc;
+}
+
 FS_API int fs_autotune(fs_solver* h, double dt, int32_t nsteps, int32_t* pre_out, int32_t* post_out,
                        double* ms_out) {
   SOLVER(h);
   if (s->prm.pressure_solver != FS_PRESSURE_MULTIGRID || !s->fused)
     return fail(s, FS_ERR_UNSUPPORTED, "fs_autotune tunes the fused multigrid step");
   if (nsteps < 1 || !std::isfinite(dt)) return fail(s, FS_ERR_INVALID_ARGUMENT, "bad dt or nsteps");
-  CU(s, cudaStreamSynchronize(s->stream));
-  // planes that a step changes and the next step reads
-  std::vector<std::pair<void*, size_t>> planes = {{s->u, 4}, {s->v, 4}};
-  if (s->mixed) {
-    planes.push_back({s->ulo, 4});
-    planes.push_back({s->vlo, 4});
-    planes.push_back({s->ph, 4});
-    planes.push_back({s->pl, 4});
-  } else {
-    planes.push_back({s->p32, 4});
-  }
-  if (s->dye) planes.push_back({s->dye, 16});
-  size_t total = sizeof(DevState);
-  for (auto& p : planes) total += p.second * (size_t)s->n;
-  char* save = nullptr;
-  CU(s, cudaMalloc(&save, total));
-  auto copy = [&](bool to_save) -> cudaError_t {
-    size_t off = 0;
-    for (auto& p : planes) {
-      size_t b = p.second * (size_t)s->n;
-      cudaError_t e = to_save ? cudaMemcpyAsync(save + off, p.first, b, cudaMemcpyDeviceToDevice, s->stream)
-                              : cudaMemcpyAsync(p.first, save + off, b, cudaMemcpyDeviceToDevice, s->stream);
-      if (e != cudaSuccess) return e;
-      off += b;
-    }
-    return to_save ? cudaMemcpyAsync(save + off, s->dev, sizeof(DevState), cudaMemcpyDeviceToDevice, s->stream)
-                   : cudaMemcpyAsync(s->dev, save + off, sizeof(DevState), cudaMemcpyDeviceToDevice, s->stream);
-  };
-  const double t0 = s->t;
-  const int64_t steps0 = s->steps, l0 = s->launches, r0 = s->graph_replays;
+  TuneState T;
+  cudaError_t e = tune_begin(s, T);
   const fs_params orig = s->prm;
   int best_pre = orig.mg_pre_smooth, best_post = orig.mg_post_smooth, rc = FS_OK;
   double best = 1e300;
-  cudaError_t e = copy(true);
-  cudaEvent_t a = nullptr, b = nullptr;
-  if (e == cudaSuccess) e = cudaEventCreate(&a);
-  if (e == cudaSuccess) e = cudaEventCreate(&b);
   for (int pre = 1; pre <= 3 && e == cudaSuccess && rc == FS_OK; pre++) {
     for (int post = 1; post <= 3 && e == cudaSuccess && rc == FS_OK; post++) {
       s->prm.mg_pre_smooth = pre;
       s->prm.mg_post_smooth = post;
-      drop_graph(s);
-      rc = step(s, dt);  // captures the graph for this candidate outside the timing
-      if (rc == FS_OK) e = copy(false);
-      if (e != cudaSuccess || rc != FS_OK) break;
-      e = cudaEventRecord(a, s->stream);
-      for (int k = 0; k < nsteps && rc == FS_OK; k++) rc = step(s, dt);
-      if (e == cudaSuccess) e = cudaEventRecord(b, s->stream);
-      if (e == cudaSuccess) e = cudaEventSynchronize(b);
-      float ms = 0;
-      if (e == cudaSuccess) cudaEventElapsedTime(&ms, a, b);
-      fs_step_stats st;
-      if (rc == FS_OK && s->stats_on_device) {
-        DevState d;
-        e = cudaMemcpy(&d, s->dev, sizeof d, cudaMemcpyDeviceToHost);
-        if (e == cudaSuccess && (!d.converged || d.nonfinite)) ms = 1e30f;  // must still meet the tolerance
-      }
-      (void)st;
-      const double per = ms / nsteps;
-      if (per < best * 0.999) {
+      double per = 0;
+      rc = tune_time(T, dt, nsteps, &per, &e);
+      if (rc == FS_OK && e == cudaSuccess && per < best * 0.999) {
         best = per;
         best_pre = pre;
         best_post = post;
       }
-      if (e == cudaSuccess) e = copy(false);
     }
   }
-  if (a) cudaEventDestroy(a);
-  if (b) cudaEventDestroy(b);
-  cudaStreamSynchronize(s->stream);
-  cudaFree(save);
-  s->t = t0;
-  s->steps = steps0;
-  s->launches = l0;
-  s->graph_replays = r0;
+  tune_end(T);
   s->prm = orig;
   s->prm.mg_pre_smooth = best_pre;
   s->prm.mg_post_smooth = best_post;
@@ -1210,6 +1246,71 @@ FS_API int fs_autotune(fs_solver* h, double dt, int32_t nsteps, int32_t* pre_out
   if (e != cudaSuccess) return fail(s, FS_ERR_CUDA, std::string("fs_autotune: ") + cudaGetErrorString(e));
   if (pre_out) *pre_out = best_pre;
   if (post_out) *post_out = best_post;
+  if (ms_out) *ms_out = best;
+  return FS_OK;
+}
+
+// the levels that run the tile kernels (the fused cycle's levels above its bottom solve)
+static int tile_levels(const Solver* s) { return s->fused ? bottom_first_level(s) : 0; }
+
+FS_API int fs_set_mg_tiles(fs_solver* h, const int32_t* tiles, int32_t count) {
+  SOLVER(h);
+  if (count < 0 || count > 16 || (count > 0 && !tiles)) return fail(s, FS_ERR_INVALID_ARGUMENT, "bad tiles");
+  for (int l = 0; l < count; l++)
+    if (tiles[l] != 0 && tiles[l] != 16 && tiles[l] != 32 && tiles[l] != 64)
+      return fail(s, FS_ERR_INVALID_ARGUMENT, "a tile side is 16, 32, 64 or 0 (the built-in rule)");
+  for (int l = 0; l < 16; l++) s->tile_level[l] = l < count ? tiles[l] : 0;
+  drop_graph(s);
+  return FS_OK;
+}
+
+FS_API int fs_get_mg_tiles(fs_solver* h, int32_t* tiles, int32_t cap, int32_t* count) {
+  SOLVER(h);
+  if (!count || cap < 0 || (cap > 0 && !tiles)) return fail(s, FS_ERR_INVALID_ARGUMENT, "bad arguments");
+  const int nl = tile_levels(s);
+  *count = nl;
+  for (int l = 0; l < nl && l < cap; l++) tiles[l] = mg_tile(s, l);
+  return FS_OK;
+}
+
+// Greedy per level: each tile level tries 64, 32 and 16 with the others fixed
+// (the tiles give the same values whatever their size, so only time counts).
+FS_API int fs_autotune_tiles(fs_solver* h, double dt, int32_t nsteps, int32_t* tiles_out, int32_t cap,
+                             int32_t* count, double* ms_out) {
+  SOLVER(h);
+  if (!s->fused) return fail(s, FS_ERR_UNSUPPORTED, "fs_autotune_tiles tunes the fused multigrid step");
+  if (nsteps < 1 || !std::isfinite(dt) || !count || cap < 0 || (cap > 0 && !tiles_out))
+    return fail(s, FS_ERR_INVALID_ARGUMENT, "bad arguments");
+  const int nl = tile_levels(s);
+  TuneState T;
+  cudaError_t e = tune_begin(s, T);
+  int rc = FS_OK;
+  double best = 1e300;
+  // the current choice first; another side must be 0.5% faster to replace it
+  for (int l = 0; l < nl && l < 16 && e == cudaSuccess && rc == FS_OK; l++) {
+    const int start = mg_tile(s, l);
+    int pick = start;
+    double here = 1e300;
+    for (int t : {start, 64, 32, 16}) {
+      if (t == start && here < 1e300) continue;
+      s->tile_level[l] = t;
+      double per = 0;
+      rc = tune_time(T, dt, nsteps, &per, &e);
+      if (rc != FS_OK || e != cudaSuccess) break;
+      if (t == start ? true : per < here * 0.995) {
+        here = per;
+        pick = t;
+      }
+    }
+    s->tile_level[l] = pick;
+    best = here;
+  }
+  tune_end(T);
+  drop_graph(s);
+  if (rc != FS_OK) return rc;
+  if (e != cudaSuccess) return fail(s, FS_ERR_CUDA, std::string("fs_autotune_tiles: ") + cudaGetErrorString(e));
+  *count = nl;
+  for (int l = 0; l < nl && l < cap; l++) tiles_out[l] = s->tile_level[l];
   if (ms_out) *ms_out = best;
   return FS_OK;
 }
@@ -1369,7 +1470,7 @@ static bool same_class(const Solver* a, const Solver* b) {
   return a->g.nx == b->g.nx && a->g.ny == b->g.ny && p.mg_pre_smooth == q.mg_pre_smooth &&
          p.mg_post_smooth == q.mg_post_smooth && p.mg_coarse_sweeps == q.mg_coarse_sweeps &&
          p.mg_min_size == q.mg_min_size && p.relax == q.relax && p.max_cycles == q.max_cycles &&
-         a->lev.size() == b->lev.size();
+         a->lev.size() == b->lev.size() && std::equal(a->tile_level, a->tile_level + 16, b->tile_level);
 }
 
 // the class's conditional loop on cs (already part of the batch capture):
@@ -1733,4 +1834,137 @@ FS_API int64_t fs_batch_launch_count(fs_batch* b) {
       for (size_t c = 0; c < it.size(); c++) n += it[c] * b->classes[c].body_launches;
   }
   return n;
+}
+
+// Settings of the batch's size classes picked by timing whole batch steps, each
+// candidate from the same saved state of every member (restored afterwards):
+// what & 1, the (pre, post) sweep pair of each class; what & 2, greedy per
+// class and tile level, the tile side (64, 32, 16; the tiles give the same
+// values whatever their size).
+static int batch_autotune(fs_batch* b, const double* dt, int32_t nsteps, int what, double* ms_out) {
+  if (!b) return bfail(nullptr, FS_ERR_INVALID_ARGUMENT, "batch is NULL");
+  if (!dt || nsteps < 1) return bfail(b, FS_ERR_INVALID_ARGUMENT, "bad dt or nsteps");
+  if (cudaSetDevice(b->device) != cudaSuccess) return bfail(b, FS_ERR_CUDA, "cudaSetDevice failed");
+  const int n = (int)b->members.size();
+  for (int i = 0; i < n; i++)
+    if (!std::isfinite(dt[i])) return bfail(b, FS_ERR_INVALID_ARGUMENT, "dt must be finite");
+  const int64_t launches_before = fs_batch_launch_count(b);
+  const int64_t replays_before = b->replays;
+  int rc = batch_build(b, dt);
+  if (rc) return rc;
+  std::vector<TuneState> T(n);
+  cudaError_t e = cudaSuccess;
+  for (int i = 0; i < n && e == cudaSuccess; i++) e = tune_begin(&b->members[i]->s, T[i]);
+  cudaEvent_t ea = nullptr, eb = nullptr;
+  if (e == cudaSuccess) e = cudaEventCreate(&ea);
+  if (e == cudaSuccess) e = cudaEventCreate(&eb);
+  // ms per batch step of the current settings from the saved state; 1e30 if a member missed its tolerance
+  auto time_batch = [&](double* per) -> int {
+    for (int i = 0; i < n && e == cudaSuccess; i++) e = tune_copy(T[i], false);
+    for (int i = 0; i < n; i++) b->members[i]->s.batch_dirty = true;
+    int r = e == cudaSuccess ? fs_batch_step(b, dt) : FS_ERR_CUDA;  // captures outside the timing
+    for (int i = 0; i < n && e == cudaSuccess && r == FS_OK; i++) e = tune_copy(T[i], false);
+    if (r == FS_OK && e == cudaSuccess) e = cudaEventRecord(ea, b->stream);
+    for (int k = 0; k < nsteps && r == FS_OK && e == cudaSuccess; k++) r = fs_batch_step(b, dt);
+    if (e == cudaSuccess) e = cudaEventRecord(eb, b->stream);
+    if (e == cudaSuccess) e = cudaEventSynchronize(eb);
+    float ms = 0;
+    if (e == cudaSuccess) cudaEventElapsedTime(&ms, ea, eb);
+    for (int i = 0; i < n && r == FS_OK && e == cudaSuccess; i++) {
+      Solver* s = &b->members[i]->s;
+      if (!s->stats_on_device) continue;
+      DevState d;
+      e = cudaMemcpy(&d, s->dev, sizeof d, cudaMemcpyDeviceToHost);
+      if (e == cudaSuccess && (!d.converged || d.nonfinite)) ms = 1e30f;
+    }
+    *per = ms / nsteps;
+    return r;
+  };
+  double best = 1e300;
+  if (e == cudaSuccess) rc = time_batch(&best);
+  const std::vector<BatchClass> classes = b->classes;
+  // sweep pairs per class: a pair must be 1% faster than the current one
+  for (const BatchClass& c : classes) {
+    if (!(what & 1) || rc != FS_OK || e != cudaSuccess) break;
+    Solver* lead = &b->members[c.idx[0]]->s;
+    int bp = lead->prm.mg_pre_smooth, bq = lead->prm.mg_post_smooth;
+    for (int pre = 1; pre <= 3 && rc == FS_OK && e == cudaSuccess; pre++)
+      for (int post = 1; post <= 3 && rc == FS_OK && e == cudaSuccess; post++) {
+        if (pre == bp && post == bq) continue;
+        const int op = lead->prm.mg_pre_smooth, oq = lead->prm.mg_post_smooth;
+        for (int i : c.idx) {
+          b->members[i]->s.prm.mg_pre_smooth = pre;
+          b->members[i]->s.prm.mg_post_smooth = post;
+        }
+        double per = 0;
+        rc = time_batch(&per);
+        if (rc == FS_OK && e == cudaSuccess && per < best * 0.99) {
+          best = per;
+          bp = pre;
+          bq = post;
+        }
+        for (int i : c.idx) {
+          b->members[i]->s.prm.mg_pre_smooth = op;
+          b->members[i]->s.prm.mg_post_smooth = oq;
+        }
+      }
+    for (int i : c.idx) {
+      b->members[i]->s.prm.mg_pre_smooth = bp;
+      b->members[i]->s.prm.mg_post_smooth = bq;
+      drop_graph(&b->members[i]->s);
+    }
+  }
+  for (const BatchClass& c : classes) {
+    if (!(what & 2) || rc != FS_OK || e != cudaSuccess) break;
+    Solver* lead = &b->members[c.idx[0]]->s;
+    const int nl = std::min(bottom_first_level(lead), 16);
+    // the class's current choice (timed as `best`) stays unless another side
+    // is 1% faster: one class level moves a whole batch step only a little,
+    // so smaller differences are within the timing noise
+    for (int l = 0; l < nl && rc == FS_OK && e == cudaSuccess; l++) {
+      const int start = lead->tile_level[l];
+      int pick = start;
+      for (int t : {64, 32, 16}) {
+        for (int i : c.idx) b->members[i]->s.tile_level[l] = t;
+        double per = 0;
+        rc = time_batch(&per);
+        if (rc != FS_OK || e != cudaSuccess) break;
+        if (per < best * 0.99) {
+          best = per;
+          pick = t;
+        }
+      }
+      // the side in use, written out (the class rule when nothing beat it)
+      for (int i : c.idx) b->members[i]->s.tile_level[l] = start;
+      if (pick == 0) pick = mg_tile_class(lead, l, (int)c.idx.size());
+      for (int i : c.idx) b->members[i]->s.tile_level[l] = pick;
+    }
+  }
+  for (int i = 0; i < n; i++) {
+    if (T[i].s) tune_end(T[i]);
+    b->members[i]->s.batch_dirty = true;
+  }
+  if (ea) cudaEventDestroy(ea);
+  if (eb) cudaEventDestroy(eb);
+  // the tuning steps are not part of the batch's history
+  if (b->exec) cudaGraphExecDestroy(b->exec);
+  b->exec = nullptr;
+  (void)replays_before;
+  b->replays = 0;  // launches_before counts every replay so far
+  b->replays_at_build = 0;
+  b->launches_done = launches_before;
+  for (int i = 0; i < n; i++) b->members[i]->s.batch_launches_fixed = 0;
+  b->classes.clear();
+  if (rc != FS_OK) return rc;
+  if (e != cudaSuccess) return bfail(b, FS_ERR_CUDA, std::string("batch autotune: ") + cudaGetErrorString(e));
+  if (ms_out) *ms_out = best;
+  return FS_OK;
+}
+
+FS_API int fs_batch_autotune_tiles(fs_batch* b, const double* dt, int32_t nsteps, double* ms_out) {
+  return batch_autotune(b, dt, nsteps, 2, ms_out);
+}
+
+FS_API int fs_batch_autotune(fs_batch* b, const double* dt, int32_t nsteps, double* ms_out) {
+  return batch_autotune(b, dt, nsteps, 1, ms_out);
 }

@@ -97,6 +97,7 @@ struct Solver {
   void* stage = nullptr;     // n doubles: host I/O conversion staging
 
   std::vector<Level> lev;
+  int tile_level[16] = {};  // tile side of each tile level's kernels; 0 = the built-in rule
   // TMA tensor maps of the advected fields, by device pointer (fs_advect.cu)
   std::vector<std::pair<const void*, CUtensorMap>> tmaps;
 
@@ -241,6 +242,11 @@ void mg_vcycle(Solver* s);
 // double-float pressure (acc_h, acc_l) in place instead of writing lev[0].x2
 void mg_vcycle_fused(Solver* s, bool first_has_x, float* acc_h = nullptr, float* acc_l = nullptr);
 bool mg_fused_supported(const Solver* s);
+// tile side of the kernels of level l (an override or the built-in rule)
+int mg_tile(const Solver* s, int l);
+// tile side of level l of a batch size class of count members led by s0
+int mg_tile_class(const Solver* s0, int l, int count);
+int bottom_first_level(const Solver* s);
 // batched refinement cycle of one size class of a batch (fs_multigrid.cu, fs_pressure.cu)
 int mg_vcycle_class(Solver* const* ms, int count, cudaStream_t st);
 void launch_refine_class(Solver* const* ms, int count, cudaStream_t st);

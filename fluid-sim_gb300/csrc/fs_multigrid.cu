@@ -711,6 +711,11 @@ static int tile_for(int n) {
   return 16;
 }
 
+int mg_tile(const Solver* s, int l) {
+  if (l >= 0 && l < 16 && s->tile_level[l]) return s->tile_level[l];
+  return tile_for(s->lev[l].n);
+}
+
 // profile name of a tile kernel: one entry per level ("mg_down_l0", ...)
 static std::string level_name(const Solver* s, const Level& L, const char* base) {
   return std::string(base) + "_l" + std::to_string(&L - s->lev.data());
@@ -729,7 +734,7 @@ static void down_t(Solver* s, Level& L, const Level& C, bool has_x) {
 
 template <int H>
 static void down(Solver* s, Level& L, const Level& C, bool has_x) {
-  switch (tile_for(L.n)) {
+  switch (mg_tile(s, (int)(&L - s->lev.data()))) {
     case 64: down_t<64, H>(s, L, C, has_x); break;
     case 32: down_t<32, H>(s, L, C, has_x); break;
     default: down_t<16, H>(s, L, C, has_x); break;
@@ -782,7 +787,7 @@ static void up_t(Solver* s, Level& L, const Level& C, float* acc_h, float* acc_l
 
 template <int H>
 static void up(Solver* s, Level& L, const Level& C, float* acc_h, float* acc_l) {
-  switch (tile_for(L.n)) {
+  switch (mg_tile(s, (int)(&L - s->lev.data()))) {
     case 64: up_t<64, H>(s, L, C, acc_h, acc_l); break;
     case 32: up_t<32, H>(s, L, C, acc_h, acc_l); break;
     default: up_t<16, H>(s, L, C, acc_h, acc_l); break;
@@ -925,9 +930,12 @@ static void down_class_t(Solver* const* ms, int count, int l, cudaStream_t st) {
                                                       (float)ms[0]->prm.relax, ms[0]->prm.max_cycles);
 }
 
-// tile side for a level of a class: like tile_for, counting the CTAs of all
-// members (the tiles give the same values whatever their size)
-static int tile_for_class(int n, int count) {
+// tile side for a level of a class: an override of the class's members, else
+// like tile_for counting the CTAs of all members (the tiles give the same
+// values whatever their size)
+static int tile_for_class(const Solver* s0, int l, int count) {
+  if (l < 16 && s0->tile_level[l]) return s0->tile_level[l];
+  const int n = s0->lev[l].n;
   for (int t : {64, 32}) {
     int c = (n + t - 1) / t;
     if (c * c * count >= 256) return t;
@@ -935,9 +943,11 @@ static int tile_for_class(int n, int count) {
   return 16;
 }
 
+int mg_tile_class(const Solver* s0, int l, int count) { return tile_for_class(s0, l, count); }
+
 template <int H>
 static void down_class(Solver* const* ms, int count, int l, cudaStream_t st) {
-  switch (tile_for_class(ms[0]->lev[l].n, count)) {
+  switch (tile_for_class(ms[0], l, count)) {
     case 64: down_class_t<64, H>(ms, count, l, st); break;
     case 32: down_class_t<32, H>(ms, count, l, st); break;
     default: down_class_t<16, H>(ms, count, l, st); break;
@@ -972,7 +982,7 @@ static void up_class_t(Solver* const* ms, int count, int l, cudaStream_t st) {
 template <int H>
 static void up_class(Solver* const* ms, int count, int l, cudaStream_t st) {
   const bool acc = l == 0;
-  switch (tile_for_class(ms[0]->lev[l].n, count)) {
+  switch (tile_for_class(ms[0], l, count)) {
     case 64: acc ? up_class_t<64, H, true>(ms, count, l, st) : up_class_t<64, H, false>(ms, count, l, st); break;
     case 32: acc ? up_class_t<32, H, true>(ms, count, l, st) : up_class_t<32, H, false>(ms, count, l, st); break;
     default: acc ? up_class_t<16, H, true>(ms, count, l, st) : up_class_t<16, H, false>(ms, count, l, st); break;

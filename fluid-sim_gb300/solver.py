@@ -312,6 +312,24 @@ class GPUFluidSolver:
         self.params.mg_pre_smooth, self.params.mg_post_smooth = pre.value, post.value
         return {"pre": pre.value, "post": post.value, "ms_per_step": ms.value}
 
+    def set_mg_tiles(self, tiles) -> None:
+        """tile side (16, 32, 64; 0 = built-in rule) of each multigrid tile level"""
+        t = (C.c_int32 * 16)(*list(tiles))
+        self._chk(self._lib.fs_set_mg_tiles(self._h, t, len(tiles)))
+
+    def mg_tiles(self) -> list:
+        """tile sides in use, one per multigrid tile level"""
+        t, n = (C.c_int32 * 16)(), C.c_int32()
+        self._chk(self._lib.fs_get_mg_tiles(self._h, t, 16, C.byref(n)))
+        return list(t[: n.value])
+
+    def autotune_tiles(self, dt: float, nsteps: int = 5) -> dict:
+        """time 64, 32 and 16 cell tiles per multigrid level from the current
+        state (greedy, level by level), keep the fastest; state restored"""
+        t, n, ms = (C.c_int32 * 16)(), C.c_int32(), C.c_double()
+        self._chk(self._lib.fs_autotune_tiles(self._h, dt, nsteps, t, 16, C.byref(n), C.byref(ms)))
+        return {"tiles": self.mg_tiles(), "ms_per_step": ms.value}
+
     def render(self, mode: str = "vorticity", exposure: float = 1.0) -> np.ndarray:
         """RENDER arithmetic (shaders.js:677-768) into an [ny, nx, 4] f32 array"""
         out = np.empty((self.ny, self.nx, 4), np.float32)
@@ -416,19 +434,31 @@ class GPUFluidBatch:
         return int(self._lib.fs_batch_launch_count(self._h))
 
     def autotune(self, dt, nsteps: int = 3) -> dict:
-        """Sweep counts per domain size: the first member of each size is tuned
-        (fs_autotune, its state restored afterwards) and its choice is applied
-        to every member of that size.  Returns {(nx, ny): (pre, post)}."""
-        d, _ = self._dts(dt)
+        """Sweep counts per size class, each candidate timed as whole batch
+        steps from one saved state (fs_batch_autotune, state restored).
+        Returns {(nx, ny): (pre, post)}."""
+        d, arr = self._dts(dt)
+        ms = C.c_double()
+        self._chk(self._lib.fs_batch_autotune(self._h, arr, nsteps, C.byref(ms)))
         picks = {}
-        for m, dtm in zip(self.members, d):
-            key = (m.nx, m.ny)
-            if key not in picks:
-                r = m.autotune(float(dtm), nsteps)
-                picks[key] = (r["pre"], r["post"])
-            else:
-                m.set_mg_sweeps(*picks[key])
+        for m in self.members:
+            p = L.Params()
+            m._chk(self._lib.fs_get_params(m._h, C.byref(p)))
+            m.params.mg_pre_smooth, m.params.mg_post_smooth = p.mg_pre_smooth, p.mg_post_smooth
+            picks.setdefault((m.nx, m.ny), (p.mg_pre_smooth, p.mg_post_smooth))
         return picks
+
+    def autotune_tiles(self, dt, nsteps: int = 3) -> dict:
+        """Tile sides per size class and multigrid level, each candidate timed
+        as whole batch steps from one saved state (fs_batch_autotune_tiles).
+        Returns {(nx, ny): tiles} and the tuned ms per batch step."""
+        d, arr = self._dts(dt)
+        ms = C.c_double()
+        self._chk(self._lib.fs_batch_autotune_tiles(self._h, arr, nsteps, C.byref(ms)))
+        picks = {}
+        for m in self.members:
+            picks.setdefault((m.nx, m.ny), m.mg_tiles())
+        return {"tiles": picks, "ms_per_step": ms.value}
 
     def destroy(self) -> None:
         if getattr(self, "_h", None):

@@ -390,6 +390,18 @@ FS_API int fs_total_cycles(fs_solver* s, int64_t* cycles);
  * keeps the fastest that still meets pressure_tol; the state, dye, time and
  * pressure are restored afterwards.  No reference counterpart. */
 FS_API int fs_autotune(fs_solver* s, double dt, int32_t nsteps, int32_t* pre, int32_t* post, double* ms_per_step);
+/* Tile sides (16, 32 or 64 cells) of the fused multigrid kernels of each tile
+ * level (the levels above the bottom solve); 0 = the built-in rule (the
+ * largest tile that still gives >= 256 CTAs).  The tiles give the same values
+ * whatever their size, so they change only the speed. */
+FS_API int fs_set_mg_tiles(fs_solver* s, const int32_t* tiles, int32_t count);
+/* the sides in use, one per tile level (*count = number of tile levels) */
+FS_API int fs_get_mg_tiles(fs_solver* s, int32_t* tiles, int32_t cap, int32_t* count);
+/* Greedy per level: every tile level tries 64, 32 and 16 (the others fixed),
+ * each timed over nsteps steps from the same saved state; keeps the fastest.
+ * The state and time are restored; tiles_out gets the picks (0 = rule kept). */
+FS_API int fs_autotune_tiles(fs_solver* s, double dt, int32_t nsteps, int32_t* tiles_out, int32_t cap,
+                             int32_t* count, double* ms_per_step);
 
 /* ------------------------------------------------------------------------
  * Diagnostics on the device (the reference reads the fields back and loops
@@ -437,6 +449,13 @@ FS_API int fs_batch_sync(fs_batch* b);
 /* nsteps batch steps between two events on the batch stream (capture first) */
 FS_API int fs_batch_time_steps(fs_batch* b, const double* dt, int32_t nsteps, double* elapsed_ms);
 FS_API int64_t fs_batch_launch_count(fs_batch* b);
+/* tile sides per size class and tile level, greedy, each candidate timed as
+ * nsteps whole batch steps from the same saved state of every member (which
+ * is restored); the picks are set on the members (fs_get_mg_tiles) */
+FS_API int fs_batch_autotune_tiles(fs_batch* b, const double* dt, int32_t nsteps, double* ms_per_step);
+/* the (pre, post) sweep pair of each size class, timed the same way; the
+ * picks are set on the members (fs_params mg_pre_smooth / mg_post_smooth) */
+FS_API int fs_batch_autotune(fs_batch* b, const double* dt, int32_t nsteps, double* ms_per_step);
 
 #ifdef __cplusplus
 }

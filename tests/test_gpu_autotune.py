@@ -42,3 +42,58 @@ def test_set_mg_sweeps(fs):
     with pytest.raises(fs.FluidError):
         j.autotune(0.01)
     j.destroy()
+
+
+def _mixed(fs, n, **kw):
+    return fs.GPUFluidSolver(n=n, nu=1e-3, advection="maccormack", pressure_solver="multigrid",
+                             pressure_iterations=1, precision="mixed", pressure_tol=1e-8, max_cycles=60, **kw)
+
+
+def test_tile_sides_do_not_change_results(fs, O):
+    """The fused tiles give the same values whatever their size: three steps at
+    1024^2 with every tile level at 16, 32 or 64 cells, or mixed, equal the
+    built-in choice bit for bit (fields and cycle counts)."""
+    n = 1024
+    u0, v0 = O.lcg_uv(73, n * n)
+    out = []
+    for tiles in (None, [16, 16, 16, 16], [64, 64, 64, 64], [32, 64, 16, 32]):
+        s = _mixed(fs, n)
+        if tiles is not None:
+            s.set_mg_tiles(tiles)
+            assert s.mg_tiles() == tiles
+        s.upload_velocity(u0, v0)
+        cyc = []
+        for _ in range(3):
+            s.step(0.002)
+            cyc.append(s.last_stats()["cycles"])
+        u, v = s.read_velocity()
+        out.append((u, v, s.read_field("pressure"), cyc))
+        s.destroy()
+    for o in out[1:]:
+        assert all(np.array_equal(a, b) for a, b in zip(o[:3], out[0][:3])) and o[3] == out[0][3]
+
+
+def test_autotune_tiles_restores_state(fs, O):
+    n = 512
+    u0, v0 = O.lcg_uv(74, n * n)
+    s = _mixed(fs, n)
+    s.upload_velocity(u0, v0)
+    s.step(0.002)
+    before = s.read_velocity()
+    t0, k0 = s.t, s.steps
+    r = s.autotune_tiles(0.002, 2)
+    assert len(r["tiles"]) == 3 and all(t in (16, 32, 64) for t in r["tiles"]) and r["ms_per_step"] > 0
+    after = s.read_velocity()
+    assert np.array_equal(before[0], after[0]) and np.array_equal(before[1], after[1])
+    assert s.t == t0 and s.steps == k0
+    # the tuned solver steps on exactly like one that was never tuned
+    ref = _mixed(fs, n)
+    ref.upload_velocity(u0, v0)
+    ref.step(0.002)
+    ref.step(0.002)
+    s.step(0.002)
+    assert np.array_equal(s.read_velocity()[0], ref.read_velocity()[0])
+    with pytest.raises(fs.FluidError):
+        s.set_mg_tiles([48])
+    s.destroy()
+    ref.destroy()

@@ -134,3 +134,34 @@ def test_batch_mixed_paths_equal_independent_solvers(pkg):
         assert b.members[i].last_stats()["cycles"] == s.last_stats()["cycles"]
         s.destroy()
     b.destroy()
+
+
+def test_batch_tile_autotune_keeps_results(pkg):
+    """fs_batch_autotune_tiles times tile sides per class and level from one
+    saved state, restores it, and the tuned batch still equals the members
+    stepped alone bit for bit (the tiles give the same values whatever their size)."""
+    sides = [128, 128, 256, 64]
+    states = _members(pkg, sides, 80)
+    b = pkg.GPUFluidBatch([dict(n=n, **CFG) for n in sides])
+    for m, (u, v, _) in zip(b.members, states):
+        m.upload_velocity(u, v)
+    dts = [dt for _, _, dt in states]
+    b.step(dts)
+    b.sync()
+    before = [m.read_velocity()[0] for m in b.members]
+    r = b.autotune_tiles(dts, 1)
+    assert r["ms_per_step"] > 0 and set(r["tiles"]) == {(128, 128), (256, 256), (64, 64)}
+    assert all(np.array_equal(x, m.read_velocity()[0]) for x, m in zip(before, b.members))
+    for _ in range(2):
+        b.step(dts)
+    b.sync()
+    for i, (n, (u, v, dt)) in enumerate(zip(sides, states)):
+        s = pkg.GPUFluidSolver(n=n, **CFG)
+        s.upload_velocity(u, v)
+        for _ in range(3):
+            s.step(dt)
+        assert np.array_equal(b.members[i].read_velocity()[0], s.read_velocity()[0]), f"member {i}"
+        assert b.members[i].steps == 3
+        s.destroy()
+    assert b.launch_count() > 0
+    b.destroy()
