@@ -647,6 +647,8 @@ __global__ void __launch_bounds__(256)
              const int* __restrict__ tiles, int nx, int ny, float dx,
              float dy, float lx, float ly, float width, double dA, float* __restrict__ imp,
              double* __restrict__ dimp) {
+  // per-warp impulse sums of every disk, folded per CTA after the loop
+  __shared__ float wsum[FS_MAX_DISKS][8][3];
   const int t = __ldg(tiles + blockIdx.x), ntx = (nx + 31) >> 5;
   int i = (t % ntx) * 32 + threadIdx.x, j = (t / ntx) * 8 + threadIdx.y;
   bool in = i < nx && j < ny;
@@ -690,32 +692,48 @@ __global__ void __launch_bounds__(256)
     tix += fx;
     tiy += fy;
     tit += tq;
-    // warp sum of this disk's impulse (only warps that touched the disk), one
-    // f64 atomic per warp; the order of the atomics is not fixed, so the
-    // impulse sums (not the velocity field) may differ in the last bits run to run
-    if (dimp && __any_sync(0xffffffffu, fx != 0.f || fy != 0.f || tq != 0.f)) {
-      float sx = fx, sy = fy, st = tq;
-      for (int o = 16; o > 0; o >>= 1) {
-        sx += __shfl_xor_sync(0xffffffffu, sx, o);
-        sy += __shfl_xor_sync(0xffffffffu, sy, o);
-        st += __shfl_xor_sync(0xffffffffu, st, o);
+    // warp sum of this disk's impulse (the shuffles only in warps that
+    // touched the disk)
+    if (dimp) {
+      float sx = 0.f, sy = 0.f, st = 0.f;
+      if (__any_sync(0xffffffffu, fx != 0.f || fy != 0.f || tq != 0.f)) {
+        sx = fx; sy = fy; st = tq;
+        for (int o = 16; o > 0; o >>= 1) {
+          sx += __shfl_xor_sync(0xffffffffu, sx, o);
+          sy += __shfl_xor_sync(0xffffffffu, sy, o);
+          st += __shfl_xor_sync(0xffffffffu, st, o);
+        }
       }
-      if ((threadIdx.x & 31) == 0) {
-        atomicAdd(dimp + 3 * k + 0, (double)sx * dA);
-        atomicAdd(dimp + 3 * k + 1, (double)sy * dA);
-        atomicAdd(dimp + 3 * k + 2, (double)st * dA);
+      if (threadIdx.x == 0) {
+        wsum[k][threadIdx.y][0] = sx;
+        wsum[k][threadIdx.y][1] = sy;
+        wsum[k][threadIdx.y][2] = st;
       }
     }
   }
-  if (!in) return;
-  if (loaded) {
-    u[c] = uu;
-    v[c] = vv;
+  if (in) {
+    if (loaded) {
+      u[c] = uu;
+      v[c] = vv;
+    }
+    if (imp) {
+      imp[c] = tix;
+      imp[(int64_t)nx * ny + c] = tiy;
+      imp[2 * (int64_t)nx * ny + c] = tit;
+    }
   }
-  if (imp) {
-    imp[c] = tix;
-    imp[(int64_t)nx * ny + c] = tiy;
-    imp[2 * (int64_t)nx * ny + c] = tit;
+  if (!dimp) return;
+  // one f64 atomic per CTA, disk and component (a per-warp atomic made the
+  // warps of a large disk queue on one address); the order of the atomics is
+  // not fixed, so the impulse sums (not the velocity field) may differ in the
+  // last bits run to run
+  __syncthreads();
+  for (int q = threadIdx.y * 32 + threadIdx.x; q < 3 * ndisk; q += 256) {
+    const int k = q / 3, comp = q - 3 * k;
+    double sum = 0.0;
+#pragma unroll
+    for (int w = 0; w < 8; w++) sum += (double)wsum[k][w][comp];
+    if (sum != 0.0) atomicAdd(dimp + q, sum * dA);
   }
 }
 

@@ -410,7 +410,9 @@ static int capture_tolerance_loop(Solver* s) {
 //    max|div u| <= tol or max_cycles.  In a captured step the loop is a
 //    conditional node evaluated on the device; otherwise the host reads the
 //    residual after every cycle.
-static int pressure_solve(Solver* s, bool capture, bool defer = false) {
+// started: launch_div_start has already set the zero-pressure residual, the
+// zeroed pressure and max|r| (MIXED, no guess, no warm start).
+static int pressure_solve(Solver* s, bool capture, bool defer = false, bool started = false) {
   const fs_params& P = s->prm;
   const int iters = P.pressure_iterations;
   const bool tol = P.pressure_tol > 0;
@@ -423,6 +425,8 @@ static int pressure_solve(Solver* s, bool capture, bool defer = false) {
     if (rc) return rc;
     if (s->mixed) launch_refine_init(s, s->dh, s->dl, s->ph, s->pl, s->r32, false);
     else if (tol) launch_absmax_residual32(s, s->p32, s->div32);
+  } else if (started) {
+    // nothing left to start
   } else if (s->mixed) {
     launch_refine_init(s, s->dh, s->dl, s->ph, s->pl, s->r32, !P.warm_start);
     if (!P.warm_start) {
@@ -482,9 +486,11 @@ static int project_finish(Solver* s, const float* wu, const float* wv) {
 
 // defer: stop after the start of the pressure solve (see pressure_solve)
 static int project_from(Solver* s, const float* wu, const float* wv, bool capture, bool defer = false) {
-  if (s->mixed) launch_div_df(s, wu, nullptr, wv, nullptr, s->dh, s->dl);
+  const bool start = s->mixed && !s->guess && !s->prm.warm_start;
+  if (start) launch_div_start(s, wu, wv);
+  else if (s->mixed) launch_div_df(s, wu, nullptr, wv, nullptr, s->dh, s->dl);
   else launch_divergence<float, float>(s, wu, wv, s->div32);
-  int rc = pressure_solve(s, capture, defer);
+  int rc = pressure_solve(s, capture, defer, start);
   if (defer) return rc;
   int rc2 = project_finish(s, wu, wv);
   return rc ? rc : rc2;
@@ -1631,10 +1637,10 @@ static int batch_build(fs_batch* b, const double* dt) {
       }
       const int count = (int)ms.size();
       launch_front_advect_class(ms.data(), count, cdt.data(), cs);
-      launch_front_project_class(ms.data(), count, wu.data(), wv.data(), cdt.data(), cs);
+      const int nproj = launch_front_project_class(ms.data(), count, wu.data(), wv.data(), cdt.data(), cs);
       rc = capture_class_loop(b, b->classes[c], cs, b->d_iters + c, 2);
       if (rc == FS_OK) launch_back_class(ms.data(), count, wu.data(), wv.data(), cdt.data(), cs);
-      class_fixed += (ms[0]->prm.advection == FS_ADVECT_MACCORMACK ? 2 : 1) + (ms[0]->prm.nu > 0 ? 1 : 0) + 3 + 2;
+      class_fixed += (ms[0]->prm.advection == FS_ADVECT_MACCORMACK ? 2 : 1) + (ms[0]->prm.nu > 0 ? 1 : 0) + nproj + 2;
       if (rc == FS_OK && cudaGetLastError() != cudaSuccess) rc = bfail(b, FS_ERR_CUDA, "batch: class launch failed");
       if (rc == FS_OK && cudaEventRecord(b->class_done[c], cs) != cudaSuccess) rc = FS_ERR_CUDA;
       if (rc == FS_OK && cudaStreamWaitEvent(b->stream, b->class_done[c], 0) != cudaSuccess) rc = FS_ERR_CUDA;

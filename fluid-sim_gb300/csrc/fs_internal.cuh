@@ -221,6 +221,8 @@ void launch_fill64(Solver* s, double* x, double value, int64_t n);
 // mixed-precision refinement (double-float pressure and divergence)
 void launch_refine_init(Solver* s, const float* dh, const float* dl, const float* ph, const float* pl,
                         float* r32, bool zero_p);
+// divergence + zero-pressure residual + zeroed pressure in one pass (MIXED)
+void launch_div_start(Solver* s, const float* wu, const float* wv);
 void launch_refine_update(Solver* s, const float* ph, const float* pl, const float* e, const float* dh,
                           const float* dl, float* poh, float* pol, float* r32);
 // reductions (results land in s->red_out)
@@ -254,8 +256,8 @@ void launch_cond_class(Solver* const* ms, int count, cudaStream_t st, cudaGraphC
                        long long* iterations);
 // the rest of the step of a class whose members are plain (fs_advect.cu, fs_pressure.cu)
 void launch_front_advect_class(Solver* const* ms, int count, const double* dts, cudaStream_t st);
-void launch_front_project_class(Solver* const* ms, int count, const float* const* wu, const float* const* wv,
-                                const double* dts, cudaStream_t st);
+int launch_front_project_class(Solver* const* ms, int count, const float* const* wu, const float* const* wv,
+                               const double* dts, cudaStream_t st);  // returns its launch count
 void launch_back_class(Solver* const* ms, int count, const float* const* wu, const float* const* wv,
                        const double* dts, cudaStream_t st);
 

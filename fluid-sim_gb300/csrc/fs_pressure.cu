@@ -286,6 +286,59 @@ __device__ __forceinline__ void div_df_body(const float* __restrict__ uh, const 
   dl[c] = d.lo;
 }
 
+// the same divergence of f32 faces (no lo planes) from the four face values
+__device__ __forceinline__ df div_f32_faces(float uc, float ur, float vc, float vt, df idx, df idy) {
+  return df_add(df_mul(two_diff(ur, uc), idx), df_mul(two_diff(vt, vc), idy));
+}
+
+// The start of a refinement from zero pressure in one pass over the cells:
+// d = div w as double-float (dh, dl), its residual against p = 0 as
+// r32 = (float) d, the pressure planes (ph, pl) zeroed and max|r| reduced --
+// the work of k_div_df, k_refine_init (zero_p) and two fills, with the same
+// arithmetic per cell.  Four consecutive cells per thread (nx a multiple of
+// 4), so a thread keeps five 16-byte loads in flight; tiles of 32 quads x 8
+// rows walked by the capped reduction grid.
+__device__ __forceinline__ void div_start4_body(const float* __restrict__ wu, const float* __restrict__ wv,
+                                                float* __restrict__ dh, float* __restrict__ dl,
+                                                float* __restrict__ ph, float* __restrict__ pl,
+                                                float* __restrict__ r32, int nx, int ny, df idx, df idy,
+                                                const RedCtx& ctx) {
+  float m = 0.f;
+  const int nq = nx >> 2;
+  for (int ty = blockIdx.y, nty = (ny + 7) >> 3; ty < nty; ty += gridDim.y)
+    for (int tx = blockIdx.x, ntx = (nq + 31) >> 5; tx < ntx; tx += gridDim.x) {
+      const int q = tx * 32 + threadIdx.x, j = ty * 8 + threadIdx.y;
+      if (q >= nq || j >= ny) continue;
+      const int i0 = q << 2;
+      const int jp = j + 1 == ny ? 0 : j + 1, ir = i0 + 4 == nx ? 0 : i0 + 4;
+      const int64_t r = (int64_t)j * nx;
+      const float4 u4 = __ldg(reinterpret_cast<const float4*>(wu + r + i0));
+      const float4 v4 = __ldg(reinterpret_cast<const float4*>(wv + r + i0));
+      const float4 t4 = __ldg(reinterpret_cast<const float4*>(wv + (int64_t)jp * nx + i0));
+      const float ur = __ldg(wu + r + ir);
+      const df d0 = div_f32_faces(u4.x, u4.y, v4.x, t4.x, idx, idy);
+      const df d1 = div_f32_faces(u4.y, u4.z, v4.y, t4.y, idx, idy);
+      const df d2 = div_f32_faces(u4.z, u4.w, v4.z, t4.z, idx, idy);
+      const df d3 = div_f32_faces(u4.w, ur, v4.w, t4.w, idx, idy);
+      const float4 rf = {df_to_f(d0), df_to_f(d1), df_to_f(d2), df_to_f(d3)};
+      const float4 zero = {0.f, 0.f, 0.f, 0.f};
+      *reinterpret_cast<float4*>(dh + r + i0) = float4{d0.hi, d1.hi, d2.hi, d3.hi};
+      *reinterpret_cast<float4*>(dl + r + i0) = float4{d0.lo, d1.lo, d2.lo, d3.lo};
+      *reinterpret_cast<float4*>(r32 + r + i0) = rf;
+      *reinterpret_cast<float4*>(ph + r + i0) = zero;
+      *reinterpret_cast<float4*>(pl + r + i0) = zero;
+      m = fmaxf(fmaxf(m, fmaxf(absnanf(rf.x), absnanf(rf.y))), fmaxf(absnanf(rf.z), absnanf(rf.w)));
+    }
+  block_max_finish(m, ctx);
+}
+
+__global__ void __launch_bounds__(256)
+    k_div_start4(const float* __restrict__ wu, const float* __restrict__ wv, float* __restrict__ dh,
+                 float* __restrict__ dl, float* __restrict__ ph, float* __restrict__ pl, float* __restrict__ r32,
+                 int nx, int ny, df idx, df idy, RedCtx ctx) {
+  div_start4_body(wu, wv, dh, dl, ph, pl, r32, nx, ny, idx, idy, ctx);
+}
+
 __global__ void __launch_bounds__(256)
     k_div_df(const float* __restrict__ uh, const float* __restrict__ ul, const float* __restrict__ vh,
              const float* __restrict__ vl, float* __restrict__ dh, float* __restrict__ dl, int nx, int ny, df idx,
@@ -516,6 +569,23 @@ void launch_refine_init(Solver* s, const float* dh, const float* dl, const float
               k_refine_init<<<red_grid2(g.nx, g.ny), kBlock, 0, s->stream>>>(
                   dh, dl, ph, pl, r32, g.nx, g.ny, lap_scale(g), zero_p ? 1 : 0, red_ctx(s, s->red_out));
             });
+}
+
+// the start of a MIXED solve from zero pressure (k_div_start4; nx a multiple
+// of 4, else the divergence, the zero-pressure residual and two fills)
+void launch_div_start(Solver* s, const float* wu, const float* wv) {
+  const Grid& g = s->g;
+  if (g.nx % 4 != 0) {
+    launch_div_df(s, wu, nullptr, wv, nullptr, s->dh, s->dl);
+    launch_refine_init(s, s->dh, s->dl, s->ph, s->pl, s->r32, true);
+    launch_fill(s, s->ph, 0.f, s->n);
+    launch_fill(s, s->pl, 0.f, s->n);
+    return;
+  }
+  FS_LAUNCH(s, "div_start", (double)s->n * 28,
+            k_div_start4<<<red_grid2(g.nx / 4, g.ny), kBlock, 0, s->stream>>>(
+                wu, wv, s->dh, s->dl, s->ph, s->pl, s->r32, g.nx, g.ny, df_host(g.idxd), df_host(g.idyd),
+                red_ctx(s, s->red_out)));
 }
 
 void launch_refine_update(Solver* s, const float* ph, const float* pl, const float* e, const float* dh,
@@ -755,6 +825,11 @@ __global__ void k_zero_p_class(const ProjTab tab, int64_t n) {
   }
 }
 
+__global__ void __launch_bounds__(256) k_div_start_class(const ProjTab tab, int nx, int ny) {
+  const auto& a = tab.m[blockIdx.z];
+  div_start4_body(a.wu, a.wv, a.dh, a.dl, a.ph, a.pl, a.r32, nx, ny, a.idx, a.idy, a.ctx);
+}
+
 __global__ void __launch_bounds__(256) k_subgrad_class(const ProjTab tab, int nx, int ny) {
   const auto& a = tab.m[blockIdx.z];
   subgrad_df_body(a.wu, nullptr, a.wv, nullptr, a.ph, a.pl, a.uh, a.ul, a.vh, a.vl, nx, ny, a.idx, a.idy);
@@ -778,10 +853,17 @@ static ProjTab proj_tab(Solver* const* ms, int count, const float* const* wu, co
 }
 
 // before the loop: divergence, initial residual (zero pressure), zeroed pressure
-void launch_front_project_class(Solver* const* ms, int count, const float* const* wu, const float* const* wv,
-                                const double* dts, cudaStream_t st) {
+// (returns the number of launches)
+int launch_front_project_class(Solver* const* ms, int count, const float* const* wu, const float* const* wv,
+                               const double* dts, cudaStream_t st) {
   const Grid& g = ms[0]->g;
   const ProjTab tab = proj_tab(ms, count, wu, wv, dts);
+  if (g.nx % 4 == 0) {  // all three in one pass
+    dim3 gq = red_grid2(g.nx / 4, g.ny);
+    gq.z = count;
+    k_div_start_class<<<gq, kBlock, 0, st>>>(tab, g.nx, g.ny);
+    return 1;
+  }
   dim3 g2 = grid2d(g.nx, g.ny, kBlock);
   g2.z = count;
   k_div_class<<<g2, kBlock, 0, st>>>(tab, g.nx, g.ny);
@@ -789,6 +871,7 @@ void launch_front_project_class(Solver* const* ms, int count, const float* const
   gr.z = count;
   k_refine_zero_class<<<gr, kBlock, 0, st>>>(tab, g.nx, g.ny, lap_scale(g));
   k_zero_p_class<<<dim3(fill_blocks(ms[0]->n), 1, count), 256, 0, st>>>(tab, ms[0]->n);
+  return 3;
 }
 
 // after the loop: gradient subtraction and the step finish

@@ -524,6 +524,35 @@ def test_graph_step_equals_eager_step(G, O, precision, n):
     assert np.array_equal(outs[0][0], outs[1][0]) and np.array_equal(outs[0][1], outs[1][1])
 
 
+@pytest.mark.parametrize("n", [256, 66])
+def test_one_pass_solve_start_equals_separate_kernels(G, O, n):
+    """A MIXED solve from zero pressure starts with one pass (divergence,
+    zero-pressure residual, zeroed pressure, max|r|; n % 4 == 0) or, for
+    n % 4 != 0, with the separate kernels.  A warm-started solver's first step
+    starts from its still-zero pressure through the divergence and the general
+    residual kernels: the step, its statistics and the pressure-dependent
+    fields agree bit for bit (graph and eager)."""
+    u0, v0 = O.lcg_uv(77, n * n)
+    res = []
+    for warm in (False, True):
+        for graph in (True, False):
+            s = G.GPUFluidSolver(n=n, nu=1e-3, advection="maccormack", pressure_solver="multigrid",
+                                 pressure_iterations=1, precision="mixed", pressure_tol=1e-7, max_cycles=40,
+                                 warm_start=warm)
+            s.upload_velocity(u0, v0)
+            s.set_solids([(2.0, 3.0, 0.4)])
+            if graph:
+                s.step(0.01)
+            else:
+                s.profile_step(0.01, 1)
+            st = s.last_stats()
+            u, v = s.read_velocity()
+            res.append((u, v, st["cycles"], st["residual_initial"], st["residual_max"]))
+    for r in res[1:]:
+        assert np.array_equal(r[0], res[0][0]) and np.array_equal(r[1], res[0][1])
+        assert r[2:] == res[0][2:] and res[0][2] >= 1
+
+
 def test_total_cycles_counts_every_projection(G, O):
     """fs_total_cycles is the sum of the per-step cycle counts of fs_last_stats."""
     n = 128
