@@ -451,10 +451,11 @@ static dim3 tile_grid(const Grid& g) { return dim3((g.nx + kTX - 1) / kTX, (g.ny
 
 
 
-// Tensor map of one f32 field for the advection tiles (box kSW x kSH), kept
-// per device pointer.  TMA needs the row pitch a multiple of 16 bytes (nx % 4
-// == 0) and a 16-byte-aligned base; otherwise, or if the CUDA driver lacks the
-// encoder, every tile uses the wrapped loads.
+// Tensor maps of f32 planes for the TMA-staged tiles (the advection tiles'
+// kSW x kSH box here, the multigrid tile boxes in fs_multigrid.cu), kept per
+// device pointer, plane and box.  TMA needs the row pitch and the box width
+// multiples of 16 bytes (nx % 4 == 0) and a 16-byte-aligned base; otherwise,
+// or if the CUDA driver lacks the encoder, every tile uses wrapped loads.
 static PFN_cuTensorMapEncodeTiled_v12000 tmap_encoder() {
   static PFN_cuTensorMapEncodeTiled_v12000 fn = [] {
     void* p = nullptr;
@@ -467,28 +468,34 @@ static PFN_cuTensorMapEncodeTiled_v12000 tmap_encoder() {
   return fn;
 }
 
-static bool tile_tmap(Solver* s, const float* f, CUtensorMap* out) {
-  const Grid& g = s->g;
-  if (g.nx % 4 != 0 || ((uintptr_t)f & 15) != 0 || g.nx < kSW || g.ny < kSH) return false;
-  for (auto& e : s->tmaps)
-    if (e.first == f) {
-      *out = e.second;
+bool box_tmap(Solver* s, const float* f, int nx, int ny, int bw, int bh, CUtensorMap* out) {
+  if (nx % 4 != 0 || bw % 4 != 0 || ((uintptr_t)f & 15) != 0 || nx < bw || ny < bh || bw > 256 || bh > 256)
+    return false;
+  for (const auto& e : s->tmaps)
+    if (e.p == f && e.nx == nx && e.ny == ny && e.bw == bw && e.bh == bh) {
+      *out = e.m;
       return true;
     }
   PFN_cuTensorMapEncodeTiled_v12000 enc = tmap_encoder();
   if (!enc) return false;
-  CUtensorMap m;
-  const cuuint64_t dims[2] = {(cuuint64_t)g.nx, (cuuint64_t)g.ny};
-  const cuuint64_t pitch[1] = {(cuuint64_t)g.nx * sizeof(float)};
-  const cuuint32_t box[2] = {(cuuint32_t)kSW, (cuuint32_t)kSH};
+  Solver::Tmap e;
+  e.p = f;
+  e.nx = nx; e.ny = ny; e.bw = bw; e.bh = bh;
+  const cuuint64_t dims[2] = {(cuuint64_t)nx, (cuuint64_t)ny};
+  const cuuint64_t pitch[1] = {(cuuint64_t)nx * sizeof(float)};
+  const cuuint32_t box[2] = {(cuuint32_t)bw, (cuuint32_t)bh};
   const cuuint32_t estr[2] = {1, 1};
-  if (enc(&m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<float*>(f), dims, pitch, box, estr,
+  if (enc(&e.m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<float*>(f), dims, pitch, box, estr,
           CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
           CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
     return false;
-  s->tmaps.emplace_back(f, m);
-  *out = m;
+  s->tmaps.push_back(e);
+  *out = e.m;
   return true;
+}
+
+static bool tile_tmap(Solver* s, const float* f, CUtensorMap* out) {
+  return box_tmap(s, f, s->g.nx, s->g.ny, kSW, kSH, out);
 }
 
 template <>

@@ -98,8 +98,14 @@ struct Solver {
 
   std::vector<Level> lev;
   int tile_level[16] = {};  // tile side of each tile level's kernels; 0 = the built-in rule
-  // TMA tensor maps of the advected fields, by device pointer (fs_advect.cu)
-  std::vector<std::pair<const void*, CUtensorMap>> tmaps;
+  // TMA tensor maps of the staged fields (advection, multigrid tiles), by
+  // device pointer, plane and box (box_tmap, fs_advect.cu)
+  struct Tmap {
+    const void* p;
+    int nx, ny, bw, bh;
+    CUtensorMap m;
+  };
+  std::vector<Tmap> tmaps;
 
   // reductions: per-block partials and the final words
   double* red_partials = nullptr;  // 2 * red_cap doubles
@@ -221,6 +227,10 @@ void launch_fill64(Solver* s, double* x, double value, int64_t n);
 // mixed-precision refinement (double-float pressure and divergence)
 void launch_refine_init(Solver* s, const float* dh, const float* dl, const float* ph, const float* pl,
                         float* r32, bool zero_p);
+// TMA tensor map of a row-major f32 plane nx x ny (pitch nx) with a bw x bh
+// box, cached per solver; false when TMA cannot copy it (nx % 4 != 0, an
+// unaligned base, a box larger than the plane, no encoder in the CUDA driver)
+bool box_tmap(Solver* s, const float* f, int nx, int ny, int bw, int bh, CUtensorMap* out);
 // divergence + zero-pressure residual + zeroed pressure in one pass (MIXED)
 void launch_div_start(Solver* s, const float* wu, const float* wv);
 void launch_refine_update(Solver* s, const float* ph, const float* pl, const float* e, const float* dh,

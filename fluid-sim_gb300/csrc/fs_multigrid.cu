@@ -19,9 +19,10 @@
 // The per-cell arithmetic is fs_stencil.cuh, shared with the one-pass-per-
 // operation kernels, so the fused cycle reproduces them bit for bit.
 //
-// Shared-memory layout: each tile row is split into its even and odd columns
-// so that the lanes of a warp, which update cells of one colour in one row
-// (stride 2 in the row), hit consecutive words.
+// Shared-memory layout: the tile region row-major, its rows padded so that a
+// tile whose region lies inside the grid is staged by one TMA copy per field
+// (cp.async.bulk.tensor.2d, completion on an mbarrier); tiles on the
+// periodic edge are staged by wrapped 4-byte cp.async copies.
 #include <atomic>
 #include <string>
 #include <utility>
@@ -29,6 +30,7 @@
 #include "fs_df.cuh"
 #include "fs_internal.cuh"
 #include "fs_stencil.cuh"
+#include "fs_tc.cuh"
 
 namespace fs {
 
@@ -59,128 +61,204 @@ __device__ __forceinline__ void prefetch_l2(const void* p) {
 // i in (-n, 2n): one correction wraps it (halo offsets are far below n)
 __device__ __forceinline__ int wrap1(int i, int n) { return i < 0 ? i + n : (i >= n ? i - n : i); }
 
-// Checkerboard layout of an R x R region (R even): the cells of one colour
-// (global parity of i + j) of row lj are stored contiguously, S = R/2 per
-// row, colour q in array q.  For a cell of colour q at (li, lj) with
-// b = index offset of its row, the four neighbours are all of colour 1-q at
-//   left  row*S + m,  right row*S + m + 1,  up/down (row -+ 1)*S + m + b
-// where li = 2m + 1 + b; array 1 starts at a word offset = 16 (mod 32) past
-// array 0 so that the paired writes of the staging loop never share a bank.
-template <int R>
-struct Checker {
-  static constexpr int S = R / 2;
-  static constexpr int N = R * S;
-  static constexpr int PAD = (16 - (N % 32) + 32) % 32;
-  static constexpr int STRIDE = N + PAD;  // offset of colour 1
-  // position of (li, lj) given the parity par0 of the global index of (0, 0)
-  __device__ static __forceinline__ int at(int li, int lj, int par0) {
-    return ((par0 + li + lj) & 1) * STRIDE + lj * S + (li >> 1);
-  }
+// ------------------------------------------------------------ tile layout
+// A tile kernel works on the R x R region around its T x T tile (halo H),
+// row-major in shared memory with pitch W.  Region column 0 sits at box
+// column OX = LP - H, so that the box starts LP columns left of the tile, LP
+// a multiple of 4: the box's first column is 16-byte aligned in the row and
+// one TMA copy of W x R floats (W a multiple of 4) stages a whole field.
+template <int T, int H>
+struct TileBox {
+  static constexpr int R = T + 2 * H;
+  static constexpr int LP = (H + 3) & ~3;
+  static constexpr int OX = LP - H;
+  static constexpr int W = (LP + T + H + 3) & ~3;
+  static constexpr int N = W * R;            // floats of one field
+  static constexpr int NA = (N + 31) & ~31;  // rounded up to 128 bytes
 };
 
-// One red-black half-sweep of colour c over li, lj in [1, R-2] (in place).
-// Cells whose neighbours are stale give stale values; they lie outside the
-// valid region and are never written back.  Each thread walks one colour
-// column m down a chunk of rows: row lj's down neighbour is one of row lj-1's
-// left/right pair and its up neighbour one of row lj+1's, so a row costs two
-// new loads of the other colour (plus the cell and its rhs) instead of four.
-template <int R>
-__device__ __forceinline__ void rb_half_smem(float* xs, const float* rs, int c, int par0, float h2, float w) {
-  using CK = Checker<R>;
-  constexpr int S = CK::S;
-  constexpr int SW = S - 1;              // cells of one colour per row inside [1, R-2]
-  constexpr int W = R - 2;               // rows
-  constexpr int NCH = kTileThreads / SW;  // row chunks
-  constexpr int CH = (W + NCH - 1) / NCH;
+// The coarse block the up kernel's prolongation reads: RC x RC coarse cells
+// from (cgi0, cgj0) = ((i0 - H)/2 - 1, (j0 - H)/2 - 1), pitch WC, column 0
+// at box column OC (the box again starts on a 16-byte boundary: i0 / 2 is a
+// multiple of 8).
+template <int T, int H>
+struct CoarseBox {
+  static constexpr int RC = (T + 2 * H) / 2 + 2;
+  static constexpr int LPC = (H / 2 + 1 + 3) & ~3;
+  static constexpr int OC = LPC - (H / 2 + 1);
+  static constexpr int WC = (OC + RC + 3) & ~3;
+  static constexpr int NC = (WC * RC + 31) & ~31;
+};
+
+template <int T, int H>
+constexpr size_t down_smem_bytes() {
+  return 2 * (size_t)TileBox<T, H>::NA * sizeof(float) + 128;
+}
+template <int T, int H>
+constexpr size_t up_smem_bytes() {
+  return (2 * (size_t)TileBox<T, H>::NA + CoarseBox<T, H>::NC) * sizeof(float) + 128;
+}
+
+// the dynamic shared memory of a tile kernel, from a 128-byte boundary (TMA destinations)
+__device__ __forceinline__ float* tile_smem(float* p) {
+  return reinterpret_cast<float*>((reinterpret_cast<uintptr_t>(p) + 127) & ~static_cast<uintptr_t>(127));
+}
+
+// wrapped 4-byte copies of the R x R region from (gi0, gj0) of a periodic n x n field
+template <int R, int W, int OX>
+__device__ __forceinline__ void stage_region(float* dst, const float* __restrict__ src, int gi0, int gj0, int n) {
+  const int tid = threadIdx.y * blockDim.x + threadIdx.x, nthr = blockDim.x * blockDim.y;
+  for (int k = tid; k < R * R; k += nthr) {
+    const int lj = k / R, li = k - lj * R;
+    cp_async4(&dst[lj * W + OX + li], src + (int64_t)wrap1(gj0 + lj, n) * n + wrap1(gi0 + li, n));
+  }
+}
+
+// Thread 0 arms the barrier and issues the TMA copies of up to three boxes,
+// every thread waits (bounded).  False on every thread if the wait gave up,
+// after one more bounded wait for the copies in flight, with *err raised.
+struct TmaBox {
+  float* dst;
+  const CUtensorMap* tm;
+  int x, y;
+};
+__device__ __forceinline__ bool tma_stage_boxes(const TmaBox* b, int count, uint32_t bytes, uint64_t* bar,
+                                                int* err) {
   const int tid = threadIdx.y * blockDim.x + threadIdx.x;
-  const int chunk = tid / SW, m = tid - chunk * SW;
+  if (tid == 0) {
+    tc::mbar_init(bar, 1);
+    tc::mbar_fence_init();
+  }
+  __syncthreads();
+  if (tid == 0) {
+    tc::mbar_arrive_expect_tx(bar, bytes);
+    for (int q = 0; q < count; q++) tc::tma_load_2d(b[q].dst, b[q].tm, b[q].x, b[q].y, bar);
+  }
+  const bool ok = __syncthreads_and(tc::mbar_wait(bar, 0)) != 0;
+  if (!ok) {
+    if (tid == 0) atomicExch(err, 1);
+    tc::mbar_wait(bar, 0);
+  }
+  return ok;
+}
+
+// One red-black half-sweep of colour c over region cells li, lj in [1, R-2]
+// (in place).  Cells whose neighbours are stale give stale values; they lie
+// outside the valid region and are never written back.  Each thread walks
+// one region column down a chunk of rows, updating every other row: the top
+// neighbour of one update (colour 1-c, not written in this half-sweep) is
+// the bottom neighbour of the next, so an update loads the cell, its rhs, its
+// left and right neighbours and one new vertical neighbour.  Lanes of a warp
+// sit in consecutive columns, half of them one row lower; with an even pitch
+// the even columns fall on even banks and the odd ones on odd banks.
+template <int R, int W, int OX>
+__device__ __forceinline__ void rb_half_tile(float* xs, const float* rs, int c, int par0, float h2, float w) {
+  constexpr int NI = R - 2;                                 // columns (and rows) swept
+  constexpr int NCH = kTileThreads / NI;                    // row chunks
+  static_assert(NCH >= 1 && W % 2 == 0, "a tile region of at most 258 columns, even pitch");
+  constexpr int CH = ((NI + NCH - 1) / NCH + 1) & ~1;       // rows per chunk, even
+  const int tid = threadIdx.y * blockDim.x + threadIdx.x;
+  const int chunk = tid / NI, m = tid - chunk * NI;
   if (chunk >= NCH) return;
+  const int li = 1 + m;
   int lj = 1 + chunk * CH;
-  const int lend = min(lj + CH, W + 1);
+  const int lend = min(lj + CH, R - 1);
+  lj += (par0 + li + lj + c) & 1;  // first row of colour c in this column
   if (lj >= lend) return;
-  float* xc = xs + c * CK::STRIDE;              // colour c (updated)
-  const float* xo = xs + (1 - c) * CK::STRIDE;  // colour 1-c (read)
-  const float* rc = rs + c * CK::STRIDE;
-  int b = ((par0 + 1 + lj) & 1) != c ? 1 : 0;   // first colour-c cell of row lj at li = 1 + b
-  int base = lj * S + m;
-  float pl = xo[base - S], pr = xo[base - S + 1];  // row lj - 1
-  float cl = xo[base], cr = xo[base + 1];          // row lj
-  for (; lj < lend; lj++) {
-    float nl = xo[base + S], nr = xo[base + S + 1];  // row lj + 1
-    int k = base + b;
-    xc[k] = gs_update(xc[k], cl, cr, b ? pr : pl, b ? nr : nl, rc[k], h2, w);
-    pl = cl; pr = cr; cl = nl; cr = nr;
-    base += S;
-    b ^= 1;
+  float* p = xs + lj * W + OX + li;
+  const float* q = rs + lj * W + OX + li;
+  float bot = p[-W];
+  for (; lj < lend; lj += 2) {
+    const float top = p[W];
+    *p = gs_update(*p, p[-1], p[1], bot, top, *q, h2, w);
+    bot = top;
+    p += 2 * W;
+    q += 2 * W;
   }
 }
 
 // ------------------------------------------------------------------ down
 // H = 2 * pre + 1.  xin == nullptr means the level starts from zero; otherwise
 // xin and xout must differ (the halo of a tile is another tile's interior).
+// Tiles whose box lies inside the grid are staged by TMA when tma != 0.
 template <int T, int H>
-__device__ __forceinline__ void mg_down_body(const float* __restrict__ rhs, const float* __restrict__ xin,
-                                             float* __restrict__ xout, float* __restrict__ crhs, int n, float h2,
-                                             int pre, float w) {
-  constexpr int R = T + 2 * H;
-  using CK = Checker<R>;
-  __shared__ float xs[CK::STRIDE + CK::N];
-  __shared__ float rs[CK::STRIDE + CK::N];
+__device__ __forceinline__ void mg_down_body(float* smem, const float* __restrict__ rhs,
+                                             const float* __restrict__ xin, float* __restrict__ xout,
+                                             float* __restrict__ crhs, int n, float h2, int pre, float w,
+                                             const CUtensorMap* tm_r, const CUtensorMap* tm_x, int tma,
+                                             int* err) {
+  using B = TileBox<T, H>;
+  static_assert(H % 2 == 1, "the halo of the down kernel is 2 * pre + 1");
+  float* const xs = smem;
+  float* const rs = smem + B::NA;
+  __shared__ uint64_t bar;
   const int i0 = blockIdx.x * T, j0 = blockIdx.y * T;
   const int gi0 = i0 - H, gj0 = j0 - H;
   const int par0 = (gi0 + gj0) & 1;  // n even: the parity of the wrapped index is the same
   const int tid = threadIdx.y * blockDim.x + threadIdx.x, nthr = blockDim.x * blockDim.y;
-  for (int k = tid; k < R * R; k += nthr) {
-    int lj = k / R, li = k - lj * R;
-    int64_t g = (int64_t)wrap1(gj0 + lj, n) * n + wrap1(gi0 + li, n);
-    int q = CK::at(li, lj, par0);
-    cp_async4(&rs[q], rhs + g);
-    if (xin) cp_async4(&xs[q], xin + g);
-    else xs[q] = 0.f;
-  }
-  cp_async_wait_all();
-  __syncthreads();
-  for (int s = 0; s < 2 * pre; s++) {
-    rb_half_smem<R>(xs, rs, s & 1, par0, h2, w);
+  const int bx = i0 - B::LP;
+  const bool boxed = tma && bx >= 0 && bx + B::W <= n && gj0 >= 0 && gj0 + B::R <= n;
+  if (!xin)
+    for (int k = tid; k < B::NA / 4; k += nthr) reinterpret_cast<float4*>(xs)[k] = make_float4(0.f, 0.f, 0.f, 0.f);
+  if (boxed) {
+    const TmaBox b[2] = {{rs, tm_r, bx, gj0}, {xs, tm_x, bx, gj0}};
+    if (!tma_stage_boxes(b, xin ? 2 : 1, (uint32_t)((xin ? 2 : 1) * B::N * sizeof(float)), &bar, err)) return;
+  } else {
+    stage_region<B::R, B::W, B::OX>(rs, rhs, gi0, gj0, n);
+    if (xin) stage_region<B::R, B::W, B::OX>(xs, xin, gi0, gj0, n);
+    cp_async_wait_all();
     __syncthreads();
   }
-  for (int k = tid; k < T * T; k += nthr) {
-    int y = k / T, x = k - y * T;
-    int gi = i0 + x, gj = j0 + y;
-    if (gi < n && gj < n) xout[(int64_t)gj * n + gi] = xs[CK::at(H + x, H + y, par0)];
+  for (int s = 0; s < 2 * pre; s++) {
+    rb_half_tile<B::R, B::W, B::OX>(xs, rs, s & 1, par0, h2, w);
+    __syncthreads();
   }
-  // residual on each 2x2 block and its restriction (multigrid.js:48-93).  A
-  // block starts at (la, lb) = (H + 2ci, H + 2cj): la is odd (H is) and la + lb
-  // even, so the block's cells and their eight outer neighbours sit at fixed
-  // offsets from one base position in the two colour arrays (XA holds the
-  // colour of (la, lb)); 12 + 4 loads per block instead of 24.
-  static_assert(H % 2 == 1, "the halo of the down kernel is 2 * pre + 1");
-  constexpr int S = CK::S;
-  const float* XA = xs + (par0 ? CK::STRIDE : 0);
-  const float* XB = xs + (par0 ? 0 : CK::STRIDE);
-  const float* RA = rs + (par0 ? CK::STRIDE : 0);
-  const float* RB = rs + (par0 ? 0 : CK::STRIDE);
+  // the tile: region cell (H + x, H + y) is box column LP + x of row H + y
+  if (boxed) {  // inside the grid, n % 4 == 0: float4 rows
+    for (int k = tid; k < T * T / 4; k += nthr) {
+      const int y = k / (T / 4), x = (k - y * (T / 4)) * 4;
+      *reinterpret_cast<float4*>(xout + (int64_t)(j0 + y) * n + i0 + x) =
+          *reinterpret_cast<const float4*>(xs + (H + y) * B::W + B::LP + x);
+    }
+  } else {
+    for (int k = tid; k < T * T; k += nthr) {
+      const int y = k / T, x = k - y * T;
+      const int gi = i0 + x, gj = j0 + y;
+      if (gi < n && gj < n) xout[(int64_t)gj * n + gi] = xs[(H + y) * B::W + B::LP + x];
+    }
+  }
+  // residual on each 2x2 block and its restriction (multigrid.js:48-93).  The
+  // block at region (H + 2ci, H + 2cj) starts on an even word (LP and W are
+  // multiples of 4), so its rows, the rows above and below it and its rhs
+  // come as float2 pairs: 10 loads per block instead of 16.
   const int nc = n >> 1;
   for (int k = tid; k < (T / 2) * (T / 2); k += nthr) {
     const int cj = k / (T / 2), ci = k - cj * (T / 2);
-    const int la = H + 2 * ci, lb = H + 2 * cj;
-    const int b0 = lb * S + (la >> 1);  // (la - 1) >> 1 == la >> 1, (la + 1) >> 1 == (la + 2) >> 1 == (la >> 1) + 1
-    const float c00 = XA[b0], c10 = XB[b0 + 1], c01 = XB[b0 + S], c11 = XA[b0 + S + 1];
-    float r4[4];
-    r4[0] = residual_at(c00, XB[b0], c10, XB[b0 - S], c01, RA[b0], h2);
-    r4[1] = residual_at(c10, c00, XA[b0 + 1], XA[b0 - S + 1], c11, RB[b0 + 1], h2);
-    r4[2] = residual_at(c01, XA[b0 + S], c11, c00, XA[b0 + 2 * S], RB[b0 + S], h2);
-    r4[3] = residual_at(c11, c01, XB[b0 + S + 1], c10, XB[b0 + 2 * S + 1], RA[b0 + S + 1], h2);
+    const int off = (H + 2 * cj) * B::W + B::LP + 2 * ci;
+    const float* X = xs + off;
+    const float* Q = rs + off;
+    const float2 x0 = *reinterpret_cast<const float2*>(X);
+    const float2 x1 = *reinterpret_cast<const float2*>(X + B::W);
+    const float2 xb = *reinterpret_cast<const float2*>(X - B::W);
+    const float2 xt = *reinterpret_cast<const float2*>(X + 2 * B::W);
+    const float2 q0 = *reinterpret_cast<const float2*>(Q);
+    const float2 q1 = *reinterpret_cast<const float2*>(Q + B::W);
+    const float r00 = residual_at(x0.x, X[-1], x0.y, xb.x, x1.x, q0.x, h2);
+    const float r10 = residual_at(x0.y, x0.x, X[2], xb.y, x1.y, q0.y, h2);
+    const float r01 = residual_at(x1.x, X[B::W - 1], x1.y, x0.x, xt.x, q1.x, h2);
+    const float r11 = residual_at(x1.y, x1.x, X[B::W + 2], x0.y, xt.y, q1.y, h2);
     const int gci = (i0 >> 1) + ci, gcj = (j0 >> 1) + cj;
-    if (gci < nc && gcj < nc) crhs[(int64_t)gcj * nc + gci] = restrict4(r4[0], r4[1], r4[2], r4[3]);
+    if (gci < nc && gcj < nc) crhs[(int64_t)gcj * nc + gci] = restrict4(r00, r10, r01, r11);
   }
 }
 
 template <int T, int H>
-__global__ void __launch_bounds__(256) k_mg_down(const float* __restrict__ rhs, const float* __restrict__ xin,
-                                                 float* __restrict__ xout, float* __restrict__ crhs, int n,
-                                                 float h2, int pre, float w) {
-  mg_down_body<T, H>(rhs, xin, xout, crhs, n, h2, pre, w);
+__global__ void __launch_bounds__(256)
+    k_mg_down(const float* __restrict__ rhs, const float* __restrict__ xin, float* __restrict__ xout,
+              float* __restrict__ crhs, int n, float h2, int pre, float w, const __grid_constant__ CUtensorMap tm_r,
+              const __grid_constant__ CUtensorMap tm_x, int tma, int* err) {
+  extern __shared__ float tile_dyn[];
+  mg_down_body<T, H>(tile_smem(tile_dyn), rhs, xin, xout, crhs, n, h2, pre, w, &tm_r, &tm_x, tma, err);
 }
 
 // -------------------------------------------------------------------- up
@@ -190,16 +268,18 @@ __global__ void __launch_bounds__(256) k_mg_down(const float* __restrict__ rhs, 
 // double-float pressure (ph, pl) in place instead of being written to xout:
 // each cell is read and written by its own tile only.
 template <int T, int H, bool ACC>
-__device__ __forceinline__ void mg_up_body(const float* __restrict__ rhs, const float* __restrict__ xin,
+__device__ __forceinline__ void mg_up_body(float* smem, const float* __restrict__ rhs, const float* __restrict__ xin,
                                            float* __restrict__ xout, const float* __restrict__ xc, int n, float h2,
-                                           int post, float* __restrict__ ph, float* __restrict__ pl, float w) {
-  constexpr int R = T + 2 * H;
-  using CK = Checker<R>;
-  static_assert(T % 2 == 0 && H % 2 == 0, "the up kernel's region starts on an even index");
-  extern __shared__ float up_smem[];  // xs, rs (checkerboard), cs (coarse block)
-  float* const xs = up_smem;
-  float* const rs = up_smem + (CK::STRIDE + CK::N);
-  float* const cs = up_smem + 2 * (CK::STRIDE + CK::N);
+                                           int post, float* __restrict__ ph, float* __restrict__ pl, float w,
+                                           const CUtensorMap* tm_r, const CUtensorMap* tm_x,
+                                           const CUtensorMap* tm_c, int tma, int* err) {
+  using B = TileBox<T, H>;
+  using C = CoarseBox<T, H>;
+  static_assert(T % 16 == 0 && H % 2 == 0, "the up kernel's region starts on an even index");
+  float* const xs = smem;
+  float* const rs = smem + B::NA;
+  float* const cs = smem + 2 * B::NA;
+  __shared__ uint64_t bar;
   const int i0 = blockIdx.x * T, j0 = blockIdx.y * T;
   const int gi0 = i0 - H, gj0 = j0 - H;
   const int par0 = (gi0 + gj0) & 1;
@@ -218,82 +298,139 @@ __device__ __forceinline__ void mg_up_body(const float* __restrict__ rhs, const 
       }
     }
   }
-  // staging, all asynchronous: the fine iterate and rhs of the R x R region
-  // and the RC x RC coarse block its prolongation reads.  gi0 is even (T and
-  // H are), so fine local column li samples coarse local columns
-  // (li + 1) / 2 and (li + 1) / 2 + 1 with weight 1/4 or 3/4 on the first
-  // (PROLONG, multigrid.js:99-131: sample at ((i+1/2)/2 - 1/2, (j+1/2)/2 - 1/2)).
-  constexpr int RC = R / 2 + 2;
+  // staging: the fine iterate and rhs of the region and the coarse block its
+  // prolongation reads.  gi0 is even (T and H are), so fine region column li
+  // samples coarse block columns (li + 1) / 2 and (li + 1) / 2 + 1 with weight
+  // 1/4 or 3/4 on the first (PROLONG, multigrid.js:99-131: sample at
+  // ((i+1/2)/2 - 1/2, (j+1/2)/2 - 1/2)).
   const int cgi0 = (gi0 >> 1) - 1, cgj0 = (gj0 >> 1) - 1;
-  for (int k = tid; k < RC * RC; k += nthr) {
-    const int lj = k / RC, li = k - lj * RC;
-    cp_async4(&cs[k], xc + (int64_t)wrap1(cgj0 + lj, nc) * nc + wrap1(cgi0 + li, nc));
+  const int bx = i0 - B::LP, cbx = cgi0 - C::OC;
+  const bool boxed = tma && bx >= 0 && bx + B::W <= n && gj0 >= 0 && gj0 + B::R <= n && cbx >= 0 &&
+                     cbx + C::WC <= nc && cgj0 >= 0 && cgj0 + C::RC <= nc;
+  if (boxed) {
+    const TmaBox b[3] = {{xs, tm_x, bx, gj0}, {rs, tm_r, bx, gj0}, {cs, tm_c, cbx, cgj0}};
+    if (!tma_stage_boxes(b, 3, (uint32_t)((2 * B::N + C::WC * C::RC) * sizeof(float)), &bar, err)) return;
+  } else {
+    for (int k = tid; k < C::RC * C::RC; k += nthr) {
+      const int lj = k / C::RC, li = k - lj * C::RC;
+      cp_async4(&cs[lj * C::WC + C::OC + li], xc + (int64_t)wrap1(cgj0 + lj, nc) * nc + wrap1(cgi0 + li, nc));
+    }
+    stage_region<B::R, B::W, B::OX>(xs, xin, gi0, gj0, n);
+    stage_region<B::R, B::W, B::OX>(rs, rhs, gi0, gj0, n);
+    cp_async_wait_all();
+    __syncthreads();
   }
-  for (int k = tid; k < R * R; k += nthr) {
-    const int lj = k / R, li = k - lj * R;
-    const int64_t g = (int64_t)wrap1(gj0 + lj, n) * n + wrap1(gi0 + li, n);
-    const int q = CK::at(li, lj, par0);
-    cp_async4(&xs[q], xin + g);
-    cp_async4(&rs[q], rhs + g);
-  }
-  cp_async_wait_all();
-  __syncthreads();
-  for (int k = tid; k < R * R; k += nthr) {
-    const int lj = k / R, li = k - lj * R;
-    const int q = CK::at(li, lj, par0);
-    const float* c = cs + ((lj + 1) >> 1) * RC + ((li + 1) >> 1);
-    const float fx = (li & 1) ? 0.25f : 0.75f, fy = (lj & 1) ? 0.25f : 0.75f;
-    xs[q] = __fadd_rn(xs[q], prolong_val(c[0], c[1], c[RC], c[RC + 1], fx, fy));
+  // prolongation-add by 2x2 fine blocks: fine columns 2a - 1 (weight 1/4 on
+  // coarse column a) and 2a (weight 3/4) read the same four coarse values,
+  // likewise rows 2b - 1 and 2b; the blocks on the region's edge are halves
+  {
+    constexpr int NB = B::R / 2 + 1;
+    for (int k = tid; k < NB * NB; k += nthr) {
+      const int b = k / NB, a = k - b * NB;
+      const float* c = cs + b * C::WC + C::OC + a;
+      const float c00 = c[0], c10 = c[1], c01 = c[C::WC], c11 = c[C::WC + 1];
+      const int col = B::OX + 2 * a - 1;
+      if (b > 0) {
+        const int o = (2 * b - 1) * B::W + col;
+        if (a > 0) xs[o] = __fadd_rn(xs[o], prolong_val(c00, c10, c01, c11, 0.25f, 0.25f));
+        if (a < NB - 1) xs[o + 1] = __fadd_rn(xs[o + 1], prolong_val(c00, c10, c01, c11, 0.75f, 0.25f));
+      }
+      if (b < NB - 1) {
+        const int o = 2 * b * B::W + col;
+        if (a > 0) xs[o] = __fadd_rn(xs[o], prolong_val(c00, c10, c01, c11, 0.25f, 0.75f));
+        if (a < NB - 1) xs[o + 1] = __fadd_rn(xs[o + 1], prolong_val(c00, c10, c01, c11, 0.75f, 0.75f));
+      }
+    }
   }
   __syncthreads();
   for (int s = 0; s < 2 * post; s++) {
-    rb_half_smem<R>(xs, rs, s & 1, par0, h2, w);
+    rb_half_tile<B::R, B::W, B::OX>(xs, rs, s & 1, par0, h2, w);
     __syncthreads();
   }
+  // the tile: region cell (H + x, H + y) is box column LP + x of row H + y
   if constexpr (ACC) {
-    // four cells' double-float pressure loads in flight per thread
-    constexpr int V = 4;
-    for (int k0 = tid; k0 < T * T; k0 += V * nthr) {
-      float hv[V], lv[V], ev[V];
-      int64_t gv[V];
+    if (boxed) {
+      // inside the grid, n % 4 == 0: float4 groups, two groups' double-float
+      // pressure loads in flight per thread
+      constexpr int G = T * T / 4, V = 2;
+      for (int k0 = tid; k0 < G; k0 += V * nthr) {
+        float4 hv[V], lv[V], ev[V];
+        int64_t gv[V];
 #pragma unroll
-      for (int u = 0; u < V; u++) {
-        const int k = k0 + u * nthr;
-        gv[u] = -1;
-        if (k < T * T) {
-          const int y = k / T, x = k - y * T;
-          const int gi = i0 + x, gj = j0 + y;
-          if (gi < n && gj < n) {
-            gv[u] = (int64_t)gj * n + gi;
-            hv[u] = ph[gv[u]];
-            lv[u] = pl[gv[u]];
-            ev[u] = xs[CK::at(H + x, H + y, par0)];
+        for (int u = 0; u < V; u++) {
+          const int k = k0 + u * nthr;
+          gv[u] = -1;
+          if (k < G) {
+            const int y = k / (T / 4), x = (k - y * (T / 4)) * 4;
+            gv[u] = (int64_t)(j0 + y) * n + i0 + x;
+            hv[u] = *reinterpret_cast<const float4*>(ph + gv[u]);
+            lv[u] = *reinterpret_cast<const float4*>(pl + gv[u]);
+            ev[u] = *reinterpret_cast<const float4*>(xs + (H + y) * B::W + B::LP + x);
           }
         }
-      }
 #pragma unroll
-      for (int u = 0; u < V; u++)
-        if (gv[u] >= 0) {
-          const df p = df_add_f(df{hv[u], lv[u]}, ev[u]);
-          ph[gv[u]] = p.hi;
-          pl[gv[u]] = p.lo;
+        for (int u = 0; u < V; u++)
+          if (gv[u] >= 0) {
+            const df p0 = df_add_f(df{hv[u].x, lv[u].x}, ev[u].x), p1 = df_add_f(df{hv[u].y, lv[u].y}, ev[u].y);
+            const df p2 = df_add_f(df{hv[u].z, lv[u].z}, ev[u].z), p3 = df_add_f(df{hv[u].w, lv[u].w}, ev[u].w);
+            *reinterpret_cast<float4*>(ph + gv[u]) = make_float4(p0.hi, p1.hi, p2.hi, p3.hi);
+            *reinterpret_cast<float4*>(pl + gv[u]) = make_float4(p0.lo, p1.lo, p2.lo, p3.lo);
+          }
+      }
+    } else {
+      // four cells' double-float pressure loads in flight per thread
+      constexpr int V = 4;
+      for (int k0 = tid; k0 < T * T; k0 += V * nthr) {
+        float hv[V], lv[V], ev[V];
+        int64_t gv[V];
+#pragma unroll
+        for (int u = 0; u < V; u++) {
+          const int k = k0 + u * nthr;
+          gv[u] = -1;
+          if (k < T * T) {
+            const int y = k / T, x = k - y * T;
+            const int gi = i0 + x, gj = j0 + y;
+            if (gi < n && gj < n) {
+              gv[u] = (int64_t)gj * n + gi;
+              hv[u] = ph[gv[u]];
+              lv[u] = pl[gv[u]];
+              ev[u] = xs[(H + y) * B::W + B::LP + x];
+            }
+          }
         }
+#pragma unroll
+        for (int u = 0; u < V; u++)
+          if (gv[u] >= 0) {
+            const df p = df_add_f(df{hv[u], lv[u]}, ev[u]);
+            ph[gv[u]] = p.hi;
+            pl[gv[u]] = p.lo;
+          }
+      }
+    }
+  } else if (boxed) {
+    for (int k = tid; k < T * T / 4; k += nthr) {
+      const int y = k / (T / 4), x = (k - y * (T / 4)) * 4;
+      *reinterpret_cast<float4*>(xout + (int64_t)(j0 + y) * n + i0 + x) =
+          *reinterpret_cast<const float4*>(xs + (H + y) * B::W + B::LP + x);
     }
   } else {
     for (int k = tid; k < T * T; k += nthr) {
       const int y = k / T, x = k - y * T;
       const int gi = i0 + x, gj = j0 + y;
-      if (gi < n && gj < n) xout[(int64_t)gj * n + gi] = xs[CK::at(H + x, H + y, par0)];
+      if (gi < n && gj < n) xout[(int64_t)gj * n + gi] = xs[(H + y) * B::W + B::LP + x];
     }
   }
 }
 
 template <int T, int H, bool ACC>
-__global__ void __launch_bounds__(256) k_mg_up(const float* __restrict__ rhs, const float* __restrict__ xin,
-                                               float* __restrict__ xout, const float* __restrict__ xc, int n,
-                                               float h2, int post, float* __restrict__ ph,
-                                               float* __restrict__ pl, float w) {
-  mg_up_body<T, H, ACC>(rhs, xin, xout, xc, n, h2, post, ph, pl, w);
+__global__ void __launch_bounds__(256)
+    k_mg_up(const float* __restrict__ rhs, const float* __restrict__ xin, float* __restrict__ xout,
+            const float* __restrict__ xc, int n, float h2, int post, float* __restrict__ ph,
+            float* __restrict__ pl, float w, const __grid_constant__ CUtensorMap tm_r,
+            const __grid_constant__ CUtensorMap tm_x, const __grid_constant__ CUtensorMap tm_c, int tma, int* err) {
+  extern __shared__ float tile_dyn[];
+  mg_up_body<T, H, ACC>(tile_smem(tile_dyn), rhs, xin, xout, xc, n, h2, post, ph, pl, w, &tm_r, &tm_x, &tm_c, tma,
+                        err);
 }
 
 // ---------------------------------------------------------------- bottom
@@ -670,17 +807,21 @@ struct BottomTab {
 template <int T, int H>
 __global__ void __launch_bounds__(256) k_mg_down_class(const DownTab tab, int n, float h2, int pre, float w,
                                                        int max_cycles) {
+  extern __shared__ float tile_dyn[];
   const auto& a = tab.m[blockIdx.z];
   if (!member_active(a.st, max_cycles)) return;
-  mg_down_body<T, H>(a.rhs, nullptr, a.xout, a.crhs, n, h2, pre, w);
+  mg_down_body<T, H>(tile_smem(tile_dyn), a.rhs, nullptr, a.xout, a.crhs, n, h2, pre, w, nullptr, nullptr, 0,
+                     nullptr);
 }
 
 template <int T, int H, bool ACC>
 __global__ void __launch_bounds__(256) k_mg_up_class(const UpTab tab, int n, float h2, int post, float w,
                                                      int max_cycles) {
+  extern __shared__ float tile_dyn[];
   const auto& a = tab.m[blockIdx.z];
   if (!member_active(a.st, max_cycles)) return;
-  mg_up_body<T, H, ACC>(a.rhs, a.xin, a.xout, a.xc, n, h2, post, a.ph, a.pl, w);
+  mg_up_body<T, H, ACC>(tile_smem(tile_dyn), a.rhs, a.xin, a.xout, a.xc, n, h2, post, a.ph, a.pl, w, nullptr,
+                        nullptr, nullptr, 0, nullptr);
 }
 
 template <int N0, int NMIN>
@@ -711,9 +852,15 @@ static int tile_for(int n) {
   return 16;
 }
 
+// A side T serves a level of n cells only if T <= n / 2 (16 always: tile
+// levels have n > 64).  Then one wrap covers a tile's halo (T + H - 1 < n) and
+// its coarse block, which the wrapped staging relies on.
+static bool tile_fits(int t, int n) { return t == 16 || 2 * t <= n; }
+
 int mg_tile(const Solver* s, int l) {
-  if (l >= 0 && l < 16 && s->tile_level[l]) return s->tile_level[l];
-  return tile_for(s->lev[l].n);
+  const int n = s->lev[l].n;
+  if (l >= 0 && l < 16 && s->tile_level[l] && tile_fits(s->tile_level[l], n)) return s->tile_level[l];
+  return tile_for(n);
 }
 
 // profile name of a tile kernel: one entry per level ("mg_down_l0", ...)
@@ -721,14 +868,44 @@ static std::string level_name(const Solver* s, const Level& L, const char* base)
   return std::string(base) + "_l" + std::to_string(&L - s->lev.data());
 }
 
+// The dynamic shared-memory limit is an attribute of the function on each
+// device; set once per (kernel, device) when the tile needs more than 48 KB.
+template <class K>
+static void tile_smem_attr(K kernel, size_t bytes, int device, std::atomic<uint64_t>& done) {
+  if (bytes <= 48 * 1024) return;
+  const uint64_t bit = 1ull << (device & 63);
+  if (!(done.load() & bit) &&
+      cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes) == cudaSuccess)
+    done.fetch_or(bit);
+}
+
+// tensor maps of a level's fields for the tile boxes of TileBox<T, H> (and the
+// coarse block); false: every tile stages with wrapped copies
+template <int T, int H>
+static bool tile_maps(Solver* s, int n, const float* const* f, CUtensorMap* const* m, int count) {
+  using B = TileBox<T, H>;
+  for (int q = 0; q < count; q++)
+    if (f[q] && !box_tmap(s, f[q], n, n, B::W, B::R, m[q])) return false;
+  return true;
+}
+
 template <int T, int H>
 static void down_t(Solver* s, Level& L, const Level& C, bool has_x) {
+  static std::atomic<uint64_t> attr{0};
+  constexpr size_t smem = down_smem_bytes<T, H>();
+  tile_smem_attr(k_mg_down<T, H>, smem, s->prm.device, attr);
   dim3 grid((L.n + T - 1) / T, (L.n + T - 1) / T);
   double bytes = (double)L.n * L.n * (has_x ? 12.0 : 8.0) + (double)C.n * C.n * 4.0;
   float* out = has_x ? L.x2 : L.x;
+  const float* xin = has_x ? L.x : nullptr;
+  CUtensorMap tr{}, tx{};
+  const float* f[2] = {L.rhs, xin};
+  CUtensorMap* m[2] = {&tr, &tx};
+  const int tma = tile_maps<T, H>(s, L.n, f, m, 2) ? 1 : 0;
   FS_LAUNCH(s, level_name(s, L, "mg_down").c_str(), bytes,
-            k_mg_down<T, H><<<grid, kTileBlock, 0, s->stream>>>(L.rhs, has_x ? L.x : nullptr, out, C.rhs, L.n,
-                                                                L.h2, s->prm.mg_pre_smooth, (float)s->prm.relax));
+            k_mg_down<T, H><<<grid, kTileBlock, smem, s->stream>>>(
+                L.rhs, xin, out, C.rhs, L.n, L.h2, s->prm.mg_pre_smooth, (float)s->prm.relax, tr, tx, tma,
+                &s->dev->async_err));
   if (has_x) std::swap(L.x, L.x2);
 }
 
@@ -741,47 +918,33 @@ static void down(Solver* s, Level& L, const Level& C, bool has_x) {
   }
 }
 
-// dynamic shared memory of k_mg_up<T, H, *>: two checkerboard arrays and the coarse block
-template <int T, int H>
-constexpr size_t up_smem_bytes() {
-  using CK = Checker<T + 2 * H>;
-  constexpr int RC = (T + 2 * H) / 2 + 2;
-  return (2 * (size_t)(CK::STRIDE + CK::N) + (size_t)RC * RC) * sizeof(float);
-}
-
-// the dynamic shared-memory limit is an attribute of the function on each device
-template <int T, int H, bool ACC>
-static void up_smem_attr(Solver* s) {
-  constexpr size_t bytes = up_smem_bytes<T, H>();
-  if (bytes <= 48 * 1024) return;
-  static std::atomic<uint64_t> attr_set{0};
-  const uint64_t bit = 1ull << (s->prm.device & 63);
-  if (!(attr_set.load() & bit)) {
-    if (cudaFuncSetAttribute(k_mg_up<T, H, ACC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes) ==
-        cudaSuccess)
-      attr_set.fetch_or(bit);
-  }
-}
-
 template <int T, int H>
 static void up_t(Solver* s, Level& L, const Level& C, float* acc_h, float* acc_l) {
+  using CB = CoarseBox<T, H>;
   dim3 grid((L.n + T - 1) / T, (L.n + T - 1) / T);
   constexpr size_t smem = up_smem_bytes<T, H>();
+  CUtensorMap tr{}, tx{}, tc{};
+  const float* f[2] = {L.rhs, L.x};
+  CUtensorMap* m[2] = {&tr, &tx};
+  const int tma = tile_maps<T, H>(s, L.n, f, m, 2) && box_tmap(s, C.x, C.n, C.n, CB::WC, CB::RC, &tc) ? 1 : 0;
+  int* err = &s->dev->async_err;
   if (acc_h) {
-    up_smem_attr<T, H, true>(s);
+    static std::atomic<uint64_t> attr{0};
+    tile_smem_attr(k_mg_up<T, H, true>, smem, s->prm.device, attr);
     double bytes = (double)L.n * L.n * 24.0 + (double)C.n * C.n * 4.0;
     FS_LAUNCH(s, "mg_up_acc", bytes,
-              k_mg_up<T, H, true><<<grid, kTileBlock, smem, s->stream>>>(L.rhs, L.x, nullptr, C.x, L.n, L.h2,
-                                                                         s->prm.mg_post_smooth, acc_h, acc_l,
-                                                                         (float)s->prm.relax));
+              k_mg_up<T, H, true><<<grid, kTileBlock, smem, s->stream>>>(
+                  L.rhs, L.x, nullptr, C.x, L.n, L.h2, s->prm.mg_post_smooth, acc_h, acc_l, (float)s->prm.relax, tr,
+                  tx, tc, tma, err));
     return;
   }
-  up_smem_attr<T, H, false>(s);
+  static std::atomic<uint64_t> attr{0};
+  tile_smem_attr(k_mg_up<T, H, false>, smem, s->prm.device, attr);
   double bytes = (double)L.n * L.n * 12.0 + (double)C.n * C.n * 4.0;
   FS_LAUNCH(s, level_name(s, L, "mg_up").c_str(), bytes,
-            k_mg_up<T, H, false><<<grid, kTileBlock, smem, s->stream>>>(L.rhs, L.x, L.x2, C.x, L.n, L.h2,
-                                                                        s->prm.mg_post_smooth, nullptr, nullptr,
-                                                                        (float)s->prm.relax));
+            k_mg_up<T, H, false><<<grid, kTileBlock, smem, s->stream>>>(
+                L.rhs, L.x, L.x2, C.x, L.n, L.h2, s->prm.mg_post_smooth, nullptr, nullptr, (float)s->prm.relax, tr,
+                tx, tc, tma, err));
   std::swap(L.x, L.x2);
 }
 
@@ -925,20 +1088,23 @@ static void down_class_t(Solver* const* ms, int count, int l, cudaStream_t st) {
     Level& L = ms[i]->lev[l];
     tab.m[i] = {L.rhs, L.x, ms[i]->lev[l + 1].rhs, ms[i]->dev};
   }
+  static std::atomic<uint64_t> attr{0};
+  constexpr size_t smem = down_smem_bytes<T, H>();
+  tile_smem_attr(k_mg_down_class<T, H>, smem, ms[0]->prm.device, attr);
   dim3 grid((L0.n + T - 1) / T, (L0.n + T - 1) / T, count);
-  k_mg_down_class<T, H><<<grid, kTileBlock, 0, st>>>(tab, L0.n, L0.h2, ms[0]->prm.mg_pre_smooth,
-                                                      (float)ms[0]->prm.relax, ms[0]->prm.max_cycles);
+  k_mg_down_class<T, H><<<grid, kTileBlock, smem, st>>>(tab, L0.n, L0.h2, ms[0]->prm.mg_pre_smooth,
+                                                         (float)ms[0]->prm.relax, ms[0]->prm.max_cycles);
 }
 
 // tile side for a level of a class: an override of the class's members, else
 // like tile_for counting the CTAs of all members (the tiles give the same
 // values whatever their size)
 static int tile_for_class(const Solver* s0, int l, int count) {
-  if (l < 16 && s0->tile_level[l]) return s0->tile_level[l];
   const int n = s0->lev[l].n;
+  if (l < 16 && s0->tile_level[l] && tile_fits(s0->tile_level[l], n)) return s0->tile_level[l];
   for (int t : {64, 32}) {
     int c = (n + t - 1) / t;
-    if (c * c * count >= 256) return t;
+    if (tile_fits(t, n) && c * c * count >= 256) return t;
   }
   return 16;
 }
@@ -965,15 +1131,9 @@ static void up_class_t(Solver* const* ms, int count, int l, cudaStream_t st) {
                 s->dev};
     if (!ACC) std::swap(L.x, L.x2);
   }
+  static std::atomic<uint64_t> attr{0};
   constexpr size_t smem = up_smem_bytes<T, H>();
-  if constexpr (smem > 48 * 1024) {
-    static std::atomic<uint64_t> attr_set{0};
-    const uint64_t bit = 1ull << (ms[0]->prm.device & 63);
-    if (!(attr_set.load() & bit) &&
-        cudaFuncSetAttribute(k_mg_up_class<T, H, ACC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) ==
-            cudaSuccess)
-      attr_set.fetch_or(bit);
-  }
+  tile_smem_attr(k_mg_up_class<T, H, ACC>, smem, ms[0]->prm.device, attr);
   dim3 grid((L0.n + T - 1) / T, (L0.n + T - 1) / T, count);
   k_mg_up_class<T, H, ACC><<<grid, kTileBlock, smem, st>>>(tab, L0.n, L0.h2, ms[0]->prm.mg_post_smooth,
                                                             (float)ms[0]->prm.relax, ms[0]->prm.max_cycles);

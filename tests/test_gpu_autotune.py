@@ -97,3 +97,50 @@ def test_autotune_tiles_restores_state(fs, O):
         s.set_mg_tiles([48])
     s.destroy()
     ref.destroy()
+
+
+def test_tile_side_larger_than_half_a_level_falls_back(fs, O):
+    """A tile side serves a level only if it is at most half the level: at
+    132^2 (tile levels 132 and 66) a 64-cell override on level 1 gives way to
+    the built-in 16, and the step equals the built-in choice bit for bit."""
+    n = 132
+    u0, v0 = O.lcg_uv(75, n * n)
+    out = []
+    for tiles in (None, [64, 64]):
+        s = _mixed(fs, n)
+        if tiles is not None:
+            s.set_mg_tiles(tiles)
+            assert s.mg_tiles() == [64, 16]
+        s.upload_velocity(u0, v0)
+        for _ in range(2):
+            s.step(0.002)
+        out.append(s.read_velocity())
+        s.destroy()
+    assert np.array_equal(out[0][0], out[1][0]) and np.array_equal(out[0][1], out[1][1])
+
+
+def test_batch_class_of_small_levels_keeps_tiles_within_half(fs, O):
+    """The class rule counts the tiles of all members (64 members of 132^2
+    would ask for 64-cell tiles on the 66-cell level); the side stays within
+    half the level and every member equals a solver stepped alone."""
+    fs._lib.load()
+    n, count = 132, 64
+    cfg = dict(nu=1e-3, advection="maccormack", pressure_solver="multigrid", pressure_iterations=1,
+               precision="mixed", pressure_tol=1e-8, max_cycles=60)
+    b = fs.GPUFluidBatch([dict(n=n, **cfg) for _ in range(count)])
+    states = [O.lcg_uv(200 + i, n * n) for i in range(count)]
+    for m, (u, v) in zip(b.members, states):
+        m.upload_velocity(u, v)
+    for _ in range(2):
+        b.step([0.002] * count)
+    b.sync()
+    for i in (0, count - 1):
+        s = _mixed(fs, n)
+        s.upload_velocity(*states[i])
+        for _ in range(2):
+            s.step(0.002)
+        ua, va = b.members[i].read_velocity()
+        ub, vb = s.read_velocity()
+        assert np.array_equal(ua, ub) and np.array_equal(va, vb)
+        s.destroy()
+    b.destroy()
