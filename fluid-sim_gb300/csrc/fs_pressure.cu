@@ -524,7 +524,7 @@ __device__ __forceinline__ void refine_init4_body(const float* __restrict__ dh, 
   block_max_finish(m, ctx);
 }
 
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(256, 5)
     k_refine_init4(const float* __restrict__ dh, const float* __restrict__ dl, const float* __restrict__ ph,
                    const float* __restrict__ pl, float* __restrict__ r32, int nx, int ny, LapScale ks, RedCtx ctx) {
   refine_init4_body(dh, dl, ph, pl, r32, nx, ny, ks, ctx);
@@ -558,12 +558,30 @@ __global__ void __launch_bounds__(256)
   block_max_finish(m, ctx);
 }
 
+// Grid of k_refine_init4: one wave (5 CTAs per SM, the register cap of its
+// launch bounds), every block walking the same number of tile rows (6 at
+// 2048^2, against two waves of up to 4 with the capped reduction grid).
+static dim3 refine4_grid(const Solver* s, int nq, int ny) {
+  static int sms[64] = {};
+  const int dev = s->prm.device & 63;
+  if (!sms[dev] && cudaDeviceGetAttribute(&sms[dev], cudaDevAttrMultiProcessorCount, s->prm.device) != cudaSuccess)
+    sms[dev] = 0;
+  const int slots = (sms[dev] > 0 ? sms[dev] : 152) * 5;
+  const int ntx = (nq + 31) >> 5, nty = (ny + 7) >> 3;
+  const int gx = ntx < slots ? ntx : slots;
+  int gy = slots / gx;
+  if (gy < 1) gy = 1;
+  const int per = (nty + gy - 1) / gy;
+  gy = (nty + per - 1) / per;
+  return dim3(gx, gy);
+}
+
 void launch_refine_init(Solver* s, const float* dh, const float* dl, const float* ph, const float* pl,
                         float* r32, bool zero_p) {
   const Grid& g = s->g;
   FS_LAUNCH(s, "refine_init", (double)s->n * (zero_p ? 12 : 20),
             if (!zero_p && g.nx % 4 == 0) {
-              k_refine_init4<<<red_grid2(g.nx / 4, g.ny), kBlock, 0, s->stream>>>(
+              k_refine_init4<<<refine4_grid(s, g.nx / 4, g.ny), kBlock, 0, s->stream>>>(
                   dh, dl, ph, pl, r32, g.nx, g.ny, lap_scale(g), red_ctx(s, s->red_out));
             } else {
               k_refine_init<<<red_grid2(g.nx, g.ny), kBlock, 0, s->stream>>>(

@@ -391,11 +391,11 @@ FS_API int fs_total_cycles(fs_solver* s, int64_t* cycles);
  * pressure are restored afterwards.  No reference counterpart. */
 FS_API int fs_autotune(fs_solver* s, double dt, int32_t nsteps, int32_t* pre, int32_t* post, double* ms_per_step);
 /* Tile sides (16, 32 or 64 cells) of the fused multigrid kernels of each tile
- * level (the levels above the bottom solve); 0 = the built-in rule (the
- * largest tile that still gives >= 256 CTAs).  A side larger than half its
- * level is not used there (the built-in rule applies; fs_get_mg_tiles reports
- * the side in use).  The tiles give the same values whatever their size, so
- * they change only the speed. */
+ * level (the levels above the bottom solve); 0 = the built-in rule (64 where
+ * that gives >= 1024 CTAs, else 32 where that gives >= 256, else 16).  A side
+ * larger than half its level is not used there (the built-in rule applies;
+ * fs_get_mg_tiles reports the side in use).  The tiles give the same values
+ * whatever their size, so they change only the speed. */
 FS_API int fs_set_mg_tiles(fs_solver* s, const int32_t* tiles, int32_t count);
 /* the sides in use, one per tile level (*count = number of tile levels) */
 FS_API int fs_get_mg_tiles(fs_solver* s, int32_t* tiles, int32_t cap, int32_t* count);
