@@ -99,9 +99,12 @@ constexpr size_t up_smem_bytes() {
   return (2 * (size_t)TileBox<T, H>::NA + CoarseBox<T, H>::NC) * sizeof(float) + 128;
 }
 
-// the dynamic shared memory of a tile kernel, from a 128-byte boundary (TMA destinations)
+// the dynamic shared memory of a tile kernel, from a 128-byte boundary (TMA
+// destinations): an offset added to the shared array itself, so that the
+// compiler still knows every access is to shared memory
 __device__ __forceinline__ float* tile_smem(float* p) {
-  return reinterpret_cast<float*>((reinterpret_cast<uintptr_t>(p) + 127) & ~static_cast<uintptr_t>(127));
+  const uint32_t a = (uint32_t)__cvta_generic_to_shared(p);
+  return p + (((128u - (a & 127u)) & 127u) >> 2);
 }
 
 // wrapped 4-byte copies of the R x R region from (gi0, gj0) of a periodic n x n field
