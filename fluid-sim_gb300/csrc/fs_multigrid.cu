@@ -53,6 +53,12 @@ __device__ __forceinline__ void cp_async4(float* sdst, const float* gsrc) {
                "l"((size_t)__cvta_generic_to_global(gsrc))
                : "memory");
 }
+// 16-byte form (both addresses 16-byte aligned), L2 only
+__device__ __forceinline__ void cp_async16(float* sdst, const float* gsrc) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"((uint32_t)__cvta_generic_to_shared(sdst)),
+               "l"((size_t)__cvta_generic_to_global(gsrc))
+               : "memory");
+}
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
 __device__ __forceinline__ void prefetch_l2(const void* p) {
   asm volatile("prefetch.global.L2 [%0];" ::"l"((size_t)__cvta_generic_to_global(p)));
@@ -459,7 +465,7 @@ struct Group {
   }
 };
 
-__device__ void bottom_smooth(float* sm, const BottomLevels& L, int l, int sweeps, Group G) {
+__device__ __forceinline__ void bottom_smooth(float* sm, const BottomLevels& L, int l, int sweeps, Group G) {
   const int n = L.n[l];
   const float h2 = L.h2[l];
   float* x = sm + L.off_x[l];
@@ -491,7 +497,7 @@ __device__ void bottom_smooth(float* sm, const BottomLevels& L, int l, int sweep
   }
 }
 
-__device__ void bottom_restrict(float* sm, const BottomLevels& L, int l, Group G) {
+__device__ __forceinline__ void bottom_restrict(float* sm, const BottomLevels& L, int l, Group G) {
   const int n = L.n[l], nc = L.n[l + 1];
   const float h2 = L.h2[l];
   const float* x = sm + L.off_x[l];
@@ -513,7 +519,7 @@ __device__ void bottom_restrict(float* sm, const BottomLevels& L, int l, Group G
   G.sync();
 }
 
-__device__ void bottom_prolong(float* sm, const BottomLevels& L, int l, Group G) {
+__device__ __forceinline__ void bottom_prolong(float* sm, const BottomLevels& L, int l, Group G) {
   const int n = L.n[l], nc = L.n[l + 1];
   float* x = sm + L.off_x[l];
   const float* c = sm + L.off_x[l + 1];
@@ -537,12 +543,15 @@ __device__ __forceinline__ void mg_bottom_body(const float* __restrict__ rhs_top
   const Group CTA{tid, (int)blockDim.x, false};
   const Group W0{tid, 32, true};
   {
+    // the top level's rhs (and iterate) by asynchronous copies, all in flight at once
     const int n = L.n[0];
     for (int k = tid; k < n * n; k += CTA.nthr) {
-      sm[L.off_r[0] + k] = __ldg(rhs_top + k);
-      sm[L.off_x[0] + k] = has_x ? x_top[k] : 0.f;
+      cp_async4(&sm[L.off_r[0] + k], rhs_top + k);
+      if (has_x) cp_async4(&sm[L.off_x[0] + k], x_top + k);
+      else sm[L.off_x[0] + k] = 0.f;
     }
   }
+  cp_async_wait_all();
   __syncthreads();
   // first level handled by warp 0 alone
   int ls = 0;
@@ -635,7 +644,7 @@ __device__ __forceinline__ void p2_sync() {
 }
 
 template <int N, bool WARP>
-__device__ void p2_smooth(float* x, const float* r, float h2, int sweeps, float w) {
+__device__ __forceinline__ void p2_smooth(float* x, const float* r, float h2, int sweeps, float w) {
   constexpr int HALF = N / 2;
   const int tid = WARP ? (int)(threadIdx.x & 31) : (int)threadIdx.x;
   const int nthr = WARP ? 32 : (int)blockDim.x;
@@ -655,7 +664,7 @@ __device__ void p2_smooth(float* x, const float* r, float h2, int sweeps, float 
 
 // residual of level N restricted into (cr, cx = 0) of level N/2
 template <int N, bool WARP>
-__device__ void p2_restrict(const float* x, const float* r, float h2, float* cr, float* cx) {
+__device__ __forceinline__ void p2_restrict(const float* x, const float* r, float h2, float* cr, float* cx) {
   constexpr int NC = N / 2;
   const int tid = WARP ? (int)(threadIdx.x & 31) : (int)threadIdx.x;
   const int nthr = WARP ? 32 : (int)blockDim.x;
@@ -678,7 +687,7 @@ __device__ void p2_restrict(const float* x, const float* r, float h2, float* cr,
 
 // x (level N) += bilinear prolongation of c (level N/2)
 template <int N, bool WARP>
-__device__ void p2_prolong(float* x, const float* c) {
+__device__ __forceinline__ void p2_prolong(float* x, const float* c) {
   constexpr int NC = N / 2;
   const int tid = WARP ? (int)(threadIdx.x & 31) : (int)threadIdx.x;
   const int nthr = WARP ? 32 : (int)blockDim.x;
@@ -694,25 +703,30 @@ __device__ void p2_prolong(float* x, const float* c) {
   p2_sync<N, WARP>();
 }
 
-// sub-cycle from level N down to NMIN and back; levels <= 16 are called by warp 0 only
-template <int N, int NMIN>
-__device__ void p2_cycle(float* const* X, float* const* R, const BottomH2& H, int lvl, int pre, int post,
-                         int coarse) {
+// sub-cycle from level N (chain level LVL, at float offset OFF of the chain's
+// x and rhs arrays) down to NMIN and back; levels <= 16 are called by warp 0
+// only.  Every level's arrays are the shared arrays plus a compile-time
+// offset, so all accesses compile as shared-memory accesses.
+template <int N, int NMIN, int LVL, int OFF>
+__device__ __forceinline__ void p2_cycle(float* sx, float* sr, const BottomH2& H, int pre, int post, int coarse) {
   constexpr bool W = N <= 16;
+  float* const x = sx + OFF;
+  float* const r = sr + OFF;
   if constexpr (N == NMIN) {
-    p2_smooth<N, W>(X[lvl], R[lvl], H.h2[lvl], coarse, H.w);
+    p2_smooth<N, W>(x, r, H.h2[LVL], coarse, H.w);
   } else {
     static_assert(N % 2 == 0, "every level above the coarsest is even");
-    p2_smooth<N, W>(X[lvl], R[lvl], H.h2[lvl], pre, H.w);
-    p2_restrict<N, W>(X[lvl], R[lvl], H.h2[lvl], R[lvl + 1], X[lvl + 1]);
+    constexpr int OFFC = OFF + N * N;
+    p2_smooth<N, W>(x, r, H.h2[LVL], pre, H.w);
+    p2_restrict<N, W>(x, r, H.h2[LVL], sr + OFFC, sx + OFFC);
     if constexpr (!W && N / 2 <= 16) {
-      if (threadIdx.x < 32) p2_cycle<N / 2, NMIN>(X, R, H, lvl + 1, pre, post, coarse);
+      if (threadIdx.x < 32) p2_cycle<N / 2, NMIN, LVL + 1, OFFC>(sx, sr, H, pre, post, coarse);
       __syncthreads();
     } else {
-      p2_cycle<N / 2, NMIN>(X, R, H, lvl + 1, pre, post, coarse);
+      p2_cycle<N / 2, NMIN, LVL + 1, OFFC>(sx, sr, H, pre, post, coarse);
     }
-    p2_prolong<N, W>(X[lvl], X[lvl + 1]);
-    p2_smooth<N, W>(X[lvl], R[lvl], H.h2[lvl], post, H.w);
+    p2_prolong<N, W>(x, sx + OFFC);
+    p2_smooth<N, W>(x, r, H.h2[LVL], post, H.w);
   }
 }
 
@@ -723,32 +737,29 @@ __device__ __forceinline__ void mg_bottom_chain_body(const float* __restrict__ r
   constexpr int L = chain_levels<N0, NMIN>();
   constexpr int SZ = chain_floats<N0, NMIN>();
   static_assert(L <= 4 && NMIN % 2 == 0, "chains of at most four even levels");
-  __shared__ float sx[SZ], sr[SZ];
-  float* X[4];
-  float* R[4];
-  {
-    int off = 0, n = N0;
-    for (int l = 0; l < L; l++) {
-      X[l] = sx + off;
-      R[l] = sr + off;
-      off += n * n;
-      n >>= 1;
-    }
-  }
+  // the chain's levels one after another, level 0 first
+  __shared__ __align__(16) float sx[SZ];
+  __shared__ __align__(16) float sr[SZ];
   const int tid = threadIdx.x;
-  for (int k = tid; k < N0 * N0; k += blockDim.x) {
-    R[0][k] = __ldg(rhs_top + k);
-    X[0][k] = has_x ? x_top[k] : 0.f;
+  // level 0's rhs (and iterate): 16-byte asynchronous copies, all in flight at
+  // once (N0 is even, so N0^2 is a multiple of 4; the level arrays are
+  // cudaMalloc'd, 256-byte aligned)
+  static_assert((N0 * N0) % 4 == 0, "whole 16-byte groups");
+  for (int k = tid; k < N0 * N0 / 4; k += blockDim.x) {
+    cp_async16(sr + 4 * k, rhs_top + 4 * k);
+    if (has_x) cp_async16(sx + 4 * k, x_top + 4 * k);
+    else reinterpret_cast<float4*>(sx)[k] = make_float4(0.f, 0.f, 0.f, 0.f);
   }
+  cp_async_wait_all();
   __syncthreads();
   if constexpr (N0 <= 16) {
-    if (tid < 32) p2_cycle<N0, NMIN>(X, R, H, 0, pre, post, coarse);
+    if (tid < 32) p2_cycle<N0, NMIN, 0, 0>(sx, sr, H, pre, post, coarse);
     __syncthreads();
   } else {
-    p2_cycle<N0, NMIN>(X, R, H, 0, pre, post, coarse);
+    p2_cycle<N0, NMIN, 0, 0>(sx, sr, H, pre, post, coarse);
   }
   for (int k = tid; k < N0 * N0; k += blockDim.x) {
-    float e = X[0][k];
+    float e = sx[k];
     if (acc_h) {
       df p = df_add_f(df{acc_h[k], acc_l[k]}, e);
       acc_h[k] = p.hi;
