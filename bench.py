@@ -418,6 +418,25 @@ def run_gpu(args):
 
 
 # ------------------------------------------------------------ CPU baselines
+def host_cpu() -> str:
+    """The host the CPU baseline ran on: architecture, logical CPUs and, where
+    the kernel reports one, the CPU model (from /proc/cpuinfo)."""
+    import platform
+    model = ""
+    try:
+        with open("/proc/cpuinfo") as f:
+            for line in f:
+                key = line.split(":")[0].strip().lower()
+                if key in ("model name", "cpu model", "hardware") and ":" in line:
+                    model = line.split(":", 1)[1].strip()
+                    break
+                if key == "cpu part" and not model:
+                    model = "cpu part " + line.split(":", 1)[1].strip()
+    except OSError:
+        pass
+    return f"{platform.machine()}, {os.cpu_count()} logical CPUs" + (f", {model}" if model else "")
+
+
 def cpu_baseline(n: int, threads: int, timed_steps: int):
     """The oracle (f64 restatement of the reference CPU solver) on the same
     workload: MacCormack, explicit diffusion, exact FFT projection, one
@@ -437,6 +456,7 @@ def cpu_baseline(n: int, threads: int, timed_steps: int):
         cpu.step(dt, advect_dye=False)
     sec = time.perf_counter() - t0
     return {"value": float(n) * n * timed_steps / sec, "unit": UNIT, "cores": threads, "kind": "port",
+            "host": host_cpu(),
             "sample": f"{timed_steps} timed step(s) of the {n}^2 workload after 1 untimed step "
                       f"({sec:.1f} s), f64 C restatement of src/cpu (FFT projection), "
                       f"max|div|={cpu.max_divergence():.1e}"}
@@ -474,7 +494,7 @@ def run_reference(args):
         "data": "synthetic (same seeded workload)",
         "config": {"workload": f"periodic {n}x{n}, {len(disks)} fixed disks, nu={NU}, MacCormack, explicit "
                                "diffusion, exact FFT projection (max|div| ~1e-13)", "n": n},
-        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "host": host_cpu(),
                          "sample": f"{timed} timed step(s) after {warm} warm-up step(s) of the {n}^2 "
                                    f"workload (of K={args.steps}); f64 C restatement of src/cpu with "
                                    f"{threads} OpenMP threads (the reference is JavaScript; no Node here)"},
