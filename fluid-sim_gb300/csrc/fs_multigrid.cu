@@ -789,15 +789,23 @@ __device__ __forceinline__ bool member_active(const DevState* st, int max_cycles
   return !st->converged && !st->nonfinite && st->cycles < max_cycles;
 }
 
+// The tile kernels' tables carry each member's TMA tensor maps (tma = 0:
+// that member's tiles stage with wrapped copies); the tables are
+// __grid_constant__ parameters, so the maps are read in place.  The maps sit
+// in their own array (a CUtensorMap is 128-byte aligned): the up table is
+// 64 x (3 x 128 + 64) bytes, within the 32,764 bytes of kernel parameters.
 struct DownTab {
+  CUtensorMap tm[kClassMax];  // rhs
   struct {
     const float* rhs;
     float* xout;
     float* crhs;
-    const DevState* st;
+    DevState* st;  // loop state; its async_err is the member's TMA error flag
+    int tma;
   } m[kClassMax];
 };
 struct UpTab {
+  CUtensorMap tm[kClassMax][3];  // rhs, fine iterate, coarse iterate
   struct {
     const float* rhs;
     const float* xin;
@@ -805,9 +813,11 @@ struct UpTab {
     const float* xc;
     float* ph;
     float* pl;
-    const DevState* st;
+    DevState* st;  // loop state; its async_err is the member's TMA error flag
+    int tma;
   } m[kClassMax];
 };
+static_assert(sizeof(UpTab) + 64 <= 32764, "kernel parameter limit");
 struct BottomTab {
   struct {
     const float* rhs;
@@ -819,23 +829,24 @@ struct BottomTab {
 };
 
 template <int T, int H>
-__global__ void __launch_bounds__(256) k_mg_down_class(const DownTab tab, int n, float h2, int pre, float w,
-                                                       int max_cycles) {
+__global__ void __launch_bounds__(256) k_mg_down_class(const __grid_constant__ DownTab tab, int n, float h2,
+                                                       int pre, float w, int max_cycles) {
   extern __shared__ float tile_dyn[];
   const auto& a = tab.m[blockIdx.z];
   if (!member_active(a.st, max_cycles)) return;
-  mg_down_body<T, H>(tile_smem(tile_dyn), a.rhs, nullptr, a.xout, a.crhs, n, h2, pre, w, nullptr, nullptr, 0,
-                     nullptr);
+  mg_down_body<T, H>(tile_smem(tile_dyn), a.rhs, nullptr, a.xout, a.crhs, n, h2, pre, w, &tab.tm[blockIdx.z],
+                     nullptr, a.tma, &a.st->async_err);
 }
 
 template <int T, int H, bool ACC>
-__global__ void __launch_bounds__(256) k_mg_up_class(const UpTab tab, int n, float h2, int post, float w,
-                                                     int max_cycles) {
+__global__ void __launch_bounds__(256) k_mg_up_class(const __grid_constant__ UpTab tab, int n, float h2, int post,
+                                                     float w, int max_cycles) {
   extern __shared__ float tile_dyn[];
   const auto& a = tab.m[blockIdx.z];
   if (!member_active(a.st, max_cycles)) return;
-  mg_up_body<T, H, ACC>(tile_smem(tile_dyn), a.rhs, a.xin, a.xout, a.xc, n, h2, post, a.ph, a.pl, w, nullptr,
-                        nullptr, nullptr, 0, nullptr);
+  const CUtensorMap* tm = tab.tm[blockIdx.z];
+  mg_up_body<T, H, ACC>(tile_smem(tile_dyn), a.rhs, a.xin, a.xout, a.xc, n, h2, post, a.ph, a.pl, w, &tm[0], &tm[1],
+                        &tm[2], a.tma, &a.st->async_err);
 }
 
 template <int N0, int NMIN>
@@ -1100,8 +1111,16 @@ static void down_class_t(Solver* const* ms, int count, int l, cudaStream_t st) {
   const Level& L0 = ms[0]->lev[l];
   DownTab tab{};
   for (int i = 0; i < count; i++) {
-    Level& L = ms[i]->lev[l];
-    tab.m[i] = {L.rhs, L.x, ms[i]->lev[l + 1].rhs, ms[i]->dev};
+    Solver* s = ms[i];
+    Level& L = s->lev[l];
+    auto& m = tab.m[i];
+    m.rhs = L.rhs;
+    m.xout = L.x;
+    m.crhs = s->lev[l + 1].rhs;
+    m.st = s->dev;
+    const float* f[1] = {L.rhs};
+    CUtensorMap* mp[1] = {&tab.tm[i]};
+    m.tma = tile_maps<T, H>(s, L.n, f, mp, 1) ? 1 : 0;
   }
   static std::atomic<uint64_t> attr{0};
   constexpr size_t smem = down_smem_bytes<T, H>();
@@ -1138,12 +1157,23 @@ static void down_class(Solver* const* ms, int count, int l, cudaStream_t st) {
 template <int T, int H, bool ACC>
 static void up_class_t(Solver* const* ms, int count, int l, cudaStream_t st) {
   const Level& L0 = ms[0]->lev[l];
-  UpTab tab{};
+  using CB = CoarseBox<T, H>;
+  UpTab tab{};  // 28 KB on the host stack, copied into the launch's parameters
   for (int i = 0; i < count; i++) {
     Solver* s = ms[i];
     Level& L = s->lev[l];
-    tab.m[i] = {L.rhs, L.x, ACC ? nullptr : L.x2, s->lev[l + 1].x, ACC ? s->ph : nullptr, ACC ? s->pl : nullptr,
-                s->dev};
+    const Level& C = s->lev[l + 1];
+    auto& m = tab.m[i];
+    m.rhs = L.rhs;
+    m.xin = L.x;
+    m.xout = ACC ? nullptr : L.x2;
+    m.xc = C.x;
+    m.ph = ACC ? s->ph : nullptr;
+    m.pl = ACC ? s->pl : nullptr;
+    m.st = s->dev;
+    const float* f[2] = {L.rhs, L.x};
+    CUtensorMap* mp[2] = {&tab.tm[i][0], &tab.tm[i][1]};
+    m.tma = tile_maps<T, H>(s, L.n, f, mp, 2) && box_tmap(s, C.x, C.n, C.n, CB::WC, CB::RC, &tab.tm[i][2]) ? 1 : 0;
     if (!ACC) std::swap(L.x, L.x2);
   }
   static std::atomic<uint64_t> attr{0};
