@@ -527,6 +527,15 @@ void launch_advect_mc<float>(Solver* s, const float* u, const float* v, float* f
 }
 
 // DIFFUSE (shaders.js:401-425; src/cpu/solver.js:56-68 operand order)
+// c + a (l + r - 2c) + b (bo + t - 2c) with every rounding spelled out, in
+// the order of DIFFUSE (shaders.js:420), so that the one-cell and the
+// four-cell forms (and the batched kernels) round identically
+__device__ __forceinline__ float diffuse_cell(float c, float l, float r, float bo, float t, float a, float b) {
+  const float c2 = __fmul_rn(2.f, c);
+  return __fadd_rn(__fadd_rn(c, __fmul_rn(a, __fsub_rn(__fadd_rn(l, r), c2))),
+                   __fmul_rn(b, __fsub_rn(__fadd_rn(bo, t), c2)));
+}
+
 __device__ __forceinline__ void diffuse_body(const float* __restrict__ u, const float* __restrict__ v,
                                              float* __restrict__ ou, float* __restrict__ ov, int nx, int ny, float a,
                                              float b) {
@@ -535,12 +544,44 @@ __device__ __forceinline__ void diffuse_body(const float* __restrict__ u, const 
   int im = i == 0 ? nx - 1 : i - 1, ip = i + 1 == nx ? 0 : i + 1;
   int jm = j == 0 ? ny - 1 : j - 1, jp = j + 1 == ny ? 0 : j + 1;
   int64_t r = (int64_t)j * nx, rm = (int64_t)jm * nx, rp = (int64_t)jp * nx;
-  float c = __ldg(u + r + i);
-  ou[r + i] = c + a * (__ldg(u + r + im) - 2.f * c + __ldg(u + r + ip)) +
-              b * (__ldg(u + rm + i) - 2.f * c + __ldg(u + rp + i));
-  c = __ldg(v + r + i);
-  ov[r + i] = c + a * (__ldg(v + r + im) - 2.f * c + __ldg(v + r + ip)) +
-              b * (__ldg(v + rm + i) - 2.f * c + __ldg(v + rp + i));
+  ou[r + i] = diffuse_cell(__ldg(u + r + i), __ldg(u + r + im), __ldg(u + r + ip), __ldg(u + rm + i),
+                           __ldg(u + rp + i), a, b);
+  ov[r + i] = diffuse_cell(__ldg(v + r + i), __ldg(v + r + im), __ldg(v + r + ip), __ldg(v + rm + i),
+                           __ldg(v + rp + i), a, b);
+}
+
+// Four consecutive cells per thread (nx a multiple of 4): float4 loads of the
+// three rows, the group's outer left and right neighbours as scalars.
+__device__ __forceinline__ void diffuse4_one(const float* __restrict__ f, float* __restrict__ o, int64_t r,
+                                             int64_t rm, int64_t rp, int i0, int il, int ir, float a, float b) {
+  const float4 c = __ldg(reinterpret_cast<const float4*>(f + r + i0));
+  const float4 bo = __ldg(reinterpret_cast<const float4*>(f + rm + i0));
+  const float4 t = __ldg(reinterpret_cast<const float4*>(f + rp + i0));
+  const float l = __ldg(f + r + il), rr = __ldg(f + r + ir);
+  float4 out;
+  out.x = diffuse_cell(c.x, l, c.y, bo.x, t.x, a, b);
+  out.y = diffuse_cell(c.y, c.x, c.z, bo.y, t.y, a, b);
+  out.z = diffuse_cell(c.z, c.y, c.w, bo.z, t.z, a, b);
+  out.w = diffuse_cell(c.w, c.z, rr, bo.w, t.w, a, b);
+  *reinterpret_cast<float4*>(o + r + i0) = out;
+}
+
+__device__ __forceinline__ void diffuse4_body(const float* __restrict__ u, const float* __restrict__ v,
+                                              float* __restrict__ ou, float* __restrict__ ov, int nx, int ny,
+                                              float a, float b) {
+  const int q = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y;
+  if (q >= (nx >> 2) || j >= ny) return;
+  const int i0 = q << 2, il = i0 == 0 ? nx - 1 : i0 - 1, ir = i0 + 4 == nx ? 0 : i0 + 4;
+  const int jm = j == 0 ? ny - 1 : j - 1, jp = j + 1 == ny ? 0 : j + 1;
+  const int64_t r = (int64_t)j * nx, rm = (int64_t)jm * nx, rp = (int64_t)jp * nx;
+  diffuse4_one(u, ou, r, rm, rp, i0, il, ir, a, b);
+  diffuse4_one(v, ov, r, rm, rp, i0, il, ir, a, b);
+}
+
+__global__ void __launch_bounds__(256) k_diffuse4(const float* __restrict__ u, const float* __restrict__ v,
+                                                  float* __restrict__ ou, float* __restrict__ ov,
+                                                  int nx, int ny, float a, float b) {
+  diffuse4_body(u, v, ou, ov, nx, ny, a, b);
 }
 
 __global__ void __launch_bounds__(256) k_diffuse(const float* __restrict__ u, const float* __restrict__ v,
@@ -554,13 +595,17 @@ void launch_diffuse(Solver* s, const float* u, const float* v, float* ou, float*
   float a = (float)(s->prm.nu * dt / (g.dxd * g.dxd));
   float b = (float)(s->prm.nu * dt / (g.dyd * g.dyd));
   FS_LAUNCH(s, "diffuse", (double)s->n * 16,
-            k_diffuse<<<grid2d(g.nx, g.ny, kBlock), kBlock, 0, s->stream>>>(u, v, ou, ov, g.nx, g.ny,
-                                                                            a, b));
+            if (g.nx % 4 == 0) {
+              k_diffuse4<<<grid2d(g.nx / 4, g.ny, kBlock), kBlock, 0, s->stream>>>(u, v, ou, ov, g.nx, g.ny, a, b);
+            } else {
+              k_diffuse<<<grid2d(g.nx, g.ny, kBlock), kBlock, 0, s->stream>>>(u, v, ou, ov, g.nx, g.ny, a, b);
+            });
 }
 
 __global__ void __launch_bounds__(256) k_diffuse_class(const DiffTab tab, int nx, int ny) {
   const auto& a = tab.m[blockIdx.z];
-  diffuse_body(a.u, a.v, a.ou, a.ov, nx, ny, a.a, a.b);
+  if ((nx & 3) == 0) diffuse4_body(a.u, a.v, a.ou, a.ov, nx, ny, a.a, a.b);
+  else diffuse_body(a.u, a.v, a.ou, a.ov, nx, ny, a.a, a.b);
 }
 
 // advection (and diffusion) of every member of a class into (wu, wv), or
@@ -593,7 +638,7 @@ void launch_front_advect_class(Solver* const* ms, int count, const double* dts, 
       const float b = (float)(s->prm.nu * (float)dts[i] / (s->g.dyd * s->g.dyd));
       dt.m[i] = {s->wu, s->wv, s->tu, s->tv, a, b};
     }
-    dim3 g2 = grid2d(g.nx, g.ny, kBlock);
+    dim3 g2 = grid2d(g.nx % 4 == 0 ? g.nx / 4 : g.nx, g.ny, kBlock);  // four cells per thread when nx % 4 == 0
     g2.z = count;
     k_diffuse_class<<<g2, kBlock, 0, st>>>(dt, g.nx, g.ny);
   }

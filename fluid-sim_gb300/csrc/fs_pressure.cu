@@ -374,6 +374,52 @@ __device__ __forceinline__ void subgrad_df_body(const float* __restrict__ wuh, c
   vh[c] = v.hi; vl[c] = v.lo;
 }
 
+// the same update for four consecutive cells (nx a multiple of 4): float4
+// loads of the pressure rows j and j - 1 and of w, the group's left
+// neighbour as a scalar; the same df operations per cell as subgrad_df_body
+__device__ __forceinline__ void subgrad4_body(const float* __restrict__ wuh, const float* __restrict__ wul,
+                                              const float* __restrict__ wvh, const float* __restrict__ wvl,
+                                              const float* __restrict__ ph, const float* __restrict__ pl,
+                                              float* __restrict__ uh, float* __restrict__ ul,
+                                              float* __restrict__ vh, float* __restrict__ vl, int nx, int ny,
+                                              df idx, df idy) {
+  const int q = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y;
+  if (q >= (nx >> 2) || j >= ny) return;
+  const int i0 = q << 2, il = i0 == 0 ? nx - 1 : i0 - 1, jm = j == 0 ? ny - 1 : j - 1;
+  const int64_t c = (int64_t)j * nx + i0, cb = (int64_t)jm * nx + i0, cl = (int64_t)j * nx + il;
+  const float4 h = __ldg(reinterpret_cast<const float4*>(ph + c));
+  const float4 l = __ldg(reinterpret_cast<const float4*>(pl + c));
+  const float4 hb = __ldg(reinterpret_cast<const float4*>(ph + cb));
+  const float4 lb = __ldg(reinterpret_cast<const float4*>(pl + cb));
+  const float4 uw = __ldg(reinterpret_cast<const float4*>(wuh + c));
+  const float4 vw = __ldg(reinterpret_cast<const float4*>(wvh + c));
+  const float4 z = {0.f, 0.f, 0.f, 0.f};
+  const float4 uwl = wul ? __ldg(reinterpret_cast<const float4*>(wul + c)) : z;
+  const float4 vwl = wvl ? __ldg(reinterpret_cast<const float4*>(wvl + c)) : z;
+  const df pw = {__ldg(ph + cl), __ldg(pl + cl)};
+  const df p0 = {h.x, l.x}, p1 = {h.y, l.y}, p2 = {h.z, l.z}, p3 = {h.w, l.w};
+  const df u0 = df_sub(df{uw.x, uwl.x}, df_mul(df_sub(p0, pw), idx));
+  const df u1 = df_sub(df{uw.y, uwl.y}, df_mul(df_sub(p1, p0), idx));
+  const df u2 = df_sub(df{uw.z, uwl.z}, df_mul(df_sub(p2, p1), idx));
+  const df u3 = df_sub(df{uw.w, uwl.w}, df_mul(df_sub(p3, p2), idx));
+  const df v0 = df_sub(df{vw.x, vwl.x}, df_mul(df_sub(p0, df{hb.x, lb.x}), idy));
+  const df v1 = df_sub(df{vw.y, vwl.y}, df_mul(df_sub(p1, df{hb.y, lb.y}), idy));
+  const df v2 = df_sub(df{vw.z, vwl.z}, df_mul(df_sub(p2, df{hb.z, lb.z}), idy));
+  const df v3 = df_sub(df{vw.w, vwl.w}, df_mul(df_sub(p3, df{hb.w, lb.w}), idy));
+  *reinterpret_cast<float4*>(uh + c) = make_float4(u0.hi, u1.hi, u2.hi, u3.hi);
+  *reinterpret_cast<float4*>(ul + c) = make_float4(u0.lo, u1.lo, u2.lo, u3.lo);
+  *reinterpret_cast<float4*>(vh + c) = make_float4(v0.hi, v1.hi, v2.hi, v3.hi);
+  *reinterpret_cast<float4*>(vl + c) = make_float4(v0.lo, v1.lo, v2.lo, v3.lo);
+}
+
+__global__ void __launch_bounds__(256)
+    k_subgrad4_df(const float* __restrict__ wuh, const float* __restrict__ wul, const float* __restrict__ wvh,
+                  const float* __restrict__ wvl, const float* __restrict__ ph, const float* __restrict__ pl,
+                  float* __restrict__ uh, float* __restrict__ ul, float* __restrict__ vh, float* __restrict__ vl,
+                  int nx, int ny, df idx, df idy) {
+  subgrad4_body(wuh, wul, wvh, wvl, ph, pl, uh, ul, vh, vl, nx, ny, idx, idy);
+}
+
 __global__ void __launch_bounds__(256)
     k_subgrad_df(const float* __restrict__ wuh, const float* __restrict__ wul, const float* __restrict__ wvh,
                  const float* __restrict__ wvl, const float* __restrict__ ph, const float* __restrict__ pl,
@@ -386,8 +432,13 @@ void launch_subgrad_df(Solver* s, const float* wuh, const float* wul, const floa
                        const float* ph, const float* pl, float* uh, float* ul, float* vh, float* vl) {
   const Grid& g = s->g;
   FS_LAUNCH(s, "subtract_gradient", (double)s->n * ((wul ? 16 : 8) + 8 + 16),
-            k_subgrad_df<<<grid2d(g.nx, g.ny, kBlock), kBlock, 0, s->stream>>>(
-                wuh, wul, wvh, wvl, ph, pl, uh, ul, vh, vl, g.nx, g.ny, df_host(g.idxd), df_host(g.idyd)));
+            if (g.nx % 4 == 0) {
+              k_subgrad4_df<<<grid2d(g.nx / 4, g.ny, kBlock), kBlock, 0, s->stream>>>(
+                  wuh, wul, wvh, wvl, ph, pl, uh, ul, vh, vl, g.nx, g.ny, df_host(g.idxd), df_host(g.idyd));
+            } else {
+              k_subgrad_df<<<grid2d(g.nx, g.ny, kBlock), kBlock, 0, s->stream>>>(
+                  wuh, wul, wvh, wvl, ph, pl, uh, ul, vh, vl, g.nx, g.ny, df_host(g.idxd), df_host(g.idyd));
+            });
 }
 
 // df Laplacian of p at (i, j).  Square cells (ih2x == ih2y, the uniform
@@ -732,7 +783,7 @@ struct CondTab {
   } m[kClassMax];
 };
 
-__global__ void __launch_bounds__(256) k_refine_class(const RefineTab tab, int nx, int ny, LapScale ks,
+__global__ void __launch_bounds__(256, 5) k_refine_class(const RefineTab tab, int nx, int ny, LapScale ks,
                                                       int max_cycles, int quad) {
   const auto& a = tab.m[blockIdx.z];
   if (!member_in_loop(a.st, max_cycles)) return;
@@ -850,7 +901,10 @@ __global__ void __launch_bounds__(256) k_div_start_class(const ProjTab tab, int 
 
 __global__ void __launch_bounds__(256) k_subgrad_class(const ProjTab tab, int nx, int ny) {
   const auto& a = tab.m[blockIdx.z];
-  subgrad_df_body(a.wu, nullptr, a.wv, nullptr, a.ph, a.pl, a.uh, a.ul, a.vh, a.vl, nx, ny, a.idx, a.idy);
+  if ((nx & 3) == 0)
+    subgrad4_body(a.wu, nullptr, a.wv, nullptr, a.ph, a.pl, a.uh, a.ul, a.vh, a.vl, nx, ny, a.idx, a.idy);
+  else
+    subgrad_df_body(a.wu, nullptr, a.wv, nullptr, a.ph, a.pl, a.uh, a.ul, a.vh, a.vl, nx, ny, a.idx, a.idy);
 }
 
 __global__ void k_finish_class(const ProjTab tab, int count) {
@@ -897,7 +951,7 @@ void launch_back_class(Solver* const* ms, int count, const float* const* wu, con
                        const double* dts, cudaStream_t st) {
   const Grid& g = ms[0]->g;
   const ProjTab tab = proj_tab(ms, count, wu, wv, dts);
-  dim3 g2 = grid2d(g.nx, g.ny, kBlock);
+  dim3 g2 = grid2d(g.nx % 4 == 0 ? g.nx / 4 : g.nx, g.ny, kBlock);  // four cells per thread when nx % 4 == 0
   g2.z = count;
   k_subgrad_class<<<g2, kBlock, 0, st>>>(tab, g.nx, g.ny);
   k_finish_class<<<1, kClassMax, 0, st>>>(tab, count);
