@@ -370,7 +370,9 @@ static void flat_cycle(Solver* s, int iterations, bool residual) {
 
 // Records the tolerance loop into a conditional WHILE node of the step graph
 // being captured on s->stream: k_cond (init) sets the condition from the
-// initial residual, the body is one multigrid cycle followed by k_cond (step).
+// initial residual, the body is one cycle followed by k_cond (step) -- for
+// the fused MIXED multigrid cycle, the residual kernel's finishing thread
+// does k_cond's step itself (one launch less per cycle).
 static int capture_tolerance_loop(Solver* s) {
   cudaStreamCaptureStatus cst;
   cudaGraph_t cg = nullptr;
@@ -394,8 +396,16 @@ static int capture_tolerance_loop(Solver* s) {
   cudaStream_t main = s->stream;
   s->stream = s->body_stream;
   int64_t l0 = s->launches;
-  mg_cycle(s, true);
-  launch_cond_step(s, h, true);
+  if (s->prm.pressure_solver == FS_PRESSURE_MULTIGRID && s->mixed && s->fused) {
+    // the fused MIXED cycle; its residual kernel also does k_cond's step
+    s->lev[0].x = s->e32;
+    s->lev[0].x2 = s->e32b;
+    mg_vcycle_fused(s, false, s->ph, s->pl);
+    if (!launch_refine_init(s, s->dh, s->dl, s->ph, s->pl, s->r32, false, &h)) launch_cond_step(s, h, true);
+  } else {
+    mg_cycle(s, true);
+    launch_cond_step(s, h, true);
+  }
   s->graph_launches_body = s->launches - l0;
   s->stream = main;
   cudaGraph_t tmp = nullptr;

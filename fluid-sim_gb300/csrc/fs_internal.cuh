@@ -225,8 +225,11 @@ void launch_prolong_add(Solver* s, const float* coarse, float* fine, int nf);
 void launch_fill(Solver* s, float* x, float value, int64_t n);
 void launch_fill64(Solver* s, double* x, double value, int64_t n);
 // mixed-precision refinement (double-float pressure and divergence)
-void launch_refine_init(Solver* s, const float* dh, const float* dl, const float* ph, const float* pl,
-                        float* r32, bool zero_p);
+// cond (a captured tolerance loop's handle): the residual kernel also does
+// the loop's step bookkeeping and sets the condition when it can (returns
+// true); otherwise the caller launches k_cond
+bool launch_refine_init(Solver* s, const float* dh, const float* dl, const float* ph, const float* pl,
+                        float* r32, bool zero_p, const cudaGraphConditionalHandle* cond = nullptr);
 // TMA tensor map of a row-major f32 plane nx x ny (pitch nx) with a bw x bh
 // box, cached per solver; false when TMA cannot copy it (nx % 4 != 0, an
 // unaligned base, a box larger than the plane, no encoder in the CUDA driver)

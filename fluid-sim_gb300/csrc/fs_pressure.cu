@@ -535,6 +535,33 @@ __global__ void __launch_bounds__(256)
   refine_init_body(dh, dl, ph, pl, r32, nx, ny, ks, zero_p, ctx);
 }
 
+// The tolerance loop's bookkeeping after a cycle (init: before the loop) from
+// the residual maximum m, and the loop condition "cycle again" -- the work of
+// k_cond, also done by the residual kernel's finishing thread when the loop
+// folds it in (CondFold).
+__device__ __forceinline__ bool cond_apply(DevState* st, double m, double tol, int max_cycles, int init) {
+  if (init) {
+    st->cycles = 0;
+    st->res_initial = m;
+  } else {
+    st->cycles += 1;
+    st->total_cycles += 1;
+  }
+  st->res_max = m;
+  const bool finite = isfinite(m);
+  st->nonfinite = finite ? 0 : 1;
+  st->converged = (finite && m <= tol) ? 1 : 0;
+  return finite && m > tol && st->cycles < max_cycles;
+}
+
+struct CondFold {
+  cudaGraphConditionalHandle h;
+  DevState* st;
+  double tol;
+  int max_cycles;
+  int on;  // 0: the kernel only reduces
+};
+
 // The same residual, four consecutive cells per thread (nx a multiple of 4):
 // float4 loads of the three pressure rows, the left / right neighbours of the
 // group from the adjacent words, so each cell costs ~1/3 of the loads and
@@ -542,7 +569,7 @@ __global__ void __launch_bounds__(256)
 __device__ __forceinline__ void refine_init4_body(const float* __restrict__ dh, const float* __restrict__ dl,
                                                   const float* __restrict__ ph, const float* __restrict__ pl,
                                                   float* __restrict__ r32, int nx, int ny, const LapScale& ks,
-                                                  const RedCtx& ctx) {
+                                                  const RedCtx& ctx, const CondFold& cf) {
   float m = 0.f;
   const int nq = nx >> 2;  // quads per row
   // tiles of 32 quads x 8 rows walked by the capped 2-D grid
@@ -572,13 +599,16 @@ __device__ __forceinline__ void refine_init4_body(const float* __restrict__ dh, 
       *reinterpret_cast<float4*>(r32 + r + i0) = out;
       m = fmaxf(fmaxf(m, fmaxf(absnanf(out.x), absnanf(out.y))), fmaxf(absnanf(out.z), absnanf(out.w)));
     }
-  block_max_finish(m, ctx);
+  float f;
+  if (block_max_finish_at(m, ctx, &f) && cf.on)
+    cudaGraphSetConditional(cf.h, cond_apply(cf.st, (double)f, cf.tol, cf.max_cycles, 0) ? 1u : 0u);
 }
 
 __global__ void __launch_bounds__(256, 5)
     k_refine_init4(const float* __restrict__ dh, const float* __restrict__ dl, const float* __restrict__ ph,
-                   const float* __restrict__ pl, float* __restrict__ r32, int nx, int ny, LapScale ks, RedCtx ctx) {
-  refine_init4_body(dh, dl, ph, pl, r32, nx, ny, ks, ctx);
+                   const float* __restrict__ pl, float* __restrict__ r32, int nx, int ny, LapScale ks, RedCtx ctx,
+                   CondFold cf) {
+  refine_init4_body(dh, dl, ph, pl, r32, nx, ny, ks, ctx, cf);
 }
 
 // p' = p + e; r = d - lap(p') in df; r32 = (float) r; max|r| reduced
@@ -627,17 +657,24 @@ static dim3 refine4_grid(const Solver* s, int nq, int ny) {
   return dim3(gx, gy);
 }
 
-void launch_refine_init(Solver* s, const float* dh, const float* dl, const float* ph, const float* pl,
-                        float* r32, bool zero_p) {
+// cond: inside a captured tolerance loop, the residual kernel also does the
+// loop's step bookkeeping and sets its condition (four-cell form); returns
+// true if it did, else the caller launches k_cond itself
+bool launch_refine_init(Solver* s, const float* dh, const float* dl, const float* ph, const float* pl,
+                        float* r32, bool zero_p, const cudaGraphConditionalHandle* cond) {
   const Grid& g = s->g;
+  const bool quad = !zero_p && g.nx % 4 == 0;
+  const CondFold cf = (quad && cond) ? CondFold{*cond, s->dev, s->prm.pressure_tol, s->prm.max_cycles, 1}
+                                     : CondFold{};
   FS_LAUNCH(s, "refine_init", (double)s->n * (zero_p ? 12 : 20),
-            if (!zero_p && g.nx % 4 == 0) {
+            if (quad) {
               k_refine_init4<<<refine4_grid(s, g.nx / 4, g.ny), kBlock, 0, s->stream>>>(
-                  dh, dl, ph, pl, r32, g.nx, g.ny, lap_scale(g), red_ctx(s, s->red_out));
+                  dh, dl, ph, pl, r32, g.nx, g.ny, lap_scale(g), red_ctx(s, s->red_out), cf);
             } else {
               k_refine_init<<<red_grid2(g.nx, g.ny), kBlock, 0, s->stream>>>(
                   dh, dl, ph, pl, r32, g.nx, g.ny, lap_scale(g), zero_p ? 1 : 0, red_ctx(s, s->red_out));
             });
+  return cf.on != 0;
 }
 
 // the start of a MIXED solve from zero pressure (k_div_start4; nx a multiple
@@ -722,19 +759,7 @@ void launch_absmax_residual32(Solver* s, const float* p, const float* d) {
 // the condition of the WHILE node that repeats the refinement cycle.
 __global__ void k_cond(cudaGraphConditionalHandle h, int use_handle, const double* __restrict__ red,
                        DevState* __restrict__ st, double tol, int max_cycles, int init) {
-  double m = red[0];
-  if (init) {
-    st->cycles = 0;
-    st->res_initial = m;
-  } else {
-    st->cycles += 1;
-    st->total_cycles += 1;
-  }
-  st->res_max = m;
-  bool finite = isfinite(m);
-  st->nonfinite = finite ? 0 : 1;
-  st->converged = (finite && m <= tol) ? 1 : 0;
-  bool again = finite && m > tol && st->cycles < max_cycles;
+  const bool again = cond_apply(st, red[0], tol, max_cycles, init);
   if (use_handle) cudaGraphSetConditional(h, again ? 1u : 0u);
 }
 
@@ -787,7 +812,7 @@ __global__ void __launch_bounds__(256, 5) k_refine_class(const RefineTab tab, in
                                                       int max_cycles, int quad) {
   const auto& a = tab.m[blockIdx.z];
   if (!member_in_loop(a.st, max_cycles)) return;
-  if (quad) refine_init4_body(a.dh, a.dl, a.ph, a.pl, a.r32, nx, ny, ks, a.ctx);
+  if (quad) refine_init4_body(a.dh, a.dl, a.ph, a.pl, a.r32, nx, ny, ks, a.ctx, CondFold{});
   else refine_init_body(a.dh, a.dl, a.ph, a.pl, a.r32, nx, ny, ks, 0, a.ctx);
 }
 

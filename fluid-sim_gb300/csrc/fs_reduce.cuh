@@ -34,8 +34,10 @@ __device__ __forceinline__ bool commit_partial_is_last(RedCtx ctx) {
   return last;
 }
 
-// every thread passes its value; the block max lands in out[0]
-__device__ __forceinline__ void block_max_finish(float m, RedCtx ctx) {
+// every thread passes its value; the block max lands in out[0].  Returns
+// true on the one thread that wrote it (thread 0 of the last block to
+// finish), with the max in *res.
+__device__ __forceinline__ bool block_max_finish_at(float m, RedCtx ctx, float* res) {
   __shared__ float sm[32];
   int tid = threadIdx.y * blockDim.x + threadIdx.x, lane = tid & 31, warp = tid >> 5;
   int nthr = blockDim.x * blockDim.y, nwarp = (nthr + 31) >> 5;
@@ -47,7 +49,7 @@ __device__ __forceinline__ void block_max_finish(float m, RedCtx ctx) {
     for (int w = 1; w < nwarp; w++) t = fmaxf(t, sm[w]);
     ctx.fpartials[blockIdx.y * gridDim.x + blockIdx.x] = t;
   }
-  if (!commit_partial_is_last(ctx)) return;
+  if (!commit_partial_is_last(ctx)) return false;
   int nblk = gridDim.x * gridDim.y;
   float t = 0.f;
   // L2 reads (the partials of the other blocks), eight in flight per thread
@@ -69,7 +71,15 @@ __device__ __forceinline__ void block_max_finish(float m, RedCtx ctx) {
     for (int w = 1; w < nwarp; w++) f = fmaxf(f, sm[w]);
     ctx.out[0] = (double)f;
     *ctx.counter = 0;  // ready for the next reduction
+    *res = f;
+    return true;
   }
+  return false;
+}
+
+__device__ __forceinline__ void block_max_finish(float m, RedCtx ctx) {
+  float r;
+  (void)block_max_finish_at(m, ctx, &r);
 }
 
 // every thread passes (a, b); the block sums land in out[0], out[1] (f64)
