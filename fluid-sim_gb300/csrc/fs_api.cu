@@ -570,7 +570,10 @@ static int build_step_graph(Solver* s, double dt) {
   cudaGraph_t g = nullptr;
   cudaError_t e = cudaStreamEndCapture(s->stream, &g);
   if (rc != FS_OK) {
-    if (g) cudaGraphDestroy(g);
+    // a failed capture (a launch refused inside the tolerance loop's body)
+    // leaves its partial graph alone: destroying a graph whose conditional
+    // body was being captured when the capture failed is not relied on
+    cudaGetLastError();
     return rc;
   }
   if (e != cudaSuccess) return fail(s, FS_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(e));

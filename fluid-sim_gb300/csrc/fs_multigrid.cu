@@ -895,12 +895,16 @@ static std::string level_name(const Solver* s, const Level& L, const char* base)
 }
 
 // The dynamic shared-memory limit is an attribute of the function on each
-// device; set once per (kernel, device) when the tile needs more than 48 KB.
+// device: by default static + dynamic may not pass 48 KB.  Set once per
+// (kernel, device) when the kernel's static shared memory plus the dynamic
+// bytes it is launched with pass that.
 template <class K>
 static void tile_smem_attr(K kernel, size_t bytes, int device, std::atomic<uint64_t>& done) {
-  if (bytes <= 48 * 1024) return;
   const uint64_t bit = 1ull << (device & 63);
-  if (!(done.load() & bit) &&
+  if (done.load() & bit) return;
+  cudaFuncAttributes fa{};
+  if (cudaFuncGetAttributes(&fa, kernel) != cudaSuccess) return;
+  if (fa.sharedSizeBytes + bytes <= 48 * 1024 ||
       cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes) == cudaSuccess)
     done.fetch_or(bit);
 }
