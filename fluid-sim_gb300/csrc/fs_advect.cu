@@ -158,6 +158,26 @@ __device__ __forceinline__ void trace_t(const TileView<FAST>& u, const TileView<
   dY = -cy * v2;
 }
 
+// The same trace from the u-face (UFACE) or the v-face of cell (i, j) for the
+// forward pass: the face's own component at the home point sits on a grid
+// point (offsets 0, 0), where the bilinear sample equals the stored value for
+// every finite field, so it is passed in (own, read from the staged block)
+// instead of sampled.  Forward kernel 55.4 -> 53.0 us at 2048^2; in the
+// combine kernel the same change measured slower (59.9 -> 63.3 us), which
+// keeps trace_t.
+template <bool FAST, bool UFACE>
+__device__ __forceinline__ void trace_face(const TileView<FAST>& u, const TileView<FAST>& v, int i, int j,
+                                           float own, float cx, float cy, float& dX, float& dY) {
+  const Home h = UFACE ? home_u() : home_v();
+  const float u1 = UFACE ? own : u.sample(i, j, h.ux, h.uy);
+  const float v1 = UFACE ? v.sample(i, j, h.vx, h.vy) : own;
+  const float mx = -0.5f * cx * u1, my = -0.5f * cy * v1;
+  const float u2 = u.sample(i, j, h.ux + mx, h.uy + my);
+  const float v2 = v.sample(i, j, h.vx + mx, h.vy + my);
+  dX = -cx * u2;
+  dY = -cy * v2;
+}
+
 // Stage the kSH x kSW blocks of F fields whose (0, 0) is global (oi, oj),
 // wrapped, one row per warp at a time; returns max |value| of the first two
 // fields (the velocities), NaN counted as infinite.
@@ -243,8 +263,9 @@ __device__ __forceinline__ void advect_rows(const TileView<FAST>& U, const TileV
     const int j = tj + r;
     if (j >= ny) break;
     const int64_t c = (int64_t)j * nx + i;
+    const int lc = (r + kHalo) * kSW + threadIdx.x + kHalo;  // this cell in the staged block
     float dX, dY, lo, hi;
-    trace_t(U, V, i, j, hu, cx, cy, dX, dY);
+    trace_face<FAST, true>(U, V, i, j, U.sm[lc], cx, cy, dX, dY);
     if (bounds) {
       ou[c] = U.template sample<true>(i, j, hu.ux + dX, hu.uy + dY, &lo, &hi);
       bounds[c] = lo;
@@ -252,7 +273,7 @@ __device__ __forceinline__ void advect_rows(const TileView<FAST>& U, const TileV
     } else {
       ou[c] = U.sample(i, j, hu.ux + dX, hu.uy + dY);
     }
-    trace_t(U, V, i, j, hv, cx, cy, dX, dY);
+    trace_face<FAST, false>(U, V, i, j, V.sm[lc], cx, cy, dX, dY);
     if (bounds) {
       ov[c] = V.template sample<true>(i, j, hv.vx + dX, hv.vy + dY, &lo, &hi);
       bounds[2 * n + c] = lo;
