@@ -717,7 +717,7 @@ __device__ __forceinline__ float wrap_delta(float d, float L, float iL) { return
 // when the disks are set); cells elsewhere are left untouched.
 __global__ void __launch_bounds__(256)
     k_solids(float* __restrict__ u, float* __restrict__ v, const DiskDev* __restrict__ disks, int ndisk,
-             const int* __restrict__ tiles, int nx, int ny, float dx,
+             const int* __restrict__ tiles, const unsigned long long* __restrict__ masks, int nx, int ny, float dx,
              float dy, float lx, float ly, float width, double dA, float* __restrict__ imp,
              double* __restrict__ dimp) {
   // per-warp impulse sums of every disk, folded per CTA after the loop
@@ -731,7 +731,10 @@ __global__ void __launch_bounds__(256)
   float uu = 0.f, vv = 0.f;
   bool loaded = false;
   float tix = 0.f, tiy = 0.f, tit = 0.f;
-  for (int k = 0; k < ndisk; k++) {
+  // only the disks that can reach this tile, in order (the others change nothing here)
+  const unsigned long long mask = __ldg(masks + blockIdx.x);
+  for (unsigned long long rest = mask; rest; rest &= rest - 1) {
+    const int k = __ffsll((long long)rest) - 1;
     const DiskDev d = disks[k];
     float fx = 0.f, fy = 0.f, tq = 0.f;
     if (in) {
@@ -803,6 +806,7 @@ __global__ void __launch_bounds__(256)
   __syncthreads();
   for (int q = threadIdx.y * 32 + threadIdx.x; q < 3 * ndisk; q += 256) {
     const int k = q / 3, comp = q - 3 * k;
+    if (!((mask >> k) & 1ull)) continue;  // this tile's warps did not write it
     double sum = 0.0;
 #pragma unroll
     for (int w = 0; w < 8; w++) sum += (double)wsum[k][w][comp];
@@ -829,7 +833,7 @@ int upload_disks(Solver* s) {
   if (cudaMemcpy(s->d_disks, hd, sizeof(DiskDev) * nd, cudaMemcpyHostToDevice) != cudaSuccess) return -1;
   // the 32x8 tiles any disk can reach (periodic), as a compact list
   const int ntx = (g.nx + 31) / 32, nty = (g.ny + 7) / 8;
-  std::vector<char> mark((size_t)ntx * nty, 0);
+  std::vector<unsigned long long> mark((size_t)ntx * nty, 0);  // per tile: the disks that reach it
   for (int k = 0; k < nd; k++) {
     const fs_disk& d = s->disks[k];
     double reach = d.r + 7.0 * width + g.dxd + g.dyd;
@@ -840,17 +844,27 @@ int upload_disks(Solver* s) {
     for (int j = j0; j <= j1; j++)
       for (int i = i0; i <= i1; i++) {
         int wi = ((i % g.nx) + g.nx) % g.nx, wj = ((j % g.ny) + g.ny) % g.ny;
-        mark[(size_t)(wj / 8) * ntx + wi / 32] = 1;
+        mark[(size_t)(wj / 8) * ntx + wi / 32] |= 1ull << k;
       }
   }
   std::vector<int> list;
+  std::vector<unsigned long long> masks;
   for (size_t t = 0; t < mark.size(); t++)
-    if (mark[t]) list.push_back((int)t);
+    if (mark[t]) {
+      list.push_back((int)t);
+      masks.push_back(mark[t]);
+    }
   if (s->d_tiles) cudaFree(s->d_tiles);
+  if (s->d_tile_masks) cudaFree(s->d_tile_masks);
   s->d_tiles = nullptr;
+  s->d_tile_masks = nullptr;
   s->n_tiles = (int)list.size();
   if (cudaMalloc((void**)&s->d_tiles, sizeof(int) * list.size()) != cudaSuccess) return -1;
+  if (cudaMalloc((void**)&s->d_tile_masks, sizeof(unsigned long long) * masks.size()) != cudaSuccess) return -1;
   if (cudaMemcpy(s->d_tiles, list.data(), sizeof(int) * list.size(), cudaMemcpyHostToDevice) != cudaSuccess) return -1;
+  if (cudaMemcpy(s->d_tile_masks, masks.data(), sizeof(unsigned long long) * masks.size(),
+                 cudaMemcpyHostToDevice) != cudaSuccess)
+    return -1;
   return 0;
 }
 
@@ -865,9 +879,9 @@ void launch_solids(Solver* s, float* u, float* v, float dt, bool record_impulse)
   if (record_impulse) cudaMemsetAsync(s->imp, 0, sizeof(float) * 3 * (size_t)s->n, s->stream);
   FS_LAUNCH(s, "solids", (double)s->n_tiles * 256 * (record_impulse ? 28 : 16),
             k_solids<<<s->n_tiles, kBlock, 0, s->stream>>>(
-                u, v, (const DiskDev*)s->d_disks, nd, s->d_tiles, g.nx, g.ny, g.dx, g.dy, (float)(g.nx * g.dxd),
-                (float)(g.ny * g.dyd), (float)width, g.dxd * g.dyd, record_impulse ? s->imp : nullptr,
-                s->d_impulse));
+                u, v, (const DiskDev*)s->d_disks, nd, s->d_tiles, s->d_tile_masks, g.nx, g.ny, g.dx, g.dy,
+                (float)(g.nx * g.dxd), (float)(g.ny * g.dyd), (float)width, g.dxd * g.dyd,
+                record_impulse ? s->imp : nullptr, s->d_impulse));
 }
 
 // ------------------------------------------------------------------- dye

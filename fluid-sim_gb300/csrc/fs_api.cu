@@ -101,7 +101,7 @@ static void free_all(Solver* s) {
   for (size_t l = 1; l < s->lev.size(); l++) { f(s->lev[l].x); f(s->lev[l].x2); f(s->lev[l].rhs); }
   f(s->stage);
   f(s->red_partials); f(s->red_out); f(s->modes); f(s->imp); f(s->d_impulse);
-  f(s->dev); f(s->d_disks); f(s->d_tiles); f(s->dye); f(s->dye2);
+  f(s->dev); f(s->d_disks); f(s->d_tiles); f(s->d_tile_masks); f(s->dye); f(s->dye2);
   if (s->graph_exec) cudaGraphExecDestroy(s->graph_exec);
   if (s->h_red) cudaFreeHost(s->h_red);
   diag_free(s);

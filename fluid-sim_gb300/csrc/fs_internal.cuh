@@ -130,6 +130,7 @@ struct Solver {
   int imp_cap = 0;
   void* d_disks = nullptr;      // device copy of the disk parameters (set by fs_set_solids)
   int* d_tiles = nullptr;       // 32x8 tiles any disk can reach
+  unsigned long long* d_tile_masks = nullptr;  // per listed tile: the disks that can reach it
   int n_tiles = 0;
 
   // device-side step state: simulation time (read by the forcing kernel) and
