@@ -1,0 +1,170 @@
+"""CPU checks of the multigrid tile kernels' index arithmetic (fs_multigrid.cu).
+
+The fused down / up kernels stage a tile's region into shared memory by TMA
+boxes whose first column must sit on a 16-byte boundary, then sweep, restrict
+and prolong by fixed offsets.  A wrong constant would read or write outside a
+shared array or outside the grid.  These tests restate the layout constants
+(TileBox, CoarseBox) and the kernels' loops over cells, for every template
+instance the library builds (tiles of 16, 32 and 64 cells, pre / post sweeps
+1..3), and check that every access stays inside its array, that each
+red-black half-sweep updates exactly the cells of its colour, and that the
+2x2-block prolongation gives every region cell the coarse values and weights
+of the per-cell formula (multigrid.js:99-131).
+"""
+from __future__ import annotations
+
+import pytest
+
+NTH = 256  # threads of a tile kernel
+TILES = (16, 32, 64)
+
+
+def tilebox(T, H):
+    R = T + 2 * H
+    LP = (H + 3) & ~3
+    OX = LP - H
+    W = (LP + T + H + 3) & ~3
+    N = W * R
+    NA = (N + 31) & ~31
+    return R, LP, OX, W, N, NA
+
+
+def coarsebox(T, H):
+    RC = (T + 2 * H) // 2 + 2
+    LPC = (H // 2 + 1 + 3) & ~3
+    OC = LPC - (H // 2 + 1)
+    WC = (OC + RC + 3) & ~3
+    NC = (WC * RC + 31) & ~31
+    return RC, LPC, OC, WC, NC
+
+
+def sweep(R, W, OX, par0, c):
+    """rb_half_tile: the (li, lj) each thread updates and every offset it reads"""
+    NI = R - 2
+    NCH = NTH // NI
+    assert NCH >= 1 and W % 2 == 0
+    CH = ((NI + NCH - 1) // NCH + 1) & ~1
+    offs, upd = [], []
+    for tid in range(NTH):
+        chunk, m = divmod(tid, NI)
+        if chunk >= NCH:
+            continue
+        li = 1 + m
+        lj = 1 + chunk * CH
+        lend = min(lj + CH, R - 1)
+        lj += (par0 + li + lj + c) & 1
+        if lj >= lend:
+            continue
+        p = lj * W + OX + li
+        offs.append(p - W)
+        while lj < lend:
+            offs += [p + W, p, p - 1, p + 1]
+            upd.append((li, lj))
+            lj += 2
+            p += 2 * W
+    return offs, upd
+
+
+@pytest.mark.parametrize("T", TILES)
+@pytest.mark.parametrize("pre", (1, 2, 3))
+def test_down_kernel_layout(T, pre):
+    H = 2 * pre + 1
+    R, LP, OX, W, N, NA = tilebox(T, H)
+    assert LP % 4 == 0 and W % 4 == 0 and OX + R <= W and W <= 256 and R <= 256 and NA % 32 == 0
+    for par0 in (0, 1):
+        for c in (0, 1):
+            offs, upd = sweep(R, W, OX, par0, c)
+            assert 0 <= min(offs) and max(offs) < N
+            want = {(li, lj) for li in range(1, R - 1) for lj in range(1, R - 1) if (par0 + li + lj) & 1 == c}
+            assert len(upd) == len(set(upd)) and set(upd) == want
+    # tile write-back (float4) and the residual's 2x2 blocks (float2 rows)
+    for y in range(T):
+        o = (H + y) * W + LP
+        assert o % 4 == 0 and o + T - 1 < N
+    for cj in range(T // 2):
+        for ci in range(T // 2):
+            off = (H + 2 * cj) * W + LP + 2 * ci
+            assert off % 2 == 0
+            for d in (0, 1, W, W + 1, -W, -W + 1, 2 * W, 2 * W + 1, -1, 2, W - 1, W + 2):
+                assert 0 <= off + d < N
+
+
+@pytest.mark.parametrize("T", TILES)
+@pytest.mark.parametrize("post", (1, 2, 3))
+def test_up_kernel_layout(T, post):
+    H = 2 * post
+    R, LP, OX, W, N, NA = tilebox(T, H)
+    RC, LPC, OC, WC, NC = coarsebox(T, H)
+    assert LPC % 4 == 0 and WC % 4 == 0 and OC + RC <= WC and WC * RC <= NC
+    for par0 in (0, 1):
+        for c in (0, 1):
+            offs, upd = sweep(R, W, OX, par0, c)
+            assert 0 <= min(offs) and max(offs) < N
+            assert len(upd) == len(set(upd)) == sum(
+                1 for li in range(1, R - 1) for lj in range(1, R - 1) if (par0 + li + lj) & 1 == c)
+    # prolongation by 2x2 fine blocks: each region cell once, with the coarse
+    # column / row and the weights of the per-cell formula
+    NB = R // 2 + 1
+    seen = set()
+    for b in range(NB):
+        for a in range(NB):
+            base = b * WC + OC + a
+            assert 0 <= base and base + WC + 1 < WC * RC
+            col = OX + 2 * a - 1
+            cells = []
+            if b > 0:
+                o = (2 * b - 1) * W + col
+                if a > 0:
+                    cells.append((o, 0.25, 0.25))
+                if a < NB - 1:
+                    cells.append((o + 1, 0.75, 0.25))
+            if b < NB - 1:
+                o = 2 * b * W + col
+                if a > 0:
+                    cells.append((o, 0.25, 0.75))
+                if a < NB - 1:
+                    cells.append((o + 1, 0.75, 0.75))
+            for o, fx, fy in cells:
+                lj, rem = divmod(o, W)
+                li = rem - OX
+                assert 0 <= li < R and 0 <= lj < R and o not in seen
+                assert (lj + 1) >> 1 == b and (li + 1) >> 1 == a
+                assert fx == (0.25 if li & 1 else 0.75) and fy == (0.25 if lj & 1 else 0.75)
+                seen.add(o)
+    assert len(seen) == R * R
+    for y in range(T):
+        o = (H + y) * W + LP
+        assert o % 4 == 0 and o + T - 1 < N
+
+
+def tile_fits(t, n):
+    """the side rule of mg_tile / tile_for_class: T <= n / 2 (16 always)"""
+    return t == 16 or 2 * t <= n
+
+
+@pytest.mark.parametrize("n", (2048, 1024, 528, 384, 200, 192, 132, 128, 72, 70, 68, 66))
+def test_tma_boxes_and_wrapped_staging(n):
+    """For every tile of every side a level may use: a TMA box that passes the
+    kernels' 'boxed' test starts 16-byte aligned and covers a tile inside the
+    grid, and the wrapped staging of the other tiles needs at most one wrap."""
+    for T in TILES:
+        if not tile_fits(T, n):
+            continue
+        k = (n + T - 1) // T
+        for H in (3, 5, 7, 2, 4, 6):
+            R, LP, OX, W, N, NA = tilebox(T, H)
+            nc = n // 2
+            for by in range(k):
+                for bx in range(k):
+                    i0, j0 = bx * T, by * T
+                    gi0, gj0 = i0 - H, j0 - H
+                    assert -n <= gi0 and gi0 + R - 1 < 2 * n and -n <= gj0 and gj0 + R - 1 < 2 * n
+                    boxed = n % 4 == 0 and i0 - LP >= 0 and i0 - LP + W <= n and gj0 >= 0 and gj0 + R <= n
+                    if boxed:
+                        assert (i0 - LP) % 4 == 0 and i0 + T <= n and j0 + T <= n and gi0 - (i0 - LP) == OX
+                    if H % 2 == 0:  # up kernel: the coarse block
+                        RC, LPC, OC, WC, NC = coarsebox(T, H)
+                        cgi0, cgj0 = (gi0 >> 1) - 1, (gj0 >> 1) - 1
+                        assert -nc <= cgi0 and cgi0 + RC - 1 < 2 * nc and -nc <= cgj0 and cgj0 + RC - 1 < 2 * nc
+                        if boxed and cgi0 - OC >= 0 and cgi0 - OC + WC <= nc:
+                            assert (cgi0 - OC) % 4 == 0
