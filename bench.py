@@ -13,7 +13,8 @@ Prints ONE JSON line (rank 0).  ``value`` is device-timed throughput with the
 fields resident in HBM; ``e2e`` adds a host->device upload of the velocity
 and a device->host read-back to every step, through the public C ABI.
 ``--impl reference`` times the reference's CPU solver (the f64 restatement in
-oracle/, all host threads) on the same workload.
+oracle/, one thread, as the reference's JavaScript solver runs) on the same
+workload.
 """
 from __future__ import annotations
 
@@ -237,7 +238,11 @@ def measure_batch(pkg, device, count, steps, warmup, seed=1, relax=RELAX):
         dts.append(dt)
     for _ in range(warmup):
         b.step(dts)
+    r0 = [m.convergence_record() for m in b.members]
     ms = b.time_steps(dts, steps)
+    r1 = [m.convergence_record() for m in b.members]
+    failed = sum(b1["failed_steps"] - a1["failed_steps"] for a1, b1 in zip(r0, r1))
+    recorded = sum(b1["steps"] - a1["steps"] for a1, b1 in zip(r0, r1))
     converged = all(m.last_stats()["converged"] for m in b.members)
     launches = b.launch_count()
     # sweep counts per domain size, then tile sides per size class and level,
@@ -261,7 +266,9 @@ def measure_batch(pkg, device, count, steps, warmup, seed=1, relax=RELAX):
             "autotuned_sweeps": {f"{k[0]}": list(v) for k, v in sorted(picks.items())},
             "autotuned_tiles": {f"{k[0]}": list(v) for k, v in sorted(tiles.items())},
             "autotuned_ms_per_step": ms_tuned / steps, "autotuned_value": cells * steps / (ms_tuned / 1e3),
-            "converged": converged, "gpu_launches_total": launches}
+            "converged": converged, "failed_member_steps": failed, "member_projections_recorded": recorded,
+            "all_steps_converged": failed == 0 and recorded == count * steps,
+            "gpu_launches_total": launches}
 
 
 def measure_variant(pkg, n, device, guess, u0, v0, disks, dt, steps, warmup, relax=RELAX):
@@ -272,12 +279,15 @@ def measure_variant(pkg, n, device, guess, u0, v0, disks, dt, steps, warmup, rel
     for _ in range(warmup):
         s.step(dt)
     c0 = s.total_cycles()
+    r0 = s.convergence_record()
     ms = s.time_steps(dt, steps)
     cyc = (s.total_cycles() - c0) / steps
+    r1 = s.convergence_record()
     md = s.max_divergence()
     s.destroy()
     return {"ms_per_step": ms / steps, "cycles_per_step": cyc,
-            "value": float(n) * n * steps / (ms / 1e3), "max_div_after": md}
+            "value": float(n) * n * steps / (ms / 1e3), "max_div_after": md,
+            "failed_steps": r1["failed_steps"] - r0["failed_steps"], "worst_max_div": r1["worst_max_div"]}
 
 
 # ------------------------------------------------------------------- GPU arm
@@ -300,12 +310,16 @@ def run_gpu(args):
     # timed region: K steps, device events on the solver's stream
     launches0 = s.launch_count()
     cycles0 = s.total_cycles()
+    rec0 = s.convergence_record()
     barrier(dist)
     with ClockSampler(local) as clk:
         ms = s.time_steps(dt, args.steps)
     barrier(dist)
     launches = s.launch_count() - launches0
     cycles_timed = (s.total_cycles() - cycles0) / max(args.steps, 1)
+    rec1 = s.convergence_record()
+    timed_rec = {"steps": rec1["steps"] - rec0["steps"], "failed_steps": rec1["failed_steps"] - rec0["failed_steps"],
+                 "worst_max_div": rec1["worst_max_div"]}
     st = s.last_stats()
     md = s.max_divergence()
     value, ms_max = aggregate(dist, float(n) * n * args.steps, ms)
@@ -367,12 +381,15 @@ def run_gpu(args):
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         cpu = cpu_baseline(n, threads=1, timed_steps=1)
+    ferr = None
+    if rank == 0 and not args.no_field_error:
+        ferr = field_error(pkg, n, local, args.relax)
 
     if rank == 0:
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f64 state / f32 advection + V-cycles",
+            "scaling": "weak", "vs_baseline": None, "dtype": "double-float state / f32 advection + V-cycles",
             "data": "synthetic (seeded stream + divergence-free perturbation + fixed disks)",
             "config": {
                 "workload": f"periodic {n}x{n} MAC grid, stream u=1 past {len(disks)} fixed disks, nu={NU}, "
@@ -384,6 +401,9 @@ def run_gpu(args):
                 "l2": "working set ~0.35 GB > 129 MB L2; no flush between steps",
                 "cycles_per_step": cycles_timed,
                 "max_div_after": md, "converged": bool(st["converged"]),
+                "all_steps_converged": timed_rec["failed_steps"] == 0 and timed_rec["steps"] == args.steps,
+                "failed_steps": timed_rec["failed_steps"], "projections_recorded": timed_rec["steps"],
+                "worst_max_div": timed_rec["worst_max_div"],
             },
             "roofline": {
                 "bound": "hbm", "kernel": top["name"], "achieved": achieved, "peak": peak, "unit": "GB/s",
@@ -411,6 +431,8 @@ def run_gpu(args):
             line["batch"] = batch
         if cpu is not None:
             line["cpu_baseline"] = cpu
+        if ferr is not None:
+            line["config"]["field_error"] = ferr
         print(json.dumps(line), flush=True)
     s.destroy()
     if dist is not None:
@@ -437,12 +459,10 @@ def host_cpu() -> str:
     return f"{platform.machine()}, {os.cpu_count()} logical CPUs" + (f", {model}" if model else "")
 
 
-def cpu_baseline(n: int, threads: int, timed_steps: int):
-    """The oracle (f64 restatement of the reference CPU solver) on the same
-    workload: MacCormack, explicit diffusion, exact FFT projection, one
-    coupling pass per disk.  One untimed step, then `timed_steps` timed."""
-    O = _oracle()
-    O.set_threads(threads)
+def oracle_solver(O, n: int):
+    """The oracle's f64 CPU solver (restatement of src/cpu/solver.js) on the
+    bench workload: MacCormack, explicit diffusion, exact FFT projection, one
+    direct-forcing pass per disk."""
     u0, v0, disks, dt = make_workload(n)
     cpu = O.CpuSolver(n=n, nu=NU, advection="maccormack", explicit_diffusion=True, projection="fft",
                       coupling_passes=1)
@@ -450,6 +470,56 @@ def cpu_baseline(n: int, threads: int, timed_steps: int):
     cpu.v[:] = v0
     for d in disks:
         cpu.add_solid(O.disk(d[0], d[1], d[2], density=8, fixed=True))
+    return cpu, dt
+
+
+FIELD_STEPS = 20
+FIELD_TOL = 1e-5
+
+
+def field_error(pkg, n, device, relax, steps=FIELD_STEPS):
+    """Field error of the measured configuration against the f64 oracle: a
+    fresh solver with the bench's settings and the oracle's CPU solver advance
+    the same initial state `steps` steps; relative L2 and relative L-inf
+    (max |a - b| / max |b|) of u and v, with the tolerance they are held to."""
+    u0, v0, disks, dt = make_workload(n)
+    s = make_solver(pkg, n, device, "zero", relax)
+    s.upload_velocity(u0, v0)
+    s.set_solids(disks)
+    for _ in range(steps):
+        s.step(dt)
+    rec = s.convergence_record()
+    gu, gv = s.read_velocity()
+    s.destroy()
+    O = _oracle()
+    threads = os.cpu_count() or 1
+    O.set_threads(threads)
+    cpu, _ = oracle_solver(O, n)
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        cpu.step(dt, advect_dye=False)
+    sec = time.perf_counter() - t0
+    out = {"steps": steps, "tol_rel_l2": FIELD_TOL, "oracle": "f64 C restatement of src/cpu/solver.js "
+           "(MacCormack, explicit diffusion, exact FFT projection), same seeded initial state and disks",
+           "oracle_threads": threads, "oracle_s": round(sec, 2), "gpu_failed_steps": rec["failed_steps"]}
+    ok = rec["failed_steps"] == 0
+    for name, a, b in (("u", gu, np.asarray(cpu.u)), ("v", gv, np.asarray(cpu.v))):
+        d = a - b
+        rl2 = float(np.linalg.norm(d) / np.linalg.norm(b))
+        linf = float(np.abs(d).max() / np.abs(b).max())
+        out[name] = {"rel_l2": rl2, "rel_linf": linf}
+        ok = ok and rl2 <= FIELD_TOL
+    out["within_tol"] = bool(ok)
+    return out
+
+
+def cpu_baseline(n: int, threads: int, timed_steps: int):
+    """The oracle (f64 restatement of the reference CPU solver) on the same
+    workload: MacCormack, explicit diffusion, exact FFT projection, one
+    coupling pass per disk.  One untimed step, then `timed_steps` timed."""
+    O = _oracle()
+    O.set_threads(threads)
+    cpu, dt = oracle_solver(O, n)
     cpu.step(dt, advect_dye=False)
     t0 = time.perf_counter()
     for _ in range(timed_steps):
@@ -462,42 +532,65 @@ def cpu_baseline(n: int, threads: int, timed_steps: int):
                       f"max|div|={cpu.max_divergence():.1e}"}
 
 
+# seconds of single-thread CPU work the reference arm may spend on its steps
+REF_BUDGET_S = 150.0
+
+
 def run_reference(args):
+    """The reference's CPU solver on the bench workload, single-threaded (the
+    reference's JavaScript solver runs on one thread; Node is absent on this
+    host, so the oracle's f64 C restatement of src/cpu stands in for it).
+    Times all K steps after W warm-up steps when they fit in REF_BUDGET_S at
+    the first step's pace, else as many as fit; `steps` / `warmup` report the
+    counts actually run.  A 3-step figure with every host thread is added
+    beside it."""
     rank, world, local = dist_env()
     if rank != 0:
         return
-    threads = os.cpu_count() or 1
     O = _oracle()
-    O.set_threads(threads)
+    O.set_threads(1)
     n = args.n
-    u0, v0, disks, dt = make_workload(n)
-    cpu = O.CpuSolver(n=n, nu=NU, advection="maccormack", explicit_diffusion=True, projection="fft",
-                      coupling_passes=1)
-    cpu.u[:] = u0
-    cpu.v[:] = v0
-    for d in disks:
-        cpu.add_solid(O.disk(d[0], d[1], d[2], density=8, fixed=True))
-    # bounded sample: at most 1 warm-up and 3 timed steps whatever K and W are
-    warm = min(args.warmup, 1)
-    timed = max(1, min(args.steps, 3))
-    for _ in range(warm):
+    cpu, dt = oracle_solver(O, n)
+    disks = make_workload(n)[2]
+    # the first warm-up step sets the pace that bounds the sample
+    t0 = time.perf_counter()
+    cpu.step(dt, advect_dye=False)
+    first = time.perf_counter() - t0
+    fit = max(2, int(REF_BUDGET_S / max(first, 1e-3)))
+    warm = min(args.warmup, max(1, fit // 8))
+    timed = max(1, min(args.steps, fit - warm))
+    for _ in range(warm - 1):
         cpu.step(dt, advect_dye=False)
     t0 = time.perf_counter()
     for _ in range(timed):
         cpu.step(dt, advect_dye=False)
     sec = time.perf_counter() - t0
     value = float(n) * n * timed / sec
+    md = cpu.max_divergence()
+    # every host thread (OpenMP), a short sample, reported beside the line
+    threads = os.cpu_count() or 1
+    O.set_threads(threads)
+    cpu2, _ = oracle_solver(O, n)
+    cpu2.step(dt, advect_dye=False)
+    t0 = time.perf_counter()
+    for _ in range(3):
+        cpu2.step(dt, advect_dye=False)
+    sec_mt = time.perf_counter() - t0
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 0,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": sec * 1e3 / timed,
+        "steps": timed, "warmup": warm, "requested_steps": args.steps, "requested_warmup": args.warmup,
+        "ms_per_step": sec * 1e3 / timed,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic (same seeded workload)",
         "config": {"workload": f"periodic {n}x{n}, {len(disks)} fixed disks, nu={NU}, MacCormack, explicit "
-                               "diffusion, exact FFT projection (max|div| ~1e-13)", "n": n},
-        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "host": host_cpu(),
+                               "diffusion, exact FFT projection", "n": n, "max_div_after": md},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": 1, "kind": "port", "host": host_cpu(),
                          "sample": f"{timed} timed step(s) after {warm} warm-up step(s) of the {n}^2 "
-                                   f"workload (of K={args.steps}); f64 C restatement of src/cpu with "
-                                   f"{threads} OpenMP threads (the reference is JavaScript; no Node here)"},
+                                   f"workload (K={args.steps}, W={args.warmup} requested; capped at "
+                                   f"{REF_BUDGET_S:.0f} s of steps); f64 C restatement of src/cpu on one "
+                                   "thread (the reference is single-threaded JavaScript; no Node here)"},
+        "all_threads": {"value": float(n) * n * 3 / sec_mt, "unit": UNIT, "cores": threads, "steps": 3,
+                        "ms_per_step": sec_mt * 1e3 / 3},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -518,6 +611,8 @@ def main():
     ap.add_argument("--no-variants", action="store_true",
                     help="skip timing the learned guess and the warm start beside the headline")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-field-error", action="store_true",
+                    help="skip the comparison of u, v after a few steps with the f64 oracle")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl != "reference":
         args.warmup = 3

@@ -85,11 +85,16 @@ class Params(C.Structure):
                 ("mg_post_smooth", C.c_int32), ("mg_coarse_sweeps", C.c_int32), ("mg_min_size", C.c_int32),
                 ("warm_start", C.c_int32), ("device", C.c_int32), ("kernel_variant", C.c_int32),
                 ("dye_fade", C.c_double),
-                ("relax", C.c_double)]
+                ("relax", C.c_double), ("pressure_tol_relative", C.c_int32)]
 
 
 class Mode(C.Structure):
     _fields_ = [("kx", C.c_double), ("ky", C.c_double), ("phase", C.c_double)]
+
+
+class Band(C.Structure):
+    _fields_ = [("kind", C.c_int32), ("kf", C.c_double), ("width", C.c_double), ("amplitude", C.c_double),
+                ("seed", C.c_uint64), ("drag", C.c_double)]
 
 
 class Disk(C.Structure):
@@ -125,6 +130,7 @@ SIGNATURES = {
     "fs_upload_field": (I, [VP, I, VP, I]),
     "fs_set_forcing": (I, [VP, C.POINTER(Mode), I, D, D, D]),
     "fs_set_solids": (I, [VP, C.POINTER(Disk), I]),
+    "fs_set_band_forcing": (I, [VP, C.POINTER(Band)]),
     "fs_solid_impulse": (I, [VP, C.POINTER(C.c_double), I]),
     "fs_step": (I, [VP, D]),
     "fs_advance": (I, [VP, D, I]),
@@ -161,6 +167,7 @@ SIGNATURES = {
     "fs_render": (I, [VP, C.c_int32, D, VP]),
     "fs_set_mg_sweeps": (I, [VP, C.c_int32, C.c_int32]),
     "fs_total_cycles": (I, [VP, C.POINTER(C.c_int64)]),
+    "fs_convergence_record": (I, [VP, C.POINTER(C.c_int64), C.POINTER(C.c_int64), C.POINTER(D)]),
     "fs_autotune": (I, [VP, D, C.c_int32, C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.POINTER(D)]),
     "fs_set_mg_tiles": (I, [VP, C.POINTER(C.c_int32), C.c_int32]),
     "fs_get_mg_tiles": (I, [VP, C.POINTER(C.c_int32), C.c_int32, C.POINTER(C.c_int32)]),

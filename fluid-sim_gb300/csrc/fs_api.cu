@@ -105,6 +105,7 @@ static void free_all(Solver* s) {
   if (s->graph_exec) cudaGraphExecDestroy(s->graph_exec);
   if (s->h_red) cudaFreeHost(s->h_red);
   diag_free(s);
+  band_free(s);
   if (s->body_stream) cudaStreamDestroy(s->body_stream);
   if (s->own_stream) {
     cudaStreamDestroy(s->own_stream);  // batch member: s->stream is the batch's
@@ -472,8 +473,9 @@ static int pressure_solve(Solver* s, bool capture, bool defer = false, bool star
   int rc = read_red(s, &m);
   if (rc) return rc;
   s->stats.residual_initial = m;
+  const double lim = P.pressure_tol_relative ? P.pressure_tol * m : P.pressure_tol;
   int c = 0;
-  while (!(m <= P.pressure_tol) && c < P.max_cycles && std::isfinite(m)) {
+  while (!(m <= lim) && c < P.max_cycles && std::isfinite(m)) {
     if (mg) mg_cycle(s, true);
     else flat_cycle(s, iters, true);
     if ((rc = read_red(s, &m))) return rc;
@@ -481,7 +483,7 @@ static int pressure_solve(Solver* s, bool capture, bool defer = false, bool star
   }
   s->stats.cycles = c;
   s->stats.residual_max = m;
-  s->stats.converged = m <= P.pressure_tol;
+  s->stats.converged = m <= lim;
   if (!std::isfinite(m)) return fail(s, FS_ERR_NONFINITE, "non-finite Poisson residual");
   if (!s->stats.converged) return fail(s, FS_ERR_NOT_CONVERGED, "pressure tolerance not met within max_cycles");
   return check_launch(s);
@@ -531,6 +533,7 @@ static int enqueue_step(Solver* s, double dt, bool capture, StepSplit* split = n
     launch_diffuse(s, cu, cv, s->tu, s->tv, fdt);
     cu = s->tu; cv = s->tv;
   }
+  if (s->band) launch_band(s, cu, cv, fdt);
   if (s->n_modes > 0) launch_forcing(s, cu, cv, fdt);
   if (!s->disks.empty()) launch_solids(s, cu, cv, fdt, false);
   int rc = project_from(s, cu, cv, capture, split != nullptr);
@@ -606,6 +609,13 @@ static int step(Solver* s, double dt) {
   int rc = enqueue_step(s, dt, false);
   s->t += dt;
   s->steps++;
+  if (s->prm.pressure_tol > 0 && !s->stats_on_device) {
+    // the eager tolerance loop ran on the host: keep the record here
+    s->host_rec_steps++;
+    if (!s->stats.converged) s->host_rec_failed++;
+    const double m = std::isfinite(s->stats.residual_max) ? s->stats.residual_max : INFINITY;
+    if (!(m <= s->host_rec_worst)) s->host_rec_worst = m;
+  }
   return rc;
 }
 
@@ -641,9 +651,10 @@ static int run_stage(Solver* s, int stage, double dt) {
       w_to_state(s, s->tu, s->tv);
       break;
     case FS_STAGE_FORCING:
-      if (s->n_modes == 0) break;
+      if (s->n_modes == 0 && !s->band) break;
       state_to_w(s);
-      launch_forcing(s, s->wu, s->wv, fdt);
+      if (s->band) launch_band(s, s->wu, s->wv, fdt);
+      if (s->n_modes > 0) launch_forcing(s, s->wu, s->wv, fdt);
       w_to_state(s, s->wu, s->wv);
       break;
     case FS_STAGE_SOLID:
@@ -903,6 +914,25 @@ FS_API int fs_set_forcing(fs_solver* h, const fs_mode* modes, int count, double 
   CU(s, cudaMemcpy(s->modes, hm.data(), hm.size() * sizeof(float), cudaMemcpyHostToDevice));
   s->n_modes = count;
   s->amp = amplitude; s->drag = drag; s->drift = phase_drift;
+  return FS_OK;
+}
+
+FS_API int fs_set_band_forcing(fs_solver* h, const fs_band* band) {
+  SOLVER(h);
+  if (band) {
+    if (band->kind != FS_BAND_REFERENCE && band->kind != FS_BAND_GAUSSIAN)
+      return fail(s, FS_ERR_INVALID_ARGUMENT, "unknown band forcing kind");
+    if (!(band->kf > 0) || !(band->width >= 0) || !(band->kf + band->width <= 256) ||
+        !std::isfinite(band->amplitude) || !(band->drag >= 0) || !std::isfinite(band->drag))
+      return fail(s, FS_ERR_INVALID_ARGUMENT, "band forcing needs kf > 0, width >= 0, kf + width <= 256, "
+                                              "a finite amplitude and drag >= 0");
+  }
+  CU(s, cudaStreamSynchronize(s->stream));
+  drop_graph(s);  // the captured step has or lacks the band kernels
+  int rc = band_set(s, band);
+  if (rc) return rc;
+  // the draws start again from step 0
+  CU(s, cudaMemsetAsync(&s->dev->band_step, 0, sizeof(unsigned long long), s->stream));
   return FS_OK;
 }
 
@@ -1366,6 +1396,17 @@ FS_API int fs_total_cycles(fs_solver* h, int64_t* cycles) {
   return FS_OK;
 }
 
+FS_API int fs_convergence_record(fs_solver* h, int64_t* steps, int64_t* failed, double* worst) {
+  SOLVER(h);
+  CU(s, cudaStreamSynchronize(s->stream));
+  DevState d;
+  CU(s, cudaMemcpy(&d, s->dev, sizeof d, cudaMemcpyDeviceToHost));
+  if (steps) *steps = d.rec_steps + s->host_rec_steps;
+  if (failed) *failed = d.rec_failed + s->host_rec_failed;
+  if (worst) *worst = std::max(d.rec_worst, s->host_rec_worst);
+  return FS_OK;
+}
+
 FS_API int64_t fs_launch_count(const fs_solver* h) {
   if (!h) return 0;
   const Solver* s = &h->s;
@@ -1473,7 +1514,7 @@ static bool class_plain(const fs_batch* b, const BatchClass& c) {
   const Solver* r = &b->members[c.idx[0]]->s;
   for (int i : c.idx) {
     const Solver* s = &b->members[i]->s;
-    if (s->n_modes > 0 || !s->disks.empty() || s->dye || s->guess || s->prm.warm_start ||
+    if (s->n_modes > 0 || s->band || !s->disks.empty() || s->dye || s->guess || s->prm.warm_start ||
         s->prm.advection != r->prm.advection || (s->prm.nu > 0) != (r->prm.nu > 0))
       return false;
   }

@@ -48,6 +48,13 @@ struct DevState {
   int converged;
   int nonfinite;
   int async_err;  // a bounded wait for an asynchronous (TMA) copy gave up
+  // record over every step whose tolerance loop ran on the device (the step
+  // finish adds to it; the per-projection fields above are overwritten by the
+  // next projection, this is not)
+  long long rec_steps;   // projections recorded
+  long long rec_failed;  // of those, projections that ended without meeting pressure_tol
+  double rec_worst;      // largest max|div u| any of them ended with (+inf for NaN)
+  unsigned long long band_step;  // steps the band forcing has run (its random draws' counter)
 };
 
 struct KernelStat {
@@ -113,6 +120,8 @@ struct Solver {
   double* red_out = nullptr;       // device: [0] max, [1] sum a, [2] sum b
   double* h_red = nullptr;         // pinned host copy
 
+  // band-limited random forcing renewed every step (fs_band.cu), or null
+  void* band = nullptr;
   // forcing (solver.js:370-385)
   float* modes = nullptr;  // kx, ky, phase triplets
   int n_modes = 0;
@@ -157,6 +166,9 @@ struct Solver {
   double t = 0;
   int64_t steps = 0;
   fs_step_stats stats{0, 1, -1.0, -1.0};
+  // the same record for projections whose tolerance loop ran on the host
+  int64_t host_rec_steps = 0, host_rec_failed = 0;
+  double host_rec_worst = 0;
   std::string err;
   int64_t launches = 0;
 
@@ -169,6 +181,13 @@ struct Solver {
   std::vector<Pending> pending;
   std::vector<KernelStat> kstats;
 };
+
+// the tolerance as the device-side loop code takes it: the absolute
+// pressure_tol, or with pressure_tol_relative its negative, meaning "times
+// the max residual the projection started from"
+inline double dev_tol(const Solver* s) {
+  return s->prm.pressure_tol_relative ? -s->prm.pressure_tol : s->prm.pressure_tol;
+}
 
 // ----------------------------------------------------------------- launching
 void prof_begin(Solver* s, const char* name, double bytes, int* slot, cudaEvent_t* a);
@@ -203,6 +222,10 @@ void launch_forcing(Solver* s, float* u, float* v, float dt);
 int upload_disks(Solver* s);
 void launch_solids(Solver* s, float* u, float* v, float dt, bool record_impulse);
 void launch_advect_dye(Solver* s, float dt);
+// fs_band.cu
+int band_set(Solver* s, const fs_band* band);  // null: remove
+void band_free(Solver* s);
+void launch_band(Solver* s, float* u, float* v, float dt);
 
 // fs_pressure.cu
 template <class TV, class TD>

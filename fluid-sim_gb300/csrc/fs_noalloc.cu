@@ -3,16 +3,17 @@
 //
 // Who needs this: hosts that own every byte of device memory through their
 // own pool (a game engine or a visualisation server that reserves the GPU at
-// start-up and forbids later cudaMalloc), frame loops where cudaMalloc /
+// start-up and forbids later cudaMalloc), and frame loops where cudaMalloc /
 // cudaFree are off limits because they can synchronise the whole device and
-// stall the frame, and code that records work into a CUDA graph, where a
-// cudaMalloc issued in the middle is not part of what gets recorded.  Such a
-// caller passes device pointers it already owns and gets the reduction done
-// with scratch that was reserved when the library was loaded.
+// stall the frame.  Such a caller passes device pointers it already owns and
+// gets the reduction done with scratch the library reserves for itself.
 //
 // The scratch is the file-scope array g_noalloc_scratch below: one f32 slot
 // per 32x8-cell block for the block maxima, then a 32-bit arrival counter.
 // Every GPU that loads the library holds it (256 KB) until the process exits.
+// Its device address is looked up on the first call on each device and kept;
+// after cudaDeviceReset on that device the kept address is stale, so a
+// process that resets a device must not call this entry point on it again.
 #include <cuda_runtime.h>
 #include <math.h>
 
@@ -99,6 +100,11 @@ extern "C" FS_API int fs_max_divergence_noalloc(const float* d_u, const float* d
   if (nx < 2 || ny < 2 || !(lx > 0) || !(ly > 0))
     return fail(FS_ERR_INVALID_ARGUMENT, "fs_max_divergence_noalloc: grid must be >= 2x2 with a positive domain");
   const int gx = (nx + kBlockX - 1) / kBlockX, gy = (ny + kBlockY - 1) / kBlockY;
+  if (gy > 65535)  // the launch's grid-y limit (a narrow, very tall grid)
+    return fail(FS_ERR_INVALID_ARGUMENT,
+                "fs_max_divergence_noalloc: ny = " + std::to_string(ny) +
+                    " needs more than 65535 rows of 32x8-cell blocks; the static scratch kernel takes "
+                    "ny <= 524280");
   if ((int64_t)gx * gy > kMaxBlocks)
     return fail(FS_ERR_INVALID_ARGUMENT,
                 "fs_max_divergence_noalloc: grid needs " + std::to_string((int64_t)gx * gy) +

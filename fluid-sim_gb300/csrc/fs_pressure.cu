@@ -539,6 +539,12 @@ __global__ void __launch_bounds__(256)
 // the residual maximum m, and the loop condition "cycle again" -- the work of
 // k_cond, also done by the residual kernel's finishing thread when the loop
 // folds it in (CondFold).
+// tol as the loop code passes it (dev_tol): > 0 absolute, < 0 relative to
+// the residual the projection started from
+__device__ __forceinline__ double tol_limit(double tol, const DevState* st) {
+  return tol < 0 ? -tol * st->res_initial : tol;
+}
+
 __device__ __forceinline__ bool cond_apply(DevState* st, double m, double tol, int max_cycles, int init) {
   if (init) {
     st->cycles = 0;
@@ -548,10 +554,11 @@ __device__ __forceinline__ bool cond_apply(DevState* st, double m, double tol, i
     st->total_cycles += 1;
   }
   st->res_max = m;
+  const double lim = tol_limit(tol, st);
   const bool finite = isfinite(m);
   st->nonfinite = finite ? 0 : 1;
-  st->converged = (finite && m <= tol) ? 1 : 0;
-  return finite && m > tol && st->cycles < max_cycles;
+  st->converged = (finite && m <= lim) ? 1 : 0;
+  return finite && m > lim && st->cycles < max_cycles;
 }
 
 struct CondFold {
@@ -664,7 +671,7 @@ bool launch_refine_init(Solver* s, const float* dh, const float* dl, const float
                         float* r32, bool zero_p, const cudaGraphConditionalHandle* cond) {
   const Grid& g = s->g;
   const bool quad = !zero_p && g.nx % 4 == 0;
-  const CondFold cf = (quad && cond) ? CondFold{*cond, s->dev, s->prm.pressure_tol, s->prm.max_cycles, 1}
+  const CondFold cf = (quad && cond) ? CondFold{*cond, s->dev, dev_tol(s), s->prm.max_cycles, 1}
                                      : CondFold{};
   FS_LAUNCH(s, "refine_init", (double)s->n * (zero_p ? 12 : 20),
             if (quad) {
@@ -763,20 +770,34 @@ __global__ void k_cond(cudaGraphConditionalHandle h, int use_handle, const doubl
   if (use_handle) cudaGraphSetConditional(h, again ? 1u : 0u);
 }
 
-__global__ void k_step_finish(DevState* __restrict__ st, double dt) { st->t += dt; }
+// end of a step: the time, and (track: the step's tolerance loop ran on the
+// device) the record of every projection -- how many, how many failed, the
+// worst final residual -- that the per-projection statistics overwrite
+__device__ __forceinline__ void finish_step(DevState* st, double dt, int track) {
+  st->t += dt;
+  if (track) {
+    st->rec_steps += 1;
+    if (!st->converged) st->rec_failed += 1;
+    const double m = isfinite(st->res_max) ? st->res_max : INFINITY;
+    if (!(m <= st->rec_worst)) st->rec_worst = m;
+  }
+}
+
+__global__ void k_step_finish(DevState* __restrict__ st, double dt, int track) { finish_step(st, dt, track); }
 
 void launch_cond_init(Solver* s, cudaGraphConditionalHandle h, bool graph) {
   FS_LAUNCH(s, "cond", 0.0,
-            k_cond<<<1, 1, 0, s->stream>>>(h, graph ? 1 : 0, s->red_out, s->dev, s->prm.pressure_tol,
+            k_cond<<<1, 1, 0, s->stream>>>(h, graph ? 1 : 0, s->red_out, s->dev, dev_tol(s),
                                            s->prm.max_cycles, 1));
 }
 void launch_cond_step(Solver* s, cudaGraphConditionalHandle h, bool graph) {
   FS_LAUNCH(s, "cond", 0.0,
-            k_cond<<<1, 1, 0, s->stream>>>(h, graph ? 1 : 0, s->red_out, s->dev, s->prm.pressure_tol,
+            k_cond<<<1, 1, 0, s->stream>>>(h, graph ? 1 : 0, s->red_out, s->dev, dev_tol(s),
                                            s->prm.max_cycles, 0));
 }
 void launch_step_finish(Solver* s, double dt) {
-  FS_LAUNCH(s, "step_finish", 0.0, k_step_finish<<<1, 1, 0, s->stream>>>(s->dev, dt));
+  FS_LAUNCH(s, "step_finish", 0.0,
+            k_step_finish<<<1, 1, 0, s->stream>>>(s->dev, dt, s->stats_on_device ? 1 : 0));
 }
 
 // ------------------------------------------- batched refinement bookkeeping
@@ -833,8 +854,9 @@ __global__ void __launch_bounds__(kClassMax) k_cond_class(const CondTab tab, int
       st->res_max = m;
       const bool finite = isfinite(m);
       st->nonfinite = finite ? 0 : 1;
-      st->converged = (finite && m <= tab.m[z].tol) ? 1 : 0;
-      again = finite && m > tab.m[z].tol && 0 < max_cycles;
+      const double lim = tol_limit(tab.m[z].tol, st);
+      st->converged = (finite && m <= lim) ? 1 : 0;
+      again = finite && m > lim && 0 < max_cycles;
     } else if (init) {
       again = member_in_loop(st, max_cycles);
     } else if (member_in_loop(st, max_cycles)) {  // this member ran the cycle
@@ -844,8 +866,9 @@ __global__ void __launch_bounds__(kClassMax) k_cond_class(const CondTab tab, int
       st->res_max = m;
       const bool finite = isfinite(m);
       st->nonfinite = finite ? 0 : 1;
-      st->converged = (finite && m <= tab.m[z].tol) ? 1 : 0;
-      again = finite && m > tab.m[z].tol && st->cycles < max_cycles;
+      const double lim = tol_limit(tab.m[z].tol, st);
+      st->converged = (finite && m <= lim) ? 1 : 0;
+      again = finite && m > lim && st->cycles < max_cycles;
     }
   }
   again = __syncthreads_or(again);
@@ -872,7 +895,7 @@ void launch_refine_class(Solver* const* ms, int count, cudaStream_t st) {
 void launch_cond_class(Solver* const* ms, int count, cudaStream_t st, cudaGraphConditionalHandle h, int init,
                        long long* iterations) {
   CondTab tab{};
-  for (int i = 0; i < count; i++) tab.m[i] = {ms[i]->red_out, ms[i]->dev, ms[i]->prm.pressure_tol};
+  for (int i = 0; i < count; i++) tab.m[i] = {ms[i]->red_out, ms[i]->dev, dev_tol(ms[i])};
   k_cond_class<<<1, kClassMax, 0, st>>>(tab, count, ms[0]->prm.max_cycles, h, init, iterations);
 }
 
@@ -934,7 +957,7 @@ __global__ void __launch_bounds__(256) k_subgrad_class(const ProjTab tab, int nx
 
 __global__ void k_finish_class(const ProjTab tab, int count) {
   const int z = threadIdx.x;
-  if (z < count) tab.m[z].st->t += tab.m[z].dt;
+  if (z < count) finish_step(tab.m[z].st, tab.m[z].dt, 1);
 }
 
 static ProjTab proj_tab(Solver* const* ms, int count, const float* const* wu, const float* const* wv,

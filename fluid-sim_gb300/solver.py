@@ -33,7 +33,7 @@ def make_params(n: int = 256, nx: int | None = None, ny: int | None = None, lx: 
                 precision: str = "f32", pressure_tol: float = 0.0, max_cycles: int = 50, mg_pre_smooth: int = 2,
                 mg_post_smooth: int = 2, mg_coarse_sweeps: int = 40, mg_min_size: int = 8,
                 warm_start: bool = False, device: int = 0, kernel_variant: int = 0, dye_fade: float = 0.0,
-                relax: float = 1.0, **camel) -> "L.Params":
+                relax: float = 1.0, pressure_tol_relative: bool = False, **camel) -> "L.Params":
     """fs_params from the reference's option names (camelCase accepted);
     unknown names are rejected (the reference silently defaults)."""
     solid_mask_width = camel.pop("solidMaskWidth", solid_mask_width)
@@ -68,6 +68,7 @@ def make_params(n: int = 256, nx: int | None = None, ny: int | None = None, lx: 
     p.kernel_variant = kernel_variant
     p.dye_fade = dye_fade
     p.relax = relax
+    p.pressure_tol_relative = int(bool(pressure_tol_relative))
     return p
 
 
@@ -192,6 +193,22 @@ class GPUFluidSolver:
 
     setForcing = set_forcing
 
+    BAND_KINDS = {"reference": 0, "gaussian": 1}
+
+    def set_band_forcing(self, kind: str | None = "reference", kf: float = 28.0, width: float = 2.0,
+                         amplitude: float = 0.4, seed: int = 1, drag: float = 0.0) -> None:
+        """bandForcing(g, u, v, {kf, width, amp, seed++}) + linearDrag(alpha)
+        every step (src/cpu/solver.js:179-237; defaults are bandForcing's).
+        kind "reference": its 24 LCG modes; "gaussian": every lattice mode in
+        the band with a Philox complex Gaussian amplitude; None removes it."""
+        if kind is None:
+            self._chk(self._lib.fs_set_band_forcing(self._h, None))
+            return
+        if kind not in self.BAND_KINDS:
+            raise L.FluidError(1, f"unknown band forcing kind {kind!r}")
+        b = L.Band(self.BAND_KINDS[kind], kf, width, amplitude, seed, drag)
+        self._chk(self._lib.fs_set_band_forcing(self._h, C.byref(b)))
+
     def set_solids(self, disks: Iterable) -> None:
         """setSolid(disk) generalised to several disks (solver.js:425-438)"""
         disks = list(disks or [])
@@ -300,6 +317,13 @@ class GPUFluidSolver:
         c = C.c_int64()
         self._chk(self._lib.fs_total_cycles(self._h, C.byref(c)))
         return c.value
+
+    def convergence_record(self) -> dict:
+        """every tolerance-loop projection since creation: how many, how many
+        missed pressure_tol, and the worst final max|div u| among them"""
+        n, f, w = C.c_int64(), C.c_int64(), C.c_double()
+        self._chk(self._lib.fs_convergence_record(self._h, C.byref(n), C.byref(f), C.byref(w)))
+        return {"steps": n.value, "failed_steps": f.value, "worst_max_div": w.value}
 
     def set_mg_sweeps(self, pre: int, post: int) -> None:
         self._chk(self._lib.fs_set_mg_sweeps(self._h, pre, post))

@@ -136,6 +136,10 @@ typedef struct fs_params {
                                  Default 1.0, the value the reference's callers pass
                                  (solver.js:716,729, multigrid.js:261); w = 1 rounds
                                  exactly like the plain update.  Must lie in (0, 2). */
+  int32_t pressure_tol_relative; /* 1: the tolerance loop stops at max|r| <= pressure_tol
+                                 times the max residual the projection started from
+                                 (a relative residual), 0 (default): at max|div u| <=
+                                 pressure_tol */
 } fs_params;
 
 /* one forcing mode, as setForcing's {kx, ky, phase} (solver.js:370-385) */
@@ -193,6 +197,37 @@ FS_API int fs_upload_field(fs_solver* s, int field, const void* data, int dtype)
  * count == 0 disables the forcing pass */
 FS_API int fs_set_forcing(fs_solver* s, const fs_mode* modes, int count, double amplitude,
                           double drag, double phase_drift);
+/* Band-limited random forcing renewed every step, plus linear drag: the
+ * forced-turbulence driver of the reference (bandForcing + linearDrag,
+ * src/cpu/solver.js:179-237, passed to FluidSolver.step as opts.force /
+ * opts.drag with a seed that grows by one per step,
+ * validate/longrun-spectrum.js:65-67).  Each step adds the curl of
+ * psi = sum_m A_m cos(kx_m x + ky_m y + phi_m), scaled by amplitude*dt/sqrt(M),
+ * to the velocity after diffusion, then multiplies it by exp(-drag dt); the
+ * fixed-mode forcing of fs_set_forcing, if also set, follows. */
+typedef enum fs_band_kind {
+  /* bandForcing itself: 24 modes drawn by its 32-bit LCG from seed + step,
+   * |k| = kf + (r - 1/2) 2 width at a random angle, rounded; A = 1 */
+  FS_BAND_REFERENCE = 0,
+  /* every integer (kx, ky) with kf - width <= |k| <= kf + width (ky, then kx
+   * ascending), each with a complex Gaussian amplitude (sigma 1 per part)
+   * from Philox4x32-10, key = seed, counter = (step, mode index, 0, 0) */
+  FS_BAND_GAUSSIAN = 1
+} fs_band_kind;
+
+typedef struct fs_band {
+  int32_t kind;       /* fs_band_kind */
+  double kf, width;   /* the band: centre and half-width in wave numbers */
+  double amplitude;   /* amp of bandForcing */
+  uint64_t seed;      /* draws of the solver's k-th forced step use seed + k
+                         (REFERENCE) or counter k (GAUSSIAN) */
+  double drag;        /* linear drag alpha >= 0 (linearDrag) */
+} fs_band;
+
+/* band == NULL removes it.  Setting it restarts the step counter of the
+ * draws at 0.  Drops the captured step. */
+FS_API int fs_set_band_forcing(fs_solver* s, const fs_band* band);
+
 /* setSolid(disk) (solver.js:425-438), generalised to count disks applied in
  * order (src/cpu/solid.js:181-230); count == 0 removes them */
 FS_API int fs_set_solids(fs_solver* s, const fs_disk* disks, int count);
@@ -255,17 +290,20 @@ FS_API void fs_host_free(void* p);
  *
  * For callers that cannot allocate device memory while they run -- hosts that
  * reserve the GPU through their own pool, frame loops that must not call
- * cudaMalloc/cudaFree (they can synchronise the device), code being recorded
- * into a CUDA graph.  It calls no cudaMalloc, cudaFree or allocating library
- * routine: its scratch (per-block maxima and an arrival counter) is a static
- * device array of 65536 + 64 floats (256 KB) that every GPU loading the library
- * holds until the process exits.
+ * cudaMalloc/cudaFree (they can synchronise the device).  It calls no
+ * cudaMalloc, cudaFree or allocating library routine: its scratch (per-block
+ * maxima and an arrival counter) is a static device array of 65536 + 64
+ * floats (256 KB) that every GPU loading the library holds until the process
+ * exits.
  *
  *  - Grids are limited to 65536 blocks of 32x8 cells (at most 16,777,216
- *    cells, e.g. 4096 x 4096); larger grids return FS_ERR_INVALID_ARGUMENT.
+ *    cells, e.g. 4096 x 4096) and to ny <= 524280 (65535 block rows); other
+ *    grids return FS_ERR_INVALID_ARGUMENT before anything is enqueued.
  *  - The first call on a device looks up the device address of that array
- *    (with the device current); make that first call before any stream
- *    capture begins.
+ *    (with the device current) and keeps it; make that first call before any
+ *    stream capture begins.  The kept address is stale after cudaDeviceReset
+ *    of that device: do not call this entry point on a device after resetting
+ *    it.
  *  - All calls share the one array: calls that can overlap on the GPU
  *    (different streams, no ordering between them) race and may return
  *    wrong maxima.  Each call clears the counter it needs before its kernel.
@@ -385,6 +423,15 @@ FS_API int fs_set_mg_sweeps(fs_solver* s, int32_t pre, int32_t post);
 /* refinement cycles run by every projection of the tolerance loop since
  * creation (a device counter; synchronises) */
 FS_API int fs_total_cycles(fs_solver* s, int64_t* cycles);
+/* Record of every tolerance-loop projection the solver's steps have run
+ * since creation: how many, how many ended without meeting pressure_tol
+ * (max_cycles reached or a non-finite residual), and the largest final
+ * max|div u| among them (+inf if one was non-finite).  fs_last_stats reports
+ * only the last projection; this covers every step of a long run, including
+ * steps replayed from a captured graph whose loop ran on the device.  No
+ * counterpart in the reference (its projection runs a fixed count and never
+ * reports convergence).  Synchronises. */
+FS_API int fs_convergence_record(fs_solver* s, int64_t* steps, int64_t* failed_steps, double* worst_residual);
 /* Autotuner: times nsteps steps of dt for every (pre, post) sweep pair the
  * fused kernels take (1..3 each), from the same saved state each time, and
  * keeps the fastest that still meets pressure_tol; the state, dye, time and

@@ -113,6 +113,18 @@ void fso_linear_drag(double* u, double* v, int64_t n, double alpha, double dt);
 /* bandForcing (src/cpu/solver.js:179) */
 void fso_band_forcing(const fso_grid* g, double* u, double* v, double kf, double width,
                       double amp, uint32_t seed, double dt);
+/* Philox4x32-10 counter-based generator (Salmon, Moraes, Dror, Shaw, "Parallel
+ * random numbers: as easy as 1, 2, 3", SC'11) */
+void fso_philox4x32_10(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]);
+/* Band forcing with a complex Gaussian amplitude per lattice mode (the forced-
+ * turbulence configuration; no reference counterpart, the reference draws 24
+ * LCG modes): every integer (kx, ky) with kf-width <= |k| <= kf+width, ky then
+ * kx ascending; mode m draws Philox(ctr = {counter, m, 0, 0}, key = {key lo,
+ * key hi}) -> u1 = (x0 + 1/2)/2^32, u2 = (x1 + 1/2)/2^32, A = sqrt(-2 ln u1),
+ * phi = 2 pi u2, and adds the curl of A cos(k.x + phi) scaled by amp dt/sqrt(M)
+ * exactly as bandForcing does with its modes. */
+void fso_gauss_band_forcing(const fso_grid* g, double* u, double* v, double kf, double width, double amp,
+                            uint64_t key, uint32_t counter, double dt);
 /* GPU FORCING semantics (src/gpu/shaders.js:532-566): u = u*exp(-drag dt) + amp dt/sqrt(M) sum */
 typedef struct { double kx, ky, phase; } fso_mode;
 void fso_forcing_modes(const fso_grid* g, double* u, double* v, const fso_mode* modes, int m,
@@ -163,6 +175,9 @@ typedef struct {
   int band_forcing;
   double band_kf, band_width, band_amp;
   uint32_t band_seed;
+  int band_kind;          /* 0: bandForcing with band_seed; 1: fso_gauss_band_forcing */
+  uint64_t band_key;      /* kind 1: Philox key */
+  uint32_t band_counter;  /* kind 1: Philox counter word 0 (the step) */
 } fso_step_opts;
 void fso_step_opts_default(fso_step_opts* o);
 void fso_step(fso_solver* s, double dt, const fso_step_opts* o);

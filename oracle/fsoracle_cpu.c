@@ -832,6 +832,52 @@ void fso_band_forcing(const fso_grid* g, double* u, double* v, double kf, double
   }
 }
 
+/* Philox4x32-10: ten rounds of two 32x32->64 multiplies (multipliers
+ * 0xD2511F53, 0xCD9E8D57) with the Weyl key schedule (0x9E3779B9, 0xBB67AE85) */
+void fso_philox4x32_10(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]) {
+  uint32_t c0 = ctr[0], c1 = ctr[1], c2 = ctr[2], c3 = ctr[3], k0 = key[0], k1 = key[1];
+  for (int r = 0; r < 10; r++) {
+    uint64_t p0 = (uint64_t)0xD2511F53u * c0, p1 = (uint64_t)0xCD9E8D57u * c2;
+    uint32_t hi0 = (uint32_t)(p0 >> 32), lo0 = (uint32_t)p0, hi1 = (uint32_t)(p1 >> 32), lo1 = (uint32_t)p1;
+    uint32_t n0 = hi1 ^ c1 ^ k0, n1 = lo1, n2 = hi0 ^ c3 ^ k1, n3 = lo0;
+    c0 = n0; c1 = n1; c2 = n2; c3 = n3;
+    k0 += 0x9E3779B9u;
+    k1 += 0xBB67AE85u;
+  }
+  out[0] = c0; out[1] = c1; out[2] = c2; out[3] = c3;
+}
+
+void fso_gauss_band_forcing(const fso_grid* g, double* u, double* v, double kf, double width, double amp,
+                            uint64_t key, uint32_t counter, double dt) {
+  const double lo = kf - width, hi = kf + width;
+  const int K = (int)ceil(hi);
+  int M = 0;
+  for (int ky = -K; ky <= K; ky++)
+    for (int kx = -K; kx <= K; kx++) {
+      double kk = (double)kx * kx + (double)ky * ky;
+      if (kk != 0 && kk >= lo * lo && kk <= hi * hi) M++;
+    }
+  if (M == 0) return;
+  const double scale = amp * dt / sqrt((double)M);
+  const uint32_t kw[2] = {(uint32_t)key, (uint32_t)(key >> 32)};
+  int m = 0;
+  for (int ky = -K; ky <= K; ky++)
+    for (int kx = -K; kx <= K; kx++) {
+      double kk = (double)kx * kx + (double)ky * ky;
+      if (kk == 0 || kk < lo * lo || kk > hi * hi) continue;
+      uint32_t ctr[4] = {counter, (uint32_t)m, 0u, 0u}, r[4];
+      fso_philox4x32_10(ctr, kw, r);
+      m++;
+      double u1 = ((double)r[0] + 0.5) / 4294967296.0, u2 = ((double)r[1] + 0.5) / 4294967296.0;
+      double A = sqrt(-2.0 * log(u1)), phi = 2 * M_PI * u2, k = sqrt(kk);
+      for (int j = 0; j < g->ny; j++)
+        for (int i = 0; i < g->nx; i++) {
+          u[IDX(g, i, j)] += scale * A * (ky / k) * cos(kx * uX(g, i) + ky * uY(g, j) + phi);
+          v[IDX(g, i, j)] += scale * A * (-kx / k) * cos(kx * vX(g, i) + ky * vY(g, j) + phi);
+        }
+    }
+}
+
 /* The GPU backend's FORCING kernel (src/gpu/shaders.js:532-566) in f64:
  * drag and forcing fused, drag applied to the incoming velocity. */
 void fso_forcing_modes(const fso_grid* g, double* u, double* v, const fso_mode* modes, int m,
@@ -1055,7 +1101,9 @@ void fso_step(fso_solver* s, double dt, const fso_step_opts* o) {
     swap_ptr(&s->u, &s->tu); swap_ptr(&s->v, &s->tv);
   }
 
-  if (o->band_forcing)
+  if (o->band_forcing && o->band_kind == 1)
+    fso_gauss_band_forcing(g, s->u, s->v, o->band_kf, o->band_width, o->band_amp, o->band_key, o->band_counter, dt);
+  else if (o->band_forcing)
     fso_band_forcing(g, s->u, s->v, o->band_kf, o->band_width, o->band_amp, o->band_seed, dt);
   if (s->n_modes > 0)
     fso_forcing_modes(g, s->u, s->v, s->modes, s->n_modes, s->mode_amp, s->mode_drag,

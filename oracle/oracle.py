@@ -48,7 +48,8 @@ class Params(C.Structure):
 class StepOpts(C.Structure):
     _fields_ = [("advect_dye", C.c_int), ("drag", C.c_double), ("gravity", C.c_double),
                 ("band_forcing", C.c_int), ("band_kf", C.c_double), ("band_width", C.c_double),
-                ("band_amp", C.c_double), ("band_seed", C.c_uint32)]
+                ("band_amp", C.c_double), ("band_seed", C.c_uint32), ("band_kind", C.c_int),
+                ("band_key", C.c_uint64), ("band_counter", C.c_uint32)]
 
 
 class Disk(C.Structure):
@@ -113,6 +114,8 @@ def lib():
             "fso_diffuse": (I, [C.POINTER(Grid), DP, DP, D, D, I, D, DP]),
             "fso_linear_drag": (None, [DP, DP, C.c_int64, D, D]),
             "fso_band_forcing": (None, [C.POINTER(Grid), DP, DP, D, D, D, C.c_uint32, D]),
+            "fso_gauss_band_forcing": (None, [C.POINTER(Grid), DP, DP, D, D, D, C.c_uint64, C.c_uint32, D]),
+            "fso_philox4x32_10": (None, [C.POINTER(C.c_uint32), C.POINTER(C.c_uint32), C.POINTER(C.c_uint32)]),
             "fso_forcing_modes": (None, [C.POINTER(Grid), DP, DP, C.POINTER(Mode), I, D, D, D, D]),
             "fso_disk_init": (None, [C.POINTER(Disk), D, D, D, D, D, D, D, I, I]),
             "fso_disk_mask": (D, [C.POINTER(Disk), D, D, D, D, D]),
@@ -338,6 +341,25 @@ def apply_coupling(g, u, v, disks, dt, mask_width=1.5, passes=1):
     return imp
 
 
+def philox4x32_10(ctr, key):
+    """Philox4x32-10 of four 32-bit counter words and two key words."""
+    c = (C.c_uint32 * 4)(*ctr)
+    k = (C.c_uint32 * 2)(*key)
+    out = (C.c_uint32 * 4)()
+    lib().fso_philox4x32_10(c, k, out)
+    return tuple(out)
+
+
+def band_forcing(g: Grid, u, v, kf, width, amp, seed, dt):
+    """bandForcing (src/cpu/solver.js:179-217) applied to u, v in place."""
+    lib().fso_band_forcing(C.byref(g), _p(u), _p(v), kf, width, amp, seed, dt)
+
+
+def gauss_band_forcing(g: Grid, u, v, kf, width, amp, key, counter, dt):
+    """The Philox Gaussian lattice band forcing applied to u, v in place."""
+    lib().fso_gauss_band_forcing(C.byref(g), _p(u), _p(v), kf, width, amp, key, counter, dt)
+
+
 def set_threads(n: int) -> None:
     lib().fso_set_threads(int(n))
 
@@ -416,7 +438,9 @@ class CpuSolver:
         arr = (Mode * len(modes))(*[Mode(m[0], m[1], m[2]) for m in modes])
         lib().fso_set_modes(self._h, arr, len(modes), amplitude, drag, phase_drift)
 
-    def step(self, dt, advect_dye=True, drag=0.0, gravity=0.0, band=None):
+    def step(self, dt, advect_dye=True, drag=0.0, gravity=0.0, band=None, gauss_band=None):
+        """band = (kf, width, amp, seed): bandForcing as opts.force;
+        gauss_band = (kf, width, amp, key, counter): the Philox Gaussian band"""
         o = StepOpts()
         lib().fso_step_opts_default(C.byref(o))
         o.advect_dye = int(advect_dye)
@@ -425,6 +449,10 @@ class CpuSolver:
         if band is not None:
             o.band_forcing = 1
             o.band_kf, o.band_width, o.band_amp, o.band_seed = band
+        if gauss_band is not None:
+            o.band_forcing = 1
+            o.band_kind = 1
+            o.band_kf, o.band_width, o.band_amp, o.band_key, o.band_counter = gauss_band
         lib().fso_step(self._h, dt, C.byref(o))
         return self
 

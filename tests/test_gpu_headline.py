@@ -1,0 +1,76 @@
+"""The benchmark's own configuration against the f64 oracle.
+
+The bench step is the periodic stream past seeded disks (fluid-sim_gb300/
+workload.py, seed 5: five disks), MacCormack advection, explicit diffusion
+nu = 1e-4, dt at CFL 0.5, the mixed-precision multigrid projection with
+red-black relaxation 1.2 iterated to max|div u| <= 1e-6 after every step.
+The oracle is the f64 CPU solver (restatement of src/cpu/solver.js:336-398:
+MacCormack, explicit diffusion, exact FFT projection, one direct-forcing pass
+per disk) from the same initial state.  Per field, relative L2 <= 1e-5 (the
+tolerance of the f32 advection paths) and relative L-inf <= 1e-4; every
+projection of the run met the tolerance (the device-side convergence record,
+not just the last step's flag).
+
+* 1024^2 with 64-cell level-0 tiles forced (the 2048^2 level-0 kernels' tile
+  side; the built-in rule picks 32 at 1024^2), 10 steps;
+* 2048^2 itself, the bench's tiles, 5 steps.
+"""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+NU, TOL, RELAX = 1e-4, 1e-6, 1.2
+
+
+@pytest.fixture(scope="module")
+def pkg(fs):
+    fs._lib.load()
+    return fs
+
+
+def _run(pkg, O, n, steps, tiles=None):
+    u0, v0, disks, dt = pkg.workload.make_workload(n, 5)
+    assert len(disks) == 5
+    s = pkg.GPUFluidSolver(n=n, nu=NU, advection="maccormack", pressure_solver="multigrid", pressure_iterations=1,
+                           precision="mixed", pressure_tol=TOL, max_cycles=60, relax=RELAX)
+    if tiles is not None:
+        s.set_mg_tiles(tiles)
+        assert s.mg_tiles()[0] == tiles[0]
+    s.upload_velocity(u0, v0)
+    s.set_solids(disks)
+    for _ in range(steps):
+        s.step(dt)
+    rec = s.convergence_record()
+    ug, vg = s.read_velocity()
+    md = s.max_divergence()
+    s.destroy()
+
+    O.set_threads(16)
+    cpu = O.CpuSolver(n=n, nu=NU, advection="maccormack", explicit_diffusion=True, projection="fft",
+                      coupling_passes=1)
+    cpu.u[:] = u0
+    cpu.v[:] = v0
+    for d in disks:
+        cpu.add_solid(O.disk(d[0], d[1], d[2], density=8, fixed=True))
+    for _ in range(steps):
+        cpu.step(dt, advect_dye=False)
+    cu, cv = np.asarray(cpu.u), np.asarray(cpu.v)
+
+    assert rec["steps"] == steps and rec["failed_steps"] == 0, rec
+    assert rec["worst_max_div"] <= TOL and md <= TOL, (rec, md)
+    for a, b in ((ug, cu), (vg, cv)):
+        rl2 = np.linalg.norm(a - b) / np.linalg.norm(b)
+        linf = np.abs(a - b).max() / np.abs(b).max()
+        assert rl2 <= 1e-5, rl2
+        assert linf <= 1e-4, linf
+
+
+def test_bench_config_1024_tile64_matches_oracle(pkg, O):
+    _run(pkg, O, 1024, 10, tiles=[64, 0, 0, 0])
+
+
+def test_bench_config_2048_matches_oracle(pkg, O):
+    _run(pkg, O, 2048, 5)

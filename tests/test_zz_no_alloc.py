@@ -2,9 +2,9 @@
 
 Callers that cannot allocate device memory while they run (a host that owns
 the GPU through its own memory pool, a frame loop that must not call
-cudaMalloc because it can synchronise the device, code recorded into a CUDA
-graph) pass device buffers they already hold; the reduction's scratch is a
-static device array reserved when the library loads.  This test calls it
+cudaMalloc because it can synchronise the device) pass device buffers they
+already hold; the reduction's scratch is a static device array the library
+reserves for itself.  This test calls it
 through the C ABI twice in a row, on two different fields, and checks each
 result against the solver's own fs_max_divergence on the same field, within
 the 1e-6 relative tolerance the f32 kernels are held to.  It allocates its own
@@ -36,6 +36,9 @@ def _cudart():
         rt.cudaMalloc.argtypes = [C.POINTER(C.c_void_p), C.c_size_t]
         rt.cudaMemcpy.argtypes = [C.c_void_p, C.c_void_p, C.c_size_t, C.c_int]
         rt.cudaFree.argtypes = [C.c_void_p]
+        rt.cudaStreamCreateWithFlags.argtypes = [C.POINTER(C.c_void_p), C.c_uint]
+        rt.cudaStreamSynchronize.argtypes = [C.c_void_p]
+        rt.cudaStreamDestroy.argtypes = [C.c_void_p]
         return rt
     pytest.skip("CUDA runtime library not found")
 
@@ -87,4 +90,49 @@ def test_noalloc_max_divergence_matches_solver_twice(G, O):
     st = lib.fs_max_divergence_noalloc(out, out, 8192, 8192, lx, ly, out, None)
     assert st == 1
     assert b"static scratch" in lib.fs_last_error(None)
+    # a narrow grid taller than 65535 rows of blocks (65536 blocks in all, within
+    # the scratch, but above the launch's grid-y limit): rejected the same way
+    st = lib.fs_max_divergence_noalloc(out, out, 32, 524288, lx, ly, out, None)
+    assert st == 1
+    assert b"static scratch" in lib.fs_last_error(None)
     rt.cudaFree(out)
+
+
+def test_noalloc_back_to_back_on_a_caller_stream(G, O):
+    """Two calls enqueued one after the other on a non-blocking stream the
+    caller created, with no synchronisation between them, each writing its own
+    output slot: the second call's counter reset and block maxima must not mix
+    with the first's.  Each result equals fs_max_divergence of its field."""
+    lib = G.load()
+    rt = _cudart()
+    nx, ny = 256, 96
+    lx = ly = 2 * math.pi
+    stream = C.c_void_p()
+    assert rt.cudaStreamCreateWithFlags(C.byref(stream), 1) == 0  # cudaStreamNonBlocking
+    out = C.c_void_p()
+    assert rt.cudaMalloc(C.byref(out), 16) == 0
+    expected, bufs = [], []
+    for seed in (17, 23):
+        a, b = O.lcg_uv(seed, nx * ny)
+        u = np.ascontiguousarray(a * (1 + seed), dtype=np.float32)
+        v = np.ascontiguousarray(b, dtype=np.float32)
+        s = G.GPUFluidSolver(nx=nx, ny=ny, lx=lx, ly=ly)
+        s.upload_velocity(u, v)
+        expected.append(s.max_divergence())
+        s.destroy()
+        bufs.append((_to_device(rt, u), _to_device(rt, v)))
+    for k, (du, dv) in enumerate(bufs):
+        slot = C.c_void_p(out.value + 8 * k)
+        st = lib.fs_max_divergence_noalloc(du, dv, nx, ny, lx, ly, slot, stream)
+        assert st == 0, lib.fs_last_error(None)
+    assert rt.cudaStreamSynchronize(stream) == 0
+    got = np.zeros(2)
+    assert rt.cudaMemcpy(got.ctypes.data, out, 16, D2H) == 0
+    for du, dv in bufs:
+        rt.cudaFree(du)
+        rt.cudaFree(dv)
+    rt.cudaFree(out)
+    rt.cudaStreamDestroy(stream)
+    assert got[0] == pytest.approx(expected[0], rel=1e-6)
+    assert got[1] == pytest.approx(expected[1], rel=1e-6)
+    assert got[0] != got[1]
