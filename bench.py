@@ -373,6 +373,20 @@ def run_gpu(args):
             variants[name]["guess"] = g
             variants[name]["relax"] = w
 
+    forced = None
+    if rank == 0 and args.forced_steps > 0:
+        r = pkg.forced.run_forced_turbulence(n=1024, steps=args.forced_steps, every=100, device=local)
+        sig = lambda x: float(f"{x:.5g}")  # noqa: E731
+        forced = {k: r[k] for k in ("n", "steps", "every", "dt", "nu", "drag", "band", "amplitude", "seed",
+                                    "tol_relative", "ms_per_step", "cell_steps_per_s", "cycles_per_step",
+                                    "failed_steps", "projections", "averaged_snapshots", "windows", "fits",
+                                    "parseval_max_rel_err")}
+        forced["ke_every_100_steps"] = [sig(x) for x in r["ke"]]
+        forced["spectrum_avg_k0_64"] = [sig(x) for x in r["spectrum_avg"][:65]]
+        forced["workload"] = ("forced 2-D turbulence: periodic 1024^2 from rest, Philox Gaussian band forcing "
+                              "8 <= |k| <= 10 renewed every step, nu=1e-4, drag 0.1, MacCormack, mixed-precision "
+                              "multigrid to relative residual 1e-6, device spectrum every 100 steps")
+
     batch = None
     if args.batch_sims > 0:
         batch = measure_batch(pkg, local, args.batch_sims, min(args.steps, 20), min(args.warmup, 3),
@@ -429,6 +443,8 @@ def run_gpu(args):
             line["guess_comparison"] = variants
         if batch is not None:
             line["batch"] = batch
+        if forced is not None:
+            line["forced_turbulence"] = forced
         if cpu is not None:
             line["cpu_baseline"] = cpu
         if ferr is not None:
@@ -610,6 +626,8 @@ def main():
                     help="also time a batch of this many uneven domains (0 = skip)")
     ap.add_argument("--no-variants", action="store_true",
                     help="skip timing the learned guess and the warm start beside the headline")
+    ap.add_argument("--forced-steps", type=int, default=5000,
+                    help="steps of the 1024^2 forced-turbulence run (spectrum every 100; 0 = skip)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-field-error", action="store_true",
                     help="skip the comparison of u, v after a few steps with the f64 oracle")

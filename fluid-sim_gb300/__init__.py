@@ -6,8 +6,8 @@ GPUFluidSolver API on top of it.
 """
 from ._lib import FluidError, build, load, LIB_PATH  # noqa: F401
 from .solver import GPUFluidBatch, GPUFluidSolver, make_params  # noqa: F401
-from . import workload  # noqa: F401
+from . import forced, workload  # noqa: F401
 from .guess import PressureGuess, normalize_pair, read_pair_file, write_pair_file  # noqa: F401
 
 __all__ = ["GPUFluidSolver", "GPUFluidBatch", "make_params", "PressureGuess", "FluidError", "build", "load", "LIB_PATH", "normalize_pair",
-           "read_pair_file", "write_pair_file", "workload"]
+           "read_pair_file", "write_pair_file", "workload", "forced"]

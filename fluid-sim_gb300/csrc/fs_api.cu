@@ -138,6 +138,8 @@ static int create(const fs_params* prm, Solver* s) {
   if (!(P.nu >= 0)) return fail(nullptr, FS_ERR_INVALID_ARGUMENT, "nu must be >= 0");
   if (!(P.dye_fade >= 0) || !(P.dye_fade <= 1)) return fail(nullptr, FS_ERR_INVALID_ARGUMENT, "dye_fade must be in [0, 1]");
   if (!(P.relax > 0) || !(P.relax < 2)) return fail(nullptr, FS_ERR_INVALID_ARGUMENT, "relax must be in (0, 2)");
+  if (P.pressure_tol_relative != 0 && P.pressure_tol_relative != 1)
+    return fail(nullptr, FS_ERR_INVALID_ARGUMENT, "pressure_tol_relative must be 0 or 1");
   if (P.confinement != 0)
     return fail(nullptr, FS_ERR_UNSUPPORTED, "vorticity confinement is not part of this path (it must stay off)");
   if (P.advection != FS_ADVECT_SEMI_LAGRANGIAN && P.advection != FS_ADVECT_MACCORMACK)
