@@ -1,9 +1,10 @@
 """Benchmark of the stable-fluids step on GB300: cell-steps/s at 2048^2 with
 max|div u| <= 1e-6 after every projection.
 
-Workload (synthetic, seeded): a 2048 x 2048 periodic MAC grid on [0, 2pi]^2,
-a unit stream u = 1 with a divergence-free random perturbation past seeded
-fixed disks (direct-forcing mask, radii 0.02-0.08 of the height), nu = 1e-4,
+Workload (synthetic, seeded): channel flow on a 2048 x 2048 MAC grid on
+[0, 2pi]^2 -- uniform inflow u = 1 through a fringe strip, no-slip walls (an
+immersed slab), seeded fixed disks (direct-forcing mask, radii 0.02-0.08 of
+the channel height), a divergence-free random perturbation -- nu = 1e-4,
 MacCormack advection, explicit diffusion, dt at CFL 0.5, and a
 mixed-precision multigrid projection iterated until max|div u| <= 1e-6.
 
@@ -67,8 +68,9 @@ def _oracle():
 
 # ------------------------------------------------------------------ workload
 def make_workload(n: int = N, seed: int = SEED):
-    """The seeded channel-flow workload (fluid-sim_gb300/workload.py)."""
-    return _package().workload.make_workload(n, seed)
+    """The seeded channel-flow workload (fluid-sim_gb300/workload.py):
+    (u, v, disks, dt, channel)."""
+    return _package().workload.channel_workload(n, seed)
 
 
 # ------------------------------------------------------------------- clocks
@@ -271,10 +273,11 @@ def measure_batch(pkg, device, count, steps, warmup, seed=1, relax=RELAX):
             "gpu_launches_total": launches}
 
 
-def measure_variant(pkg, n, device, guess, u0, v0, disks, dt, steps, warmup, relax=RELAX):
+def measure_variant(pkg, n, device, guess, u0, v0, disks, ch, dt, steps, warmup, relax=RELAX):
     """ms/step, cycles/step and cell-steps/s of one initial-pressure choice."""
     s = make_solver(pkg, n, device, guess, relax)
     s.upload_velocity(u0, v0)
+    s.set_channel(ch)
     s.set_solids(disks)
     for _ in range(warmup):
         s.step(dt)
@@ -297,9 +300,10 @@ def run_gpu(args):
     pkg = _package()
     pkg.load()
     n = args.n
-    u0, v0, disks, dt = make_workload(n)
+    u0, v0, disks, dt, ch = make_workload(n)
     s = make_solver(pkg, n, local, args.guess, args.relax)
     s.upload_velocity(u0, v0)
+    s.set_channel(ch)
     s.set_solids(disks)
     # warm-up
     cycles = []
@@ -369,7 +373,7 @@ def run_gpu(args):
                            ("nn_guess_mg", "nn", args.relax), ("warm_start_mg", "warm", args.relax)):
             if name != "plain_mg" and g == args.guess and w == args.relax:
                 continue
-            variants[name] = measure_variant(pkg, n, local, g, u0, v0, disks, dt, args.steps, args.warmup, w)
+            variants[name] = measure_variant(pkg, n, local, g, u0, v0, disks, ch, dt, args.steps, args.warmup, w)
             variants[name]["guess"] = g
             variants[name]["relax"] = w
 
@@ -404,9 +408,11 @@ def run_gpu(args):
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "double-float state / f32 advection + V-cycles",
-            "data": "synthetic (seeded stream + divergence-free perturbation + fixed disks)",
+            "data": "synthetic (seeded channel flow: inflow fringe, wall slab, divergence-free perturbation, "
+                    "fixed disks)",
             "config": {
-                "workload": f"periodic {n}x{n} MAC grid, stream u=1 past {len(disks)} fixed disks, nu={NU}, "
+                "workload": f"{n}x{n} MAC grid, channel flow (inflow u=1 through a fringe strip, no-slip wall "
+                            f"slab) past {len(disks)} fixed disks, nu={NU}, "
                             "MacCormack, explicit diffusion, mixed-precision multigrid V(2,2) "
                             f"(red-black relaxation {args.relax}) iterated to "
                             f"max|div u| <= {TOL}",
@@ -479,11 +485,12 @@ def oracle_solver(O, n: int):
     """The oracle's f64 CPU solver (restatement of src/cpu/solver.js) on the
     bench workload: MacCormack, explicit diffusion, exact FFT projection, one
     direct-forcing pass per disk."""
-    u0, v0, disks, dt = make_workload(n)
+    u0, v0, disks, dt, ch = make_workload(n)
     cpu = O.CpuSolver(n=n, nu=NU, advection="maccormack", explicit_diffusion=True, projection="fft",
                       coupling_passes=1)
     cpu.u[:] = u0
     cpu.v[:] = v0
+    cpu.set_channel(ch)
     for d in disks:
         cpu.add_solid(O.disk(d[0], d[1], d[2], density=8, fixed=True))
     return cpu, dt
@@ -498,9 +505,10 @@ def field_error(pkg, n, device, relax, steps=FIELD_STEPS):
     fresh solver with the bench's settings and the oracle's CPU solver advance
     the same initial state `steps` steps; relative L2 and relative L-inf
     (max |a - b| / max |b|) of u and v, with the tolerance they are held to."""
-    u0, v0, disks, dt = make_workload(n)
+    u0, v0, disks, dt, ch = make_workload(n)
     s = make_solver(pkg, n, device, "zero", relax)
     s.upload_velocity(u0, v0)
+    s.set_channel(ch)
     s.set_solids(disks)
     for _ in range(steps):
         s.step(dt)
@@ -516,7 +524,8 @@ def field_error(pkg, n, device, relax, steps=FIELD_STEPS):
         cpu.step(dt, advect_dye=False)
     sec = time.perf_counter() - t0
     out = {"steps": steps, "tol_rel_l2": FIELD_TOL, "oracle": "f64 C restatement of src/cpu/solver.js "
-           "(MacCormack, explicit diffusion, exact FFT projection), same seeded initial state and disks",
+           "(MacCormack, explicit diffusion, exact FFT projection, the same channel forcing), same seeded "
+           "initial state and disks",
            "oracle_threads": threads, "oracle_s": round(sec, 2), "gpu_failed_steps": rec["failed_steps"]}
     ok = rec["failed_steps"] == 0
     for name, a, b in (("u", gu, np.asarray(cpu.u)), ("v", gv, np.asarray(cpu.v))):
@@ -598,7 +607,7 @@ def run_reference(args):
         "ms_per_step": sec * 1e3 / timed,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic (same seeded workload)",
-        "config": {"workload": f"periodic {n}x{n}, {len(disks)} fixed disks, nu={NU}, MacCormack, explicit "
+        "config": {"workload": f"{n}x{n} channel flow past {len(disks)} fixed disks, nu={NU}, MacCormack, explicit "
                                "diffusion, exact FFT projection", "n": n, "max_div_after": md},
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": 1, "kind": "port", "host": host_cpu(),
                          "sample": f"{timed} timed step(s) after {warm} warm-up step(s) of the {n}^2 "

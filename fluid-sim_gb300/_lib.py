@@ -97,6 +97,11 @@ class Band(C.Structure):
                 ("seed", C.c_uint64), ("drag", C.c_double)]
 
 
+class Channel(C.Structure):
+    _fields_ = [("wall_y", C.c_double), ("wall_half", C.c_double), ("fringe_x", C.c_double),
+                ("fringe_half", C.c_double), ("fringe_ramp", C.c_double), ("inflow_u", C.c_double)]
+
+
 class Disk(C.Structure):
     _fields_ = [("x", C.c_double), ("y", C.c_double), ("r", C.c_double), ("vx", C.c_double),
                 ("vy", C.c_double), ("omega", C.c_double)]
@@ -131,6 +136,7 @@ SIGNATURES = {
     "fs_set_forcing": (I, [VP, C.POINTER(Mode), I, D, D, D]),
     "fs_set_solids": (I, [VP, C.POINTER(Disk), I]),
     "fs_set_band_forcing": (I, [VP, C.POINTER(Band)]),
+    "fs_set_channel": (I, [VP, C.POINTER(Channel)]),
     "fs_solid_impulse": (I, [VP, C.POINTER(C.c_double), I]),
     "fs_step": (I, [VP, D]),
     "fs_advance": (I, [VP, D, I]),

@@ -537,6 +537,7 @@ static int enqueue_step(Solver* s, double dt, bool capture, StepSplit* split = n
   }
   if (s->band) launch_band(s, cu, cv, fdt);
   if (s->n_modes > 0) launch_forcing(s, cu, cv, fdt);
+  if (s->channel_on) launch_channel(s, cu, cv);
   if (!s->disks.empty()) launch_solids(s, cu, cv, fdt, false);
   int rc = project_from(s, cu, cv, capture, split != nullptr);
   if (split) {
@@ -660,9 +661,10 @@ static int run_stage(Solver* s, int stage, double dt) {
       w_to_state(s, s->wu, s->wv);
       break;
     case FS_STAGE_SOLID:
-      if (s->disks.empty()) break;
+      if (s->disks.empty() && !s->channel_on) break;
       state_to_w(s);
-      launch_solids(s, s->wu, s->wv, fdt, s->imp != nullptr);
+      if (s->channel_on) launch_channel(s, s->wu, s->wv);
+      if (!s->disks.empty()) launch_solids(s, s->wu, s->wv, fdt, s->imp != nullptr);
       w_to_state(s, s->wu, s->wv);
       break;
     case FS_STAGE_DIVERGENCE:
@@ -936,6 +938,22 @@ FS_API int fs_set_band_forcing(fs_solver* h, const fs_band* band) {
   // the draws start again from step 0
   CU(s, cudaMemsetAsync(&s->dev->band_step, 0, sizeof(unsigned long long), s->stream));
   return FS_OK;
+}
+
+FS_API int fs_set_channel(fs_solver* h, const fs_channel* c) {
+  SOLVER(h);
+  if (c) {
+    const double v[6] = {c->wall_y, c->wall_half, c->fringe_x, c->fringe_half, c->fringe_ramp, c->inflow_u};
+    for (double x : v)
+      if (!std::isfinite(x)) return fail(s, FS_ERR_INVALID_ARGUMENT, "channel parameters must be finite");
+    if (!(c->wall_half > 0) || !(c->wall_half < 0.5 * s->prm.ly) || !(c->fringe_half > 0) ||
+        !(c->fringe_half < 0.5 * s->prm.lx) || !(c->fringe_ramp > 0))
+      return fail(s, FS_ERR_INVALID_ARGUMENT,
+                  "channel needs 0 < wall_half < ly/2, 0 < fringe_half < lx/2 and fringe_ramp > 0");
+  }
+  CU(s, cudaStreamSynchronize(s->stream));
+  drop_graph(s);  // the captured step has or lacks the channel kernel
+  return channel_set(s, c);
 }
 
 FS_API int fs_set_solids(fs_solver* h, const fs_disk* disks, int count) {
@@ -1516,7 +1534,7 @@ static bool class_plain(const fs_batch* b, const BatchClass& c) {
   const Solver* r = &b->members[c.idx[0]]->s;
   for (int i : c.idx) {
     const Solver* s = &b->members[i]->s;
-    if (s->n_modes > 0 || s->band || !s->disks.empty() || s->dye || s->guess || s->prm.warm_start ||
+    if (s->n_modes > 0 || s->band || s->channel_on || !s->disks.empty() || s->dye || s->guess || s->prm.warm_start ||
         s->prm.advection != r->prm.advection || (s->prm.nu > 0) != (r->prm.nu > 0))
       return false;
   }

@@ -122,6 +122,9 @@ struct Solver {
 
   // band-limited random forcing renewed every step (fs_band.cu), or null
   void* band = nullptr;
+  // channel walls and inflow fringe (fs_channel.cu)
+  fs_channel channel{};
+  bool channel_on = false;
   // forcing (solver.js:370-385)
   float* modes = nullptr;  // kx, ky, phase triplets
   int n_modes = 0;
@@ -222,6 +225,9 @@ void launch_forcing(Solver* s, float* u, float* v, float dt);
 int upload_disks(Solver* s);
 void launch_solids(Solver* s, float* u, float* v, float dt, bool record_impulse);
 void launch_advect_dye(Solver* s, float dt);
+// fs_channel.cu
+int channel_set(Solver* s, const fs_channel* c);  // null: remove
+void launch_channel(Solver* s, float* u, float* v);
 // fs_band.cu
 int band_set(Solver* s, const fs_band* band);  // null: remove
 void band_free(Solver* s);

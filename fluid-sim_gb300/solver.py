@@ -209,6 +209,16 @@ class GPUFluidSolver:
         b = L.Band(self.BAND_KINDS[kind], kf, width, amplitude, seed, drag)
         self._chk(self._lib.fs_set_band_forcing(self._h, C.byref(b)))
 
+    def set_channel(self, channel: dict | None) -> None:
+        """Channel walls and inflow fringe (fs_set_channel): a dict with
+        wall_y, wall_half, fringe_x, fringe_half, fringe_ramp, inflow_u, or
+        None to remove them."""
+        if channel is None:
+            self._chk(self._lib.fs_set_channel(self._h, None))
+            return
+        c = L.Channel(**channel)
+        self._chk(self._lib.fs_set_channel(self._h, C.byref(c)))
+
     def set_solids(self, disks: Iterable) -> None:
         """setSolid(disk) generalised to several disks (solver.js:425-438)"""
         disks = list(disks or [])

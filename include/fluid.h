@@ -228,6 +228,28 @@ typedef struct fs_band {
  * draws at 0.  Drops the captured step. */
 FS_API int fs_set_band_forcing(fs_solver* s, const fs_band* band);
 
+/* A channel with inflow, outflow and no-slip walls on the periodic grid.  No
+ * counterpart in the reference, which is periodic only (README.md:139); the
+ * walls use the reference's immersed-disk direct forcing
+ * (src/cpu/solid.js:165-233) on a slab instead of a disk, and the inflow /
+ * outflow a fringe strip (the fringe-region method of spectral channel
+ * codes).  Each step, after the forces and before the disks:
+ *   fringe: chi_f = 1/2 (1 - tanh((|x - fringe_x| - fringe_half) / fringe_ramp))
+ *           u += chi_f (inflow_u - u), v += chi_f (0 - v)   where chi_f >= 1e-6
+ *   walls:  chi_w = 1/2 (1 - tanh((|y - wall_y| - wall_half) / w)),
+ *           w = solid_mask_width cells;
+ *           u += chi_w (0 - u), v += chi_w (0 - v)          where chi_w >= 1e-6
+ * at each face's position (distances periodic).  The slab's two edges are
+ * the walls; flow leaves through the fringe and re-enters past it as the
+ * uniform inflow u = inflow_u.  The pressure stays periodic. */
+typedef struct fs_channel {
+  double wall_y, wall_half;                     /* wall slab centre and half-thickness (y) */
+  double fringe_x, fringe_half, fringe_ramp;    /* fringe centre, half-width, ramp width (x) */
+  double inflow_u;                              /* U_in */
+} fs_channel;
+/* c == NULL removes it; drops the captured step */
+FS_API int fs_set_channel(fs_solver* s, const fs_channel* c);
+
 /* setSolid(disk) (solver.js:425-438), generalised to count disks applied in
  * order (src/cpu/solid.js:181-230); count == 0 removes them */
 FS_API int fs_set_solids(fs_solver* s, const fs_disk* disks, int count);

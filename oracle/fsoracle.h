@@ -144,6 +144,15 @@ void fso_disk_integrate(fso_disk* d, double dt, double gravity);
 void fso_apply_coupling(const fso_grid* g, double* u, double* v, fso_disk* solids, int n_solids,
                         double dt, double mask_width, int passes, double* impulse_out);
 
+/* A channel on the periodic grid (no reference counterpart; the reference is
+ * periodic only): a fringe strip driving (u, v) to (inflow_u, 0), then a
+ * no-slip wall slab, both as direct forcing with the reference disks' tanh
+ * mask (src/cpu/solid.js:101-114,165-233) on a slab instead of a disk. */
+typedef struct {
+  double wall_y, wall_half, fringe_x, fringe_half, fringe_ramp, inflow_u;
+} fso_channel;
+void fso_channel_forcing(const fso_grid* g, double* u, double* v, const fso_channel* c, double mask_width);
+
 /* --------------------------------------------------------------- solver */
 enum { FSO_PROJ_CG = 0, FSO_PROJ_FFT = 1, FSO_PROJ_JACOBI = 2 };
 typedef struct {
@@ -166,6 +175,8 @@ const fso_grid* fso_solver_grid(fso_solver* s);
 int fso_add_solid(fso_solver* s, const fso_disk* d);
 fso_disk* fso_get_solid(fso_solver* s, int i);
 void fso_set_modes(fso_solver* s, const fso_mode* modes, int m, double amp, double drag, double drift);
+/* c == NULL removes it; applied after the forces and drag, before the disks */
+void fso_set_channel(fso_solver* s, const fso_channel* c);
 /* step: advect, diffuse, forces (gpu-style modes if set), drag, solids, project, dye.
  * band_seed > 0 applies bandForcing(kf, width, amp) as opts.force. */
 typedef struct {

@@ -1011,6 +1011,8 @@ struct fso_solver {
   int n_modes;
   fso_mode* modes;
   double mode_amp, mode_drag, mode_drift;
+  int channel_on;
+  fso_channel channel;
 };
 
 /* defaults of src/cpu/solver.js:250-260 */
@@ -1083,6 +1085,30 @@ void fso_set_modes(fso_solver* s, const fso_mode* modes, int m, double amp, doub
   s->n_modes = m; s->mode_amp = amp; s->mode_drag = drag; s->mode_drift = drift;
 }
 
+void fso_set_channel(fso_solver* s, const fso_channel* c) {
+  s->channel_on = c != NULL;
+  if (c) s->channel = *c;
+}
+
+/* 1/2 (1 - tanh((|d| - half) / w)), the disk mask's profile across a slab */
+static double slab_chi(double d, double half, double w) { return 0.5 * (1 - tanh((fabs(d) - half) / w)); }
+
+void fso_channel_forcing(const fso_grid* g, double* u, double* v, const fso_channel* c, double mask_width) {
+  const double w = mask_width * g->dx;
+  for (int j = 0; j < g->ny; j++)
+    for (int i = 0; i < g->nx; i++) {
+      int64_t k = IDX(g, i, j);
+      double cu = slab_chi(wrap_delta(uX(g, i) - c->fringe_x, g->lx), c->fringe_half, c->fringe_ramp);
+      double cv = slab_chi(wrap_delta(vX(g, i) - c->fringe_x, g->lx), c->fringe_half, c->fringe_ramp);
+      if (cu >= 1e-6) u[k] += cu * (c->inflow_u - u[k]);
+      if (cv >= 1e-6) v[k] += cv * (0.0 - v[k]);
+      cu = slab_chi(wrap_delta(uY(g, j) - c->wall_y, g->ly), c->wall_half, w);
+      cv = slab_chi(wrap_delta(vY(g, j) - c->wall_y, g->ly), c->wall_half, w);
+      if (cu >= 1e-6) u[k] += cu * (0.0 - u[k]);
+      if (cv >= 1e-6) v[k] += cv * (0.0 - v[k]);
+    }
+}
+
 static void swap_ptr(double** a, double** b) { double* t = *a; *a = *b; *b = t; }
 
 /* src/cpu/solver.js:336-398 */
@@ -1109,6 +1135,7 @@ void fso_step(fso_solver* s, double dt, const fso_step_opts* o) {
     fso_forcing_modes(g, s->u, s->v, s->modes, s->n_modes, s->mode_amp, s->mode_drag,
                       s->mode_drift * s->t, dt);
   if (o->drag > 0) fso_linear_drag(s->u, s->v, n, o->drag, dt);
+  if (s->channel_on) fso_channel_forcing(g, s->u, s->v, &s->channel, s->prm.mask_width);
 
   if (s->n_solids) {
     fso_apply_coupling(g, s->u, s->v, s->solids, s->n_solids, dt, s->prm.mask_width,

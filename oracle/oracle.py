@@ -52,6 +52,11 @@ class StepOpts(C.Structure):
                 ("band_key", C.c_uint64), ("band_counter", C.c_uint32)]
 
 
+class Channel(C.Structure):
+    _fields_ = [("wall_y", C.c_double), ("wall_half", C.c_double), ("fringe_x", C.c_double),
+                ("fringe_half", C.c_double), ("fringe_ramp", C.c_double), ("inflow_u", C.c_double)]
+
+
 class Disk(C.Structure):
     _fields_ = [("x", C.c_double), ("y", C.c_double), ("r", C.c_double), ("density", C.c_double),
                 ("vx", C.c_double), ("vy", C.c_double), ("omega", C.c_double),
@@ -114,6 +119,8 @@ def lib():
             "fso_diffuse": (I, [C.POINTER(Grid), DP, DP, D, D, I, D, DP]),
             "fso_linear_drag": (None, [DP, DP, C.c_int64, D, D]),
             "fso_band_forcing": (None, [C.POINTER(Grid), DP, DP, D, D, D, C.c_uint32, D]),
+            "fso_channel_forcing": (None, [C.POINTER(Grid), DP, DP, C.POINTER(Channel), D]),
+            "fso_set_channel": (None, [VP, C.POINTER(Channel)]),
             "fso_gauss_band_forcing": (None, [C.POINTER(Grid), DP, DP, D, D, D, C.c_uint64, C.c_uint32, D]),
             "fso_philox4x32_10": (None, [C.POINTER(C.c_uint32), C.POINTER(C.c_uint32), C.POINTER(C.c_uint32)]),
             "fso_forcing_modes": (None, [C.POINTER(Grid), DP, DP, C.POINTER(Mode), I, D, D, D, D]),
@@ -360,6 +367,11 @@ def gauss_band_forcing(g: Grid, u, v, kf, width, amp, key, counter, dt):
     lib().fso_gauss_band_forcing(C.byref(g), _p(u), _p(v), kf, width, amp, key, counter, dt)
 
 
+def channel_forcing(g: Grid, u, v, channel: dict, mask_width: float = 1.5):
+    """The channel's fringe and wall forcing applied to u, v in place."""
+    lib().fso_channel_forcing(C.byref(g), _p(u), _p(v), C.byref(Channel(**channel)), mask_width)
+
+
 def set_threads(n: int) -> None:
     lib().fso_set_threads(int(n))
 
@@ -437,6 +449,10 @@ class CpuSolver:
     def set_forcing(self, modes, amplitude=1.0, drag=0.0, phase_drift=0.3):
         arr = (Mode * len(modes))(*[Mode(m[0], m[1], m[2]) for m in modes])
         lib().fso_set_modes(self._h, arr, len(modes), amplitude, drag, phase_drift)
+
+    def set_channel(self, channel):
+        """channel: dict of fso_channel fields, or None to remove it"""
+        lib().fso_set_channel(self._h, C.byref(Channel(**channel)) if channel else None)
 
     def step(self, dt, advect_dye=True, drag=0.0, gravity=0.0, band=None, gauss_band=None):
         """band = (kf, width, amp, seed): bandForcing as opts.force;

@@ -1,12 +1,13 @@
 """The benchmark's own configuration against the f64 oracle.
 
-The bench step is the periodic stream past seeded disks (fluid-sim_gb300/
-workload.py, seed 5: five disks), MacCormack advection, explicit diffusion
+The bench step is the channel flow past seeded disks (fluid-sim_gb300/
+workload.py channel_workload, seed 5: inflow u = 1 through the fringe,
+no-slip walls, five disks), MacCormack advection, explicit diffusion
 nu = 1e-4, dt at CFL 0.5, the mixed-precision multigrid projection with
 red-black relaxation 1.2 iterated to max|div u| <= 1e-6 after every step.
 The oracle is the f64 CPU solver (restatement of src/cpu/solver.js:336-398:
-MacCormack, explicit diffusion, exact FFT projection, one direct-forcing pass
-per disk) from the same initial state.  Per field, relative L2 <= 1e-5 (the
+MacCormack, explicit diffusion, exact FFT projection, the same channel
+forcing, one direct-forcing pass per disk) from the same initial state.  Per field, relative L2 <= 1e-5 (the
 tolerance of the f32 advection paths) and relative L-inf <= 1e-4; every
 projection of the run met the tolerance (the device-side convergence record,
 not just the last step's flag).
@@ -32,7 +33,7 @@ def pkg(fs):
 
 
 def _run(pkg, O, n, steps, tiles=None):
-    u0, v0, disks, dt = pkg.workload.make_workload(n, 5)
+    u0, v0, disks, dt, ch = pkg.workload.channel_workload(n, 5)
     assert len(disks) == 5
     s = pkg.GPUFluidSolver(n=n, nu=NU, advection="maccormack", pressure_solver="multigrid", pressure_iterations=1,
                            precision="mixed", pressure_tol=TOL, max_cycles=60, relax=RELAX)
@@ -40,6 +41,7 @@ def _run(pkg, O, n, steps, tiles=None):
         s.set_mg_tiles(tiles)
         assert s.mg_tiles()[0] == tiles[0]
     s.upload_velocity(u0, v0)
+    s.set_channel(ch)
     s.set_solids(disks)
     for _ in range(steps):
         s.step(dt)
@@ -53,6 +55,7 @@ def _run(pkg, O, n, steps, tiles=None):
                       coupling_passes=1)
     cpu.u[:] = u0
     cpu.v[:] = v0
+    cpu.set_channel(ch)
     for d in disks:
         cpu.add_solid(O.disk(d[0], d[1], d[2], density=8, fixed=True))
     for _ in range(steps):
