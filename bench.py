@@ -203,13 +203,20 @@ GUESS_WEIGHTS = ROOT / "fluid-sim_gb300" / "weights" / "guess_2048_f2.fsguess"
 GUESS_FACTOR = 2
 
 
-def make_solver(pkg, n, device, guess="zero", relax=RELAX):
+# red-black sweeps on the coarsest (8^2) multigrid level.  The reference runs
+# 40; at 2048^2 the channel flow needs the same 5 cycles per step with 8, and
+# the step is 1.4% faster (same-box A/B, 0.845 -> 0.833 ms)
+COARSE_SWEEPS = 8
+
+
+def make_solver(pkg, n, device, guess="zero", relax=RELAX, coarse=None):
     """guess: "zero" (the reference's zero initial pressure), "warm" (the
     previous step's pressure) or "nn" (the trained pressure-guess network at
     half resolution, weights committed under fluid-sim_gb300/weights/)."""
     s = pkg.GPUFluidSolver(n=n, nu=NU, advection="maccormack", pressure_solver="multigrid",
                            pressure_iterations=1, precision="mixed", pressure_tol=TOL, max_cycles=60,
-                           warm_start=(guess == "warm"), device=device, relax=relax)
+                           warm_start=(guess == "warm"), device=device, relax=relax,
+                           mg_coarse_sweeps=COARSE_SWEEPS if coarse is None else coarse)
     if guess == "nn":
         g = pkg.PressureGuess(device=device)
         g.load(GUESS_WEIGHTS)
@@ -417,6 +424,7 @@ def run_gpu(args):
                             f"(red-black relaxation {args.relax}) iterated to "
                             f"max|div u| <= {TOL}",
                 "n": n, "disks": len(disks), "dt": dt, "tol": TOL, "guess": args.guess, "relax": args.relax,
+                "coarse_sweeps": args.coarse_sweeps,
                 "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
                 "l2": "working set ~0.35 GB > 129 MB L2; no flush between steps",
                 "cycles_per_step": cycles_timed,
@@ -635,12 +643,15 @@ def main():
                     help="also time a batch of this many uneven domains (0 = skip)")
     ap.add_argument("--no-variants", action="store_true",
                     help="skip timing the learned guess and the warm start beside the headline")
+    ap.add_argument("--coarse-sweeps", type=int, default=COARSE_SWEEPS,
+                    help="red-black sweeps on the coarsest multigrid level (the reference runs 40)")
     ap.add_argument("--forced-steps", type=int, default=5000,
                     help="steps of the 1024^2 forced-turbulence run (spectrum every 100; 0 = skip)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-field-error", action="store_true",
                     help="skip the comparison of u, v after a few steps with the f64 oracle")
     args = ap.parse_args()
+    globals()["COARSE_SWEEPS"] = args.coarse_sweeps
     if args.warmup < 3 and args.impl != "reference":
         args.warmup = 3
     if args.impl == "reference":

@@ -241,6 +241,7 @@ __device__ __forceinline__ void mg_down_body(float* smem, const float* __restric
   // multiples of 4), so its rows, the rows above and below it and its rhs
   // come as float2 pairs: 10 loads per block instead of 16.
   const int nc = n >> 1;
+  const float ih2 = inv_h2(h2);
   for (int k = tid; k < (T / 2) * (T / 2); k += nthr) {
     const int cj = k / (T / 2), ci = k - cj * (T / 2);
     const int off = (H + 2 * cj) * B::W + B::LP + 2 * ci;
@@ -252,10 +253,10 @@ __device__ __forceinline__ void mg_down_body(float* smem, const float* __restric
     const float2 xt = *reinterpret_cast<const float2*>(X + 2 * B::W);
     const float2 q0 = *reinterpret_cast<const float2*>(Q);
     const float2 q1 = *reinterpret_cast<const float2*>(Q + B::W);
-    const float r00 = residual_at(x0.x, X[-1], x0.y, xb.x, x1.x, q0.x, h2);
-    const float r10 = residual_at(x0.y, x0.x, X[2], xb.y, x1.y, q0.y, h2);
-    const float r01 = residual_at(x1.x, X[B::W - 1], x1.y, x0.x, xt.x, q1.x, h2);
-    const float r11 = residual_at(x1.y, x1.x, X[B::W + 2], x0.y, xt.y, q1.y, h2);
+    const float r00 = residual_at(x0.x, X[-1], x0.y, xb.x, x1.x, q0.x, ih2);
+    const float r10 = residual_at(x0.y, x0.x, X[2], xb.y, x1.y, q0.y, ih2);
+    const float r01 = residual_at(x1.x, X[B::W - 1], x1.y, x0.x, xt.x, q1.x, ih2);
+    const float r11 = residual_at(x1.y, x1.x, X[B::W + 2], x0.y, xt.y, q1.y, ih2);
     const int gci = (i0 >> 1) + ci, gcj = (j0 >> 1) + cj;
     if (gci < nc && gcj < nc) crhs[(int64_t)gcj * nc + gci] = restrict4(r00, r10, r01, r11);
   }
@@ -499,7 +500,7 @@ __device__ __forceinline__ void bottom_smooth(float* sm, const BottomLevels& L, 
 
 __device__ __forceinline__ void bottom_restrict(float* sm, const BottomLevels& L, int l, Group G) {
   const int n = L.n[l], nc = L.n[l + 1];
-  const float h2 = L.h2[l];
+  const float ih2 = inv_h2(L.h2[l]);
   const float* x = sm + L.off_x[l];
   const float* r = sm + L.off_r[l];
   float* cr = sm + L.off_r[l + 1];
@@ -511,7 +512,7 @@ __device__ __forceinline__ void bottom_restrict(float* sm, const BottomLevels& L
       int i = 2 * ci + (q & 1), j = 2 * cj + (q >> 1);
       int im = i == 0 ? n - 1 : i - 1, ip = i + 1 == n ? 0 : i + 1;
       int jm = j == 0 ? n - 1 : j - 1, jp = j + 1 == n ? 0 : j + 1;
-      r4[q] = residual_at(x[j * n + i], x[j * n + im], x[j * n + ip], x[jm * n + i], x[jp * n + i], r[j * n + i], h2);
+      r4[q] = residual_at(x[j * n + i], x[j * n + im], x[j * n + ip], x[jm * n + i], x[jp * n + i], r[j * n + i], ih2);
     }
     cr[k] = restrict4(r4[0], r4[1], r4[2], r4[3]);
     cx[k] = 0.f;
@@ -668,6 +669,7 @@ __device__ __forceinline__ void p2_restrict(const float* x, const float* r, floa
   constexpr int NC = N / 2;
   const int tid = WARP ? (int)(threadIdx.x & 31) : (int)threadIdx.x;
   const int nthr = WARP ? 32 : (int)blockDim.x;
+  const float ih2 = inv_h2(h2);
   for (int k = tid; k < NC * NC; k += nthr) {
     const int cj = k / NC, ci = k - cj * NC;
     float r4[4];
@@ -677,7 +679,7 @@ __device__ __forceinline__ void p2_restrict(const float* x, const float* r, floa
       const int row = j * N;
       const int rm = (j == 0 ? N - 1 : j - 1) * N, rp = (j + 1 == N ? 0 : j + 1) * N;
       const int im = i == 0 ? N - 1 : i - 1, ip = i + 1 == N ? 0 : i + 1;
-      r4[q] = residual_at(x[row + i], x[row + im], x[row + ip], x[rm + i], x[rp + i], r[row + i], h2);
+      r4[q] = residual_at(x[row + i], x[row + im], x[row + ip], x[rm + i], x[rp + i], r[row + i], ih2);
     }
     cr[k] = restrict4(r4[0], r4[1], r4[2], r4[3]);
     cx[k] = 0.f;

@@ -124,7 +124,7 @@ __global__ void __launch_bounds__(256) k_residual(const float* __restrict__ x, c
   int jm = j == 0 ? n - 1 : j - 1, jp = j + 1 == n ? 0 : j + 1;
   int64_t r = (int64_t)j * n;
   o[r + i] = residual_at(__ldg(x + r + i), __ldg(x + r + im), __ldg(x + r + ip), __ldg(x + (int64_t)jm * n + i),
-                         __ldg(x + (int64_t)jp * n + i), __ldg(rhs + r + i), h2);
+                         __ldg(x + (int64_t)jp * n + i), __ldg(rhs + r + i), inv_h2(h2));
 }
 
 void launch_residual(Solver* s, const float* x, const float* rhs, float* out, float h2, int n) {

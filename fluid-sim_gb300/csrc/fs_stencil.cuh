@@ -26,11 +26,17 @@ __device__ __forceinline__ float gs_update(float cur, float l, float r, float b,
   return __fadd_rn(cur, __fmul_rn(w, __fsub_rn(gs, cur)));
 }
 
-// rhs - (l + r + b + t - 4c) / h2
-__device__ __forceinline__ float residual_at(float c, float l, float r, float b, float t, float rhs, float h2) {
-  float lap = __fdiv_rn(__fmaf_rn(-4.f, c, sum4(l, r, b, t)), h2);
+// rhs - (l + r + b + t - 4c) / h2, the division taken as a product with
+// ih2 = RN(1/h2) (inv_h2): the reference's WGSL divide is itself not
+// correctly rounded (2.5 ulp allowed), and a correctly rounded divide per cell
+// costs the tile kernels several instructions where one multiply does
+__device__ __forceinline__ float residual_at(float c, float l, float r, float b, float t, float rhs, float ih2) {
+  float lap = __fmul_rn(__fmaf_rn(-4.f, c, sum4(l, r, b, t)), ih2);
   return __fsub_rn(rhs, lap);
 }
+
+// the reciprocal every residual_at caller passes: RN(1 / h2)
+__device__ __forceinline__ float inv_h2(float h2) { return __frcp_rn(h2); }
 
 // a (1 - t) + b t
 __device__ __forceinline__ float mix_rn(float a, float b, float t) {

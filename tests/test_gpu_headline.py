@@ -4,7 +4,8 @@ The bench step is the channel flow past seeded disks (fluid-sim_gb300/
 workload.py channel_workload, seed 5: inflow u = 1 through the fringe,
 no-slip walls, five disks), MacCormack advection, explicit diffusion
 nu = 1e-4, dt at CFL 0.5, the mixed-precision multigrid projection with
-red-black relaxation 1.2 iterated to max|div u| <= 1e-6 after every step.
+red-black relaxation 1.2 and 8 sweeps on the coarsest level iterated to
+max|div u| <= 1e-6 after every step.
 The oracle is the f64 CPU solver (restatement of src/cpu/solver.js:336-398:
 MacCormack, explicit diffusion, exact FFT projection, the same channel
 forcing, one direct-forcing pass per disk) from the same initial state.  Per field, relative L2 <= 1e-5 (the
@@ -23,7 +24,7 @@ import pytest
 
 pytestmark = pytest.mark.gpu
 
-NU, TOL, RELAX = 1e-4, 1e-6, 1.2
+NU, TOL, RELAX, COARSE = 1e-4, 1e-6, 1.2, 8
 
 
 @pytest.fixture(scope="module")
@@ -36,7 +37,8 @@ def _run(pkg, O, n, steps, tiles=None):
     u0, v0, disks, dt, ch = pkg.workload.channel_workload(n, 5)
     assert len(disks) == 5
     s = pkg.GPUFluidSolver(n=n, nu=NU, advection="maccormack", pressure_solver="multigrid", pressure_iterations=1,
-                           precision="mixed", pressure_tol=TOL, max_cycles=60, relax=RELAX)
+                           precision="mixed", pressure_tol=TOL, max_cycles=60, relax=RELAX,
+                           mg_coarse_sweeps=COARSE)
     if tiles is not None:
         s.set_mg_tiles(tiles)
         assert s.mg_tiles()[0] == tiles[0]
