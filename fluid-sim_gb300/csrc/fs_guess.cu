@@ -13,9 +13,9 @@
 // copy, flattened layer by layer as w[co][ci][3][3] then b[co]) and repacked
 // to bf16 after every update, once in the forward layout and once transposed
 // and flipped, so that the gradient with respect to a layer's input is the
-// same tensor-core convolution.  Weight gradients are a correlation over all
-// pixels, done on the FP32 cores with register blocking and deterministic
-// per-CTA partials.
+// same tensor-core convolution.  Weight gradients are a tcgen05 GEMM too,
+// with the pixels as its K dimension (k_wgrad_tc), and deterministic per-CTA
+// partial sums.
 //
 // Normalisation (the guess is linear-equivariant in the divergence): with
 // h the net's grid spacing and sigma = RMS(h^2 d), the input is h^2 d / sigma
@@ -27,6 +27,7 @@
 #include <stdio.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstring>
 #include <string>
@@ -36,6 +37,7 @@
 #include "fs_df.cuh"
 #include "fs_internal.cuh"
 #include "fs_reduce.cuh"
+#include "fs_tc.cuh"
 
 namespace fs {
 namespace conv {
@@ -67,7 +69,6 @@ constexpr int kBufLevel[NBUF] = {0, 0, 0, 1, 1, 2, 2, 3, 3, 3, 2, 2, 1, 1, 0, 0,
 constexpr int kBufCh[NBUF] = {16, 16, 16, 16, 32, 32, 64, 64, 128, 64, 64, 32, 32, 16, 16, 16,
                               16, 16, 16, 16, 32, 32, 64, 64, 128, 64, 32, 16, 16};
 
-constexpr int kCorrCTAs = 152 * 2;
 
 struct Net {
   int device = 0;
@@ -298,111 +299,221 @@ __global__ void k_loss_seed(const float* __restrict__ out, const float* __restri
   }
 }
 
-// ------------------------------------------------------ weight gradients
-// dW[co][ci][ky][kx] = sum_p G[p][co] X[p + (ky-1, kx-1)][ci],  db[co] = sum_p G[p][co].
-// Thread blocks of 4 ci x 4 co for one tap (16 accumulators); a CTA owns up
-// to 256 such blocks (blockIdx.y picks the group) and a strided share of the
-// 8 x 16-pixel tiles (blockIdx.x); partials go to part[x][block * 16 + i*4 + j]
-// and k_corr_reduce adds them in a fixed order.  The bias blocks come after
-// the weight blocks and use X = 1.
-constexpr int kCTY = 8, kCTX = 16;
-__global__ void __launch_bounds__(256) k_corr(const bf* __restrict__ X, const bf* __restrict__ G, int B, int H, int W,
-                                              int cin, int cout, float* __restrict__ part) {
-  extern __shared__ __align__(16) unsigned char csm[];
-  bf* xs = reinterpret_cast<bf*>(csm);                                   // [10][18][cin]
-  bf* gs = reinterpret_cast<bf*>(csm + (kCTY + 2) * (kCTX + 2) * cin * 2);  // [8][16][cout]
-  const int ci4 = cin / 4, co4 = cout / 4;
-  const int nbw = 9 * ci4 * co4, nb = nbw + co4;
-  const int blk = blockIdx.y * 256 + threadIdx.x;
-  const bool active = blk < nb;
-  int tap = 0, c0 = 0, o0 = 0;
-  bool is_bias = false;
-  if (active) {
-    if (blk < nbw) {
-      tap = blk / (ci4 * co4);
-      int r = blk % (ci4 * co4);
-      c0 = 4 * (r / co4);
-      o0 = 4 * (r % co4);
-    } else {
-      is_bias = true;
-      o0 = 4 * (blk - nbw);
+// ------------------------------------------ weight gradients on tcgen05
+// dW[co][ci][tap] = sum_p G[p][co] X[p + s_tap][ci] as a GEMM with K = pixels:
+// D[m][n] += sum_k A[m][k] B[n][k], rows m = tap * CIN + ci of the shifted
+// input X (A), n = co of the output gradient G (B), accumulated in TMEM over
+// every pixel a CTA visits.  Rows are packed nine taps deep, so M-blocks of
+// 128 rows cover 9 CIN rows (two blocks for 16 input channels, nine for 128);
+// a CTA owns NMB consecutive M-blocks (blockIdx.y picks the group) so that
+// its accumulators fit the 512 TMEM columns.  Both operands are NHWC bf16 in
+// global memory (channels contiguous); the CTA stages them K-major (pixels
+// contiguous per row) by transposing blocks of 8 pixels x 8 channels in
+// registers, into the no-swizzle core-matrix layout of fs_tc_gemm_check (LBO
+// 128, SBO 256 bytes).  Per-CTA partial sums (and the bias sums of G, by the
+// CTAs of blockIdx.y == 0) go to global memory; k_wgrad_reduce adds them in a
+// fixed order, so the gradient is deterministic.
+constexpr int kWgThreads = 128;
+constexpr int kWgTile = 128;  // pixels per K tile
+
+template <int CIN, int COUT, int NMB>
+struct WgCfg {
+  static constexpr int MROWS = 9 * CIN;                    // rows of D
+  static constexpr int MBLK = (MROWS + 127) / 128;         // M-blocks in all
+  static constexpr int A_BYTES = NMB * 128 * kWgTile * 2;  // this CTA's A operand
+  static constexpr int B_BYTES = COUT * kWgTile * 2;
+  static constexpr int SMEM = A_BYTES + B_BYTES + 128;     // + barrier, TMEM slot, flag
+  static constexpr int NCOL_USED = NMB * COUT;
+  static constexpr int NCOL = NCOL_USED <= 32    ? 32
+                              : NCOL_USED <= 64  ? 64
+                              : NCOL_USED <= 128 ? 128
+                              : NCOL_USED <= 256 ? 256
+                                                 : 512;
+  static_assert(NCOL_USED <= 512 && COUT % 16 == 0 && CIN % 8 == 0, "TMEM columns, channel counts");
+};
+
+// 8 rows of 8 bf16 (r[i] = pixel i, channels 0..7) -> t[c] = channel c, pixels 0..7
+__device__ __forceinline__ void transpose8x8(const uint4* r, uint4* t) {
+  const uint32_t* w = reinterpret_cast<const uint32_t*>(r);  // w[4 i + j]: pixel i, channels 2j, 2j+1
+  uint32_t* o = reinterpret_cast<uint32_t*>(t);               // o[4 c + j']: channel c, pixels 2j', 2j'+1
+#pragma unroll
+  for (int j = 0; j < 4; j++)
+#pragma unroll
+    for (int jp = 0; jp < 4; jp++) {
+      const uint32_t a = w[4 * (2 * jp) + j], b = w[4 * (2 * jp + 1) + j];
+      o[4 * (2 * j) + jp] = __byte_perm(a, b, 0x5410);
+      o[4 * (2 * j + 1) + jp] = __byte_perm(a, b, 0x7632);
     }
+}
+
+// byte offset of the 8x8 block (rows 8g.., pixels 8q..) of a K-major operand of R rows
+__device__ __forceinline__ int kmaj_block(int R, int g, int q) { return (q >> 1) * (R * 32) + g * 256 + (q & 1) * 128; }
+
+template <int CIN, int COUT, int NMB>
+__global__ void __launch_bounds__(kWgThreads) k_wgrad_tc(const uint4* __restrict__ X, const uint4* __restrict__ G,
+                                                         int B, int H, int W, float* __restrict__ part,
+                                                         float* __restrict__ bpart, int* __restrict__ err) {
+  using C = WgCfg<CIN, COUT, NMB>;
+  extern __shared__ __align__(128) unsigned char smem[];
+  unsigned char* sa = smem;
+  unsigned char* sb = smem + C::A_BYTES;
+  uint64_t* bar = reinterpret_cast<uint64_t*>(smem + C::A_BYTES + C::B_BYTES);
+  uint32_t* tslot = reinterpret_cast<uint32_t*>(bar + 1);
+  int* failed = reinterpret_cast<int*>(bar + 2);
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int mb0 = blockIdx.y * NMB;  // first M-block of this CTA
+  const int64_t npix = (int64_t)B * H * W, ntiles = (npix + kWgTile - 1) / kWgTile;
+  constexpr int KC = CIN / 8, OC = COUT / 8;
+  if (warp == 0) {
+    tc::tmem_alloc(tslot, C::NCOL);
+    tc::tmem_relinquish();
+    tc::fence_before_sync();
   }
-  const int ky = tap / 3, kx = tap % 3;
-  float acc[16] = {};
-  const int ntx = (W + kCTX - 1) / kCTX, nty = (H + kCTY - 1) / kCTY;
-  const int64_t ntiles = (int64_t)B * nty * ntx;
-  const int cin8 = cin / 8, cout8 = cout / 8;
+  if (tid == 0) {
+    tc::mbar_init(bar, 1);
+    tc::mbar_fence_init();
+    *failed = 0;
+  }
+  __syncthreads();
+  tc::fence_after_sync();
+  const uint32_t taddr = *tslot;
+  const uint32_t sa_s = tc::smem_u32(sa), sb_s = tc::smem_u32(sb);
+  constexpr uint32_t IDESC = tc::idesc_bf16(128, COUT);
+  float bsum = 0.f;  // bias partial of output channel tid (tid < COUT, blockIdx.y == 0)
+  uint32_t phase = 0;
+  int issued = 0;
   for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
-    const int tx = (int)(t % ntx), ty = (int)((t / ntx) % nty), b = (int)(t / ((int64_t)ntx * nty));
-    const int x0 = tx * kCTX, y0 = ty * kCTY;
-    __syncthreads();
-    for (int k = threadIdx.x; k < (kCTY + 2) * (kCTX + 2) * cin8; k += 256) {
-      int c = k % cin8, r = k / cin8;
-      int xx = r % (kCTX + 2), yy = r / (kCTX + 2);
-      int gy = (y0 - 1 + yy) % H, gx = (x0 - 1 + xx) % W;
-      gy = gy < 0 ? gy + H : gy;
-      gx = gx < 0 ? gx + W : gx;
-      reinterpret_cast<uint4*>(xs)[k] =
-          reinterpret_cast<const uint4*>(X)[(((int64_t)b * H + gy) * W + gx) * cin8 + c];
+    const int64_t p0 = t * kWgTile;
+    if (issued) {
+      // the MMAs of the previous tile read the staging buffers
+      if (tid == 0 && !tc::mbar_wait(bar, phase)) *failed = 1;
+      phase ^= 1;
+      __syncthreads();
+      if (*failed) break;
     }
-    for (int k = threadIdx.x; k < kCTY * kCTX * cout8; k += 256) {
-      int c = k % cout8, r = k / cout8;
-      int xx = r % kCTX, yy = r / kCTX;
-      int gy = y0 + yy, gx = x0 + xx;
-      uint4 v = make_uint4(0, 0, 0, 0);
-      if (gy < H && gx < W) v = reinterpret_cast<const uint4*>(G)[(((int64_t)b * H + gy) * W + gx) * cout8 + c];
-      reinterpret_cast<uint4*>(gs)[k] = v;
+    // B: G[p][co] -> rows co, K = pixels (zero beyond the last pixel)
+    for (int k = tid; k < (kWgTile / 8) * OC; k += kWgThreads) {
+      const int q = k / OC, oc = k - q * OC;
+      uint4 r[8];
+#pragma unroll
+      for (int i = 0; i < 8; i++) {
+        const int64_t p = p0 + 8 * q + i;
+        r[i] = p < npix ? G[p * OC + oc] : make_uint4(0, 0, 0, 0);
+      }
+      uint4 tt[8];
+      transpose8x8(r, tt);
+      uint4* dst = reinterpret_cast<uint4*>(sb + kmaj_block(COUT, oc, q));
+#pragma unroll
+      for (int c = 0; c < 8; c++) dst[c] = tt[c];
     }
-    __syncthreads();
-    if (!active) continue;
-    for (int py = 0; py < kCTY; py++) {
-#pragma unroll 4
-      for (int px = 0; px < kCTX; px++) {
-        float xv[4], gv[4];
-        if (is_bias) {
-          xv[0] = 1.f;
-          xv[1] = xv[2] = xv[3] = 0.f;
-        } else {
-          uint2 q = *reinterpret_cast<const uint2*>(xs + ((py + ky) * (kCTX + 2) + px + kx) * cin + c0);
-          float2 a = __bfloat1622float2(*reinterpret_cast<__nv_bfloat162*>(&q.x));
-          float2 c = __bfloat1622float2(*reinterpret_cast<__nv_bfloat162*>(&q.y));
-          xv[0] = a.x; xv[1] = a.y; xv[2] = c.x; xv[3] = c.y;
+    // A: for each row group (tap, input chunk) of this CTA's M-blocks, X at the
+    // tap's shifted pixel (periodic) -> rows ci, K = pixels; padding groups zero
+    for (int k = tid; k < (kWgTile / 8) * NMB * 16; k += kWgThreads) {
+      const int q = k / (NMB * 16), gl = k - q * (NMB * 16);
+      const int gg = mb0 * 16 + gl;  // global row group
+      uint4 r[8];
+      if (gg < 9 * KC) {
+        const int tap = gg / KC, kc = gg - tap * KC, dy = tap / 3 - 1, dx = tap % 3 - 1;
+#pragma unroll
+        for (int i = 0; i < 8; i++) {
+          const int64_t p = p0 + 8 * q + i;
+          uint4 v = make_uint4(0, 0, 0, 0);
+          if (p < npix) {
+            const int64_t b = p / ((int64_t)H * W);
+            const int rem = (int)(p - b * H * W), y = rem / W, x = rem - y * W;
+            int ys = y + dy, xs = x + dx;
+            ys = ys < 0 ? ys + H : (ys >= H ? ys - H : ys);
+            xs = xs < 0 ? xs + W : (xs >= W ? xs - W : xs);
+            v = X[((b * H + ys) * W + xs) * KC + kc];
+          }
+          r[i] = v;
         }
-        uint2 q = *reinterpret_cast<const uint2*>(gs + (py * kCTX + px) * cout + o0);
-        float2 a = __bfloat1622float2(*reinterpret_cast<__nv_bfloat162*>(&q.x));
-        float2 c = __bfloat1622float2(*reinterpret_cast<__nv_bfloat162*>(&q.y));
-        gv[0] = a.x; gv[1] = a.y; gv[2] = c.x; gv[3] = c.y;
+      } else {
 #pragma unroll
-        for (int i = 0; i < 4; i++)
+        for (int i = 0; i < 8; i++) r[i] = make_uint4(0, 0, 0, 0);
+      }
+      uint4 tt[8];
+      transpose8x8(r, tt);
+      const int blk = gl >> 4, g = gl & 15;  // M-block of this CTA, row group in it
+      uint4* dst = reinterpret_cast<uint4*>(sa + blk * (128 * kWgTile * 2) + kmaj_block(128, g, q));
 #pragma unroll
-          for (int j = 0; j < 4; j++) acc[i * 4 + j] = fmaf(xv[i], gv[j], acc[i * 4 + j]);
+      for (int c = 0; c < 8; c++) dst[c] = tt[c];
+    }
+    tc::fence_async_smem();
+    __syncthreads();
+    tc::fence_after_sync();
+    if (tid == 0) {
+#pragma unroll 1
+      for (int j = 0; j < NMB; j++)
+#pragma unroll
+        for (int s = 0; s < kWgTile / 16; s++)
+          tc::mma_bf16(taddr + j * COUT, tc::sdesc(sa_s + j * (128 * kWgTile * 2) + s * (128 * 32), 128, 256),
+                       tc::sdesc(sb_s + s * (COUT * 32), 128, 256), IDESC, (issued || s > 0) ? 1u : 0u);
+      tc::mma_commit(bar);
+    }
+    issued = 1;
+    // bias partial: output channel tid sums its staged row (read only, like the MMAs)
+    if (blockIdx.y == 0 && tid < COUT) {
+#pragma unroll 4
+      for (int q = 0; q < kWgTile / 8; q++) {
+        const uint4 v = *reinterpret_cast<const uint4*>(sb + kmaj_block(COUT, tid >> 3, q) + (tid & 7) * 16);
+        const __nv_bfloat162* h = reinterpret_cast<const __nv_bfloat162*>(&v);
+#pragma unroll
+        for (int e = 0; e < 4; e++) {
+          const float2 f = __bfloat1622float2(h[e]);
+          bsum += f.x + f.y;
+        }
       }
     }
   }
-  if (active) {
-    float* dst = part + ((int64_t)blockIdx.x * nb + blk) * 16;
-#pragma unroll
-    for (int k = 0; k < 16; k++) dst[k] = acc[k];
+  if (tid == 0 && issued) {
+    if (!*failed) {
+      if (!tc::mbar_wait(bar, phase)) *failed = 1;
+    } else {
+      tc::mbar_wait(bar, phase, 1u << 20);  // let what was issued drain before the TMEM is released
+    }
   }
+  if (tid == 0 && *failed) atomicExch(err, 1);
+  __syncthreads();
+  tc::fence_after_sync();
+  const int64_t cta = blockIdx.x;
+  if (!*failed) {
+    const int m = 32 * (warp & 3) + lane;
+    for (int j = 0; j < NMB; j++) {
+      const int row = (mb0 + j) * 128 + m;
+#pragma unroll 1
+      for (int c0 = 0; c0 < COUT; c0 += 16) {
+        float v[16];
+        tc::tmem_ld16(taddr + ((uint32_t)(32 * (warp & 3)) << 16) + j * COUT + c0, v);
+        if (row < C::MROWS) {
+          float* dst = part + (cta * C::MROWS + row) * COUT + c0;
+#pragma unroll
+          for (int k = 0; k < 16; k++) dst[k] = issued ? v[k] : 0.f;
+        }
+      }
+    }
+    if (blockIdx.y == 0 && tid < COUT) bpart[cta * COUT + tid] = bsum;
+  }
+  tc::fence_before_sync();
+  __syncthreads();
+  if (warp == 0) tc::tmem_dealloc(taddr, C::NCOL);
 }
 
-// grad[off_w + OIHW] / grad[off_b + co] = sum over the P partials
-__global__ void k_corr_reduce(const float* __restrict__ part, int P, int cin, int cout, float* __restrict__ gw,
-                              float* __restrict__ gb) {
-  const int ci4 = cin / 4, co4 = cout / 4;
-  const int nbw = 9 * ci4 * co4, nb = nbw + co4;
-  GRID_STRIDE(e, (int64_t)nb * 16) {
-    const int blk = (int)(e / 16), ij = (int)(e % 16), i = ij / 4, j = ij % 4;
-    if (blk >= nbw && i > 0) continue;
+// grad[off_w + OIHW] = sum over the P partials of row tap * cin + ci, column
+// co; grad[off_b + co] = sum of the bias partials
+__global__ void k_wgrad_reduce(const float* __restrict__ part, const float* __restrict__ bpart, int P, int cin,
+                               int cout, float* __restrict__ gw, float* __restrict__ gb) {
+  const int64_t mrows = 9 * (int64_t)cin, nw = mrows * cout;
+  GRID_STRIDE(e, nw + cout) {
     float s = 0.f;
-    for (int p = 0; p < P; p++) s += part[((int64_t)p * nb + blk) * 16 + ij];
-    if (blk < nbw) {
-      int tap = blk / (ci4 * co4), r = blk % (ci4 * co4);
-      int ci = 4 * (r / co4) + i, co = 4 * (r % co4) + j;
+    if (e < nw) {
+      for (int p = 0; p < P; p++) s += part[(int64_t)p * nw + e];
+      const int row = (int)(e / cout), co = (int)(e % cout), tap = row / cin, ci = row % cin;
       gw[((int64_t)co * cin + ci) * 9 + tap] = s;
     } else {
-      gb[4 * (blk - nbw) + j] = s;
+      const int co = (int)(e - nw);
+      for (int p = 0; p < P; p++) s += bpart[(int64_t)p * cout + co];
+      gb[co] = s;
     }
   }
 }
@@ -575,24 +686,48 @@ static cudaError_t ensure_corr(Net* g, int64_t floats) {
   return cudaSuccess;
 }
 
-static cudaError_t wgrad(const Ctx& c, int l, Buf xbuf, Buf gbuf, int B, int H, int W) {
+template <int CIN, int COUT, int NMB>
+static cudaError_t wgrad_tc(const Ctx& c, int l, Buf xbuf, Buf gbuf, int B, int H, int W) {
+  using C = WgCfg<CIN, COUT, NMB>;
   Net* g = c.g;
-  const int ci = kCI[l], co = kCO[l];
-  const int nb = 9 * (ci / 4) * (co / 4) + co / 4;
-  const int ngroups = (nb + 255) / 256;
-  const int64_t ntiles = (int64_t)B * ((H + kCTY - 1) / kCTY) * ((W + kCTX - 1) / kCTX);
-  int P = kCorrCTAs / ngroups;
-  if (P < 1) P = 1;
-  if (P > ntiles) P = (int)ntiles;
-  CK(ensure_corr(g, (int64_t)P * nb * 16));
-  const int smem = (kCTY + 2) * (kCTX + 2) * ci * 2 + kCTY * kCTX * co * 2;
-  GL(c, "guess_wgrad", (double)(ci + co) * 2 * B * H * W,
-     k_corr<<<dim3(P, ngroups), 256, smem, c.st>>>(g->buf[xbuf], g->buf[gbuf], B, H, W, ci, co, g->corr_part));
+  static std::atomic<uint64_t> attr{0};
+  const uint64_t bit = 1ull << (g->device & 63);
+  if (!(attr.load() & bit)) {
+    CK(cudaFuncSetAttribute(k_wgrad_tc<CIN, COUT, NMB>, cudaFuncAttributeMaxDynamicSharedMemorySize, C::SMEM));
+    attr.fetch_or(bit);
+  }
+  const int groups = (C::MBLK + NMB - 1) / NMB;
+  const int64_t ntiles = ((int64_t)B * H * W + kWgTile - 1) / kWgTile;
+  const int P = (int)std::max<int64_t>(1, std::min<int64_t>(ntiles, 4 * 152 / groups));
+  const int64_t nw = (int64_t)C::MROWS * COUT;
+  CK(ensure_corr(g, (int64_t)P * (nw + COUT)));
+  float* part = g->corr_part;
+  float* bpart = part + (int64_t)P * nw;
+  GL(c, "guess_wgrad", (double)(CIN + COUT) * 2 * B * H * W,
+     (k_wgrad_tc<CIN, COUT, NMB><<<dim3(P, groups), kWgThreads, C::SMEM, c.st>>>(
+         reinterpret_cast<const uint4*>(g->buf[xbuf]), reinterpret_cast<const uint4*>(g->buf[gbuf]), B, H, W, part,
+         bpart, g->err)));
   CK(cudaGetLastError());
-  GL(c, "guess_wgrad_reduce", (double)P * nb * 64,
-     k_corr_reduce<<<blocks_for((int64_t)nb * 16), 256, 0, c.st>>>(g->corr_part, P, ci, co,
-                                                                    g->grad + g->off_w[l], g->grad + g->off_b[l]));
+  GL(c, "guess_wgrad_reduce", (double)P * (nw + COUT) * 4,
+     k_wgrad_reduce<<<blocks_for(nw + COUT), 256, 0, c.st>>>(part, bpart, P, CIN, COUT, g->grad + g->off_w[l],
+                                                            g->grad + g->off_b[l]));
   return cudaGetLastError();
+}
+
+// the (c_in, c_out) pairs of the network, M-blocks per CTA
+static cudaError_t wgrad(const Ctx& c, int l, Buf xbuf, Buf gbuf, int B, int H, int W) {
+  const int ci = kCI[l], co = kCO[l];
+#define FS_WG(a, b, nmb) \
+  if (ci == a && co == b) return wgrad_tc<a, b, nmb>(c, l, xbuf, gbuf, B, H, W);
+  FS_WG(16, 16, 2)
+  FS_WG(16, 32, 2)
+  FS_WG(32, 16, 3)
+  FS_WG(32, 64, 3)
+  FS_WG(64, 128, 3)
+  FS_WG(128, 64, 3)
+  FS_WG(64, 32, 3)
+#undef FS_WG
+  return cudaErrorInvalidValue;
 }
 
 // loss against target (f32 [B][H][W]) and the gradient of every parameter into g->grad
@@ -912,10 +1047,6 @@ extern "C" FS_API int fs_guess_create(int32_t device, uint64_t seed, fs_guess** 
   GA(g->err, 4);
   GA(g->acc, 4096 * 8);
 #undef GA
-  if ((e = cudaFuncSetAttribute(k_corr, cudaFuncAttributeMaxDynamicSharedMemorySize, 96 * 1024)) != cudaSuccess) {
-    fs_guess_destroy(reinterpret_cast<fs_guess*>(g));
-    return gcuda(nullptr, e, "cudaFuncSetAttribute");
-  }
   if ((e = cudaStreamCreateWithFlags(&g->stream, cudaStreamNonBlocking)) != cudaSuccess) {
     fs_guess_destroy(reinterpret_cast<fs_guess*>(g));
     return gcuda(nullptr, e, "cudaStreamCreate");
