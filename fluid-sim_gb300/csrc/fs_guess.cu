@@ -309,20 +309,29 @@ __global__ void k_loss_seed(const float* __restrict__ out, const float* __restri
 // its accumulators fit the 512 TMEM columns.  Both operands are NHWC bf16 in
 // global memory (channels contiguous); the CTA stages them K-major (pixels
 // contiguous per row) by transposing blocks of 8 pixels x 8 channels in
-// registers, into the no-swizzle core-matrix layout of fs_tc_gemm_check (LBO
-// 128, SBO 256 bytes).  Per-CTA partial sums (and the bias sums of G, by the
-// CTAs of blockIdx.y == 0) go to global memory; k_wgrad_reduce adds them in a
-// fixed order, so the gradient is deterministic.
+// registers, into the no-swizzle core-matrix layout of fs_tc_gemm_check with
+// the 8-row groups 272 bytes apart (LBO 128, SBO 272): the 16 bytes of
+// padding per group put neighbouring threads' blocks 16 bytes apart modulo
+// 128, so the eight threads of one 128-bit store phase write eight different
+// bank quads (with SBO 256 every block starts on the same banks).  Per-CTA
+// partial sums (and the bias sums of G, by the CTAs of blockIdx.y == 0) go to
+// global memory; k_wgrad_reduce adds them in a fixed order, so the gradient
+// is deterministic.
 constexpr int kWgThreads = 128;
 constexpr int kWgTile = 128;  // pixels per K tile
+constexpr int kWgSBO = 272;   // bytes between consecutive 8-row groups of a staged operand
 
 template <int CIN, int COUT, int NMB>
 struct WgCfg {
   static constexpr int MROWS = 9 * CIN;                    // rows of D
   static constexpr int MBLK = (MROWS + 127) / 128;         // M-blocks in all
-  static constexpr int A_BYTES = NMB * 128 * kWgTile * 2;  // this CTA's A operand
-  static constexpr int B_BYTES = COUT * kWgTile * 2;
-  static constexpr int SMEM = A_BYTES + B_BYTES + 128;     // + barrier, TMEM slot, flag
+  static constexpr int A_STEP = 16 * kWgSBO;               // one K step (16 pixels) of an M-block
+  static constexpr int A_MB = (kWgTile / 16) * A_STEP;      // one M-block
+  static constexpr int A_BYTES = NMB * A_MB;                // this CTA's A operand
+  static constexpr int B_STEP = (COUT / 8) * kWgSBO;
+  static constexpr int B_BYTES = (kWgTile / 16) * B_STEP;
+  static constexpr int R_BYTES = 3 * (kWgTile + 2) * (CIN / 8) * 16;  // three input rows of the tile, halo 1
+  static constexpr int SMEM = A_BYTES + B_BYTES + R_BYTES + 128;      // + barrier, TMEM slot, flag
   static constexpr int NCOL_USED = NMB * COUT;
   static constexpr int NCOL = NCOL_USED <= 32    ? 32
                               : NCOL_USED <= 64  ? 64
@@ -346,9 +355,16 @@ __device__ __forceinline__ void transpose8x8(const uint4* r, uint4* t) {
     }
 }
 
-// byte offset of the 8x8 block (rows 8g.., pixels 8q..) of a K-major operand of R rows
-__device__ __forceinline__ int kmaj_block(int R, int g, int q) { return (q >> 1) * (R * 32) + g * 256 + (q & 1) * 128; }
+// byte offset of the 8x8 block (rows 8g.., pixels 8q..) of a staged operand of R rows
+__device__ __forceinline__ int kmaj_block(int R, int g, int q) {
+  return (q >> 1) * ((R / 8) * kWgSBO) + g * kWgSBO + (q & 1) * 128;
+}
 
+// A tile is a segment of up to 128 pixels of one image row; its three input
+// rows (y - 1 .. y + 1, x0 - 1 .. x0 + 128, wrapped) are staged once with
+// coalesced loads, and the nine taps' shifted operands are transposed out of
+// that copy.  The next tile's rows are loaded while the previous tile's MMAs
+// run (the row copy is not an MMA operand).
 template <int CIN, int COUT, int NMB>
 __global__ void __launch_bounds__(kWgThreads) k_wgrad_tc(const uint4* __restrict__ X, const uint4* __restrict__ G,
                                                          int B, int H, int W, float* __restrict__ part,
@@ -357,13 +373,15 @@ __global__ void __launch_bounds__(kWgThreads) k_wgrad_tc(const uint4* __restrict
   extern __shared__ __align__(128) unsigned char smem[];
   unsigned char* sa = smem;
   unsigned char* sb = smem + C::A_BYTES;
-  uint64_t* bar = reinterpret_cast<uint64_t*>(smem + C::A_BYTES + C::B_BYTES);
+  uint4* xr = reinterpret_cast<uint4*>(smem + C::A_BYTES + C::B_BYTES);  // [3][kWgTile + 2][KC]
+  uint64_t* bar = reinterpret_cast<uint64_t*>(smem + C::A_BYTES + C::B_BYTES + C::R_BYTES);
   uint32_t* tslot = reinterpret_cast<uint32_t*>(bar + 1);
   int* failed = reinterpret_cast<int*>(bar + 2);
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int mb0 = blockIdx.y * NMB;  // first M-block of this CTA
-  const int64_t npix = (int64_t)B * H * W, ntiles = (npix + kWgTile - 1) / kWgTile;
-  constexpr int KC = CIN / 8, OC = COUT / 8;
+  const int ntx = (W + kWgTile - 1) / kWgTile;
+  const int64_t ntiles = (int64_t)B * H * ntx;
+  constexpr int KC = CIN / 8, OC = COUT / 8, RW = kWgTile + 2;
   if (warp == 0) {
     tc::tmem_alloc(tslot, C::NCOL);
     tc::tmem_relinquish();
@@ -383,22 +401,35 @@ __global__ void __launch_bounds__(kWgThreads) k_wgrad_tc(const uint4* __restrict
   uint32_t phase = 0;
   int issued = 0;
   for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
-    const int64_t p0 = t * kWgTile;
+    const int xt = (int)(t % ntx);
+    const int64_t by = t / ntx;  // b * H + y
+    const int y = (int)(by % H);
+    const int64_t b = by / H;
+    const int x0 = xt * kWgTile;
+    // the tile's three input rows (the previous tile's transposes, the only
+    // readers, finished before the __syncthreads ahead of its MMAs)
+    for (int k = tid; k < 3 * RW * KC; k += kWgThreads) {
+      const int rc = k / KC, kc = k - rc * KC, r = rc / RW, c = rc - r * RW;
+      int gy = y - 1 + r, gx = x0 - 1 + c;
+      gy = gy < 0 ? gy + H : (gy >= H ? gy - H : gy);
+      gx = ((gx % W) + W) % W;
+      xr[k] = X[((b * H + gy) * W + gx) * KC + kc];
+    }
     if (issued) {
-      // the MMAs of the previous tile read the staging buffers
+      // the MMAs of the previous tile read the operand buffers
       if (tid == 0 && !tc::mbar_wait(bar, phase)) *failed = 1;
       phase ^= 1;
-      __syncthreads();
-      if (*failed) break;
     }
-    // B: G[p][co] -> rows co, K = pixels (zero beyond the last pixel)
+    __syncthreads();
+    if (*failed) break;
+    // B: G[p][co] -> rows co, K = pixels (zero beyond the row's end)
     for (int k = tid; k < (kWgTile / 8) * OC; k += kWgThreads) {
       const int q = k / OC, oc = k - q * OC;
       uint4 r[8];
 #pragma unroll
       for (int i = 0; i < 8; i++) {
-        const int64_t p = p0 + 8 * q + i;
-        r[i] = p < npix ? G[p * OC + oc] : make_uint4(0, 0, 0, 0);
+        const int x = x0 + 8 * q + i;
+        r[i] = x < W ? G[(by * W + x) * OC + oc] : make_uint4(0, 0, 0, 0);
       }
       uint4 tt[8];
       transpose8x8(r, tt);
@@ -406,28 +437,17 @@ __global__ void __launch_bounds__(kWgThreads) k_wgrad_tc(const uint4* __restrict
 #pragma unroll
       for (int c = 0; c < 8; c++) dst[c] = tt[c];
     }
-    // A: for each row group (tap, input chunk) of this CTA's M-blocks, X at the
-    // tap's shifted pixel (periodic) -> rows ci, K = pixels; padding groups zero
+    // A: for each row group (tap, input chunk) of this CTA's M-blocks, the
+    // staged rows at the tap's shift -> rows ci, K = pixels; padding groups zero
     for (int k = tid; k < (kWgTile / 8) * NMB * 16; k += kWgThreads) {
       const int q = k / (NMB * 16), gl = k - q * (NMB * 16);
       const int gg = mb0 * 16 + gl;  // global row group
       uint4 r[8];
       if (gg < 9 * KC) {
-        const int tap = gg / KC, kc = gg - tap * KC, dy = tap / 3 - 1, dx = tap % 3 - 1;
+        const int tap = gg / KC, kc = gg - tap * KC;
+        const uint4* src = xr + ((tap / 3) * RW + 8 * q + (tap % 3)) * KC + kc;
 #pragma unroll
-        for (int i = 0; i < 8; i++) {
-          const int64_t p = p0 + 8 * q + i;
-          uint4 v = make_uint4(0, 0, 0, 0);
-          if (p < npix) {
-            const int64_t b = p / ((int64_t)H * W);
-            const int rem = (int)(p - b * H * W), y = rem / W, x = rem - y * W;
-            int ys = y + dy, xs = x + dx;
-            ys = ys < 0 ? ys + H : (ys >= H ? ys - H : ys);
-            xs = xs < 0 ? xs + W : (xs >= W ? xs - W : xs);
-            v = X[((b * H + ys) * W + xs) * KC + kc];
-          }
-          r[i] = v;
-        }
+        for (int i = 0; i < 8; i++) r[i] = src[i * KC];
       } else {
 #pragma unroll
         for (int i = 0; i < 8; i++) r[i] = make_uint4(0, 0, 0, 0);
@@ -435,7 +455,7 @@ __global__ void __launch_bounds__(kWgThreads) k_wgrad_tc(const uint4* __restrict
       uint4 tt[8];
       transpose8x8(r, tt);
       const int blk = gl >> 4, g = gl & 15;  // M-block of this CTA, row group in it
-      uint4* dst = reinterpret_cast<uint4*>(sa + blk * (128 * kWgTile * 2) + kmaj_block(128, g, q));
+      uint4* dst = reinterpret_cast<uint4*>(sa + blk * C::A_MB + kmaj_block(128, g, q));
 #pragma unroll
       for (int c = 0; c < 8; c++) dst[c] = tt[c];
     }
@@ -447,8 +467,8 @@ __global__ void __launch_bounds__(kWgThreads) k_wgrad_tc(const uint4* __restrict
       for (int j = 0; j < NMB; j++)
 #pragma unroll
         for (int s = 0; s < kWgTile / 16; s++)
-          tc::mma_bf16(taddr + j * COUT, tc::sdesc(sa_s + j * (128 * kWgTile * 2) + s * (128 * 32), 128, 256),
-                       tc::sdesc(sb_s + s * (COUT * 32), 128, 256), IDESC, (issued || s > 0) ? 1u : 0u);
+          tc::mma_bf16(taddr + j * COUT, tc::sdesc(sa_s + j * C::A_MB + s * C::A_STEP, 128, kWgSBO),
+                       tc::sdesc(sb_s + s * C::B_STEP, 128, kWgSBO), IDESC, (issued || s > 0) ? 1u : 0u);
       tc::mma_commit(bar);
     }
     issued = 1;
@@ -697,7 +717,7 @@ static cudaError_t wgrad_tc(const Ctx& c, int l, Buf xbuf, Buf gbuf, int B, int 
     attr.fetch_or(bit);
   }
   const int groups = (C::MBLK + NMB - 1) / NMB;
-  const int64_t ntiles = ((int64_t)B * H * W + kWgTile - 1) / kWgTile;
+  const int64_t ntiles = (int64_t)B * H * ((W + kWgTile - 1) / kWgTile);
   const int P = (int)std::max<int64_t>(1, std::min<int64_t>(ntiles, 4 * 152 / groups));
   const int64_t nw = (int64_t)C::MROWS * COUT;
   CK(ensure_corr(g, (int64_t)P * (nw + COUT)));
