@@ -317,7 +317,7 @@ __global__ void k_loss_seed(const float* __restrict__ out, const float* __restri
 // partial sums (and the bias sums of G, by the CTAs of blockIdx.y == 0) go to
 // global memory; k_wgrad_reduce adds them in a fixed order, so the gradient
 // is deterministic.
-constexpr int kWgThreads = 128;
+constexpr int kWgThreads = 512;  // 16 warps: staging parallelism (one CTA per SM by shared memory)
 constexpr int kWgTile = 128;  // pixels per K tile
 constexpr int kWgSBO = 272;   // bytes between consecutive 8-row groups of a staged operand
 
@@ -331,7 +331,13 @@ struct WgCfg {
   static constexpr int B_STEP = (COUT / 8) * kWgSBO;
   static constexpr int B_BYTES = (kWgTile / 16) * B_STEP;
   static constexpr int R_BYTES = 3 * (kWgTile + 2) * (CIN / 8) * 16;  // three input rows of the tile, halo 1
-  static constexpr int SMEM = A_BYTES + B_BYTES + R_BYTES + 128;      // + barrier, TMEM slot, flag
+  static constexpr int GR_BYTES = kWgTile * (COUT / 8) * 16;          // the tile's output-gradient row
+  static constexpr int SMEM = A_BYTES + B_BYTES + R_BYTES + GR_BYTES + 128;  // + barrier, TMEM slot, flag
+  // row groups (tap, chunk) this CTA stages each tile; the rest of its M-blocks are zero padding
+  static constexpr int real_groups(int mb0) {
+    return 9 * (CIN / 8) - mb0 * 16 < NMB * 16 ? (9 * (CIN / 8) - mb0 * 16 > 0 ? 9 * (CIN / 8) - mb0 * 16 : 0)
+                                               : NMB * 16;
+  }
   static constexpr int NCOL_USED = NMB * COUT;
   static constexpr int NCOL = NCOL_USED <= 32    ? 32
                               : NCOL_USED <= 64  ? 64
@@ -339,6 +345,8 @@ struct WgCfg {
                               : NCOL_USED <= 256 ? 256
                                                  : 512;
   static_assert(NCOL_USED <= 512 && COUT % 16 == 0 && CIN % 8 == 0, "TMEM columns, channel counts");
+  static_assert(A_BYTES + B_BYTES + 3 * (kWgTile + 2) * (CIN / 8) * 16 + kWgTile * (COUT / 8) * 16 + 128 <= 227 * 1024,
+                "shared memory of one CTA");
 };
 
 // 8 rows of 8 bf16 (r[i] = pixel i, channels 0..7) -> t[c] = channel c, pixels 0..7
@@ -374,7 +382,8 @@ __global__ void __launch_bounds__(kWgThreads) k_wgrad_tc(const uint4* __restrict
   unsigned char* sa = smem;
   unsigned char* sb = smem + C::A_BYTES;
   uint4* xr = reinterpret_cast<uint4*>(smem + C::A_BYTES + C::B_BYTES);  // [3][kWgTile + 2][KC]
-  uint64_t* bar = reinterpret_cast<uint64_t*>(smem + C::A_BYTES + C::B_BYTES + C::R_BYTES);
+  uint4* gr = reinterpret_cast<uint4*>(smem + C::A_BYTES + C::B_BYTES + C::R_BYTES);  // [kWgTile][OC]
+  uint64_t* bar = reinterpret_cast<uint64_t*>(smem + C::A_BYTES + C::B_BYTES + C::R_BYTES + C::GR_BYTES);
   uint32_t* tslot = reinterpret_cast<uint32_t*>(bar + 1);
   int* failed = reinterpret_cast<int*>(bar + 2);
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
@@ -400,6 +409,14 @@ __global__ void __launch_bounds__(kWgThreads) k_wgrad_tc(const uint4* __restrict
   float bsum = 0.f;  // bias partial of output channel tid (tid < COUT, blockIdx.y == 0)
   uint32_t phase = 0;
   int issued = 0;
+  // the padding row groups of the last M-block are zero for every tile: written once
+  const int nreal = C::real_groups(mb0);
+  for (int k = tid; k < (kWgTile / 8) * (NMB * 16 - nreal); k += kWgThreads) {
+    const int q = k / (NMB * 16 - nreal), gl = nreal + (k - q * (NMB * 16 - nreal));
+    uint4* dst = reinterpret_cast<uint4*>(sa + (gl >> 4) * C::A_MB + kmaj_block(128, gl & 15, q));
+#pragma unroll
+    for (int c = 0; c < 8; c++) dst[c] = make_uint4(0, 0, 0, 0);
+  }
   for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
     const int xt = (int)(t % ntx);
     const int64_t by = t / ntx;  // b * H + y
@@ -415,6 +432,11 @@ __global__ void __launch_bounds__(kWgThreads) k_wgrad_tc(const uint4* __restrict
       gx = ((gx % W) + W) % W;
       xr[k] = X[((b * H + gy) * W + gx) * KC + kc];
     }
+    // and its output-gradient row (zero beyond the row's end)
+    for (int k = tid; k < kWgTile * OC; k += kWgThreads) {
+      const int x = x0 + k / OC;
+      gr[k] = x < W ? G[(by * W + x0) * OC + k] : make_uint4(0, 0, 0, 0);
+    }
     if (issued) {
       // the MMAs of the previous tile read the operand buffers
       if (tid == 0 && !tc::mbar_wait(bar, phase)) *failed = 1;
@@ -422,15 +444,12 @@ __global__ void __launch_bounds__(kWgThreads) k_wgrad_tc(const uint4* __restrict
     }
     __syncthreads();
     if (*failed) break;
-    // B: G[p][co] -> rows co, K = pixels (zero beyond the row's end)
+    // B: G[p][co] -> rows co, K = pixels, from the staged row
     for (int k = tid; k < (kWgTile / 8) * OC; k += kWgThreads) {
       const int q = k / OC, oc = k - q * OC;
       uint4 r[8];
 #pragma unroll
-      for (int i = 0; i < 8; i++) {
-        const int x = x0 + 8 * q + i;
-        r[i] = x < W ? G[(by * W + x) * OC + oc] : make_uint4(0, 0, 0, 0);
-      }
+      for (int i = 0; i < 8; i++) r[i] = gr[(8 * q + i) * OC + oc];
       uint4 tt[8];
       transpose8x8(r, tt);
       uint4* dst = reinterpret_cast<uint4*>(sb + kmaj_block(COUT, oc, q));
@@ -439,19 +458,14 @@ __global__ void __launch_bounds__(kWgThreads) k_wgrad_tc(const uint4* __restrict
     }
     // A: for each row group (tap, input chunk) of this CTA's M-blocks, the
     // staged rows at the tap's shift -> rows ci, K = pixels; padding groups zero
-    for (int k = tid; k < (kWgTile / 8) * NMB * 16; k += kWgThreads) {
-      const int q = k / (NMB * 16), gl = k - q * (NMB * 16);
-      const int gg = mb0 * 16 + gl;  // global row group
+    for (int k = tid; k < (kWgTile / 8) * nreal; k += kWgThreads) {
+      const int q = k / nreal, gl = k - q * nreal;
+      const int gg = mb0 * 16 + gl;  // global row group, < 9 KC
+      const int tap = gg / KC, kc = gg - tap * KC;
+      const uint4* src = xr + ((tap / 3) * RW + 8 * q + (tap % 3)) * KC + kc;
       uint4 r[8];
-      if (gg < 9 * KC) {
-        const int tap = gg / KC, kc = gg - tap * KC;
-        const uint4* src = xr + ((tap / 3) * RW + 8 * q + (tap % 3)) * KC + kc;
 #pragma unroll
-        for (int i = 0; i < 8; i++) r[i] = src[i * KC];
-      } else {
-#pragma unroll
-        for (int i = 0; i < 8; i++) r[i] = make_uint4(0, 0, 0, 0);
-      }
+      for (int i = 0; i < 8; i++) r[i] = src[i * KC];
       uint4 tt[8];
       transpose8x8(r, tt);
       const int blk = gl >> 4, g = gl & 15;  // M-block of this CTA, row group in it
@@ -498,18 +512,19 @@ __global__ void __launch_bounds__(kWgThreads) k_wgrad_tc(const uint4* __restrict
   tc::fence_after_sync();
   const int64_t cta = blockIdx.x;
   if (!*failed) {
-    const int m = 32 * (warp & 3) + lane;
-    for (int j = 0; j < NMB; j++) {
-      const int row = (mb0 + j) * 128 + m;
+    // warp w reads TMEM lanes 32 (w % 4) ..; the four warp groups share the
+    // (M-block, 16-column) chunks
+    const int m = 32 * (warp & 3) + lane, grp = warp >> 2;
 #pragma unroll 1
-      for (int c0 = 0; c0 < COUT; c0 += 16) {
-        float v[16];
-        tc::tmem_ld16(taddr + ((uint32_t)(32 * (warp & 3)) << 16) + j * COUT + c0, v);
-        if (row < C::MROWS) {
-          float* dst = part + (cta * C::MROWS + row) * COUT + c0;
+    for (int jc = grp; jc < NMB * (COUT / 16); jc += kWgThreads / 128) {
+      const int j = jc / (COUT / 16), c0 = (jc - j * (COUT / 16)) * 16;
+      const int row = (mb0 + j) * 128 + m;
+      float v[16];
+      tc::tmem_ld16(taddr + ((uint32_t)(32 * (warp & 3)) << 16) + j * COUT + c0, v);
+      if (row < C::MROWS) {
+        float* dst = part + (cta * C::MROWS + row) * COUT + c0;
 #pragma unroll
-          for (int k = 0; k < 16; k++) dst[k] = issued ? v[k] : 0.f;
-        }
+        for (int k = 0; k < 16; k++) dst[k] = issued ? v[k] : 0.f;
       }
     }
     if (blockIdx.y == 0 && tid < COUT) bpart[cta * COUT + tid] = bsum;
@@ -744,7 +759,7 @@ static cudaError_t wgrad(const Ctx& c, int l, Buf xbuf, Buf gbuf, int B, int H, 
   FS_WG(32, 16, 3)
   FS_WG(32, 64, 3)
   FS_WG(64, 128, 3)
-  FS_WG(128, 64, 3)
+  FS_WG(128, 64, 2)
   FS_WG(64, 32, 3)
 #undef FS_WG
   return cudaErrorInvalidValue;

@@ -59,7 +59,7 @@ def test_transpose8x8():
 
 
 @pytest.mark.parametrize("cin,cout,nmb,B,H,W", [(16, 16, 2, 1, 3, 200), (32, 16, 3, 2, 4, 8),
-                                                 (64, 128, 3, 1, 2, 128), (128, 64, 3, 1, 2, 64)])
+                                                 (64, 128, 3, 1, 2, 128), (128, 64, 2, 1, 2, 64)])
 def test_wgrad_staging_equals_correlation(cin, cout, nmb, B, H, W):
     """Tiles are segments of up to 128 pixels of one image row (the last one
     of a row partial); the three input rows around a tile (halo 1, periodic)
