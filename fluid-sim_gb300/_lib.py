@@ -193,6 +193,7 @@ SIGNATURES = {
     "fs_batch_autotune_tiles": (I, [VP, C.POINTER(D), C.c_int32, C.POINTER(D)]),
     "fs_batch_autotune": (I, [VP, C.POINTER(D), C.c_int32, C.POINTER(D)]),
     "fs_dump_pair": (I, [VP, C.c_int32, VP, VP, VP]),
+    "fs_dump_pair_device": (I, [VP, C.c_int32, VP, VP, VP]),
     "fs_write_pair_file": (I, [C.c_char_p, C.c_int32, C.c_int32, D, VP, VP, VP]),
     "fs_read_pair_file": (I, [C.c_char_p, C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.POINTER(D), VP, VP, VP]),
 }

@@ -1017,6 +1017,14 @@ FS_API int fs_dump_pair(fs_solver* h, int32_t factor, float* div, float* mask, f
   return dump_pair(s, factor, div, mask, p);
 }
 
+FS_API int fs_dump_pair_device(fs_solver* h, int32_t factor, float* d_div, float* d_mask, float* d_p) {
+  SOLVER(h);
+  if (!d_div || !d_mask || !d_p) return fail(s, FS_ERR_INVALID_ARGUMENT, "fs_dump_pair_device: NULL output");
+  if (factor < 1 || s->g.nx % factor || s->g.ny % factor)
+    return fail(s, FS_ERR_INVALID_ARGUMENT, "fs_dump_pair_device: factor must divide nx and ny");
+  return dump_pair_device(s, factor, d_div, d_mask, d_p);
+}
+
 FS_API int fs_upload_dye(fs_solver* h, const float* rgba) {
   SOLVER(h);
   if (!rgba) return fail(s, FS_ERR_INVALID_ARGUMENT, "rgba is NULL");

@@ -1023,6 +1023,23 @@ int dump_pair(Solver* s, int f, float* div, float* mask, float* p) {
   return FS_OK;
 }
 
+// the same pair into caller-owned device buffers, enqueued on the solver's
+// stream (no allocation, no synchronisation)
+int dump_pair_device(Solver* s, int f, float* div, float* mask, float* p) {
+  const Grid& gr = s->g;
+  const double width = s->prm.solid_mask_width * gr.dxd;
+  const int nd = (int)s->disks.size();
+  const int64_t n = (int64_t)(gr.nx / f) * (gr.ny / f);
+  k_pair<<<guess::blocks_for(n), 256, 0, s->stream>>>(
+      s->mixed ? s->dh : s->div32, s->mixed ? s->dl : nullptr, s->mixed ? s->ph : s->p32, s->mixed ? s->pl : nullptr,
+      gr.nx, gr.ny, f, div, mask, p, static_cast<const float*>(s->d_disks), nd, (float)(f * gr.dxd),
+      (float)(f * gr.dyd), (float)s->prm.lx, (float)s->prm.ly, (float)width);
+  s->launches++;
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return fail_status(s, FS_ERR_CUDA, std::string("fs_dump_pair_device: ") + cudaGetErrorString(e));
+  return FS_OK;
+}
+
 }  // namespace fs
 
 // ====================================================================== C ABI

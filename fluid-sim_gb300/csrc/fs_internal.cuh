@@ -313,6 +313,7 @@ bool guess_supported(const Solver* s, int factor);
 int guess_prepare(Solver* s, fs_guess* g, int factor);  // buffers for this grid (outside any capture)
 int guess_enqueue(Solver* s, fs_guess* g, int factor);  // initial pressure from the divergence
 int dump_pair(Solver* s, int factor, float* div, float* mask, float* p);
+int dump_pair_device(Solver* s, int factor, float* div, float* mask, float* p);  // enqueued, device outputs
 
 // diagnostics (fs_diag.cu)
 void diag_free(Solver* s);

@@ -1,18 +1,20 @@
 """Train the pressure guess on pairs the solver dumps from its own runs, and
 measure what it saves.
 
-    python fluid-sim_gb300/guess_train.py --n 2048 --runs 8 --steps 48 \\
-        --iters 2000 --out weights/guess_2048.fsguess [--pairs-dir DIR]
+    python fluid-sim_gb300/guess_train.py --n 2048 --pairs 20000 --seeds 16 \
+        --out weights/guess_2048_f2.fsguess
 
-1. Pairs: for `runs` fresh workload seeds (disjoint from the benchmark's),
-   the solver steps the seeded channel flow with a mixed-precision multigrid
-   projection to max|div u| <= tol and, every `every` steps, dumps the
-   (divergence, solid mask, pressure) of that projection at half resolution
-   (fs_dump_pair, factor 2); optionally each pair is also written as an
-   FSPAIR file.  Pairs are normalised (normalize_pair) and kept on the device.
-2. Training: Adam on random minibatches, cosine learning-rate decay, loss
-   w_p * mean-free pressure MSE + w_r * mean (lap error)^2 (the second term
-   is the initial residual of the projection the guess seeds).
+1. Pairs, streamed: `seeds` fresh seeds of the channel workload (disjoint
+   from the benchmark's) are stepped in rotation with the benchmark's
+   projection (mixed-precision multigrid to max|div u| <= tol, relaxation
+   1.2); after every step the solver writes the (divergence, solid mask,
+   pressure) of that projection at 1/factor resolution straight into a ring
+   buffer on the device (fs_dump_pair_device), where it is normalised
+   (h^2 d / sigma, (p - mean p) / sigma).  `pairs` pairs in all, every one
+   distinct; training batches are drawn from the ring.
+2. Training: Adam on random minibatches from the ring, cosine learning-rate
+   decay, loss w_p * mean-free pressure MSE + w_r * mean (lap error)^2 (the
+   second term is the initial residual of the projection the guess seeds).
 3. Evaluation on a held-out seed: V-cycles per step and ms per step with and
    without the guess, and the initial residual max|d - lap p0| of each.
 """
@@ -42,37 +44,71 @@ def _package():
     return mod
 
 
-def make_solver(pkg, n, disks, tol=1e-6, guess=None, factor=2, warm=False):
+RELAX, COARSE = 1.2, 8  # the benchmark's projection
+
+
+def make_solver(pkg, n, disks, channel, tol=1e-6, guess=None, factor=2, warm=False):
     s = pkg.GPUFluidSolver(n=n, nu=1e-4, advection="maccormack", pressureSolver="multigrid", pressureIterations=1,
-                           precision="mixed", pressure_tol=tol, max_cycles=60, warm_start=warm)
+                           precision="mixed", pressure_tol=tol, max_cycles=60, warm_start=warm, relax=RELAX,
+                           mg_coarse_sweeps=COARSE)
+    s.set_channel(channel)
     s.set_solids(disks)
     if guess is not None:
         s.set_guess(guess, factor)
     return s
 
 
-def dump_pairs(pkg, n, runs, steps, every=2, factor=2, seed0=1000, tol=1e-6, pairs_dir=None):
-    """-> device tensors (div_n, mask, p_n) of shape [P, n/factor, n/factor]."""
+def stream_train(pkg, guess, n, pairs, seeds, factor=2, ring=512, batch=4, steps_per_round=4, lr=2e-3,
+                 seed0=1000, tol=1e-6, warmup=20, log_every=100):
+    """Step `seeds` channel-flow solvers in rotation; every step's pair goes
+    into a device ring of `ring` pairs; after each round (one step of every
+    seed) `steps_per_round` Adam steps on batches drawn from the filled part
+    of the ring.  Returns (loss history, pairs made, train steps)."""
     import torch
 
-    divs, masks, ps = [], [], []
-    for r in range(runs):
-        u, v, disks, dt = pkg.workload.make_workload(n, seed0 + r)
-        s = make_solver(pkg, n, disks, tol)
+    m = n // factor
+    div = torch.empty((ring, m, m), device="cuda")
+    msk = torch.empty_like(div)
+    prs = torch.empty_like(div)
+    sols, dts = [], []
+    for r in range(seeds):
+        u, v, disks, dt, ch = pkg.workload.channel_workload(n, seed0 + r)
+        s = make_solver(pkg, n, disks, ch, tol)
         s.upload_velocity(u, v)
-        for k in range(steps):
+        for _ in range(warmup):  # past the start-up transient
             s.step(dt)
-            if k % every:
-                continue
-            d, m, p, dx = s.dump_pair(factor)
-            if pairs_dir is not None:
-                pkg.write_pair_file(Path(pairs_dir) / f"pair_{seed0 + r}_{k:04d}.fspair", d, m, p, dx)
-            dn, mn, pn, _ = pkg.normalize_pair(d, m, p, dx)
-            divs.append(torch.from_numpy(dn).cuda())
-            masks.append(torch.from_numpy(mn).cuda())
-            ps.append(torch.from_numpy(pn).cuda())
+        sols.append(s)
+        dts.append(dt)
+    gen = torch.Generator(device="cpu").manual_seed(0)
+    made = it = 0
+    rounds = (pairs + seeds - 1) // seeds
+    iters = rounds * steps_per_round
+    hist = []
+    for rnd in range(rounds):
+        for s, dt in zip(sols, dts):
+            if made >= pairs:
+                break
+            s.step(dt)
+            k = made % ring
+            h = s.dump_pair_device(factor, div[k].data_ptr(), msk[k].data_ptr(), prs[k].data_ptr())
+            s.sync()
+            x = div[k] * (h * h)
+            sigma = torch.sqrt(torch.mean(x * x)).clamp_min(1e-30)
+            div[k] = x / sigma
+            prs[k] = (prs[k] - prs[k].mean()) / sigma
+            made += 1
+        filled = min(made, ring)
+        for _ in range(steps_per_round):
+            idx = torch.randint(0, filled, (batch,), generator=gen).cuda()
+            lr_t = max(lr * 0.5 * (1 + math.cos(math.pi * it / iters)), lr * 1e-3)
+            want = it % log_every == 0 or it == iters - 1
+            loss = guess.train_step(div[idx], msk[idx], prs[idx], lr_t, want_loss=want)
+            if want:
+                hist.append((it, loss))
+            it += 1
+    for s in sols:
         s.destroy()
-    return torch.stack(divs), torch.stack(masks), torch.stack(ps)
+    return hist, made, it
 
 
 def train(guess, data, iters, batch, lr, seed=0, log_every=100):
@@ -99,13 +135,13 @@ def _initial_residual(s, dt):
 
 
 def evaluate(pkg, n, guess, factor=2, seed=77, steps=30, tol=1e-6):
-    """Cycles per step and ms per step on a held-out seed: zero initial
-    pressure (plain, as the reference), the learned guess, and the previous
-    step's pressure (warm start, for comparison)."""
-    u, v, disks, dt = pkg.workload.make_workload(n, seed)
+    """Cycles per step and ms per step on a held-out seed of the channel
+    workload: zero initial pressure (plain, as the reference), the learned
+    guess, and the previous step's pressure (warm start, for comparison)."""
+    u, v, disks, dt, ch = pkg.workload.channel_workload(n, seed)
     out = {}
     for name, g, warm in (("plain", None, False), ("guess", guess, False), ("warm", None, True)):
-        s = make_solver(pkg, n, disks, tol, g, factor, warm)
+        s = make_solver(pkg, n, disks, ch, tol, g, factor, warm)
         s.upload_velocity(u, v)
         cyc, r0 = [], []
         for _ in range(steps):
@@ -122,11 +158,11 @@ def evaluate(pkg, n, guess, factor=2, seed=77, steps=30, tol=1e-6):
 def main(argv=None):
     ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
     ap.add_argument("--n", type=int, default=2048)
-    ap.add_argument("--runs", type=int, default=8)
-    ap.add_argument("--steps", type=int, default=48)
-    ap.add_argument("--every", type=int, default=2)
+    ap.add_argument("--pairs", type=int, default=20000, help="distinct solver-dumped pairs to train on")
+    ap.add_argument("--seeds", type=int, default=16, help="channel-flow seeds stepped in rotation")
+    ap.add_argument("--ring", type=int, default=512, help="pairs held on the device at once")
+    ap.add_argument("--steps-per-round", type=int, default=4, help="Adam steps per round of one pair per seed")
     ap.add_argument("--factor", type=int, default=2, help="the network runs at 1/factor of the grid")
-    ap.add_argument("--iters", type=int, default=2000)
     ap.add_argument("--batch", type=int, default=4)
     ap.add_argument("--lr", type=float, default=2e-3)
     ap.add_argument("--w-pressure", type=float, default=0.05)
@@ -134,25 +170,23 @@ def main(argv=None):
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--out", type=str, default=None, help="weights file (FSGUESS)")
     ap.add_argument("--report", type=str, default=None, help="JSON summary")
-    ap.add_argument("--pairs-dir", type=str, default=None)
     ap.add_argument("--eval-steps", type=int, default=30)
     a = ap.parse_args(argv)
     pkg = _package()
-    t0 = time.time()
-    data = dump_pairs(pkg, a.n, a.runs, a.steps, a.every, a.factor, pairs_dir=a.pairs_dir)
-    t1 = time.time()
     g = pkg.PressureGuess(seed=a.seed)
     g.set_loss(a.w_pressure, a.w_residual)
-    hist = train(g, data, a.iters, a.batch, a.lr, a.seed)
+    t0 = time.time()
+    hist, made, iters = stream_train(pkg, g, a.n, a.pairs, a.seeds, a.factor, a.ring, a.batch, a.steps_per_round,
+                                     a.lr)
     g.sync()
-    t2 = time.time()
+    t1 = time.time()
     if a.out:
         Path(a.out).parent.mkdir(parents=True, exist_ok=True)
         g.save(a.out)
     ev = evaluate(pkg, a.n, g, a.factor, steps=a.eval_steps)
-    rep = {"n": a.n, "factor": a.factor, "pairs": int(data[0].shape[0]), "net_resolution": int(data[0].shape[-1]),
-           "params": g.n_params, "iters": a.iters, "batch": a.batch, "lr": a.lr,
-           "loss_weights": [a.w_pressure, a.w_residual], "dump_s": t1 - t0, "train_s": t2 - t1,
+    rep = {"n": a.n, "factor": a.factor, "pairs": made, "seeds": a.seeds, "ring": a.ring,
+           "net_resolution": a.n // a.factor, "params": g.n_params, "train_steps": iters, "batch": a.batch,
+           "lr": a.lr, "loss_weights": [a.w_pressure, a.w_residual], "stream_and_train_s": t1 - t0,
            "loss_history": hist, "eval": ev}
     print(json.dumps(rep))
     if a.report:

@@ -420,6 +420,14 @@ class GPUFluidSolver:
         self._chk(self._lib.fs_dump_pair(self._h, factor, _ptr(d), _ptr(m), _ptr(p)))
         return d, m, p, self.dx * factor
 
+    def dump_pair_device(self, factor: int, d_div: int, d_mask: int, d_p: int) -> float:
+        """The same pair into device buffers (addresses of f32 arrays of
+        (ny/factor) * (nx/factor)), enqueued on the solver's stream; returns
+        the pair's grid spacing.  Call sync() before another stream reads them."""
+        self._chk(self._lib.fs_dump_pair_device(self._h, factor, C.c_void_p(d_div), C.c_void_p(d_mask),
+                                                C.c_void_p(d_p)))
+        return self.dx * factor
+
 
 class GPUFluidBatch:
     """Many independent solvers of uneven sizes advanced by one CUDA graph

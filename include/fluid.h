@@ -412,6 +412,10 @@ FS_API int fs_set_guess(fs_solver* s, fs_guess* g, int32_t factor);
  * pressure averaged over factor x factor cells (mask at the coarse cell
  * centres), host f32 arrays of (nx/factor) x (ny/factor).  Synchronises. */
 FS_API int fs_dump_pair(fs_solver* s, int32_t factor, float* div, float* mask, float* p);
+/* The same pair into device buffers the caller owns (f32, (nx/factor) x
+ * (ny/factor) each), enqueued on the solver's stream without synchronising:
+ * a training loop streams pairs straight from the solver into its batches. */
+FS_API int fs_dump_pair_device(fs_solver* s, int32_t factor, float* d_div, float* d_mask, float* d_p);
 
 /* Training-pair file ("FSPAIR" v1): 40-byte header {magic "FSPAIR\0\1",
  * u32 version = 1, u32 nx, u32 ny, u32 dtype = 0 (f32), f64 dx, u32 nfields =
