@@ -454,6 +454,16 @@ def run_gpu(args):
             "clocks": clk.summary(),
         }
         if variants:
+            # throughput ratios against the zero initial pressure at this
+            # relaxation ("plain"), and against the reference's own multigrid
+            # configuration (zero initial pressure, relaxation 1.0)
+            base = variants.get("plain_mg", {}).get("value")
+            ref = variants.get("relax_1.0_mg", {}).get("value")
+            for v in variants.values():
+                if base:
+                    v["vs_plain_mg"] = v["value"] / base
+                if ref:
+                    v["vs_reference_config_mg"] = v["value"] / ref
             line["guess_comparison"] = variants
         if batch is not None:
             line["batch"] = batch

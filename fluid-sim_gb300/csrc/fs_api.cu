@@ -570,6 +570,12 @@ static void drop_graph(Solver* s) {
 // and the loop statistics live on the device.
 static int build_step_graph(Solver* s, double dt) {
   drop_graph(s);
+  // each failed capture leaves its partial graph behind (below): after a few
+  // the handle stops capturing, so that a caller retrying in a loop cannot
+  // make the leak grow without bound
+  if (s->failed_captures >= kMaxFailedCaptures)
+    return fail(s, FS_ERR_CUDA, "step capture failed " + std::to_string(s->failed_captures) +
+                                    " times on this handle; it no longer captures (recreate the solver)");
   int64_t l0 = s->launches;
   CU(s, cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal));
   int rc = enqueue_step(s, dt, true);
@@ -580,6 +586,7 @@ static int build_step_graph(Solver* s, double dt) {
     // leaves its partial graph alone: destroying a graph whose conditional
     // body was being captured when the capture failed is not relied on
     cudaGetLastError();
+    s->failed_captures++;
     return rc;
   }
   if (e != cudaSuccess) return fail(s, FS_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(e));

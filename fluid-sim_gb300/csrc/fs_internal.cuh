@@ -153,6 +153,7 @@ struct Solver {
   cudaGraphExec_t graph_exec = nullptr;
   double graph_dt = 0;
   bool graph_ok = false;        // graph_exec matches the current forcing / solids
+  int failed_captures = 0;      // step captures that failed (each leaves its partial graph)
   bool stats_on_device = false; // the last projection ran inside a graph
   cudaStream_t body_stream = nullptr;  // captures the body of the tolerance loop
   // batch membership: eager work goes to the batch's shared stream; own_stream
@@ -209,6 +210,9 @@ void prof_end(Solver* s, int slot, cudaEvent_t a);
   } while (0)
 
 inline dim3 grid2d(int nx, int ny, dim3 b) { return dim3((nx + b.x - 1) / b.x, (ny + b.y - 1) / b.y); }
+
+// failed step captures after which a handle refuses to capture again
+constexpr int kMaxFailedCaptures = 4;
 
 // members of one batched launch (a size class of a batch; larger classes are split)
 constexpr int kClassMax = 64;
