@@ -165,3 +165,36 @@ def test_batch_tile_autotune_keeps_results(pkg):
         s.destroy()
     assert b.launch_count() > 0
     b.destroy()
+
+
+def test_batch_members_with_channel_and_band_forcing(pkg):
+    """Members with the channel (walls and inflow fringe) or the renewed band
+    forcing leave the batched launches of their class and run their own
+    captured step; they still equal independently stepped solvers bit for
+    bit, and the band forcing's draws advance per member."""
+    sides = [128, 128, 128]
+    ch = pkg.workload.channel_geometry()
+    states = _members(pkg, sides, seed0=40)
+    b = pkg.GPUFluidBatch([dict(n=n, **CFG) for n in sides])
+    for m, (u, v, _) in zip(b.members, states):
+        m.upload_velocity(u, v)
+    b.members[0].set_channel(ch)
+    b.members[1].set_band_forcing("gaussian", kf=6.0, width=1.0, amplitude=2.0, seed=5, drag=0.1)
+    dts = [dt for _, _, dt in states]
+    for _ in range(3):
+        b.step(dts)
+    b.sync()
+    for i, (n, (u, v, dt)) in enumerate(zip(sides, states)):
+        s = pkg.GPUFluidSolver(n=n, **CFG)
+        s.upload_velocity(u, v)
+        if i == 0:
+            s.set_channel(ch)
+        if i == 1:
+            s.set_band_forcing("gaussian", kf=6.0, width=1.0, amplitude=2.0, seed=5, drag=0.1)
+        for _ in range(3):
+            s.step(dt)
+        ua, va = b.members[i].read_velocity()
+        ub, vb = s.read_velocity()
+        assert np.array_equal(ua, ub) and np.array_equal(va, vb), f"member {i}"
+        s.destroy()
+    b.destroy()
