@@ -155,6 +155,27 @@ def evaluate(pkg, n, guess, factor=2, seed=77, steps=30, tol=1e-6):
     return out
 
 
+def time_train_steps(pkg, res=1024, batch=4, steps=20, warm=3, seed=0):
+    """ms per fs_guess_train_step on random inputs of [batch][res][res]
+    (the training configuration's shape: 2048^2 grids at factor 2)."""
+    import torch
+
+    gen = torch.Generator(device="cuda").manual_seed(seed)
+    d = torch.randn(batch, res, res, device="cuda", generator=gen)
+    m = (torch.rand(batch, res, res, device="cuda", generator=gen) > 0.9).float()
+    t = torch.randn(batch, res, res, device="cuda", generator=gen)
+    g = pkg.PressureGuess(seed=seed)
+    g.set_loss(0.05, 1.0)
+    for _ in range(warm):
+        g.train_step(d, m, t, 1e-3, want_loss=False)
+    g.sync()
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        g.train_step(d, m, t, 1e-3, want_loss=False)
+    g.sync()
+    return (time.perf_counter() - t0) / max(steps, 1) * 1e3
+
+
 def main(argv=None):
     ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
     ap.add_argument("--n", type=int, default=2048)
@@ -171,8 +192,14 @@ def main(argv=None):
     ap.add_argument("--out", type=str, default=None, help="weights file (FSGUESS)")
     ap.add_argument("--report", type=str, default=None, help="JSON summary")
     ap.add_argument("--eval-steps", type=int, default=30)
+    ap.add_argument("--time-steps", type=int, default=0,
+                    help="only time this many training steps on random 1024^2 batches of 4 and exit")
     a = ap.parse_args(argv)
     pkg = _package()
+    if a.time_steps > 0:
+        ms = time_train_steps(pkg, steps=a.time_steps)
+        print(json.dumps({"train_step_ms": ms, "res": 1024, "batch": 4, "steps": a.time_steps}))
+        return {"train_step_ms": ms}
     g = pkg.PressureGuess(seed=a.seed)
     g.set_loss(a.w_pressure, a.w_residual)
     t0 = time.time()
