@@ -869,12 +869,18 @@ FS_API int fs_upload_velocity(fs_solver* h, const void* u, const void* v, int dt
   return FS_OK;
 }
 
+// The double-float velocity is always a normalised pair -- written by the
+// error-free sums of the gradient subtraction (hi = RN(hi + lo) by
+// construction) or by an upload (hi = RN(x), lo the exact remainder, or lo =
+// 0) -- so its f32 value RN(hi + lo) is hi itself: an f32 read-back copies the
+// hi planes, with no conversion kernel.
 FS_API int fs_read_velocity(fs_solver* h, void* u, void* v, int dtype) {
   SOLVER(h);
   if (!u || !v) return fail(s, FS_ERR_INVALID_ARGUMENT, "u or v is NULL");
-  int rc = download_from(s, s->u, s->ulo, u, dtype, false);  // one synchronisation for both
+  const bool hi_only = dtype == FS_DTYPE_F32;
+  int rc = download_from(s, s->u, hi_only ? nullptr : s->ulo, u, dtype, false);  // one synchronisation for both
   if (rc) return rc;
-  return download_from(s, s->v, s->vlo, v, dtype);
+  return download_from(s, s->v, hi_only ? nullptr : s->vlo, v, dtype);
 }
 
 FS_API int fs_read_field(fs_solver* h, int field, void* out, int dtype) {

@@ -586,3 +586,28 @@ def test_graph_step_reports_tolerance_failure(G, O):
     st = s2.last_stats()
     assert st["converged"] and st["residual_max"] <= 1e-6
     assert s2.launch_count() - l0 > 2 * 10 * st["cycles"] // 2
+
+
+def test_f32_velocity_readback_is_the_rounded_double_float(G, O):
+    """An f32 read-back of the mixed-precision velocity copies the hi planes;
+    that equals the double-float value rounded to f32 (the pairs are
+    normalised) -- after an f64 upload (hi = RN(x) and its remainder), after
+    steps (the gradient subtraction's error-free sums), and after an f32
+    upload (lo = 0)."""
+    n = 128
+    a, b = O.lcg_uv(606, n * n)
+    s = G.GPUFluidSolver(n=n, nu=1e-3, advection="maccormack", pressure_solver="multigrid", pressure_iterations=1,
+                         precision="mixed", pressure_tol=1e-9, max_cycles=60)
+    for stage in ("f64 upload", "steps", "f32 upload"):
+        if stage == "f64 upload":
+            s.upload_velocity(a, b)
+        elif stage == "steps":
+            for _ in range(3):
+                s.step(0.01)
+        else:
+            s.upload_velocity(np.asarray(a, np.float32), np.asarray(b, np.float32))
+        u64, v64 = s.read_velocity(np.float64)
+        u32, v32 = s.read_velocity(np.float32)
+        assert np.array_equal(u32, u64.astype(np.float32)), stage
+        assert np.array_equal(v32, v64.astype(np.float32)), stage
+    s.destroy()
