@@ -330,25 +330,40 @@ __device__ __forceinline__ void mg_up_body(float* smem, const float* __restrict_
     cp_async_wait_all();
     __syncthreads();
   }
-  // prolongation-add by 2x2 fine blocks: fine columns 2a - 1 (weight 1/4 on
-  // coarse column a) and 2a (weight 3/4) read the same four coarse values,
-  // likewise rows 2b - 1 and 2b; the blocks on the region's edge are halves
+  // prolongation-add by even-aligned 2x2 fine blocks: block (d, e) holds
+  // region rows 2d, 2d + 1 and columns 2e, 2e + 1.  Fine column 2e
+  // interpolates coarse block columns e, e + 1 (weight 3/4 on e + 1), column
+  // 2e + 1 columns e + 1, e + 2 (weight 1/4 on e + 2); likewise the rows.  A
+  // thread walks one column of blocks down a chunk of block rows and keeps
+  // the two coarse rows it shares with the next block in registers: three
+  // coarse loads and two float2 read-modify-writes per block (OX and W are
+  // even, so each block row is one aligned float2).
   {
-    constexpr int NB = B::R / 2 + 1;
-    for (int k = tid; k < NB * NB; k += nthr) {
-      const int b = k / NB, a = k - b * NB;
-      const float* c = cs + b * C::WC + C::OC + a;
-      const float c00 = c[0], c10 = c[1], c01 = c[C::WC], c11 = c[C::WC + 1];
-      const int col = B::OX + 2 * a - 1;
-      if (b > 0) {
-        const int o = (2 * b - 1) * B::W + col;
-        if (a > 0) xs[o] = __fadd_rn(xs[o], prolong_val(c00, c10, c01, c11, 0.25f, 0.25f));
-        if (a < NB - 1) xs[o + 1] = __fadd_rn(xs[o + 1], prolong_val(c00, c10, c01, c11, 0.75f, 0.25f));
-      }
-      if (b < NB - 1) {
-        const int o = 2 * b * B::W + col;
-        if (a > 0) xs[o] = __fadd_rn(xs[o], prolong_val(c00, c10, c01, c11, 0.25f, 0.75f));
-        if (a < NB - 1) xs[o + 1] = __fadd_rn(xs[o + 1], prolong_val(c00, c10, c01, c11, 0.75f, 0.75f));
+    constexpr int NBC = B::R / 2;                // blocks per region row and column
+    constexpr int NCK = kTileThreads / NBC;      // chunks of block rows
+    constexpr int CL = (NBC + NCK - 1) / NCK;    // block rows per chunk
+    static_assert(NCK >= 1 && B::OX % 2 == 0 && B::W % 2 == 0, "float2 blocks of a region of <= 512 columns");
+    const int chunk = tid / NBC, e = tid - chunk * NBC;
+    int d = chunk * CL;
+    const int dend = min(d + CL, NBC);
+    if (chunk < NCK && d < dend) {
+      const float* c = cs + d * C::WC + C::OC + e;
+      float a0 = c[0], a1 = c[1], a2 = c[2];
+      float b0 = c[C::WC], b1 = c[C::WC + 1], b2 = c[C::WC + 2];
+      float2* o = reinterpret_cast<float2*>(xs + 2 * d * B::W + B::OX + 2 * e);
+      for (; d < dend; d++) {
+        c += C::WC;
+        const float n0 = c[C::WC], n1 = c[C::WC + 1], n2 = c[C::WC + 2];
+        float2 top = o[0], bot = o[B::W / 2];
+        top.x = __fadd_rn(top.x, prolong_val(a0, a1, b0, b1, 0.75f, 0.75f));
+        top.y = __fadd_rn(top.y, prolong_val(a1, a2, b1, b2, 0.25f, 0.75f));
+        bot.x = __fadd_rn(bot.x, prolong_val(b0, b1, n0, n1, 0.75f, 0.25f));
+        bot.y = __fadd_rn(bot.y, prolong_val(b1, b2, n1, n2, 0.25f, 0.25f));
+        o[0] = top;
+        o[B::W / 2] = bot;
+        a0 = b0, a1 = b1, a2 = b2;
+        b0 = n0, b1 = n1, b2 = n2;
+        o += B::W;  // two fine rows
       }
     }
   }

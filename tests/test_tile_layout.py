@@ -102,33 +102,30 @@ def test_up_kernel_layout(T, post):
             assert 0 <= min(offs) and max(offs) < N
             assert len(upd) == len(set(upd)) == sum(
                 1 for li in range(1, R - 1) for lj in range(1, R - 1) if (par0 + li + lj) & 1 == c)
-    # prolongation by 2x2 fine blocks: each region cell once, with the coarse
-    # column / row and the weights of the per-cell formula
-    NB = R // 2 + 1
+    # prolongation by even-aligned 2x2 fine blocks, a thread walking one
+    # column of blocks down a chunk of block rows: each region cell once,
+    # with the coarse column / row and the weights of the per-cell formula,
+    # every float2 aligned and every coarse load inside the block
+    NBC = R // 2
+    NCK = 256 // NBC
+    CL = (NBC + NCK - 1) // NCK
+    assert NCK >= 1 and OX % 2 == 0 and W % 2 == 0
     seen = set()
-    for b in range(NB):
-        for a in range(NB):
-            base = b * WC + OC + a
-            assert 0 <= base and base + WC + 1 < WC * RC
-            col = OX + 2 * a - 1
-            cells = []
-            if b > 0:
-                o = (2 * b - 1) * W + col
-                if a > 0:
-                    cells.append((o, 0.25, 0.25))
-                if a < NB - 1:
-                    cells.append((o + 1, 0.75, 0.25))
-            if b < NB - 1:
-                o = 2 * b * W + col
-                if a > 0:
-                    cells.append((o, 0.25, 0.75))
-                if a < NB - 1:
-                    cells.append((o + 1, 0.75, 0.75))
-            for o, fx, fy in cells:
+    for tid in range(256):
+        chunk, e = divmod(tid, NBC)
+        for d in range(chunk * CL, min(chunk * CL + CL, NBC)) if chunk < NCK else ():
+            for r in range(3):
+                for q in range(3):
+                    assert 0 <= (d + r) * WC + OC + e + q < WC * RC and OC + e + q < WC
+            top = 2 * d * W + OX + 2 * e
+            assert top % 2 == 0
+            # (offset, first coarse column, first coarse row, fx, fy)
+            for o, cx, cy, fx, fy in ((top, e, d, 0.75, 0.75), (top + 1, e + 1, d, 0.25, 0.75),
+                                      (top + W, e, d + 1, 0.75, 0.25), (top + W + 1, e + 1, d + 1, 0.25, 0.25)):
                 lj, rem = divmod(o, W)
                 li = rem - OX
                 assert 0 <= li < R and 0 <= lj < R and o not in seen
-                assert (lj + 1) >> 1 == b and (li + 1) >> 1 == a
+                assert (li + 1) >> 1 == cx and (lj + 1) >> 1 == cy
                 assert fx == (0.25 if li & 1 else 0.75) and fy == (0.25 if lj & 1 else 0.75)
                 seen.add(o)
     assert len(seen) == R * R
