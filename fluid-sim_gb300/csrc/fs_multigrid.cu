@@ -295,28 +295,43 @@ __device__ __forceinline__ void mg_up_body(float* smem, const float* __restrict_
   const int par0 = (gi0 + gj0) & 1;
   const int tid = threadIdx.y * blockDim.x + threadIdx.x, nthr = blockDim.x * blockDim.y;
   const int nc = n >> 1;
-  if constexpr (ACC) {
-    // the tile's double-float pressure, read and written after the sweeps:
-    // start its DRAM reads now (one 128-byte line per thread and array)
-    constexpr int LPR = (T + 31) / 32;  // 128-byte lines per tile row
-    for (int k = tid; k < T * LPR; k += nthr) {
-      const int y = k / LPR, x = (k - y * LPR) * 32;
-      const int gi = i0 + x, gj = j0 + y;
-      if (gi < n && gj < n) {
-        prefetch_l2(ph + (int64_t)gj * n + gi);
-        prefetch_l2(pl + (int64_t)gj * n + gi);
-      }
-    }
-  }
   // staging: the fine iterate and rhs of the region and the coarse block its
   // prolongation reads.  gi0 is even (T and H are), so fine region column li
   // samples coarse block columns (li + 1) / 2 and (li + 1) / 2 + 1 with weight
-  // 1/4 or 3/4 on the first (PROLONG, multigrid.js:99-131: sample at
+  // 1/4 or 3/4 on the second (PROLONG, multigrid.js:99-131: sample at
   // ((i+1/2)/2 - 1/2, (j+1/2)/2 - 1/2)).
   const int cgi0 = (gi0 >> 1) - 1, cgj0 = (gj0 >> 1) - 1;
   const int bx = i0 - B::LP, cbx = cgi0 - C::OC;
   const bool boxed = tma && bx >= 0 && bx + B::W <= n && gj0 >= 0 && gj0 + B::R <= n && cbx >= 0 &&
                      cbx + C::WC <= nc && cgj0 >= 0 && cgj0 + C::RC <= nc;
+  // The tile's double-float pressure, read and written after the sweeps.  A
+  // boxed tile (inside the grid, n % 4 == 0) loads its hi plane into
+  // registers now, PG float4 groups per thread, and prefetches its lo plane
+  // into L2; other tiles prefetch both planes (one 128-byte line per thread
+  // and array).
+  constexpr int G4 = T * T / 4, PG = (G4 + kTileThreads - 1) / kTileThreads;
+  float4 hpre[PG];
+  if constexpr (ACC) {
+    if (boxed) {
+#pragma unroll
+      for (int u = 0; u < PG; u++) {
+        const int k = tid + u * kTileThreads;
+        if (k < G4) {
+          const int y = k / (T / 4), x = (k - y * (T / 4)) * 4;
+          hpre[u] = *reinterpret_cast<const float4*>(ph + (int64_t)(j0 + y) * n + i0 + x);
+        }
+      }
+    }
+    constexpr int LPR = (T + 31) / 32;  // 128-byte lines per tile row
+    for (int k = tid; k < T * LPR; k += nthr) {
+      const int y = k / LPR, x = (k - y * LPR) * 32;
+      const int gi = i0 + x, gj = j0 + y;
+      if (gi < n && gj < n) {
+        if (!boxed) prefetch_l2(ph + (int64_t)gj * n + gi);
+        prefetch_l2(pl + (int64_t)gj * n + gi);
+      }
+    }
+  }
   if (boxed) {
     const TmaBox b[3] = {{xs, tm_x, bx, gj0}, {rs, tm_r, bx, gj0}, {cs, tm_c, cbx, cgj0}};
     if (!tma_stage_boxes(b, 3, (uint32_t)((2 * B::N + C::WC * C::RC) * sizeof(float)), &bar, err)) return;
@@ -375,32 +390,29 @@ __device__ __forceinline__ void mg_up_body(float* smem, const float* __restrict_
   // the tile: region cell (H + x, H + y) is box column LP + x of row H + y
   if constexpr (ACC) {
     if (boxed) {
-      // inside the grid, n % 4 == 0: float4 groups, two groups' double-float
-      // pressure loads in flight per thread
-      constexpr int G = T * T / 4, V = 2;
-      for (int k0 = tid; k0 < G; k0 += V * nthr) {
-        float4 hv[V], lv[V], ev[V];
-        int64_t gv[V];
+      // float4 groups: the hi plane loaded at the start, every lo load of the
+      // thread in flight at once
+      float4 lv[PG];
 #pragma unroll
-        for (int u = 0; u < V; u++) {
-          const int k = k0 + u * nthr;
-          gv[u] = -1;
-          if (k < G) {
-            const int y = k / (T / 4), x = (k - y * (T / 4)) * 4;
-            gv[u] = (int64_t)(j0 + y) * n + i0 + x;
-            hv[u] = *reinterpret_cast<const float4*>(ph + gv[u]);
-            lv[u] = *reinterpret_cast<const float4*>(pl + gv[u]);
-            ev[u] = *reinterpret_cast<const float4*>(xs + (H + y) * B::W + B::LP + x);
-          }
+      for (int u = 0; u < PG; u++) {
+        const int k = tid + u * kTileThreads;
+        if (k < G4) {
+          const int y = k / (T / 4), x = (k - y * (T / 4)) * 4;
+          lv[u] = *reinterpret_cast<const float4*>(pl + (int64_t)(j0 + y) * n + i0 + x);
         }
+      }
 #pragma unroll
-        for (int u = 0; u < V; u++)
-          if (gv[u] >= 0) {
-            const df p0 = df_add_f(df{hv[u].x, lv[u].x}, ev[u].x), p1 = df_add_f(df{hv[u].y, lv[u].y}, ev[u].y);
-            const df p2 = df_add_f(df{hv[u].z, lv[u].z}, ev[u].z), p3 = df_add_f(df{hv[u].w, lv[u].w}, ev[u].w);
-            *reinterpret_cast<float4*>(ph + gv[u]) = make_float4(p0.hi, p1.hi, p2.hi, p3.hi);
-            *reinterpret_cast<float4*>(pl + gv[u]) = make_float4(p0.lo, p1.lo, p2.lo, p3.lo);
-          }
+      for (int u = 0; u < PG; u++) {
+        const int k = tid + u * kTileThreads;
+        if (k < G4) {
+          const int y = k / (T / 4), x = (k - y * (T / 4)) * 4;
+          const int64_t g = (int64_t)(j0 + y) * n + i0 + x;
+          const float4 hv = hpre[u], ev = *reinterpret_cast<const float4*>(xs + (H + y) * B::W + B::LP + x);
+          const df p0 = df_add_f(df{hv.x, lv[u].x}, ev.x), p1 = df_add_f(df{hv.y, lv[u].y}, ev.y);
+          const df p2 = df_add_f(df{hv.z, lv[u].z}, ev.z), p3 = df_add_f(df{hv.w, lv[u].w}, ev.w);
+          *reinterpret_cast<float4*>(ph + g) = make_float4(p0.hi, p1.hi, p2.hi, p3.hi);
+          *reinterpret_cast<float4*>(pl + g) = make_float4(p0.lo, p1.lo, p2.lo, p3.lo);
+        }
       }
     } else {
       // four cells' double-float pressure loads in flight per thread
