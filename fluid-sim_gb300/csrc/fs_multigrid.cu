@@ -151,6 +151,31 @@ __device__ __forceinline__ bool tma_stage_boxes(const TmaBox* b, int count, uint
   return ok;
 }
 
+// The cells of a TMA box (pitch x rows, origin (bx, by) on an n x n grid)
+// that lie outside the grid, which the copy filled with zeros, take their
+// periodic images (one wrap: a tile is at most half the grid and the box at
+// most the grid).  Called after the copy completed; the caller synchronises.
+__device__ __forceinline__ void wrap_box_ring(float* dst, int pitch, int rows, const float* __restrict__ src,
+                                              int bx, int by, int n) {
+  const int tid = threadIdx.y * blockDim.x + threadIdx.x, nthr = blockDim.x * blockDim.y;
+  const int cl = max(0, -bx), cr = max(0, bx + pitch - n);
+  const int rb = max(0, -by), rt = max(0, by + rows - n);
+  // whole rows outside the grid
+  for (int k = tid; k < (rb + rt) * pitch; k += nthr) {
+    const int q = k / pitch, c = k - q * pitch;
+    const int r = q < rb ? q : rows - rt + (q - rb);
+    dst[r * pitch + c] = __ldg(src + (int64_t)wrap1(by + r, n) * n + wrap1(bx + c, n));
+  }
+  // the columns outside the grid of the other rows
+  const int nco = cl + cr;
+  if (nco > 0)
+    for (int k = tid; k < (rows - rb - rt) * nco; k += nthr) {
+      const int q = k / nco, m = k - q * nco;
+      const int r = rb + q, c = m < cl ? m : pitch - cr + (m - cl);
+      dst[r * pitch + c] = __ldg(src + (int64_t)(by + r) * n + wrap1(bx + c, n));
+    }
+}
+
 // One red-black half-sweep of colour c over region cells li, lj in [1, R-2]
 // (in place).  Cells whose neighbours are stale give stale values; they lie
 // outside the valid region and are never written back.  Each thread walks
@@ -189,7 +214,10 @@ __device__ __forceinline__ void rb_half_tile(float* xs, const float* rs, int c, 
 // ------------------------------------------------------------------ down
 // H = 2 * pre + 1.  xin == nullptr means the level starts from zero; otherwise
 // xin and xout must differ (the halo of a tile is another tile's interior).
-// Tiles whose box lies inside the grid are staged by TMA when tma != 0.
+// Staging (the up kernel's too), by the level's mode tma: 0 wrapped copies
+// everywhere; 1 a TMA copy for the tiles whose box lies inside the grid,
+// wrapped copies for the others; 2 a TMA copy for every tile, boxes across
+// the grid's edge fixed up afterwards (wrap_box_ring).
 template <int T, int H>
 __device__ __forceinline__ void mg_down_body(float* smem, const float* __restrict__ rhs,
                                              const float* __restrict__ xin, float* __restrict__ xout,
@@ -207,11 +235,20 @@ __device__ __forceinline__ void mg_down_body(float* smem, const float* __restric
   const int tid = threadIdx.y * blockDim.x + threadIdx.x, nthr = blockDim.x * blockDim.y;
   const int bx = i0 - B::LP;
   const bool boxed = tma && bx >= 0 && bx + B::W <= n && gj0 >= 0 && gj0 + B::R <= n;
+  const bool tile_in = tma && i0 + T <= n && j0 + T <= n;
   if (!xin)
     for (int k = tid; k < B::NA / 4; k += nthr) reinterpret_cast<float4*>(xs)[k] = make_float4(0.f, 0.f, 0.f, 0.f);
-  if (boxed) {
+  if (boxed || tma == 2) {
+    // the box's x is a multiple of 4 (16 bytes) wherever it lies; a box
+    // across the grid's edge (tma == 2) is copied with zero fill and its
+    // outer cells replaced by their periodic images
     const TmaBox b[2] = {{rs, tm_r, bx, gj0}, {xs, tm_x, bx, gj0}};
     if (!tma_stage_boxes(b, xin ? 2 : 1, (uint32_t)((xin ? 2 : 1) * B::N * sizeof(float)), &bar, err)) return;
+    if (!boxed) {
+      wrap_box_ring(rs, B::W, B::R, rhs, bx, gj0, n);
+      if (xin) wrap_box_ring(xs, B::W, B::R, xin, bx, gj0, n);
+      __syncthreads();
+    }
   } else {
     stage_region<B::R, B::W, B::OX>(rs, rhs, gi0, gj0, n);
     if (xin) stage_region<B::R, B::W, B::OX>(xs, xin, gi0, gj0, n);
@@ -223,7 +260,7 @@ __device__ __forceinline__ void mg_down_body(float* smem, const float* __restric
     __syncthreads();
   }
   // the tile: region cell (H + x, H + y) is box column LP + x of row H + y
-  if (boxed) {  // inside the grid, n % 4 == 0: float4 rows
+  if (tile_in) {  // inside the grid, n % 4 == 0: float4 rows
     for (int k = tid; k < T * T / 4; k += nthr) {
       const int y = k / (T / 4), x = (k - y * (T / 4)) * 4;
       *reinterpret_cast<float4*>(xout + (int64_t)(j0 + y) * n + i0 + x) =
@@ -304,15 +341,15 @@ __device__ __forceinline__ void mg_up_body(float* smem, const float* __restrict_
   const int bx = i0 - B::LP, cbx = cgi0 - C::OC;
   const bool boxed = tma && bx >= 0 && bx + B::W <= n && gj0 >= 0 && gj0 + B::R <= n && cbx >= 0 &&
                      cbx + C::WC <= nc && cgj0 >= 0 && cgj0 + C::RC <= nc;
+  const bool tile_in = tma && i0 + T <= n && j0 + T <= n;
   // The tile's double-float pressure, read and written after the sweeps.  A
-  // boxed tile (inside the grid, n % 4 == 0) loads its hi plane into
-  // registers now, PG float4 groups per thread, and prefetches its lo plane
-  // into L2; other tiles prefetch both planes (one 128-byte line per thread
-  // and array).
+  // tile inside the grid (n % 4 == 0) loads its hi plane into registers now,
+  // PG float4 groups per thread, and prefetches its lo plane into L2; other
+  // tiles prefetch both planes (one 128-byte line per thread and array).
   constexpr int G4 = T * T / 4, PG = (G4 + kTileThreads - 1) / kTileThreads;
   float4 hpre[PG];
   if constexpr (ACC) {
-    if (boxed) {
+    if (tile_in) {
 #pragma unroll
       for (int u = 0; u < PG; u++) {
         const int k = tid + u * kTileThreads;
@@ -327,14 +364,23 @@ __device__ __forceinline__ void mg_up_body(float* smem, const float* __restrict_
       const int y = k / LPR, x = (k - y * LPR) * 32;
       const int gi = i0 + x, gj = j0 + y;
       if (gi < n && gj < n) {
-        if (!boxed) prefetch_l2(ph + (int64_t)gj * n + gi);
+        if (!tile_in) prefetch_l2(ph + (int64_t)gj * n + gi);
         prefetch_l2(pl + (int64_t)gj * n + gi);
       }
     }
   }
-  if (boxed) {
+  if (boxed || tma == 2) {
+    // x of every box is a multiple of 4 (16 bytes) wherever it lies; boxes
+    // across the grid's edge (tma == 2) are copied with zero fill and their
+    // outer cells replaced by their periodic images
     const TmaBox b[3] = {{xs, tm_x, bx, gj0}, {rs, tm_r, bx, gj0}, {cs, tm_c, cbx, cgj0}};
     if (!tma_stage_boxes(b, 3, (uint32_t)((2 * B::N + C::WC * C::RC) * sizeof(float)), &bar, err)) return;
+    if (!boxed) {
+      wrap_box_ring(xs, B::W, B::R, xin, bx, gj0, n);
+      wrap_box_ring(rs, B::W, B::R, rhs, bx, gj0, n);
+      wrap_box_ring(cs, C::WC, C::RC, xc, cbx, cgj0, nc);
+      __syncthreads();
+    }
   } else {
     for (int k = tid; k < C::RC * C::RC; k += nthr) {
       const int lj = k / C::RC, li = k - lj * C::RC;
@@ -389,7 +435,7 @@ __device__ __forceinline__ void mg_up_body(float* smem, const float* __restrict_
   }
   // the tile: region cell (H + x, H + y) is box column LP + x of row H + y
   if constexpr (ACC) {
-    if (boxed) {
+    if (tile_in) {
       // float4 groups: the hi plane loaded at the start, every lo load of the
       // thread in flight at once
       float4 lv[PG];
@@ -444,7 +490,7 @@ __device__ __forceinline__ void mg_up_body(float* smem, const float* __restrict_
           }
       }
     }
-  } else if (boxed) {
+  } else if (tile_in) {
     for (int k = tid; k < T * T / 4; k += nthr) {
       const int y = k / (T / 4), x = (k - y * (T / 4)) * 4;
       *reinterpret_cast<float4*>(xout + (int64_t)(j0 + y) * n + i0 + x) =
@@ -940,6 +986,19 @@ static void tile_smem_attr(K kernel, size_t bytes, int device, std::atomic<uint6
 
 // tensor maps of a level's fields for the tile boxes of TileBox<T, H> (and the
 // coarse block); false: every tile stages with wrapped copies
+//
+// Staging mode of a level with tensor maps: the 64-cell tiles (>= 1024 CTAs,
+// 4 per SM by shared memory: more than one wave) stage every tile by TMA and
+// fix up the edge tiles' wrapped ring, which takes the edge tiles' per-element
+// copies out of the instruction stream the other CTAs share (2048^2: level-0
+// up 32.1 -> 28.7 us, down 23.8 -> 22.7 us); the smaller tiles run in one wave,
+// where the slowest CTA sets the time and the fix-up's second round trip
+// after the copy made the edge CTAs, and the launch, slower (levels 2-4 by
+// 1.2-3.2 us each), so their edge tiles keep the wrapped copies.
+template <int T>
+constexpr int tile_tma_mode() {
+  return T == 64 ? 2 : 1;
+}
 template <int T, int H>
 static bool tile_maps(Solver* s, int n, const float* const* f, CUtensorMap* const* m, int count) {
   using B = TileBox<T, H>;
@@ -960,7 +1019,7 @@ static void down_t(Solver* s, Level& L, const Level& C, bool has_x) {
   CUtensorMap tr{}, tx{};
   const float* f[2] = {L.rhs, xin};
   CUtensorMap* m[2] = {&tr, &tx};
-  const int tma = tile_maps<T, H>(s, L.n, f, m, 2) ? 1 : 0;
+  const int tma = tile_maps<T, H>(s, L.n, f, m, 2) ? tile_tma_mode<T>() : 0;
   FS_LAUNCH(s, level_name(s, L, "mg_down").c_str(), bytes,
             k_mg_down<T, H><<<grid, kTileBlock, smem, s->stream>>>(
                 L.rhs, xin, out, C.rhs, L.n, L.h2, s->prm.mg_pre_smooth, (float)s->prm.relax, tr, tx, tma,
@@ -985,7 +1044,8 @@ static void up_t(Solver* s, Level& L, const Level& C, float* acc_h, float* acc_l
   CUtensorMap tr{}, tx{}, tc{};
   const float* f[2] = {L.rhs, L.x};
   CUtensorMap* m[2] = {&tr, &tx};
-  const int tma = tile_maps<T, H>(s, L.n, f, m, 2) && box_tmap(s, C.x, C.n, C.n, CB::WC, CB::RC, &tc) ? 1 : 0;
+  const int tma =
+      tile_maps<T, H>(s, L.n, f, m, 2) && box_tmap(s, C.x, C.n, C.n, CB::WC, CB::RC, &tc) ? tile_tma_mode<T>() : 0;
   int* err = &s->dev->async_err;
   if (acc_h) {
     static std::atomic<uint64_t> attr{0};
@@ -1153,7 +1213,7 @@ static void down_class_t(Solver* const* ms, int count, int l, cudaStream_t st) {
     m.st = s->dev;
     const float* f[1] = {L.rhs};
     CUtensorMap* mp[1] = {&tab.tm[i]};
-    m.tma = tile_maps<T, H>(s, L.n, f, mp, 1) ? 1 : 0;
+    m.tma = tile_maps<T, H>(s, L.n, f, mp, 1) ? tile_tma_mode<T>() : 0;
   }
   static std::atomic<uint64_t> attr{0};
   constexpr size_t smem = down_smem_bytes<T, H>();
@@ -1206,7 +1266,9 @@ static void up_class_t(Solver* const* ms, int count, int l, cudaStream_t st) {
     m.st = s->dev;
     const float* f[2] = {L.rhs, L.x};
     CUtensorMap* mp[2] = {&tab.tm[i][0], &tab.tm[i][1]};
-    m.tma = tile_maps<T, H>(s, L.n, f, mp, 2) && box_tmap(s, C.x, C.n, C.n, CB::WC, CB::RC, &tab.tm[i][2]) ? 1 : 0;
+    m.tma = tile_maps<T, H>(s, L.n, f, mp, 2) && box_tmap(s, C.x, C.n, C.n, CB::WC, CB::RC, &tab.tm[i][2])
+                ? tile_tma_mode<T>()
+                : 0;
     if (!ACC) std::swap(L.x, L.x2);
   }
   static std::atomic<uint64_t> attr{0};

@@ -13,6 +13,7 @@ of the per-cell formula (multigrid.js:99-131).
 """
 from __future__ import annotations
 
+import numpy as np
 import pytest
 
 NTH = 256  # threads of a tile kernel
@@ -141,9 +142,14 @@ def tile_fits(t, n):
 
 @pytest.mark.parametrize("n", (2048, 1024, 528, 384, 200, 192, 132, 128, 72, 70, 68, 66))
 def test_tma_boxes_and_wrapped_staging(n):
-    """For every tile of every side a level may use: a TMA box that passes the
-    kernels' 'boxed' test starts 16-byte aligned and covers a tile inside the
-    grid, and the wrapped staging of the other tiles needs at most one wrap."""
+    """For every tile of every side a level may use: on a level with tensor
+    maps (n % 4 == 0, the box no larger than the grid) every tile's boxes --
+    the region's and the up kernel's coarse block -- start on a multiple of 4
+    columns (16 bytes), also where they cross the grid's edge, and every cell
+    of a box outside the grid (zero-filled by the copy, then replaced by its
+    periodic image) needs at most one wrap; a tile inside the grid writes back
+    in aligned float4 rows; the wrapped staging of levels without tensor maps
+    needs at most one wrap."""
     for T in TILES:
         if not tile_fits(T, n):
             continue
@@ -156,12 +162,56 @@ def test_tma_boxes_and_wrapped_staging(n):
                     i0, j0 = bx * T, by * T
                     gi0, gj0 = i0 - H, j0 - H
                     assert -n <= gi0 and gi0 + R - 1 < 2 * n and -n <= gj0 and gj0 + R - 1 < 2 * n
-                    boxed = n % 4 == 0 and i0 - LP >= 0 and i0 - LP + W <= n and gj0 >= 0 and gj0 + R <= n
-                    if boxed:
-                        assert (i0 - LP) % 4 == 0 and i0 + T <= n and j0 + T <= n and gi0 - (i0 - LP) == OX
+                    tma = n % 4 == 0 and W <= n and R <= n
+                    if tma:
+                        bx0 = i0 - LP
+                        assert bx0 % 4 == 0 and gi0 - bx0 == OX
+                        assert -n < bx0 and bx0 + W - 1 < 2 * n and -n < gj0 and gj0 + R - 1 < 2 * n
+                        if i0 + T <= n and j0 + T <= n:
+                            assert (j0 * n + i0) % 4 == 0 and T % 4 == 0
                     if H % 2 == 0:  # up kernel: the coarse block
                         RC, LPC, OC, WC, NC = coarsebox(T, H)
                         cgi0, cgj0 = (gi0 >> 1) - 1, (gj0 >> 1) - 1
                         assert -nc <= cgi0 and cgi0 + RC - 1 < 2 * nc and -nc <= cgj0 and cgj0 + RC - 1 < 2 * nc
-                        if boxed and cgi0 - OC >= 0 and cgi0 - OC + WC <= nc:
-                            assert (cgi0 - OC) % 4 == 0
+                        if tma and nc % 4 == 0 and WC <= nc and RC <= nc:
+                            cbx = cgi0 - OC
+                            assert cbx % 4 == 0 and -nc < cbx and cbx + WC - 1 < 2 * nc
+
+
+def _wrap_box_ring(dst, pitch, rows, src, bx, by, n):
+    """wrap_box_ring (fs_multigrid.cu) restated: the thread loops flattened."""
+    cl, cr = max(0, -bx), max(0, bx + pitch - n)
+    rb, rt = max(0, -by), max(0, by + rows - n)
+    w1 = lambda i: i + n if i < 0 else (i - n if i >= n else i)  # noqa: E731
+    for k in range((rb + rt) * pitch):
+        q, c = divmod(k, pitch)
+        r = q if q < rb else rows - rt + (q - rb)
+        dst[r * pitch + c] = src[w1(by + r) * n + w1(bx + c)]
+    nco = cl + cr
+    for k in range((rows - rb - rt) * nco):
+        q, m = divmod(k, nco)
+        r, c = rb + q, (m if m < cl else pitch - cr + (m - cl))
+        dst[r * pitch + c] = src[(by + r) * n + w1(bx + c)]
+
+
+@pytest.mark.parametrize("n,T,H", [(64, 16, 5), (68, 16, 4), (72, 32, 4), (132, 64, 5), (200, 16, 6), (128, 64, 4)])
+def test_edge_box_fixup_equals_periodic_staging(n, T, H):
+    """A box copied with zero fill outside the grid and then fixed up holds,
+    in every cell, the periodic image the wrapped staging would read."""
+    R, LP, OX, W, N, NA = tilebox(T, H)
+    if W > n or R > n:
+        pytest.skip("no tensor map for this level")
+    src = np.arange(n * n, dtype=np.float64) + 1.0
+    k = (n + T - 1) // T
+    for tby in range(k):
+        for tbx in range(k):
+            bx, by = tbx * T - LP, tby * T - H
+            box = np.zeros(W * R)
+            for r in range(R):
+                for c in range(W):
+                    gx, gy = bx + c, by + r
+                    if 0 <= gx < n and 0 <= gy < n:
+                        box[r * W + c] = src[gy * n + gx]
+            _wrap_box_ring(box, W, R, src, bx, by, n)
+            want = np.array([src[((by + r) % n) * n + (bx + c) % n] for r in range(R) for c in range(W)])
+            assert np.array_equal(box, want), (tbx, tby)
