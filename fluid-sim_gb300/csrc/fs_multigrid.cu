@@ -152,28 +152,97 @@ __device__ __forceinline__ bool tma_stage_boxes(const TmaBox* b, int count, uint
 }
 
 // The cells of a TMA box (pitch x rows, origin (bx, by) on an n x n grid)
-// that lie outside the grid, which the copy filled with zeros, take their
-// periodic images (one wrap: a tile is at most half the grid and the box at
-// most the grid).  Called after the copy completed; the caller synchronises.
-__device__ __forceinline__ void wrap_box_ring(float* dst, int pitch, int rows, const float* __restrict__ src,
-                                              int bx, int by, int n) {
-  const int tid = threadIdx.y * blockDim.x + threadIdx.x, nthr = blockDim.x * blockDim.y;
-  const int cl = max(0, -bx), cr = max(0, bx + pitch - n);
-  const int rb = max(0, -by), rt = max(0, by + rows - n);
-  // whole rows outside the grid
-  for (int k = tid; k < (rb + rt) * pitch; k += nthr) {
-    const int q = k / pitch, c = k - q * pitch;
-    const int r = q < rb ? q : rows - rt + (q - rb);
-    dst[r * pitch + c] = __ldg(src + (int64_t)wrap1(by + r, n) * n + wrap1(bx + c, n));
+// that lie outside the grid -- whole rows below / above it, then the columns
+// left / right of it in the other rows -- which the copy filled with zeros,
+// take their periodic images (one wrap: a tile is at most half the grid and
+// the box at most the grid).
+struct RingBox {
+  float* dst;
+  const float* src;
+  int pitch, rows, bx, by, n;
+};
+__device__ __forceinline__ int ring_cells(const RingBox& b) {
+  const int cl = max(0, -b.bx), cr = max(0, b.bx + b.pitch - b.n);
+  const int rb = max(0, -b.by), rt = max(0, b.by + b.rows - b.n);
+  return (rb + rt) * b.pitch + (b.rows - rb - rt) * (cl + cr);
+}
+// cell k < ring_cells(b): its shared-memory slot and the global value
+__device__ __forceinline__ float* ring_cell(const RingBox& b, int k, const float** src) {
+  const int cl = max(0, -b.bx), cr = max(0, b.bx + b.pitch - b.n);
+  const int rb = max(0, -b.by), rt = max(0, b.by + b.rows - b.n);
+  const int nrow = (rb + rt) * b.pitch;
+  int r, c;
+  if (k < nrow) {
+    const int q = k / b.pitch;
+    c = k - q * b.pitch;
+    r = q < rb ? q : b.rows - rt + (q - rb);
+  } else {
+    k -= nrow;
+    const int nco = cl + cr, q = k / nco, m = k - q * nco;
+    r = rb + q;
+    c = m < cl ? m : b.pitch - cr + (m - cl);
   }
-  // the columns outside the grid of the other rows
-  const int nco = cl + cr;
-  if (nco > 0)
-    for (int k = tid; k < (rows - rb - rt) * nco; k += nthr) {
-      const int q = k / nco, m = k - q * nco;
-      const int r = rb + q, c = m < cl ? m : pitch - cr + (m - cl);
-      dst[r * pitch + c] = __ldg(src + (int64_t)(by + r) * n + wrap1(bx + c, n));
+  *src = b.src + (int64_t)wrap1(b.by + r, b.n) * b.n + wrap1(b.bx + c, b.n);
+  return b.dst + r * b.pitch + c;
+}
+
+// TMA staging of a tile's boxes where some box crosses the grid's edge: the
+// copies are issued, then each thread loads up to RB ring cells into
+// registers while they are in flight, and after the (bounded) wait stores
+// them over the zero fill; ring cells beyond RB per thread (partial tiles)
+// are copied after the wait.  With no ring cell it is tma_stage_boxes.
+template <int RB>
+__device__ __forceinline__ bool tma_stage_ringed(const TmaBox* b, const RingBox* rg, int count, uint32_t bytes,
+                                                 uint64_t* bar, int* err) {
+  const int tid = threadIdx.y * blockDim.x + threadIdx.x, nthr = blockDim.x * blockDim.y;
+  if (tid == 0) {
+    tc::mbar_init(bar, 1);
+    tc::mbar_fence_init();
+  }
+  __syncthreads();
+  if (tid == 0) {
+    tc::mbar_arrive_expect_tx(bar, bytes);
+    for (int q = 0; q < count; q++) tc::tma_load_2d(b[q].dst, b[q].tm, b[q].x, b[q].y, bar);
+  }
+  // the rings of the boxes concatenated (constant indices only: the boxes
+  // stay in registers)
+  const int c0 = ring_cells(rg[0]), c1 = count > 1 ? ring_cells(rg[1]) : 0, c2 = count > 2 ? ring_cells(rg[2]) : 0;
+  const int total = c0 + c1 + c2;
+  auto cell = [&](int k, const float** src) -> float* {
+    if (k < c0) return ring_cell(rg[0], k, src);
+    if (k < c0 + c1) return ring_cell(rg[1], k - c0, src);
+    return ring_cell(rg[2], k - c0 - c1, src);
+  };
+  float rv[RB > 0 ? RB : 1];
+  float* rd[RB > 0 ? RB : 1];
+#pragma unroll
+  for (int u = 0; u < RB; u++) {
+    const int k = tid + u * nthr;
+    rd[u] = nullptr;
+    if (k < total) {
+      const float* src;
+      rd[u] = cell(k, &src);
+      rv[u] = __ldg(src);
     }
+  }
+  const bool ok = __syncthreads_and(tc::mbar_wait(bar, 0)) != 0;
+  if (!ok) {
+    if (tid == 0) atomicExch(err, 1);
+    tc::mbar_wait(bar, 0);
+    return false;
+  }
+  if (total > 0) {
+#pragma unroll
+    for (int u = 0; u < RB; u++)
+      if (rd[u]) *rd[u] = rv[u];
+    for (int k = tid + RB * nthr; k < total; k += nthr) {
+      const float* src;
+      float* d = cell(k, &src);
+      *d = __ldg(src);
+    }
+    __syncthreads();
+  }
+  return true;
 }
 
 // One red-black half-sweep of colour c over region cells li, lj in [1, R-2]
@@ -211,13 +280,21 @@ __device__ __forceinline__ void rb_half_tile(float* xs, const float* rs, int c, 
   }
 }
 
+// ring cells a thread loads before the TMA wait: the 64-cell tiles copy
+// their ring after the wait (the level-0 up kernel of a refinement cycle has
+// no registers to spare: 62 of the 64 that keep 4 CTAs per SM)
+template <int T, bool ACC>
+constexpr int ring_regs() {
+  return T == 64 ? 0 : 4;
+}
+
 // ------------------------------------------------------------------ down
 // H = 2 * pre + 1.  xin == nullptr means the level starts from zero; otherwise
 // xin and xout must differ (the halo of a tile is another tile's interior).
 // Staging (the up kernel's too), by the level's mode tma: 0 wrapped copies
 // everywhere; 1 a TMA copy for the tiles whose box lies inside the grid,
 // wrapped copies for the others; 2 a TMA copy for every tile, boxes across
-// the grid's edge fixed up afterwards (wrap_box_ring).
+// the grid's edge fixed up (tma_stage_ringed).
 template <int T, int H>
 __device__ __forceinline__ void mg_down_body(float* smem, const float* __restrict__ rhs,
                                              const float* __restrict__ xin, float* __restrict__ xout,
@@ -243,11 +320,12 @@ __device__ __forceinline__ void mg_down_body(float* smem, const float* __restric
     // across the grid's edge (tma == 2) is copied with zero fill and its
     // outer cells replaced by their periodic images
     const TmaBox b[2] = {{rs, tm_r, bx, gj0}, {xs, tm_x, bx, gj0}};
-    if (!tma_stage_boxes(b, xin ? 2 : 1, (uint32_t)((xin ? 2 : 1) * B::N * sizeof(float)), &bar, err)) return;
-    if (!boxed) {
-      wrap_box_ring(rs, B::W, B::R, rhs, bx, gj0, n);
-      if (xin) wrap_box_ring(xs, B::W, B::R, xin, bx, gj0, n);
-      __syncthreads();
+    const uint32_t bytes = (uint32_t)((xin ? 2 : 1) * B::N * sizeof(float));
+    if (boxed) {
+      if (!tma_stage_boxes(b, xin ? 2 : 1, bytes, &bar, err)) return;
+    } else {
+      const RingBox rg[2] = {{rs, rhs, B::W, B::R, bx, gj0, n}, {xs, xin, B::W, B::R, bx, gj0, n}};
+      if (!tma_stage_ringed<ring_regs<T, false>()>(b, rg, xin ? 2 : 1, bytes, &bar, err)) return;
     }
   } else {
     stage_region<B::R, B::W, B::OX>(rs, rhs, gi0, gj0, n);
@@ -374,12 +452,13 @@ __device__ __forceinline__ void mg_up_body(float* smem, const float* __restrict_
     // across the grid's edge (tma == 2) are copied with zero fill and their
     // outer cells replaced by their periodic images
     const TmaBox b[3] = {{xs, tm_x, bx, gj0}, {rs, tm_r, bx, gj0}, {cs, tm_c, cbx, cgj0}};
-    if (!tma_stage_boxes(b, 3, (uint32_t)((2 * B::N + C::WC * C::RC) * sizeof(float)), &bar, err)) return;
-    if (!boxed) {
-      wrap_box_ring(xs, B::W, B::R, xin, bx, gj0, n);
-      wrap_box_ring(rs, B::W, B::R, rhs, bx, gj0, n);
-      wrap_box_ring(cs, C::WC, C::RC, xc, cbx, cgj0, nc);
-      __syncthreads();
+    const uint32_t bytes = (uint32_t)((2 * B::N + C::WC * C::RC) * sizeof(float));
+    if (boxed) {
+      if (!tma_stage_boxes(b, 3, bytes, &bar, err)) return;
+    } else {
+      const RingBox rg[3] = {{xs, xin, B::W, B::R, bx, gj0, n}, {rs, rhs, B::W, B::R, bx, gj0, n},
+                             {cs, xc, C::WC, C::RC, cbx, cgj0, nc}};
+      if (!tma_stage_ringed<ring_regs<T, ACC>()>(b, rg, 3, bytes, &bar, err)) return;
     }
   } else {
     for (int k = tid; k < C::RC * C::RC; k += nthr) {
@@ -987,17 +1066,17 @@ static void tile_smem_attr(K kernel, size_t bytes, int device, std::atomic<uint6
 // tensor maps of a level's fields for the tile boxes of TileBox<T, H> (and the
 // coarse block); false: every tile stages with wrapped copies
 //
-// Staging mode of a level with tensor maps: the 64-cell tiles (>= 1024 CTAs,
-// 4 per SM by shared memory: more than one wave) stage every tile by TMA and
-// fix up the edge tiles' wrapped ring, which takes the edge tiles' per-element
-// copies out of the instruction stream the other CTAs share (2048^2: level-0
-// up 32.1 -> 28.7 us, down 23.8 -> 22.7 us); the smaller tiles run in one wave,
-// where the slowest CTA sets the time and the fix-up's second round trip
-// after the copy made the edge CTAs, and the launch, slower (levels 2-4 by
-// 1.2-3.2 us each), so their edge tiles keep the wrapped copies.
+// Staging mode of a level with tensor maps: every tile by TMA, the edge
+// tiles' ring fixed up (2).  On the 64-cell tiles (>= 1024 CTAs, 4 per SM by
+// shared memory: more than one wave) this takes the edge tiles' per-element
+// wrapped copies out of the instruction stream the other CTAs share
+// (2048^2: level-0 up 32.1 -> 28.7 us, down 23.8 -> 22.7 us).  The smaller
+// tiles run in one wave, where the slowest CTA sets the time: there the ring
+// loads must be in flight during the copy (tma_stage_ringed's registers); a
+// fix-up after the wait made levels 2-4 slower by 1.2-3.2 us per launch.
 template <int T>
 constexpr int tile_tma_mode() {
-  return T == 64 ? 2 : 1;
+  return 2;
 }
 template <int T, int H>
 static bool tile_maps(Solver* s, int n, const float* const* f, CUtensorMap* const* m, int count) {

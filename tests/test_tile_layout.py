@@ -178,20 +178,31 @@ def test_tma_boxes_and_wrapped_staging(n):
                             assert cbx % 4 == 0 and -nc < cbx and cbx + WC - 1 < 2 * nc
 
 
-def _wrap_box_ring(dst, pitch, rows, src, bx, by, n):
-    """wrap_box_ring (fs_multigrid.cu) restated: the thread loops flattened."""
+def _ring(pitch, rows, bx, by, n):
+    """ring_cells / ring_cell (fs_multigrid.cu) restated: the (row, column)
+    of every box cell outside the grid, in the kernel's order."""
     cl, cr = max(0, -bx), max(0, bx + pitch - n)
     rb, rt = max(0, -by), max(0, by + rows - n)
+    cells = []
+    for k in range((rb + rt) * pitch + (rows - rb - rt) * (cl + cr)):
+        nrow = (rb + rt) * pitch
+        if k < nrow:
+            q, c = divmod(k, pitch)
+            r = q if q < rb else rows - rt + (q - rb)
+        else:
+            q, m = divmod(k - nrow, cl + cr)
+            r, c = rb + q, (m if m < cl else pitch - cr + (m - cl))
+        cells.append((r, c))
+    return cells
+
+
+def _wrap_box_ring(dst, pitch, rows, src, bx, by, n):
     w1 = lambda i: i + n if i < 0 else (i - n if i >= n else i)  # noqa: E731
-    for k in range((rb + rt) * pitch):
-        q, c = divmod(k, pitch)
-        r = q if q < rb else rows - rt + (q - rb)
+    cells = _ring(pitch, rows, bx, by, n)
+    assert len(set(cells)) == len(cells)
+    for r, c in cells:
+        assert 0 <= r < rows and 0 <= c < pitch
         dst[r * pitch + c] = src[w1(by + r) * n + w1(bx + c)]
-    nco = cl + cr
-    for k in range((rows - rb - rt) * nco):
-        q, m = divmod(k, nco)
-        r, c = rb + q, (m if m < cl else pitch - cr + (m - cl))
-        dst[r * pitch + c] = src[(by + r) * n + w1(bx + c)]
 
 
 @pytest.mark.parametrize("n,T,H", [(64, 16, 5), (68, 16, 4), (72, 32, 4), (132, 64, 5), (200, 16, 6), (128, 64, 4)])
