@@ -280,12 +280,12 @@ __device__ __forceinline__ void rb_half_tile(float* xs, const float* rs, int c, 
   }
 }
 
-// ring cells a thread loads before the TMA wait: the 64-cell tiles copy
-// their ring after the wait (the level-0 up kernel of a refinement cycle has
-// no registers to spare: 62 of the 64 that keep 4 CTAs per SM)
+// ring cells a thread loads before the TMA wait: the level-0 up kernel of a
+// refinement cycle on 64-cell tiles copies its ring after the wait (no
+// registers to spare: 62 of the 64 that keep 4 CTAs per SM)
 template <int T, bool ACC>
 constexpr int ring_regs() {
-  return T == 64 ? 0 : 4;
+  return ACC && T == 64 ? 0 : 4;
 }
 
 // ------------------------------------------------------------------ down
