@@ -109,6 +109,22 @@ constexpr int kSW = kTX + 2 * kHalo, kSH = kTY + 2 * kHalo;
 // its velocity is bounded by the staged maximum too.
 constexpr float kFastDisp = 3.0f;
 
+// The two row interpolations of a bilinear sample, top = a + (b - a) fx and
+// bot = c + (d - c) fx, as one packed f32x2 subtract and one packed fused
+// multiply-add (sm_100 and later): the same two roundings per row as the
+// scalar difference and the contracted multiply-add.
+__device__ __forceinline__ void lerp_rows(float a, float b, float c, float d, float fx, float& top, float& bot) {
+  asm("{\n\t.reg .b64 lo, hi, df, f2, r;\n\t"
+      "mov.b64 lo, {%2, %4};\n\t"
+      "mov.b64 hi, {%3, %5};\n\t"
+      "mov.b64 f2, {%6, %6};\n\t"
+      "sub.rn.f32x2 df, hi, lo;\n\t"
+      "fma.rn.f32x2 r, df, f2, lo;\n\t"
+      "mov.b64 {%0, %1}, r;\n\t}"
+      : "=f"(top), "=f"(bot)
+      : "f"(a), "f"(b), "f"(c), "f"(d), "f"(fx));
+}
+
 template <bool FAST>
 struct TileView {
   const float* sm;  // kSH x kSW staged block
@@ -139,8 +155,8 @@ struct TileView {
       *lo = fminf(fminf(a, b), fminf(c, d));
       *hi = fmaxf(fmaxf(a, b), fmaxf(c, d));
     }
-    const float top = a + (b - a) * fx;
-    const float bot = c + (d - c) * fx;
+    float top, bot;
+    lerp_rows(a, b, c, d, fx, top, bot);
     return top + (bot - top) * fy;
   }
 };
