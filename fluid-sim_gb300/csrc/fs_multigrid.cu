@@ -790,27 +790,48 @@ constexpr int chain_floats() {
   return N0 == NMIN ? N0 * N0 : N0 * N0 + chain_floats<N0 / 2, NMIN>();
 }
 
+constexpr int kBottomThreads = 256;  // threads of the bottom-chain kernels
+
 template <int N, bool WARP>
 __device__ __forceinline__ void p2_sync() {
   if (WARP) __syncwarp();
   else __syncthreads();
 }
 
+// The chain's loops run a compile-time number of cells per thread (the CTA
+// has kBottomThreads threads, warp 0 has 32), fully unrolled, every result of
+// a phase computed before any is stored: the cells a phase writes are not
+// read in that phase (a colour's cells read only the other colour; restrict
+// and prolong write the other level's array, or the cell itself), so the
+// loads of a thread's cells are in flight together instead of waiting on the
+// stores of the cells before them.  The levels are latency-bound, one phase
+// between two barriers after another.
 template <int N, bool WARP>
 __device__ __forceinline__ void p2_smooth(float* x, const float* r, float h2, int sweeps, float w) {
-  constexpr int HALF = N / 2;
+  constexpr int HALF = N / 2, NT = WARP ? 32 : kBottomThreads;
+  constexpr int CELLS = N * HALF, PER = (CELLS + NT - 1) / NT;
   const int tid = WARP ? (int)(threadIdx.x & 31) : (int)threadIdx.x;
-  const int nthr = WARP ? 32 : (int)blockDim.x;
   for (int s = 0; s < 2 * sweeps; s++) {
     const int c = s & 1;
-    for (int idx = tid; idx < N * HALF; idx += nthr) {
-      const int j = idx / HALF, m = idx - j * HALF;
-      const int i = 2 * m + ((j + c) & 1);
-      const int row = j * N, k = row + i;
-      const int rm = (j == 0 ? N - 1 : j - 1) * N, rp = (j + 1 == N ? 0 : j + 1) * N;
-      const int im = i == 0 ? N - 1 : i - 1, ip = i + 1 == N ? 0 : i + 1;
-      x[k] = gs_update(x[k], x[row + im], x[row + ip], x[rm + i], x[rp + i], r[k], h2, w);
+    float nv[PER];
+    int kk[PER];
+#pragma unroll
+    for (int u = 0; u < PER; u++) {
+      const int idx = tid + u * NT;
+      kk[u] = -1;
+      if (CELLS % NT == 0 || idx < CELLS) {
+        const int j = idx / HALF, m = idx - j * HALF;
+        const int i = 2 * m + ((j + c) & 1);
+        const int row = j * N, k = row + i;
+        const int rm = (j == 0 ? N - 1 : j - 1) * N, rp = (j + 1 == N ? 0 : j + 1) * N;
+        const int im = i == 0 ? N - 1 : i - 1, ip = i + 1 == N ? 0 : i + 1;
+        kk[u] = k;
+        nv[u] = gs_update(x[k], x[row + im], x[row + ip], x[rm + i], x[rp + i], r[k], h2, w);
+      }
     }
+#pragma unroll
+    for (int u = 0; u < PER; u++)
+      if (CELLS % NT == 0 || kk[u] >= 0) x[kk[u]] = nv[u];
     p2_sync<N, WARP>();
   }
 }
@@ -818,11 +839,14 @@ __device__ __forceinline__ void p2_smooth(float* x, const float* r, float h2, in
 // residual of level N restricted into (cr, cx = 0) of level N/2
 template <int N, bool WARP>
 __device__ __forceinline__ void p2_restrict(const float* x, const float* r, float h2, float* cr, float* cx) {
-  constexpr int NC = N / 2;
+  constexpr int NC = N / 2, NT = WARP ? 32 : kBottomThreads, PER = (NC * NC + NT - 1) / NT;
   const int tid = WARP ? (int)(threadIdx.x & 31) : (int)threadIdx.x;
-  const int nthr = WARP ? 32 : (int)blockDim.x;
   const float ih2 = inv_h2(h2);
-  for (int k = tid; k < NC * NC; k += nthr) {
+  float rv[PER];
+#pragma unroll
+  for (int u = 0; u < PER; u++) {
+    const int k = tid + u * NT;
+    if ((NC * NC) % NT != 0 && k >= NC * NC) break;
     const int cj = k / NC, ci = k - cj * NC;
     float r4[4];
 #pragma unroll
@@ -833,7 +857,13 @@ __device__ __forceinline__ void p2_restrict(const float* x, const float* r, floa
       const int im = i == 0 ? N - 1 : i - 1, ip = i + 1 == N ? 0 : i + 1;
       r4[q] = residual_at(x[row + i], x[row + im], x[row + ip], x[rm + i], x[rp + i], r[row + i], ih2);
     }
-    cr[k] = restrict4(r4[0], r4[1], r4[2], r4[3]);
+    rv[u] = restrict4(r4[0], r4[1], r4[2], r4[3]);
+  }
+#pragma unroll
+  for (int u = 0; u < PER; u++) {
+    const int k = tid + u * NT;
+    if ((NC * NC) % NT != 0 && k >= NC * NC) break;
+    cr[k] = rv[u];
     cx[k] = 0.f;
   }
   p2_sync<N, WARP>();
@@ -842,17 +872,26 @@ __device__ __forceinline__ void p2_restrict(const float* x, const float* r, floa
 // x (level N) += bilinear prolongation of c (level N/2)
 template <int N, bool WARP>
 __device__ __forceinline__ void p2_prolong(float* x, const float* c) {
-  constexpr int NC = N / 2;
+  constexpr int NC = N / 2, NT = WARP ? 32 : kBottomThreads, PER = (N * N + NT - 1) / NT;
   const int tid = WARP ? (int)(threadIdx.x & 31) : (int)threadIdx.x;
-  const int nthr = WARP ? 32 : (int)blockDim.x;
-  for (int k = tid; k < N * N; k += nthr) {
+  float pv[PER];
+#pragma unroll
+  for (int u = 0; u < PER; u++) {
+    const int k = tid + u * NT;
+    if ((N * N) % NT != 0 && k >= N * N) break;
     const int j = k / N, i = k - j * N;
     const int ci0 = (i & 1) ? (i >> 1) : (i >> 1) - 1;
     const int cj0 = (j & 1) ? (j >> 1) : (j >> 1) - 1;
     const float fx = (i & 1) ? 0.25f : 0.75f, fy = (j & 1) ? 0.25f : 0.75f;
     const int x0 = ci0 < 0 ? ci0 + NC : ci0, x1 = ci0 + 1 >= NC ? ci0 + 1 - NC : ci0 + 1;
     const int y0 = (cj0 < 0 ? cj0 + NC : cj0) * NC, y1 = (cj0 + 1 >= NC ? cj0 + 1 - NC : cj0 + 1) * NC;
-    x[k] = __fadd_rn(x[k], prolong_val(c[y0 + x0], c[y0 + x1], c[y1 + x0], c[y1 + x1], fx, fy));
+    pv[u] = __fadd_rn(x[k], prolong_val(c[y0 + x0], c[y0 + x1], c[y1 + x0], c[y1 + x1], fx, fy));
+  }
+#pragma unroll
+  for (int u = 0; u < PER; u++) {
+    const int k = tid + u * NT;
+    if ((N * N) % NT != 0 && k >= N * N) break;
+    x[k] = pv[u];
   }
   p2_sync<N, WARP>();
 }
@@ -925,7 +964,7 @@ __device__ __forceinline__ void mg_bottom_chain_body(const float* __restrict__ r
 }
 
 template <int N0, int NMIN>
-__global__ void __launch_bounds__(256) k_mg_bottom_chain(const float* __restrict__ rhs_top,
+__global__ void __launch_bounds__(kBottomThreads) k_mg_bottom_chain(const float* __restrict__ rhs_top,
                                                          float* __restrict__ x_top, int has_x, BottomH2 H, int pre,
                                                          int post, int coarse, float* __restrict__ acc_h,
                                                          float* __restrict__ acc_l) {
@@ -1004,7 +1043,7 @@ __global__ void __launch_bounds__(256) k_mg_up_class(const __grid_constant__ UpT
 }
 
 template <int N0, int NMIN>
-__global__ void __launch_bounds__(256) k_mg_bottom_chain_class(const BottomTab tab, BottomH2 H, int pre, int post,
+__global__ void __launch_bounds__(kBottomThreads) k_mg_bottom_chain_class(const BottomTab tab, BottomH2 H, int pre, int post,
                                                                int coarse, int max_cycles) {
   const auto& a = tab.m[blockIdx.z];
   if (!member_active(a.st, max_cycles)) return;
@@ -1240,7 +1279,7 @@ void mg_vcycle_fused(Solver* s, bool first_has_x, float* acc_h, float* acc_l) {
     const BottomH2 H = bottom_h2(s, lb);
 #define FS_CHAIN(N0, NM)                                                                                     \
   FS_LAUNCH(s, "mg_bottom", bytes,                                                                           \
-            k_mg_bottom_chain<N0, NM><<<1, 256, 0, s->stream>>>(L[lb].rhs, L[lb].x, hx ? 1 : 0, H,            \
+            k_mg_bottom_chain<N0, NM><<<1, kBottomThreads, 0, s->stream>>>(L[lb].rhs, L[lb].x, hx ? 1 : 0, H,            \
                                                                  P.mg_pre_smooth, P.mg_post_smooth,            \
                                                                  P.mg_coarse_sweeps, bah, bal))
     switch (chain) {
@@ -1396,7 +1435,7 @@ int mg_vcycle_class(Solver* const* ms, int count, cudaStream_t st) {
     const BottomH2 H = bottom_h2(s0, lb);
     const dim3 grid(1, 1, count);
 #define FS_CHAIN(N0, NM)                                                                                        \
-  k_mg_bottom_chain_class<N0, NM><<<grid, 256, 0, st>>>(tab, H, P.mg_pre_smooth, P.mg_post_smooth,             \
+  k_mg_bottom_chain_class<N0, NM><<<grid, kBottomThreads, 0, st>>>(tab, H, P.mg_pre_smooth, P.mg_post_smooth,             \
                                                          P.mg_coarse_sweeps, P.max_cycles)
     switch (chain) {
       case 64: FS_CHAIN(64, 8); break;
