@@ -811,28 +811,52 @@ __device__ __forceinline__ void p2_smooth(float* x, const float* r, float h2, in
   constexpr int HALF = N / 2, NT = WARP ? 32 : kBottomThreads;
   constexpr int CELLS = N * HALF, PER = (CELLS + NT - 1) / NT;
   const int tid = WARP ? (int)(threadIdx.x & 31) : (int)threadIdx.x;
-  for (int s = 0; s < 2 * sweeps; s++) {
-    const int c = s & 1;
-    float nv[PER];
-    int kk[PER];
+  // When the threads cover whole rows of a colour (NT a multiple of N/2)
+  // and step an even number of rows, a thread's cells share their column and
+  // its neighbours' offsets: rows j0, j0 + RS, ...; only the first and last
+  // rows of the level wrap vertically.
+  constexpr bool ROWS = NT % HALF == 0 && (NT / HALF) % 2 == 0 && CELLS % NT == 0;
+  if constexpr (ROWS) {
+    constexpr int RS = NT / HALF;
+    const int j0 = tid / HALF, m = tid - j0 * HALF;
+    for (int s = 0; s < 2 * sweeps; s++) {
+      const int i = 2 * m + ((j0 + (s & 1)) & 1);
+      const int dl = i == 0 ? N - 1 : -1, dr = i + 1 == N ? 1 - N : 1;
+      float nv[PER];
 #pragma unroll
-    for (int u = 0; u < PER; u++) {
-      const int idx = tid + u * NT;
-      kk[u] = -1;
-      if (CELLS % NT == 0 || idx < CELLS) {
-        const int j = idx / HALF, m = idx - j * HALF;
-        const int i = 2 * m + ((j + c) & 1);
-        const int row = j * N, k = row + i;
-        const int rm = (j == 0 ? N - 1 : j - 1) * N, rp = (j + 1 == N ? 0 : j + 1) * N;
-        const int im = i == 0 ? N - 1 : i - 1, ip = i + 1 == N ? 0 : i + 1;
-        kk[u] = k;
-        nv[u] = gs_update(x[k], x[row + im], x[row + ip], x[rm + i], x[rp + i], r[k], h2, w);
+      for (int u = 0; u < PER; u++) {
+        const int j = j0 + u * RS, k = j * N + i;
+        const int db = j == 0 ? (N - 1) * N : -N, dt = j + 1 == N ? -(N - 1) * N : N;
+        nv[u] = gs_update(x[k], x[k + dl], x[k + dr], x[k + db], x[k + dt], r[k], h2, w);
       }
-    }
 #pragma unroll
-    for (int u = 0; u < PER; u++)
-      if (CELLS % NT == 0 || kk[u] >= 0) x[kk[u]] = nv[u];
-    p2_sync<N, WARP>();
+      for (int u = 0; u < PER; u++) x[(j0 + u * RS) * N + i] = nv[u];
+      p2_sync<N, WARP>();
+    }
+  } else {
+    for (int s = 0; s < 2 * sweeps; s++) {
+      const int c = s & 1;
+      float nv[PER];
+      int kk[PER];
+#pragma unroll
+      for (int u = 0; u < PER; u++) {
+        const int idx = tid + u * NT;
+        kk[u] = -1;
+        if (CELLS % NT == 0 || idx < CELLS) {
+          const int j = idx / HALF, m = idx - j * HALF;
+          const int i = 2 * m + ((j + c) & 1);
+          const int row = j * N, k = row + i;
+          const int rm = (j == 0 ? N - 1 : j - 1) * N, rp = (j + 1 == N ? 0 : j + 1) * N;
+          const int im = i == 0 ? N - 1 : i - 1, ip = i + 1 == N ? 0 : i + 1;
+          kk[u] = k;
+          nv[u] = gs_update(x[k], x[row + im], x[row + ip], x[rm + i], x[rp + i], r[k], h2, w);
+        }
+      }
+#pragma unroll
+      for (int u = 0; u < PER; u++)
+        if (CELLS % NT == 0 || kk[u] >= 0) x[kk[u]] = nv[u];
+      p2_sync<N, WARP>();
+    }
   }
 }
 
@@ -875,23 +899,44 @@ __device__ __forceinline__ void p2_prolong(float* x, const float* c) {
   constexpr int NC = N / 2, NT = WARP ? 32 : kBottomThreads, PER = (N * N + NT - 1) / NT;
   const int tid = WARP ? (int)(threadIdx.x & 31) : (int)threadIdx.x;
   float pv[PER];
-#pragma unroll
-  for (int u = 0; u < PER; u++) {
-    const int k = tid + u * NT;
-    if ((N * N) % NT != 0 && k >= N * N) break;
-    const int j = k / N, i = k - j * N;
+  // threads covering whole rows with an even row step: a thread's cells share
+  // their column, its coarse columns and both weights; only the first and
+  // last rows wrap to the other edge of the coarse level
+  constexpr bool ROWS = NT % N == 0 && (NT / N) % 2 == 0 && (N * N) % NT == 0;
+  if constexpr (ROWS) {
+    constexpr int RS = NT / N;
+    const int j0 = tid / N, i = tid - j0 * N;
     const int ci0 = (i & 1) ? (i >> 1) : (i >> 1) - 1;
-    const int cj0 = (j & 1) ? (j >> 1) : (j >> 1) - 1;
-    const float fx = (i & 1) ? 0.25f : 0.75f, fy = (j & 1) ? 0.25f : 0.75f;
+    const float fx = (i & 1) ? 0.25f : 0.75f, fy = (j0 & 1) ? 0.25f : 0.75f;
     const int x0 = ci0 < 0 ? ci0 + NC : ci0, x1 = ci0 + 1 >= NC ? ci0 + 1 - NC : ci0 + 1;
-    const int y0 = (cj0 < 0 ? cj0 + NC : cj0) * NC, y1 = (cj0 + 1 >= NC ? cj0 + 1 - NC : cj0 + 1) * NC;
-    pv[u] = __fadd_rn(x[k], prolong_val(c[y0 + x0], c[y0 + x1], c[y1 + x0], c[y1 + x1], fx, fy));
-  }
 #pragma unroll
-  for (int u = 0; u < PER; u++) {
-    const int k = tid + u * NT;
-    if ((N * N) % NT != 0 && k >= N * N) break;
-    x[k] = pv[u];
+    for (int u = 0; u < PER; u++) {
+      const int j = j0 + u * RS, k = j * N + i;
+      const int cj0 = (j & 1) ? (j >> 1) : (j >> 1) - 1;
+      const int y0 = (cj0 < 0 ? cj0 + NC : cj0) * NC, y1 = (cj0 + 1 >= NC ? cj0 + 1 - NC : cj0 + 1) * NC;
+      pv[u] = __fadd_rn(x[k], prolong_val(c[y0 + x0], c[y0 + x1], c[y1 + x0], c[y1 + x1], fx, fy));
+    }
+#pragma unroll
+    for (int u = 0; u < PER; u++) x[(j0 + u * RS) * N + i] = pv[u];
+  } else {
+#pragma unroll
+    for (int u = 0; u < PER; u++) {
+      const int k = tid + u * NT;
+      if ((N * N) % NT != 0 && k >= N * N) break;
+      const int j = k / N, i = k - j * N;
+      const int ci0 = (i & 1) ? (i >> 1) : (i >> 1) - 1;
+      const int cj0 = (j & 1) ? (j >> 1) : (j >> 1) - 1;
+      const float fx = (i & 1) ? 0.25f : 0.75f, fy = (j & 1) ? 0.25f : 0.75f;
+      const int x0 = ci0 < 0 ? ci0 + NC : ci0, x1 = ci0 + 1 >= NC ? ci0 + 1 - NC : ci0 + 1;
+      const int y0 = (cj0 < 0 ? cj0 + NC : cj0) * NC, y1 = (cj0 + 1 >= NC ? cj0 + 1 - NC : cj0 + 1) * NC;
+      pv[u] = __fadd_rn(x[k], prolong_val(c[y0 + x0], c[y0 + x1], c[y1 + x0], c[y1 + x1], fx, fy));
+    }
+#pragma unroll
+    for (int u = 0; u < PER; u++) {
+      const int k = tid + u * NT;
+      if ((N * N) % NT != 0 && k >= N * N) break;
+      x[k] = pv[u];
+    }
   }
   p2_sync<N, WARP>();
 }
