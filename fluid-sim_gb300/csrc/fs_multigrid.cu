@@ -867,28 +867,55 @@ __device__ __forceinline__ void p2_restrict(const float* x, const float* r, floa
   const int tid = WARP ? (int)(threadIdx.x & 31) : (int)threadIdx.x;
   const float ih2 = inv_h2(h2);
   float rv[PER];
+  // threads covering whole coarse rows: a thread's blocks share their two
+  // fine columns and the columns' neighbour offsets; only the level's first
+  // and last fine rows wrap
+  constexpr bool ROWS = NT % NC == 0 && (NC * NC) % NT == 0;
+  if constexpr (ROWS) {
+    constexpr int RS = NT / NC;
+    const int cj0 = tid / NC, ci = tid - cj0 * NC;
+    const int i0 = 2 * ci;
+    const int dl0 = i0 == 0 ? N - 1 : -1, dr1 = i0 + 2 == N ? 1 - N : 1;  // left of column i0, right of i0 + 1
 #pragma unroll
-  for (int u = 0; u < PER; u++) {
-    const int k = tid + u * NT;
-    if ((NC * NC) % NT != 0 && k >= NC * NC) break;
-    const int cj = k / NC, ci = k - cj * NC;
-    float r4[4];
-#pragma unroll
-    for (int q = 0; q < 4; q++) {
-      const int i = 2 * ci + (q & 1), j = 2 * cj + (q >> 1);
-      const int row = j * N;
-      const int rm = (j == 0 ? N - 1 : j - 1) * N, rp = (j + 1 == N ? 0 : j + 1) * N;
-      const int im = i == 0 ? N - 1 : i - 1, ip = i + 1 == N ? 0 : i + 1;
-      r4[q] = residual_at(x[row + i], x[row + im], x[row + ip], x[rm + i], x[rp + i], r[row + i], ih2);
+    for (int u = 0; u < PER; u++) {
+      const int j = 2 * (cj0 + u * RS), k0 = j * N + i0, k1 = k0 + N;
+      const int db = j == 0 ? (N - 1) * N : -N, dt = j + 2 == N ? -(N - 1) * N : N;  // below row j, above row j + 1
+      const float r00 = residual_at(x[k0], x[k0 + dl0], x[k0 + 1], x[k0 + db], x[k1], r[k0], ih2);
+      const float r10 = residual_at(x[k0 + 1], x[k0], x[k0 + 1 + dr1], x[k0 + 1 + db], x[k1 + 1], r[k0 + 1], ih2);
+      const float r01 = residual_at(x[k1], x[k1 + dl0], x[k1 + 1], x[k0], x[k1 + dt], r[k1], ih2);
+      const float r11 = residual_at(x[k1 + 1], x[k1], x[k1 + 1 + dr1], x[k0 + 1], x[k1 + 1 + dt], r[k1 + 1], ih2);
+      rv[u] = restrict4(r00, r10, r01, r11);
     }
-    rv[u] = restrict4(r4[0], r4[1], r4[2], r4[3]);
-  }
 #pragma unroll
-  for (int u = 0; u < PER; u++) {
-    const int k = tid + u * NT;
-    if ((NC * NC) % NT != 0 && k >= NC * NC) break;
-    cr[k] = rv[u];
-    cx[k] = 0.f;
+    for (int u = 0; u < PER; u++) {
+      const int k = (cj0 + u * RS) * NC + ci;
+      cr[k] = rv[u];
+      cx[k] = 0.f;
+    }
+  } else {
+#pragma unroll
+    for (int u = 0; u < PER; u++) {
+      const int k = tid + u * NT;
+      if ((NC * NC) % NT != 0 && k >= NC * NC) break;
+      const int cj = k / NC, ci = k - cj * NC;
+      float r4[4];
+#pragma unroll
+      for (int q = 0; q < 4; q++) {
+        const int i = 2 * ci + (q & 1), j = 2 * cj + (q >> 1);
+        const int row = j * N;
+        const int rm = (j == 0 ? N - 1 : j - 1) * N, rp = (j + 1 == N ? 0 : j + 1) * N;
+        const int im = i == 0 ? N - 1 : i - 1, ip = i + 1 == N ? 0 : i + 1;
+        r4[q] = residual_at(x[row + i], x[row + im], x[row + ip], x[rm + i], x[rp + i], r[row + i], ih2);
+      }
+      rv[u] = restrict4(r4[0], r4[1], r4[2], r4[3]);
+    }
+#pragma unroll
+    for (int u = 0; u < PER; u++) {
+      const int k = tid + u * NT;
+      if ((NC * NC) % NT != 0 && k >= NC * NC) break;
+      cr[k] = rv[u];
+      cx[k] = 0.f;
+    }
   }
   p2_sync<N, WARP>();
 }
