@@ -11,8 +11,9 @@
 //               the residual and its 2x2 restriction are formed; only the
 //               tile's x and the coarse right-hand side go back to HBM;
 //   k_mg_bottom one CTA runs every level <= 64 in shared memory: levels >= 32
-//               with the whole CTA, levels <= 16 (including the 40 coarse
-//               sweeps) with one warp and __syncwarp between half-sweeps;
+//               with the whole CTA, levels <= 16 (including the coarse
+//               sweeps, 40 by default) with one warp and __syncwarp between
+//               half-sweeps;
 //   k_mg_up     per level n > 64: prolongation-add of the coarse correction on
 //               the tile plus a halo of 2*post, then the post-smoothing sweeps.
 //
@@ -20,9 +21,10 @@
 // operation kernels, so the fused cycle reproduces them bit for bit.
 //
 // Shared-memory layout: the tile region row-major, its rows padded so that a
-// tile whose region lies inside the grid is staged by one TMA copy per field
-// (cp.async.bulk.tensor.2d, completion on an mbarrier); tiles on the
-// periodic edge are staged by wrapped 4-byte cp.async copies.
+// tile is staged by one TMA copy per field (cp.async.bulk.tensor.2d,
+// completion on an mbarrier); a tile on the periodic edge issues the same
+// copy and replaces the zero-filled cells outside the grid by their periodic
+// images.  Levels without tensor maps use wrapped 4-byte cp.async copies.
 #include <atomic>
 #include <string>
 #include <utility>
