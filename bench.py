@@ -208,6 +208,17 @@ GUESS_FACTOR = 2
 # the step is 1.4% faster (same-box A/B, 0.845 -> 0.833 ms)
 COARSE_SWEEPS = 8
 
+# red-black sweeps on the finest level in the first V-cycle of each projection
+# (pre, post; -1 = the cycle's 2, as the reference runs every cycle).  A first
+# cycle without them (the divergence restricted, the coarse levels' V(2,2)
+# prolongated into the pressure) leaves a larger residual that the next cycles
+# remove at the same count, 5 per step on this flow: the V-cycle model of the
+# solver (fluid-sim_gb300/vcycle_model.py) on right-hand sides dumped at steps
+# 20 .. 420 ends every projection below 1e-6, and on the GPU the 400 timed
+# steps all converge (worst max|div u| 8.3e-7 against 7.1e-7) in 0.7219
+# against 0.7380 ms (same box; (0, 1) 0.7262, (0, 2) 0.7303, (1, 1) 0.7314).
+FIRST_PRE, FIRST_POST = 0, 0
+
 
 def make_solver(pkg, n, device, guess="zero", relax=RELAX, coarse=None):
     """guess: "zero" (the reference's zero initial pressure), "warm" (the
@@ -216,7 +227,8 @@ def make_solver(pkg, n, device, guess="zero", relax=RELAX, coarse=None):
     s = pkg.GPUFluidSolver(n=n, nu=NU, advection="maccormack", pressure_solver="multigrid",
                            pressure_iterations=1, precision="mixed", pressure_tol=TOL, max_cycles=60,
                            warm_start=(guess == "warm"), device=device, relax=relax,
-                           mg_coarse_sweeps=COARSE_SWEEPS if coarse is None else coarse)
+                           mg_coarse_sweeps=COARSE_SWEEPS if coarse is None else coarse,
+                           mg_first_pre=FIRST_PRE, mg_first_post=FIRST_POST)
     if guess == "nn":
         g = pkg.PressureGuess(device=device)
         g.load(GUESS_WEIGHTS)
@@ -421,10 +433,12 @@ def run_gpu(args):
                 "workload": f"{n}x{n} MAC grid, channel flow (inflow u=1 through a fringe strip, no-slip wall "
                             f"slab) past {len(disks)} fixed disks, nu={NU}, "
                             "MacCormack, explicit diffusion, mixed-precision multigrid V(2,2) "
-                            f"(red-black relaxation {args.relax}) iterated to "
+                            f"(red-black relaxation {args.relax}; finest-level sweeps of each projection's "
+                            f"first cycle {args.first_pre}/{args.first_post}, -1 = 2) iterated to "
                             f"max|div u| <= {TOL}",
                 "n": n, "disks": len(disks), "dt": dt, "tol": TOL, "guess": args.guess, "relax": args.relax,
                 "coarse_sweeps": args.coarse_sweeps,
+                "first_cycle_finest_sweeps": [args.first_pre, args.first_post],
                 "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
                 "l2": "working set ~0.35 GB > 129 MB L2; no flush between steps",
                 "cycles_per_step": cycles_timed,
@@ -655,6 +669,10 @@ def main():
                     help="skip timing the learned guess and the warm start beside the headline")
     ap.add_argument("--coarse-sweeps", type=int, default=COARSE_SWEEPS,
                     help="red-black sweeps on the coarsest multigrid level (the reference runs 40)")
+    ap.add_argument("--first-pre", type=int, default=FIRST_PRE,
+                    help="finest-level sweeps before restriction in a projection's first V-cycle (-1 = 2)")
+    ap.add_argument("--first-post", type=int, default=FIRST_POST,
+                    help="finest-level sweeps after prolongation in a projection's first V-cycle (-1 = 2)")
     ap.add_argument("--forced-steps", type=int, default=5000,
                     help="steps of the 1024^2 forced-turbulence run (spectrum every 100; 0 = skip)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -662,6 +680,7 @@ def main():
                     help="skip the comparison of u, v after a few steps with the f64 oracle")
     args = ap.parse_args()
     globals()["COARSE_SWEEPS"] = args.coarse_sweeps
+    globals()["FIRST_PRE"], globals()["FIRST_POST"] = args.first_pre, args.first_post
     if args.warmup < 3 and args.impl != "reference":
         args.warmup = 3
     if args.impl == "reference":

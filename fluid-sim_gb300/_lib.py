@@ -85,7 +85,8 @@ class Params(C.Structure):
                 ("mg_post_smooth", C.c_int32), ("mg_coarse_sweeps", C.c_int32), ("mg_min_size", C.c_int32),
                 ("warm_start", C.c_int32), ("device", C.c_int32), ("kernel_variant", C.c_int32),
                 ("dye_fade", C.c_double),
-                ("relax", C.c_double), ("pressure_tol_relative", C.c_int32)]
+                ("relax", C.c_double), ("pressure_tol_relative", C.c_int32), ("mg_first_pre", C.c_int32),
+                ("mg_first_post", C.c_int32)]
 
 
 class Mode(C.Structure):

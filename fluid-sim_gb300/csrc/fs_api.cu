@@ -152,6 +152,11 @@ static int create(const fs_params* prm, Solver* s) {
     return fail(nullptr, FS_ERR_INVALID_ARGUMENT, "bad iteration settings");
   if (P.mg_pre_smooth < 0 || P.mg_post_smooth < 0 || P.mg_coarse_sweeps < 0 || P.mg_min_size < 2)
     return fail(nullptr, FS_ERR_INVALID_ARGUMENT, "bad multigrid settings");
+  if (P.mg_first_pre < -1 || P.mg_first_pre > P.mg_pre_smooth || P.mg_first_post < -1 ||
+      P.mg_first_post > P.mg_post_smooth)
+    return fail(nullptr, FS_ERR_INVALID_ARGUMENT, "mg_first_pre / mg_first_post must be -1 or 0 .. the cycle's sweeps");
+  if ((P.mg_first_pre >= 0 || P.mg_first_post >= 0) && P.kernel_variant != 0)
+    return fail(nullptr, FS_ERR_UNSUPPORTED, "mg_first_pre / mg_first_post need the fused multigrid kernels");
   if (!(P.solid_mask_width > 0)) return fail(nullptr, FS_ERR_INVALID_ARGUMENT, "solid_mask_width must be > 0");
   if (P.kernel_variant < 0 || P.kernel_variant > 1) return fail(nullptr, FS_ERR_INVALID_ARGUMENT, "unknown kernel_variant");
 
@@ -749,6 +754,9 @@ FS_API void fs_params_default(fs_params* p) {
   p->kernel_variant = 0;
   p->dye_fade = 0.0;
   p->relax = 1.0;
+  p->pressure_tol_relative = 0;
+  p->mg_first_pre = -1;
+  p->mg_first_post = -1;
 }
 
 FS_API int fs_create(const fs_params* params, fs_solver** out) {
@@ -1564,7 +1572,8 @@ static bool class_plain(const fs_batch* b, const BatchClass& c) {
 
 // a member that can run its loop in a size class, and the settings a class shares
 static bool class_eligible(const Solver* s) {
-  return s->mixed && s->fused && s->prm.pressure_tol > 0 && !s->guess && s->g.nx == s->g.ny;
+  return s->mixed && s->fused && s->prm.pressure_tol > 0 && !s->guess && s->g.nx == s->g.ny &&
+         s->prm.mg_first_pre < 0 && s->prm.mg_first_post < 0;
 }
 static bool same_class(const Solver* a, const Solver* b) {
   const fs_params &p = a->prm, &q = b->prm;

@@ -33,7 +33,8 @@ def make_params(n: int = 256, nx: int | None = None, ny: int | None = None, lx: 
                 precision: str = "f32", pressure_tol: float = 0.0, max_cycles: int = 50, mg_pre_smooth: int = 2,
                 mg_post_smooth: int = 2, mg_coarse_sweeps: int = 40, mg_min_size: int = 8,
                 warm_start: bool = False, device: int = 0, kernel_variant: int = 0, dye_fade: float = 0.0,
-                relax: float = 1.0, pressure_tol_relative: bool = False, **camel) -> "L.Params":
+                relax: float = 1.0, pressure_tol_relative: bool = False, mg_first_pre: int = -1,
+                mg_first_post: int = -1, **camel) -> "L.Params":
     """fs_params from the reference's option names (camelCase accepted);
     unknown names are rejected (the reference silently defaults)."""
     solid_mask_width = camel.pop("solidMaskWidth", solid_mask_width)
@@ -69,6 +70,7 @@ def make_params(n: int = 256, nx: int | None = None, ny: int | None = None, lx: 
     p.dye_fade = dye_fade
     p.relax = relax
     p.pressure_tol_relative = int(bool(pressure_tol_relative))
+    p.mg_first_pre, p.mg_first_post = mg_first_pre, mg_first_post
     return p
 
 

@@ -140,6 +140,12 @@ typedef struct fs_params {
                                  times the max residual the projection started from
                                  (a relative residual), 0 (default): at max|div u| <=
                                  pressure_tol */
+  int32_t mg_first_pre;       /* red-black sweeps on the finest level before restriction
+                                 in the first V-cycle of each MIXED projection, 0 ..
+                                 mg_pre_smooth; -1 (default): mg_pre_smooth, as every
+                                 cycle of the reference.  Fused multigrid only. */
+  int32_t mg_first_post;      /* likewise after prolongation, 0 .. mg_post_smooth;
+                                 -1 (default): mg_post_smooth */
 } fs_params;
 
 /* one forcing mode, as setForcing's {kx, ky, phase} (solver.js:370-385) */

@@ -44,6 +44,9 @@ def test_params_default_matches_reference_defaults(lib):
     assert p.pressure_solver == 0 and p.pressure_iterations == 40  # jacobi, 40
     # Multigrid(solver, {preSmooth: 2, postSmooth: 2, coarseSweeps: 40}), minSize 8
     assert (p.mg_pre_smooth, p.mg_post_smooth, p.mg_coarse_sweeps, p.mg_min_size) == (2, 2, 40, 8)
+    # every V-cycle smooths the finest level like the others, as the reference's do
+    assert (p.mg_first_pre, p.mg_first_post) == (-1, -1)
+    assert p.relax == 1.0 and p.pressure_tol_relative == 0
 
 
 def test_invalid_parameters_fail_before_touching_a_device(lib):
@@ -65,6 +68,10 @@ def test_invalid_parameters_fail_before_touching_a_device(lib):
     st, msg = create(confinement=0.5)
     assert st == 6 and "confinement" in msg
     assert create(pressure_solver=2, nx=64, ny=32)[0] == 1  # multigrid needs a square grid
+    assert create(mg_first_pre=3)[0] == 1  # more than the cycle's mg_pre_smooth
+    assert create(mg_first_post=-2)[0] == 1
+    st, msg = create(mg_first_pre=0, kernel_variant=1)
+    assert st == 6 and "fused" in msg
     assert lib.fs_status_string(4) == b"pressure tolerance not met"
 
 

@@ -15,7 +15,9 @@ not just the last step's flag).
 
 * 1024^2 with 64-cell level-0 tiles forced (the 2048^2 level-0 kernels' tile
   side; the built-in rule picks 32 at 1024^2), 10 steps;
-* 2048^2 itself, the bench's tiles, 5 steps.
+* 2048^2 itself, the bench's tiles and first-cycle setting, 5 steps;
+* the first V-cycle of each projection without the finest level's sweeps
+  (fs_params mg_first_pre / mg_first_post).
 """
 from __future__ import annotations
 
@@ -33,12 +35,16 @@ def pkg(fs):
     return fs
 
 
-def _run(pkg, O, n, steps, tiles=None):
+def _gpu(pkg, n, first=(-1, -1)):
+    return pkg.GPUFluidSolver(n=n, nu=NU, advection="maccormack", pressure_solver="multigrid", pressure_iterations=1,
+                              precision="mixed", pressure_tol=TOL, max_cycles=60, relax=RELAX,
+                              mg_coarse_sweeps=COARSE, mg_first_pre=first[0], mg_first_post=first[1])
+
+
+def _run(pkg, O, n, steps, tiles=None, first=(-1, -1)):
     u0, v0, disks, dt, ch = pkg.workload.channel_workload(n, 5)
     assert len(disks) == 5
-    s = pkg.GPUFluidSolver(n=n, nu=NU, advection="maccormack", pressure_solver="multigrid", pressure_iterations=1,
-                           precision="mixed", pressure_tol=TOL, max_cycles=60, relax=RELAX,
-                           mg_coarse_sweeps=COARSE)
+    s = _gpu(pkg, n, first)
     if tiles is not None:
         s.set_mg_tiles(tiles)
         assert s.mg_tiles()[0] == tiles[0]
@@ -78,4 +84,36 @@ def test_bench_config_1024_tile64_matches_oracle(pkg, O):
 
 
 def test_bench_config_2048_matches_oracle(pkg, O):
-    _run(pkg, O, 2048, 5)
+    """the bench's settings, the first V-cycle of each projection without the
+    finest level's sweeps included"""
+    _run(pkg, O, 2048, 5, first=(0, 0))
+
+
+def test_first_cycle_without_finest_sweeps_matches_oracle(pkg, O):
+    """mg_first_pre = mg_first_post = 0: the first V-cycle of each projection
+    runs no sweeps on the finest level (restriction of the divergence, the
+    coarse levels' V(2,2), prolongation into the pressure); every projection
+    still meets 1e-6 and the fields match the oracle."""
+    _run(pkg, O, 1024, 10, tiles=[64, 0, 0, 0], first=(0, 0))
+
+
+def test_first_cycle_sweeps_of_the_cycle_change_nothing(pkg):
+    """mg_first_pre / mg_first_post equal to the cycle's sweeps (2, 2) give the
+    default (-1, -1) bit for bit; (0, 0) meets the tolerance every step."""
+    n, steps = 512, 6
+    u0, v0, disks, dt, ch = pkg.workload.channel_workload(n, 5)
+    out = []
+    for first in ((-1, -1), (2, 2), (0, 0)):
+        s = _gpu(pkg, n, first)
+        s.upload_velocity(u0, v0)
+        s.set_channel(ch)
+        s.set_solids(disks)
+        c0 = s.total_cycles()
+        for _ in range(steps):
+            s.step(dt)
+        out.append((s.read_velocity(), s.total_cycles() - c0, s.convergence_record()))
+        s.destroy()
+    (a, ca, _), (b, cb, _), (_, cz, rz) = out
+    assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1]) and ca == cb
+    assert rz["failed_steps"] == 0 and rz["steps"] == steps, rz
+    assert cz <= ca + steps, (cz, ca)
