@@ -457,7 +457,11 @@ static int pressure_solve(Solver* s, bool capture, bool defer = false, bool star
   }
   if (!tol) {
     if (mg) {
-      for (int k = 0; k < iters; k++) mg_cycle(s, false);
+      for (int k = 0; k < iters; k++) {
+        s->mg_cycle_index = k;
+        mg_cycle(s, false);
+      }
+      s->mg_cycle_index = -1;
     } else if (s->mixed) {
       flat_cycle(s, iters, false);
     } else {
@@ -483,8 +487,10 @@ static int pressure_solve(Solver* s, bool capture, bool defer = false, bool star
   const double lim = P.pressure_tol_relative ? P.pressure_tol * m : P.pressure_tol;
   int c = 0;
   while (!(m <= lim) && c < P.max_cycles && std::isfinite(m)) {
+    s->mg_cycle_index = c;
     if (mg) mg_cycle(s, true);
     else flat_cycle(s, iters, true);
+    s->mg_cycle_index = -1;
     if ((rc = read_red(s, &m))) return rc;
     c++;
   }

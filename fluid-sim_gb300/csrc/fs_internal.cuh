@@ -154,6 +154,10 @@ struct Solver {
   double graph_dt = 0;
   bool graph_ok = false;        // graph_exec matches the current forcing / solids
   int failed_captures = 0;      // step captures that failed (each leaves its partial graph)
+  // the cycle being enqueued when the host knows it (eager loops, fixed cycle
+  // counts: 0, 1, ...), -1 inside a captured tolerance loop, where the device's
+  // cycle count tells the kernels (fs_params mg_first_pre / mg_first_post)
+  int mg_cycle_index = -1;
   bool stats_on_device = false; // the last projection ran inside a graph
   cudaStream_t body_stream = nullptr;  // captures the body of the tolerance loop
   // batch membership: eager work goes to the batch's shared stream; own_stream

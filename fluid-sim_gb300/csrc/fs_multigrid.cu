@@ -385,9 +385,10 @@ __global__ void __launch_bounds__(256)
               float* __restrict__ crhs, int n, float h2, int pre, float w, const __grid_constant__ CUtensorMap tm_r,
               const __grid_constant__ CUtensorMap tm_x, int tma, int* err, const int* first_cycle, int first_pre) {
   extern __shared__ float tile_dyn[];
-  // the first cycle of a projection (the loop's cycle count still 0) may run
-  // fewer sweeps on this level (fs_params mg_first_pre, at most pre)
-  if (first_cycle && *first_cycle == 0) pre = first_pre;
+  // the first cycle of a projection may run fewer sweeps on this level
+  // (fs_params mg_first_pre, at most pre): first_pre >= 0 applies it, inside
+  // a captured loop only while the loop's cycle count is still 0
+  if (first_pre >= 0 && (!first_cycle || *first_cycle == 0)) pre = first_pre;
   mg_down_body<T, H>(tile_smem(tile_dyn), rhs, xin, xout, crhs, n, h2, pre, w, &tm_r, &tm_x, tma, err);
 }
 
@@ -597,7 +598,7 @@ __global__ void __launch_bounds__(256)
             const __grid_constant__ CUtensorMap tm_x, const __grid_constant__ CUtensorMap tm_c, int tma, int* err,
             const int* first_cycle, int first_post) {
   extern __shared__ float tile_dyn[];
-  if (first_cycle && *first_cycle == 0) post = first_post;  // as k_mg_down
+  if (first_post >= 0 && (!first_cycle || *first_cycle == 0)) post = first_post;  // as k_mg_down
   mg_up_body<T, H, ACC>(tile_smem(tile_dyn), rhs, xin, xout, xc, n, h2, post, ph, pl, w, &tm_r, &tm_x, &tm_c, tma,
                         err);
 }
@@ -1204,10 +1205,11 @@ static bool tile_maps(Solver* s, int n, const float* const* f, CUtensorMap* cons
   return true;
 }
 
-// first >= 0: the sweeps of this level in the first cycle of a projection
-// (read on the device from the loop's cycle count)
+// first >= 0: the sweeps of this level in the first cycle of a projection;
+// cyc: the loop's cycle count on the device that decides (nullptr: the host
+// knows this is the first cycle)
 template <int T, int H>
-static void down_t(Solver* s, Level& L, const Level& C, bool has_x, int first) {
+static void down_t(Solver* s, Level& L, const Level& C, bool has_x, int first, const int* cyc) {
   static std::atomic<uint64_t> attr{0};
   constexpr size_t smem = down_smem_bytes<T, H>();
   tile_smem_attr(k_mg_down<T, H>, smem, s->prm.device, attr);
@@ -1219,25 +1221,26 @@ static void down_t(Solver* s, Level& L, const Level& C, bool has_x, int first) {
   const float* f[2] = {L.rhs, xin};
   CUtensorMap* m[2] = {&tr, &tx};
   const int tma = tile_maps<T, H>(s, L.n, f, m, 2) ? tile_tma_mode<T>() : 0;
-  FS_LAUNCH(s, level_name(s, L, "mg_down").c_str(), bytes,
+  // a first cycle the host knows is profiled under its own name
+  const std::string name = level_name(s, L, "mg_down") + (first >= 0 && !cyc ? "_first" : "");
+  FS_LAUNCH(s, name.c_str(), bytes,
             k_mg_down<T, H><<<grid, kTileBlock, smem, s->stream>>>(
                 L.rhs, xin, out, C.rhs, L.n, L.h2, s->prm.mg_pre_smooth, (float)s->prm.relax, tr, tx, tma,
-                &s->dev->async_err, first >= 0 ? &s->dev->cycles : nullptr,
-                first < s->prm.mg_pre_smooth ? first : s->prm.mg_pre_smooth));
+                &s->dev->async_err, cyc, first < s->prm.mg_pre_smooth ? first : s->prm.mg_pre_smooth));
   if (has_x) std::swap(L.x, L.x2);
 }
 
 template <int H>
-static void down(Solver* s, Level& L, const Level& C, bool has_x, int first) {
+static void down(Solver* s, Level& L, const Level& C, bool has_x, int first, const int* cyc) {
   switch (mg_tile(s, (int)(&L - s->lev.data()))) {
-    case 64: down_t<64, H>(s, L, C, has_x, first); break;
-    case 32: down_t<32, H>(s, L, C, has_x, first); break;
-    default: down_t<16, H>(s, L, C, has_x, first); break;
+    case 64: down_t<64, H>(s, L, C, has_x, first, cyc); break;
+    case 32: down_t<32, H>(s, L, C, has_x, first, cyc); break;
+    default: down_t<16, H>(s, L, C, has_x, first, cyc); break;
   }
 }
 
 template <int T, int H>
-static void up_t(Solver* s, Level& L, const Level& C, float* acc_h, float* acc_l, int first) {
+static void up_t(Solver* s, Level& L, const Level& C, float* acc_h, float* acc_l, int first, const int* cyc) {
   using CB = CoarseBox<T, H>;
   dim3 grid((L.n + T - 1) / T, (L.n + T - 1) / T);
   constexpr size_t smem = up_smem_bytes<T, H>();
@@ -1251,11 +1254,10 @@ static void up_t(Solver* s, Level& L, const Level& C, float* acc_h, float* acc_l
     static std::atomic<uint64_t> attr{0};
     tile_smem_attr(k_mg_up<T, H, true>, smem, s->prm.device, attr);
     double bytes = (double)L.n * L.n * 24.0 + (double)C.n * C.n * 4.0;
-    FS_LAUNCH(s, "mg_up_acc", bytes,
+    FS_LAUNCH(s, first >= 0 && !cyc ? "mg_up_acc_first" : "mg_up_acc", bytes,
               k_mg_up<T, H, true><<<grid, kTileBlock, smem, s->stream>>>(
                   L.rhs, L.x, nullptr, C.x, L.n, L.h2, s->prm.mg_post_smooth, acc_h, acc_l, (float)s->prm.relax, tr,
-                  tx, tc, tma, err, first >= 0 ? &s->dev->cycles : nullptr,
-                  first < s->prm.mg_post_smooth ? first : s->prm.mg_post_smooth));
+                  tx, tc, tma, err, cyc, first < s->prm.mg_post_smooth ? first : s->prm.mg_post_smooth));
     return;
   }
   static std::atomic<uint64_t> attr{0};
@@ -1264,17 +1266,16 @@ static void up_t(Solver* s, Level& L, const Level& C, float* acc_h, float* acc_l
   FS_LAUNCH(s, level_name(s, L, "mg_up").c_str(), bytes,
             k_mg_up<T, H, false><<<grid, kTileBlock, smem, s->stream>>>(
                 L.rhs, L.x, L.x2, C.x, L.n, L.h2, s->prm.mg_post_smooth, nullptr, nullptr, (float)s->prm.relax, tr,
-                tx, tc, tma, err, first >= 0 ? &s->dev->cycles : nullptr,
-                first < s->prm.mg_post_smooth ? first : s->prm.mg_post_smooth));
+                tx, tc, tma, err, cyc, first < s->prm.mg_post_smooth ? first : s->prm.mg_post_smooth));
   std::swap(L.x, L.x2);
 }
 
 template <int H>
-static void up(Solver* s, Level& L, const Level& C, float* acc_h, float* acc_l, int first) {
+static void up(Solver* s, Level& L, const Level& C, float* acc_h, float* acc_l, int first, const int* cyc) {
   switch (mg_tile(s, (int)(&L - s->lev.data()))) {
-    case 64: up_t<64, H>(s, L, C, acc_h, acc_l, first); break;
-    case 32: up_t<32, H>(s, L, C, acc_h, acc_l, first); break;
-    default: up_t<16, H>(s, L, C, acc_h, acc_l, first); break;
+    case 64: up_t<64, H>(s, L, C, acc_h, acc_l, first, cyc); break;
+    case 32: up_t<32, H>(s, L, C, acc_h, acc_l, first, cyc); break;
+    default: up_t<16, H>(s, L, C, acc_h, acc_l, first, cyc); break;
   }
 }
 
@@ -1345,15 +1346,24 @@ void mg_vcycle_fused(Solver* s, bool first_has_x, float* acc_h, float* acc_l) {
   const int lb = bottom_first_level(s);
   const fs_params& P = s->prm;
   // the finest level of a MIXED refinement cycle (acc_h: the correction goes
-  // into the double-float pressure) may run fewer sweeps in the first cycle
-  const int fpre = acc_h ? P.mg_first_pre : -1, fpost = acc_h ? P.mg_first_post : -1;
+  // into the double-float pressure) may run fewer sweeps in the first cycle of
+  // a projection: the host knows which cycle it enqueues (mg_cycle_index >= 0)
+  // except inside a captured tolerance loop, where the kernels read the loop's
+  // cycle count on the device
+  int fpre = -1, fpost = -1;
+  const int* cyc = nullptr;
+  if (acc_h && s->mg_cycle_index <= 0) {
+    fpre = P.mg_first_pre;
+    fpost = P.mg_first_post;
+    if (s->mg_cycle_index < 0 && (fpre >= 0 || fpost >= 0)) cyc = &s->dev->cycles;
+  }
   for (int l = 0; l < lb; l++) {
     bool hx = l == 0 && first_has_x;
     const int f = l == 0 ? fpre : -1;
     switch (P.mg_pre_smooth) {
-      case 1: down<3>(s, L[l], L[l + 1], hx, f); break;
-      case 2: down<5>(s, L[l], L[l + 1], hx, f); break;
-      default: down<7>(s, L[l], L[l + 1], hx, f); break;
+      case 1: down<3>(s, L[l], L[l + 1], hx, f, cyc); break;
+      case 2: down<5>(s, L[l], L[l + 1], hx, f, cyc); break;
+      default: down<7>(s, L[l], L[l + 1], hx, f, cyc); break;
     }
   }
   int nb = L[lb].n;
@@ -1393,9 +1403,9 @@ void mg_vcycle_fused(Solver* s, bool first_has_x, float* acc_h, float* acc_l) {
     float* al = l == 0 ? acc_l : nullptr;
     const int f = l == 0 ? fpost : -1;
     switch (P.mg_post_smooth) {
-      case 1: up<2>(s, L[l], L[l + 1], ah, al, f); break;
-      case 2: up<4>(s, L[l], L[l + 1], ah, al, f); break;
-      default: up<6>(s, L[l], L[l + 1], ah, al, f); break;
+      case 1: up<2>(s, L[l], L[l + 1], ah, al, f, cyc); break;
+      case 2: up<4>(s, L[l], L[l + 1], ah, al, f, cyc); break;
+      default: up<6>(s, L[l], L[l + 1], ah, al, f, cyc); break;
     }
   }
 }

@@ -117,3 +117,29 @@ def test_first_cycle_sweeps_of_the_cycle_change_nothing(pkg):
     assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1]) and ca == cb
     assert rz["failed_steps"] == 0 and rz["steps"] == steps, rz
     assert cz <= ca + steps, (cz, ca)
+
+
+def test_first_cycle_setting_in_eager_and_captured_steps_agree(pkg):
+    """The eager step (the host knows which cycle it enqueues) and the captured
+    step (the kernels read the loop's cycle count on the device) run the same
+    cycles with mg_first_pre = mg_first_post = 0: equal fields, bit for bit; the
+    eager profile names the first cycle's finest-level launches apart."""
+    n, steps = 512, 3
+    u0, v0, disks, dt, ch = pkg.workload.channel_workload(n, 5)
+    res = []
+    for eager in (False, True):
+        s = _gpu(pkg, n, (0, 0))
+        s.upload_velocity(u0, v0)
+        s.set_channel(ch)
+        s.set_solids(disks)
+        if eager:
+            prof = s.profile_step(dt, steps)
+            names = {k["name"]: k["launches"] for k in prof}
+            assert names.get("mg_up_acc_first") == steps and names.get("mg_down_l0_first") == steps, names
+            assert names.get("mg_up_acc", 0) >= steps, names
+        else:
+            for _ in range(steps):
+                s.step(dt)
+        res.append(s.read_velocity())
+        s.destroy()
+    assert np.array_equal(res[0][0], res[1][0]) and np.array_equal(res[0][1], res[1][1])
