@@ -220,7 +220,7 @@ COARSE_SWEEPS = 8
 FIRST_PRE, FIRST_POST = 0, 0
 
 
-def make_solver(pkg, n, device, guess="zero", relax=RELAX, coarse=None):
+def make_solver(pkg, n, device, guess="zero", relax=RELAX, coarse=None, first=None):
     """guess: "zero" (the reference's zero initial pressure), "warm" (the
     previous step's pressure) or "nn" (the trained pressure-guess network at
     half resolution, weights committed under fluid-sim_gb300/weights/)."""
@@ -228,7 +228,8 @@ def make_solver(pkg, n, device, guess="zero", relax=RELAX, coarse=None):
                            pressure_iterations=1, precision="mixed", pressure_tol=TOL, max_cycles=60,
                            warm_start=(guess == "warm"), device=device, relax=relax,
                            mg_coarse_sweeps=COARSE_SWEEPS if coarse is None else coarse,
-                           mg_first_pre=FIRST_PRE, mg_first_post=FIRST_POST)
+                           mg_first_pre=FIRST_PRE if first is None else first[0],
+                           mg_first_post=FIRST_POST if first is None else first[1])
     if guess == "nn":
         g = pkg.PressureGuess(device=device)
         g.load(GUESS_WEIGHTS)
@@ -292,9 +293,14 @@ def measure_batch(pkg, device, count, steps, warmup, seed=1, relax=RELAX):
             "gpu_launches_total": launches}
 
 
-def measure_variant(pkg, n, device, guess, u0, v0, disks, ch, dt, steps, warmup, relax=RELAX):
-    """ms/step, cycles/step and cell-steps/s of one initial-pressure choice."""
-    s = make_solver(pkg, n, device, guess, relax)
+def measure_variant(pkg, n, device, guess, u0, v0, disks, ch, dt, steps, warmup, relax=RELAX, reference_mg=False):
+    """ms/step, cycles/step and cell-steps/s of one initial-pressure choice;
+    reference_mg: the reference's multigrid configuration (relaxation 1.0, 40
+    coarse sweeps, every cycle smoothing the finest level)"""
+    if reference_mg:
+        s = make_solver(pkg, n, device, guess, 1.0, coarse=40, first=(-1, -1))
+    else:
+        s = make_solver(pkg, n, device, guess, relax)
     s.upload_velocity(u0, v0)
     s.set_channel(ch)
     s.set_solids(disks)
@@ -383,18 +389,23 @@ def run_gpu(args):
     lib.fs_host_free(hu)
     lib.fs_host_free(hv)
 
-    # the learned guess, the warm start and the reference's relaxation factor
-    # against the measured configuration, same workload, same tolerance, each
-    # timed over the same K steps
+    # the learned guess, the warm start and the reference's multigrid
+    # configuration against the measured one, same workload, same tolerance,
+    # each timed over the same K steps
     variants = {}
     if not args.no_variants:
-        for name, g, w in (("plain_mg", args.guess, args.relax), ("relax_1.0_mg", args.guess, 1.0),
+        for name, g, w in (("plain_mg", args.guess, args.relax), ("reference_config_mg", args.guess, 1.0),
                            ("nn_guess_mg", "nn", args.relax), ("warm_start_mg", "warm", args.relax)):
-            if name != "plain_mg" and g == args.guess and w == args.relax:
+            if name not in ("plain_mg", "reference_config_mg") and g == args.guess and w == args.relax:
                 continue
-            variants[name] = measure_variant(pkg, n, local, g, u0, v0, disks, ch, dt, args.steps, args.warmup, w)
+            ref = name == "reference_config_mg"
+            variants[name] = measure_variant(pkg, n, local, g, u0, v0, disks, ch, dt, args.steps, args.warmup, w,
+                                             reference_mg=ref)
             variants[name]["guess"] = g
             variants[name]["relax"] = w
+            if ref:
+                variants[name]["coarse_sweeps"] = 40
+                variants[name]["first_cycle_finest_sweeps"] = [-1, -1]
 
     forced = None
     if rank == 0 and args.forced_steps > 0:
@@ -468,11 +479,12 @@ def run_gpu(args):
             "clocks": clk.summary(),
         }
         if variants:
-            # throughput ratios against the zero initial pressure at this
-            # relaxation ("plain"), and against the reference's own multigrid
-            # configuration (zero initial pressure, relaxation 1.0)
+            # throughput ratios against the zero initial pressure with this
+            # multigrid ("plain"), and against the reference's own multigrid
+            # configuration (zero initial pressure, relaxation 1.0, 40 coarse
+            # sweeps, every cycle smoothing the finest level)
             base = variants.get("plain_mg", {}).get("value")
-            ref = variants.get("relax_1.0_mg", {}).get("value")
+            ref = variants.get("reference_config_mg", {}).get("value")
             for v in variants.values():
                 if base:
                     v["vs_plain_mg"] = v["value"] / base
