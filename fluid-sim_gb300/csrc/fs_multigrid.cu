@@ -453,26 +453,35 @@ __device__ __forceinline__ void mg_up_body(float* smem, const float* __restrict_
       }
     }
   }
+  // With no sweeps on this level (the first cycle of a MIXED projection whose
+  // finest-level sweeps are skipped) the correction is the prolongation alone:
+  // the iterate the down kernel left is zero and the rhs is not read, so only
+  // the coarse block is staged and the prolongation writes instead of adding
+  // (0 + P = P, and a -0 from P gives the same pressure sum as +0).
+  const bool pfast = ACC && post == 0;
   if (boxed || tma == 2) {
     // x of every box is a multiple of 4 (16 bytes) wherever it lies; boxes
     // across the grid's edge (tma == 2) are copied with zero fill and their
     // outer cells replaced by their periodic images
-    const TmaBox b[3] = {{xs, tm_x, bx, gj0}, {rs, tm_r, bx, gj0}, {cs, tm_c, cbx, cgj0}};
-    const uint32_t bytes = (uint32_t)((2 * B::N + C::WC * C::RC) * sizeof(float));
+    const TmaBox b[3] = {{cs, tm_c, cbx, cgj0}, {xs, tm_x, bx, gj0}, {rs, tm_r, bx, gj0}};
+    const int nb = pfast ? 1 : 3;
+    const uint32_t bytes = (uint32_t)(((pfast ? 0 : 2 * B::N) + C::WC * C::RC) * sizeof(float));
     if (boxed) {
-      if (!tma_stage_boxes(b, 3, bytes, &bar, err)) return;
+      if (!tma_stage_boxes(b, nb, bytes, &bar, err)) return;
     } else {
-      const RingBox rg[3] = {{xs, xin, B::W, B::R, bx, gj0, n}, {rs, rhs, B::W, B::R, bx, gj0, n},
-                             {cs, xc, C::WC, C::RC, cbx, cgj0, nc}};
-      if (!tma_stage_ringed<ring_regs<T, ACC>()>(b, rg, 3, bytes, &bar, err)) return;
+      const RingBox rg[3] = {{cs, xc, C::WC, C::RC, cbx, cgj0, nc}, {xs, xin, B::W, B::R, bx, gj0, n},
+                             {rs, rhs, B::W, B::R, bx, gj0, n}};
+      if (!tma_stage_ringed<ring_regs<T, ACC>()>(b, rg, nb, bytes, &bar, err)) return;
     }
   } else {
     for (int k = tid; k < C::RC * C::RC; k += nthr) {
       const int lj = k / C::RC, li = k - lj * C::RC;
       cp_async4(&cs[lj * C::WC + C::OC + li], xc + (int64_t)wrap1(cgj0 + lj, nc) * nc + wrap1(cgi0 + li, nc));
     }
-    stage_region<B::R, B::W, B::OX>(xs, xin, gi0, gj0, n);
-    stage_region<B::R, B::W, B::OX>(rs, rhs, gi0, gj0, n);
+    if (!pfast) {
+      stage_region<B::R, B::W, B::OX>(xs, xin, gi0, gj0, n);
+      stage_region<B::R, B::W, B::OX>(rs, rhs, gi0, gj0, n);
+    }
     cp_async_wait_all();
     __syncthreads();
   }
@@ -500,11 +509,13 @@ __device__ __forceinline__ void mg_up_body(float* smem, const float* __restrict_
       for (; d < dend; d++) {
         c += C::WC;
         const float n0 = c[C::WC], n1 = c[C::WC + 1], n2 = c[C::WC + 2];
-        float2 top = o[0], bot = o[B::W / 2];
-        top.x = __fadd_rn(top.x, prolong_val(a0, a1, b0, b1, 0.75f, 0.75f));
-        top.y = __fadd_rn(top.y, prolong_val(a1, a2, b1, b2, 0.25f, 0.75f));
-        bot.x = __fadd_rn(bot.x, prolong_val(b0, b1, n0, n1, 0.75f, 0.25f));
-        bot.y = __fadd_rn(bot.y, prolong_val(b1, b2, n1, n2, 0.25f, 0.25f));
+        float2 top = pfast ? make_float2(0.f, 0.f) : o[0], bot = pfast ? make_float2(0.f, 0.f) : o[B::W / 2];
+        const float pt0 = prolong_val(a0, a1, b0, b1, 0.75f, 0.75f), pt1 = prolong_val(a1, a2, b1, b2, 0.25f, 0.75f);
+        const float pb0 = prolong_val(b0, b1, n0, n1, 0.75f, 0.25f), pb1 = prolong_val(b1, b2, n1, n2, 0.25f, 0.25f);
+        top.x = pfast ? pt0 : __fadd_rn(top.x, pt0);
+        top.y = pfast ? pt1 : __fadd_rn(top.y, pt1);
+        bot.x = pfast ? pb0 : __fadd_rn(bot.x, pb0);
+        bot.y = pfast ? pb1 : __fadd_rn(bot.y, pb1);
         o[0] = top;
         o[B::W / 2] = bot;
         a0 = b0, a1 = b1, a2 = b2;
