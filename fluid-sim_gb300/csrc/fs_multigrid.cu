@@ -302,13 +302,30 @@ __device__ __forceinline__ void mg_down_body(float* smem, const float* __restric
                                              const float* __restrict__ xin, float* __restrict__ xout,
                                              float* __restrict__ crhs, int n, float h2, int pre, float w,
                                              const CUtensorMap* tm_r, const CUtensorMap* tm_x, int tma,
-                                             int* err) {
+                                             int* err, bool restrict_only = false) {
   using B = TileBox<T, H>;
   static_assert(H % 2 == 1, "the halo of the down kernel is 2 * pre + 1");
   float* const xs = smem;
   float* const rs = smem + B::NA;
   __shared__ uint64_t bar;
   const int i0 = blockIdx.x * T, j0 = blockIdx.y * T;
+  if (restrict_only) {
+    // no sweeps from a zero iterate that nothing reads afterwards (the first
+    // cycle of a MIXED projection without finest-level sweeps): the residual
+    // is the rhs itself (rhs - lap 0 rounds to rhs), restricted straight from
+    // global memory by float2 row pairs; no iterate is written
+    const int nc = n >> 1, tid = threadIdx.y * blockDim.x + threadIdx.x, nthr = blockDim.x * blockDim.y;
+    for (int k = tid; k < (T / 2) * (T / 2); k += nthr) {
+      const int cj = k / (T / 2), ci = k - cj * (T / 2);
+      const int gci = (i0 >> 1) + ci, gcj = (j0 >> 1) + cj;
+      if (gci >= nc || gcj >= nc) continue;
+      const float* q = rhs + (int64_t)(2 * gcj) * n + 2 * gci;
+      const float2 q0 = __ldg(reinterpret_cast<const float2*>(q));
+      const float2 q1 = __ldg(reinterpret_cast<const float2*>(q + n));
+      crhs[(int64_t)gcj * nc + gci] = restrict4(q0.x, q0.y, q1.x, q1.y);
+    }
+    return;
+  }
   const int gi0 = i0 - H, gj0 = j0 - H;
   const int par0 = (gi0 + gj0) & 1;  // n even: the parity of the wrapped index is the same
   const int tid = threadIdx.y * blockDim.x + threadIdx.x, nthr = blockDim.x * blockDim.y;
@@ -383,13 +400,18 @@ template <int T, int H>
 __global__ void __launch_bounds__(256)
     k_mg_down(const float* __restrict__ rhs, const float* __restrict__ xin, float* __restrict__ xout,
               float* __restrict__ crhs, int n, float h2, int pre, float w, const __grid_constant__ CUtensorMap tm_r,
-              const __grid_constant__ CUtensorMap tm_x, int tma, int* err, const int* first_cycle, int first_pre) {
+              const __grid_constant__ CUtensorMap tm_x, int tma, int* err, const int* first_cycle, int first_pre,
+              int first_x_unused) {
   extern __shared__ float tile_dyn[];
   // the first cycle of a projection may run fewer sweeps on this level
   // (fs_params mg_first_pre, at most pre): first_pre >= 0 applies it, inside
-  // a captured loop only while the loop's cycle count is still 0
-  if (first_pre >= 0 && (!first_cycle || *first_cycle == 0)) pre = first_pre;
-  mg_down_body<T, H>(tile_smem(tile_dyn), rhs, xin, xout, crhs, n, h2, pre, w, &tm_r, &tm_x, tma, err);
+  // a captured loop only while the loop's cycle count is still 0;
+  // first_x_unused: that cycle's up kernel on this level runs no sweeps
+  // either and does not read the iterate
+  const bool first = first_pre >= 0 && (!first_cycle || *first_cycle == 0);
+  if (first) pre = first_pre;
+  mg_down_body<T, H>(tile_smem(tile_dyn), rhs, xin, xout, crhs, n, h2, pre, w, &tm_r, &tm_x, tma, err,
+                     first && pre == 0 && first_x_unused && !xin);
 }
 
 // -------------------------------------------------------------------- up
@@ -1220,7 +1242,7 @@ static bool tile_maps(Solver* s, int n, const float* const* f, CUtensorMap* cons
 // cyc: the loop's cycle count on the device that decides (nullptr: the host
 // knows this is the first cycle)
 template <int T, int H>
-static void down_t(Solver* s, Level& L, const Level& C, bool has_x, int first, const int* cyc) {
+static void down_t(Solver* s, Level& L, const Level& C, bool has_x, int first, const int* cyc, bool x_unused) {
   static std::atomic<uint64_t> attr{0};
   constexpr size_t smem = down_smem_bytes<T, H>();
   tile_smem_attr(k_mg_down<T, H>, smem, s->prm.device, attr);
@@ -1237,16 +1259,17 @@ static void down_t(Solver* s, Level& L, const Level& C, bool has_x, int first, c
   FS_LAUNCH(s, name.c_str(), bytes,
             k_mg_down<T, H><<<grid, kTileBlock, smem, s->stream>>>(
                 L.rhs, xin, out, C.rhs, L.n, L.h2, s->prm.mg_pre_smooth, (float)s->prm.relax, tr, tx, tma,
-                &s->dev->async_err, cyc, first < s->prm.mg_pre_smooth ? first : s->prm.mg_pre_smooth));
+                &s->dev->async_err, cyc, first < s->prm.mg_pre_smooth ? first : s->prm.mg_pre_smooth,
+                x_unused ? 1 : 0));
   if (has_x) std::swap(L.x, L.x2);
 }
 
 template <int H>
-static void down(Solver* s, Level& L, const Level& C, bool has_x, int first, const int* cyc) {
+static void down(Solver* s, Level& L, const Level& C, bool has_x, int first, const int* cyc, bool x_unused) {
   switch (mg_tile(s, (int)(&L - s->lev.data()))) {
-    case 64: down_t<64, H>(s, L, C, has_x, first, cyc); break;
-    case 32: down_t<32, H>(s, L, C, has_x, first, cyc); break;
-    default: down_t<16, H>(s, L, C, has_x, first, cyc); break;
+    case 64: down_t<64, H>(s, L, C, has_x, first, cyc, x_unused); break;
+    case 32: down_t<32, H>(s, L, C, has_x, first, cyc, x_unused); break;
+    default: down_t<16, H>(s, L, C, has_x, first, cyc, x_unused); break;
   }
 }
 
@@ -1371,10 +1394,11 @@ void mg_vcycle_fused(Solver* s, bool first_has_x, float* acc_h, float* acc_l) {
   for (int l = 0; l < lb; l++) {
     bool hx = l == 0 && first_has_x;
     const int f = l == 0 ? fpre : -1;
+    const bool xu = l == 0 && fpost == 0;  // the first cycle's up kernel reads no iterate here
     switch (P.mg_pre_smooth) {
-      case 1: down<3>(s, L[l], L[l + 1], hx, f, cyc); break;
-      case 2: down<5>(s, L[l], L[l + 1], hx, f, cyc); break;
-      default: down<7>(s, L[l], L[l + 1], hx, f, cyc); break;
+      case 1: down<3>(s, L[l], L[l + 1], hx, f, cyc, xu); break;
+      case 2: down<5>(s, L[l], L[l + 1], hx, f, cyc, xu); break;
+      default: down<7>(s, L[l], L[l + 1], hx, f, cyc, xu); break;
     }
   }
   int nb = L[lb].n;
