@@ -425,7 +425,7 @@ __device__ __forceinline__ void mg_up_body(float* smem, const float* __restrict_
                                            float* __restrict__ xout, const float* __restrict__ xc, int n, float h2,
                                            int post, float* __restrict__ ph, float* __restrict__ pl, float w,
                                            const CUtensorMap* tm_r, const CUtensorMap* tm_x,
-                                           const CUtensorMap* tm_c, int tma, int* err) {
+                                           const CUtensorMap* tm_c, int tma, int* err, bool pfast = false) {
   using B = TileBox<T, H>;
   using C = CoarseBox<T, H>;
   static_assert(T % 16 == 0 && H % 2 == 0, "the up kernel's region starts on an even index");
@@ -475,12 +475,12 @@ __device__ __forceinline__ void mg_up_body(float* smem, const float* __restrict_
       }
     }
   }
-  // With no sweeps on this level (the first cycle of a MIXED projection whose
-  // finest-level sweeps are skipped) the correction is the prolongation alone:
-  // the iterate the down kernel left is zero and the rhs is not read, so only
-  // the coarse block is staged and the prolongation writes instead of adding
-  // (0 + P = P, and a -0 from P gives the same pressure sum as +0).
-  const bool pfast = ACC && post == 0;
+  // pfast: no sweeps on this level and a zero iterate from the down kernel (the
+  // first cycle of a MIXED projection whose finest-level sweeps are skipped on
+  // both sides): the correction is the prolongation alone and the rhs is not
+  // read, so only the coarse block is staged and the prolongation writes
+  // instead of adding (0 + P = P, and a -0 from P gives the same pressure sum
+  // as +0).
   if (boxed || tma == 2) {
     // x of every box is a multiple of 4 (16 bytes) wherever it lies; boxes
     // across the grid's edge (tma == 2) are copied with zero fill and their
@@ -629,11 +629,15 @@ __global__ void __launch_bounds__(256)
             const float* __restrict__ xc, int n, float h2, int post, float* __restrict__ ph,
             float* __restrict__ pl, float w, const __grid_constant__ CUtensorMap tm_r,
             const __grid_constant__ CUtensorMap tm_x, const __grid_constant__ CUtensorMap tm_c, int tma, int* err,
-            const int* first_cycle, int first_post) {
+            const int* first_cycle, int first_post, int first_x_zero) {
   extern __shared__ float tile_dyn[];
-  if (first_post >= 0 && (!first_cycle || *first_cycle == 0)) post = first_post;  // as k_mg_down
+  // as k_mg_down; first_x_zero: that cycle's down kernel on this level ran no
+  // sweeps, so the iterate is zero
+  const bool first = first_post >= 0 && (!first_cycle || *first_cycle == 0);
+  if (first) post = first_post;
+  const bool pfast = ACC && first && post == 0 && first_x_zero;
   mg_up_body<T, H, ACC>(tile_smem(tile_dyn), rhs, xin, xout, xc, n, h2, post, ph, pl, w, &tm_r, &tm_x, &tm_c, tma,
-                        err);
+                        err, pfast);
 }
 
 // ---------------------------------------------------------------- bottom
@@ -1274,7 +1278,8 @@ static void down(Solver* s, Level& L, const Level& C, bool has_x, int first, con
 }
 
 template <int T, int H>
-static void up_t(Solver* s, Level& L, const Level& C, float* acc_h, float* acc_l, int first, const int* cyc) {
+static void up_t(Solver* s, Level& L, const Level& C, float* acc_h, float* acc_l, int first, const int* cyc,
+                 bool x_zero) {
   using CB = CoarseBox<T, H>;
   dim3 grid((L.n + T - 1) / T, (L.n + T - 1) / T);
   constexpr size_t smem = up_smem_bytes<T, H>();
@@ -1291,7 +1296,8 @@ static void up_t(Solver* s, Level& L, const Level& C, float* acc_h, float* acc_l
     FS_LAUNCH(s, first >= 0 && !cyc ? "mg_up_acc_first" : "mg_up_acc", bytes,
               k_mg_up<T, H, true><<<grid, kTileBlock, smem, s->stream>>>(
                   L.rhs, L.x, nullptr, C.x, L.n, L.h2, s->prm.mg_post_smooth, acc_h, acc_l, (float)s->prm.relax, tr,
-                  tx, tc, tma, err, cyc, first < s->prm.mg_post_smooth ? first : s->prm.mg_post_smooth));
+                  tx, tc, tma, err, cyc, first < s->prm.mg_post_smooth ? first : s->prm.mg_post_smooth,
+                  x_zero ? 1 : 0));
     return;
   }
   static std::atomic<uint64_t> attr{0};
@@ -1300,16 +1306,18 @@ static void up_t(Solver* s, Level& L, const Level& C, float* acc_h, float* acc_l
   FS_LAUNCH(s, level_name(s, L, "mg_up").c_str(), bytes,
             k_mg_up<T, H, false><<<grid, kTileBlock, smem, s->stream>>>(
                 L.rhs, L.x, L.x2, C.x, L.n, L.h2, s->prm.mg_post_smooth, nullptr, nullptr, (float)s->prm.relax, tr,
-                tx, tc, tma, err, cyc, first < s->prm.mg_post_smooth ? first : s->prm.mg_post_smooth));
+                tx, tc, tma, err, cyc, first < s->prm.mg_post_smooth ? first : s->prm.mg_post_smooth,
+                  x_zero ? 1 : 0));
   std::swap(L.x, L.x2);
 }
 
 template <int H>
-static void up(Solver* s, Level& L, const Level& C, float* acc_h, float* acc_l, int first, const int* cyc) {
+static void up(Solver* s, Level& L, const Level& C, float* acc_h, float* acc_l, int first, const int* cyc,
+               bool x_zero) {
   switch (mg_tile(s, (int)(&L - s->lev.data()))) {
-    case 64: up_t<64, H>(s, L, C, acc_h, acc_l, first, cyc); break;
-    case 32: up_t<32, H>(s, L, C, acc_h, acc_l, first, cyc); break;
-    default: up_t<16, H>(s, L, C, acc_h, acc_l, first, cyc); break;
+    case 64: up_t<64, H>(s, L, C, acc_h, acc_l, first, cyc, x_zero); break;
+    case 32: up_t<32, H>(s, L, C, acc_h, acc_l, first, cyc, x_zero); break;
+    default: up_t<16, H>(s, L, C, acc_h, acc_l, first, cyc, x_zero); break;
   }
 }
 
@@ -1437,10 +1445,11 @@ void mg_vcycle_fused(Solver* s, bool first_has_x, float* acc_h, float* acc_l) {
     float* ah = l == 0 ? acc_h : nullptr;
     float* al = l == 0 ? acc_l : nullptr;
     const int f = l == 0 ? fpost : -1;
+    const bool xz = l == 0 && fpre == 0;  // the first cycle's down kernel left a zero iterate here
     switch (P.mg_post_smooth) {
-      case 1: up<2>(s, L[l], L[l + 1], ah, al, f, cyc); break;
-      case 2: up<4>(s, L[l], L[l + 1], ah, al, f, cyc); break;
-      default: up<6>(s, L[l], L[l + 1], ah, al, f, cyc); break;
+      case 1: up<2>(s, L[l], L[l + 1], ah, al, f, cyc, xz); break;
+      case 2: up<4>(s, L[l], L[l + 1], ah, al, f, cyc, xz); break;
+      default: up<6>(s, L[l], L[l + 1], ah, al, f, cyc, xz); break;
     }
   }
 }
