@@ -1230,10 +1230,7 @@ static void tile_smem_attr(K kernel, size_t bytes, int device, std::atomic<uint6
 // tiles run in one wave, where the slowest CTA sets the time: there the ring
 // loads must be in flight during the copy (tma_stage_ringed's registers); a
 // fix-up after the wait made levels 2-4 slower by 1.2-3.2 us per launch.
-template <int T>
-constexpr int tile_tma_mode() {
-  return 2;
-}
+constexpr int kTileTmaMode = 2;
 template <int T, int H>
 static bool tile_maps(Solver* s, int n, const float* const* f, CUtensorMap* const* m, int count) {
   using B = TileBox<T, H>;
@@ -1257,7 +1254,7 @@ static void down_t(Solver* s, Level& L, const Level& C, bool has_x, int first, c
   CUtensorMap tr{}, tx{};
   const float* f[2] = {L.rhs, xin};
   CUtensorMap* m[2] = {&tr, &tx};
-  const int tma = tile_maps<T, H>(s, L.n, f, m, 2) ? tile_tma_mode<T>() : 0;
+  const int tma = tile_maps<T, H>(s, L.n, f, m, 2) ? kTileTmaMode : 0;
   // a first cycle the host knows is profiled under its own name
   const std::string name = level_name(s, L, "mg_down") + (first >= 0 && !cyc ? "_first" : "");
   FS_LAUNCH(s, name.c_str(), bytes,
@@ -1287,7 +1284,7 @@ static void up_t(Solver* s, Level& L, const Level& C, float* acc_h, float* acc_l
   const float* f[2] = {L.rhs, L.x};
   CUtensorMap* m[2] = {&tr, &tx};
   const int tma =
-      tile_maps<T, H>(s, L.n, f, m, 2) && box_tmap(s, C.x, C.n, C.n, CB::WC, CB::RC, &tc) ? tile_tma_mode<T>() : 0;
+      tile_maps<T, H>(s, L.n, f, m, 2) && box_tmap(s, C.x, C.n, C.n, CB::WC, CB::RC, &tc) ? kTileTmaMode : 0;
   int* err = &s->dev->async_err;
   if (acc_h) {
     static std::atomic<uint64_t> attr{0};
@@ -1474,7 +1471,7 @@ static void down_class_t(Solver* const* ms, int count, int l, cudaStream_t st) {
     m.st = s->dev;
     const float* f[1] = {L.rhs};
     CUtensorMap* mp[1] = {&tab.tm[i]};
-    m.tma = tile_maps<T, H>(s, L.n, f, mp, 1) ? tile_tma_mode<T>() : 0;
+    m.tma = tile_maps<T, H>(s, L.n, f, mp, 1) ? kTileTmaMode : 0;
   }
   static std::atomic<uint64_t> attr{0};
   constexpr size_t smem = down_smem_bytes<T, H>();
@@ -1528,7 +1525,7 @@ static void up_class_t(Solver* const* ms, int count, int l, cudaStream_t st) {
     const float* f[2] = {L.rhs, L.x};
     CUtensorMap* mp[2] = {&tab.tm[i][0], &tab.tm[i][1]};
     m.tma = tile_maps<T, H>(s, L.n, f, mp, 2) && box_tmap(s, C.x, C.n, C.n, CB::WC, CB::RC, &tab.tm[i][2])
-                ? tile_tma_mode<T>()
+                ? kTileTmaMode
                 : 0;
     if (!ACC) std::swap(L.x, L.x2);
   }
